@@ -186,7 +186,7 @@ def _normalize(value):
         arr = arr.astype(np.float64)
     if arr.dtype.byteorder == ">":
         arr = arr.astype(arr.dtype.newbyteorder("<"))
-    return np.ascontiguousarray(arr)
+    return arr.copy(order="C")  # keeps 0-d scalars 0-d (ascontiguousarray would not)
 
 
 class _Node:
