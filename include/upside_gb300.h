@@ -1,0 +1,71 @@
+/* Batched GB300 Upside engine: many systems (replicas, or proteins of uneven
+ * length) advanced together by one set of sm_103a kernels and one captured
+ * CUDA graph.  These entry points have no counterpart in the reference C
+ * library; they expose the GPU form of the reference driver's per-system loop
+ * (src/main.cpp:915-999) and replica exchange (src/main.cpp:147-317).
+ *
+ * All arrays are host arrays, copied at the call; positions and momenta of
+ * the whole batch are concatenated in the order the systems were given.
+ * Functions return 0 on success and non-zero on error (ug_last_error()).
+ */
+#ifndef UPSIDE_GB300_BATCH_H
+#define UPSIDE_GB300_BATCH_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct UgBatch UgBatch;
+
+const char* ug_last_error(void);
+
+/* Build one engine over n_sys `.up` files (identical node graphs). */
+UgBatch* ug_create(int n_sys, const char* const* paths, const int* n_atom);
+void ug_free(UgBatch* b);
+int ug_atom_total(UgBatch* b);
+
+int ug_set_pos(UgBatch* b, const float* pos);
+int ug_get_pos(UgBatch* b, float* pos);
+int ug_set_mom(UgBatch* b, const float* mom);
+int ug_get_mom(UgBatch* b, float* mom);
+
+/* Potential + derivative for every system; energy[n_sys] (FP64 sums), deriv
+ * (atom_total,3) may be NULL. */
+int ug_evaluate(UgBatch* b, double* energy, float* deriv);
+
+/* Thermostat state: per-system temperature and seed, common timescale; the
+ * per-system invocation counter (the thermostat's RNG counter) is set by
+ * ug_set_round. */
+int ug_set_thermostat(UgBatch* b, const float* temperature, const uint32_t* seed);
+int ug_set_round(UgBatch* b, const uint64_t* round);
+
+/* Advance n_round rounds of {thermostat; 3 x (force, p -= dt F, x += dt p)}.
+ * use_graph != 0 replays a captured CUDA graph of graph_rounds rounds. */
+int ug_run(UgBatch* b, int n_round, float dt, float timescale, int use_graph, int graph_rounds);
+
+/* Node introspection over the whole batch (rows of all systems concatenated). */
+int ug_node_dims(UgBatch* b, const char* node, int* n_elem, int* width);
+int ug_node_output(UgBatch* b, const char* node, float* out, int n);
+int ug_node_sens(UgBatch* b, const char* node, float* out, int n);
+int ug_node_edges(UgBatch* b, const char* node, int32_t* pairs, int cap);
+int ug_value_by_name(UgBatch* b, const char* node, const char* what, float* out, int n);
+/* per-node potential of each system after ug_evaluate: out[n_sys] */
+int ug_node_potential(UgBatch* b, const char* node, double* out);
+
+/* Replica exchange over the batch: energies of all systems are evaluated,
+ * then Metropolis swaps of coordinates between the neighbour pairs of the
+ * given swap set (pairs[2*k], pairs[2*k+1]) with FP64 acceptance
+ * (src/main.cpp:243-316).  accepted[k] receives 0/1. */
+int ug_replica_exchange(UgBatch* b, int n_pairs, const int* pairs, uint32_t seed, uint64_t round, int* accepted);
+
+/* status bits: 1 pair list overflow (grown automatically), 2 BP hit max_iter,
+ * 4 residue-pair storage overflow */
+int ug_status(UgBatch* b, int clear);
+/* kernel launches per force evaluation and device bytes held */
+int ug_info(UgBatch* b, int* launches_per_eval, int64_t* device_bytes);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

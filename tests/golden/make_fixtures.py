@@ -1,0 +1,147 @@
+"""Generate the golden fixtures the parity tests compare against.
+
+Run here, where the reference checkout exists; writes small files next to
+this script, which are committed (the GPU host has no reference checkout):
+
+  chig.up            the reference's own ff_2.1 example config
+                     (example/15.SpatialTransformation/inputs/chig.up)
+  chig_frames.npz    the 20 logged frames of the reference's example run
+                     (outputs/simple_test/chig.run.up /output/pos, /output/potential)
+                     plus the locally built reference engine's energy and
+                     derivative at each frame
+  syn<N>_ref.npz     seeded synthetic ff_2.1 proteins (config_gen): sequence,
+                     seed, coordinates (initial + perturbed frames), and the
+                     reference engine's energy, derivative, per-node outputs,
+                     sensitivities, potentials and pair-list counts by type
+
+The reference engine is oracle/_ref/libupside_ref.so (oracle/build.py).
+"""
+import ctypes
+import os
+import shutil
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.abspath(os.path.join(HERE, "..", ".."))
+sys.path.insert(0, os.path.join(ROOT, "upside2-md_gb300"))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+import config_gen  # noqa: E402
+from h5lite import H5File  # noqa: E402
+import build as oracle_build  # noqa: E402
+
+REF = os.environ.get("UPSIDE_REFERENCE", "/root/reference")
+EX = os.path.join(REF, "example", "15.SpatialTransformation")
+
+
+class RefEngine:
+    def __init__(self, lib, path, n_atom):
+        self.L = lib
+        self.e = lib.construct_deriv_engine(n_atom, path.encode(), True)
+        assert self.e
+        self.n = n_atom
+
+    def eval(self, pos):
+        pos = np.ascontiguousarray(pos, np.float32)
+        en = ctypes.c_float()
+        assert self.L.evaluate_energy(ctypes.byref(en), self.e, pos.ctypes.data) == 0
+        d = np.zeros_like(pos)
+        assert self.L.evaluate_deriv(d.ctypes.data, self.e, pos.ctypes.data) == 0
+        return en.value, d
+
+    def dims(self, nm):
+        n, w = ctypes.c_int(), ctypes.c_int()
+        assert self.L.get_output_dims(ctypes.byref(n), ctypes.byref(w), self.e, nm.encode()) == 0
+        return n.value, w.value
+
+    def node(self, nm, sens=False):
+        n, w = self.dims(nm)
+        o = np.zeros((n, w), np.float32)
+        fn = self.L.get_sens if sens else self.L.get_output
+        assert fn(o.size, o.ctypes.data, self.e, nm.encode()) == 0
+        return o
+
+    def value(self, nm, what, n):
+        o = np.zeros(n, np.float32)
+        r = self.L.get_value_by_name(n, o.ctypes.data, self.e, nm.encode(), what.encode())
+        return o if r == 0 else None
+
+
+def load_ref():
+    path = oracle_build.build_reference()
+    L = ctypes.CDLL(path)
+    L.construct_deriv_engine.restype = ctypes.c_void_p
+    L.construct_deriv_engine.argtypes = [ctypes.c_int, ctypes.c_char_p, ctypes.c_bool]
+    L.evaluate_energy.argtypes = [ctypes.POINTER(ctypes.c_float), ctypes.c_void_p, ctypes.c_void_p]
+    L.evaluate_deriv.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+    L.get_output.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_char_p]
+    L.get_sens.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_char_p]
+    L.get_output_dims.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_char_p]
+    L.get_value_by_name.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_char_p, ctypes.c_char_p]
+    return L
+
+
+GRAPH_NODES = ["rotamer", "hbond_coverage", "hbond_coverage_hydrophobe", "protein_hbond"]
+
+
+def chig(L):
+    shutil.copyfile(os.path.join(EX, "inputs", "chig.up"), os.path.join(HERE, "chig.up"))
+    run = H5File(os.path.join(EX, "outputs", "simple_test", "chig.run.up"))
+    pos = run.read("/output/pos")[:, 0].astype(np.float32)
+    pot = run.read("/output/potential")[:, 0]
+    eng = RefEngine(L, os.path.join(HERE, "chig.up"), pos.shape[1])
+    E, D = [], []
+    for x in pos:
+        e, d = eng.eval(x)
+        E.append(e)
+        D.append(d)
+    np.savez_compressed(os.path.join(HERE, "chig_frames.npz"), pos=pos, logged_potential=pot,
+                        ref_energy=np.array(E), ref_deriv=np.array(D))
+
+
+def synthetic(L, n_res, seed, n_frames=3, tmpdir="/tmp"):
+    rng = np.random.RandomState(seed)
+    seq = config_gen.random_sequence(n_res, rng)
+    path = os.path.join(tmpdir, "syn%d_%d.up" % (n_res, seed))
+    pos0 = config_gen.write_config(path, seq, seed)
+    # every frame carries coordinate noise: the initial structure of a random
+    # chain has residue 0's N, CA, C exactly coplanar with the reference frame
+    # geometry, a degenerate case in which the reference eigen-solver returns
+    # a non-maximal eigenvector (parity notes)
+    frames = []
+    prng = np.random.RandomState(seed + 1000)
+    for k in range(n_frames):
+        frames.append((pos0 + (0.02 if k == 0 else 0.05) * prng.randn(*pos0.shape)).astype(np.float32))
+    eng = RefEngine(L, path, pos0.shape[0])
+    out = {"seq": np.array([s.encode() for s in seq]), "seed": np.int64(seed), "pos": np.array(frames)}
+    E, D = [], []
+    names = H5File(path).list("/input/potential")
+    for k, x in enumerate(frames):
+        e, d = eng.eval(x)
+        E.append(e)
+        D.append(d)
+        if k == 0:
+            for nm in names:
+                out["out/" + nm] = eng.node(nm)
+                out["sens/" + nm] = eng.node(nm, sens=True)
+            for nm in GRAPH_NODES:
+                n_t = {"rotamer": 400, "hbond_coverage": 8 * 20, "hbond_coverage_hydrophobe": 12 * 20}.get(nm)
+                if n_t:
+                    v = eng.value(nm, "count_edges_by_type", n_t)
+                    if v is not None:
+                        out["count/" + nm] = v
+    out["ref_energy"] = np.array(E)
+    out["ref_deriv"] = np.array(D)
+    np.savez_compressed(os.path.join(HERE, "syn%d_ref.npz" % n_res), **out)
+
+
+def main():
+    L = load_ref()
+    chig(L)
+    synthetic(L, 60, 1)
+    synthetic(L, 150, 2, n_frames=2)
+
+
+if __name__ == "__main__":
+    main()

@@ -237,7 +237,9 @@ def write_config(path, seq, seed, chain_first_residue=(), pos=None, environment_
 
     # ---- Rama map potential (synthetic maps; see module docstring)
     g = c.grp("rama_map_pot", ["rama_coord"], integrator_level=0)
-    maps = synthetic_rama_maps(seq, rng)
+    # maps get their own stream so a config is the same whether or not the
+    # caller supplies coordinates
+    maps = synthetic_rama_maps(seq, np.random.RandomState(seed + 104729))
     c.ds(g + "/residue_id", np.arange(n_res))
     c.ds(g + "/rama_map_id", np.arange(n_res))
     c.ds(g + "/rama_pot", maps)

@@ -1,0 +1,443 @@
+// C ABI of the GB300 engine: the reference's engine C library entry points
+// (drop-in, src/engine_c_library.h:6-33) and the batch API (upside_gb300.h).
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "engine.h"
+#include "../../include/engine_c_library.h"
+#include "../../include/upside_gb300.h"
+
+using ug::Engine;
+
+namespace {
+thread_local std::string g_err;
+
+// -------------------------------------------------- clamped spline helpers ---
+// uniform cubic B-spline weights
+void bsp4h(float y, float b[4]) {
+    float y2 = y * y, y3 = y2 * y, o = 1.f - y;
+    b[0] = o * o * o / 6.f;
+    b[1] = (3.f * y3 - 6.f * y2 + 4.f) / 6.f;
+    b[2] = (-3.f * y3 + 3.f * y2 + 3.f * y + 1.f) / 6.f;
+    b[3] = y3 / 6.f;
+}
+void clamped_h(const float* c, float x, int n, float& v, float& d) {
+    if (x <= 1.f) { v = c[0] / 6.f + c[1] * (2.f / 3.f) + c[2] / 6.f; d = 0.f; return; }
+    if (x >= float(n - 2)) { v = c[n - 3] / 6.f + c[n - 2] * (2.f / 3.f) + c[n - 1] / 6.f; d = 0.f; return; }
+    int xb = int(x);
+    float y = x - float(xb), b[4], o = 1.f - y;
+    bsp4h(y, b);
+    float db[4] = {-0.5f * o * o, 1.5f * y * y - 2.f * y, -1.5f * y * y + y + 0.5f, 0.5f * y * y};
+    v = d = 0.f;
+    for (int k = 0; k < 4; ++k) { v += c[xb - 1 + k] * b[k]; d += c[xb - 1 + k] * db[k]; }
+}
+}  // namespace
+
+// opaque handle type of the drop-in ABI
+struct DerivEngine {
+    std::unique_ptr<Engine> e;
+    int n_atom;
+};
+struct UgBatch {
+    std::unique_ptr<Engine> e;
+};
+
+#define GUARD_BEGIN try {
+#define GUARD_END(ret)                                   \
+    }                                                    \
+    catch (const std::exception& ex) {                   \
+        g_err = ex.what();                               \
+        fprintf(stderr, "\n\nERROR: %s\n", ex.what());   \
+        return ret;                                      \
+    }
+
+extern "C" {
+
+// ============================================================ drop-in ABI ===
+DerivEngine* construct_deriv_engine(int n_atom, const char* potential_file, bool quiet) {
+    (void)quiet;
+    GUARD_BEGIN
+    auto* d = new DerivEngine;
+    d->n_atom = n_atom;
+    d->e.reset(new Engine({std::string(potential_file)}, {n_atom}));
+    return d;
+    GUARD_END(nullptr)
+}
+
+void free_deriv_engine(DerivEngine* engine) { delete engine; }
+
+int evaluate_energy(float* energy, DerivEngine* engine, const float* pos) {
+    GUARD_BEGIN
+    engine->e->set_pos(pos);
+    engine->e->compute_checked(true);
+    double en = 0;
+    engine->e->energies(&en);
+    *energy = float(en);
+    return 0;
+    GUARD_END(1)
+}
+
+int evaluate_deriv(float* deriv, DerivEngine* engine, const float* pos) {
+    GUARD_BEGIN
+    engine->e->set_pos(pos);
+    engine->e->compute_checked(true);
+    engine->e->get_deriv(deriv);
+    return 0;
+    GUARD_END(1)
+}
+
+int set_param(int n_param, const float* param, DerivEngine* engine, const char* node_name) {
+    GUARD_BEGIN
+    engine->e->node(node_name).set_param(*engine->e, std::vector<float>(param, param + n_param));
+    return 0;
+    GUARD_END(1)
+}
+
+int get_param(int n_param, float* param, DerivEngine* engine, const char* node_name) {
+    GUARD_BEGIN
+    auto v = engine->e->node(node_name).get_param(*engine->e);
+    if (v.size() != size_t(n_param))
+        throw ug::Error("Wrong number of parameters, expected " + std::to_string(v.size()) + " but got " +
+                        std::to_string(n_param));
+    std::copy(v.begin(), v.end(), param);
+    return 0;
+    GUARD_END(1)
+}
+
+int get_param_deriv(int n_param, float* deriv, DerivEngine* engine, const char* node_name) {
+    GUARD_BEGIN
+    auto v = engine->e->node(node_name).param_deriv(*engine->e);
+    if (v.size() != size_t(n_param))
+        throw ug::Error("Wrong number of parameters, expected " + std::to_string(v.size()) + " but got " +
+                        std::to_string(n_param));
+    std::copy(v.begin(), v.end(), deriv);
+    return 0;
+    GUARD_END(1)
+}
+
+static int node_copy(Engine& e, const char* name, float* out, int n, bool sens) {
+    auto& nd = e.node(name);
+    if (nd.potential) {
+        if (n != 1) throw ug::Error("wrong size for potential node");
+        double v = 0;
+        UG_CK(cudaMemcpy(&v, e.d_pot + size_t(nd.pot_slot) * e.n_sys, sizeof(double), cudaMemcpyDeviceToHost));
+        *out = float(v);
+        return 0;
+    }
+    if (n != nd.total * nd.width) throw ug::Error("wrong size for CoordNode");
+    e.sync();
+    UG_CK(cudaMemcpy(out, sens ? nd.sens : nd.out, sizeof(float) * size_t(n), cudaMemcpyDeviceToHost));
+    return 0;
+}
+
+int get_sens(int n_output, float* output, DerivEngine* engine, const char* node_name) {
+    GUARD_BEGIN
+    return node_copy(*engine->e, node_name, output, n_output, true);
+    GUARD_END(1)
+}
+
+int get_output(int n_output, float* output, DerivEngine* engine, const char* node_name) {
+    GUARD_BEGIN
+    return node_copy(*engine->e, node_name, output, n_output, false);
+    GUARD_END(1)
+}
+
+int get_output_dims(int* n_elem, int* elem_width, DerivEngine* engine, const char* node_name) {
+    GUARD_BEGIN
+    auto& nd = engine->e->node(node_name);
+    *n_elem = nd.potential ? 1 : nd.total;
+    *elem_width = nd.potential ? 1 : nd.width;
+    return 0;
+    GUARD_END(1)
+}
+
+int get_value_by_name(int n_output, float* output, DerivEngine* engine, const char* node_name, const char* log_name) {
+    GUARD_BEGIN
+    auto v = engine->e->node(node_name).value_by_name(*engine->e, log_name);
+    if (n_output != int(v.size()))
+        throw ug::Error("expected size (" + std::to_string(n_output) + " elements) inconsistent with actual size (" +
+                        std::to_string(v.size()) + ")");
+    std::copy(v.begin(), v.end(), output);
+    return 0;
+    GUARD_END(1)
+}
+
+// Clamped spline helpers: B-spline coefficients whose clamped spline
+// interpolates `values` at the interior knots, with zero end slopes
+// (clamped_spline_solve, src/engine_c_library.cpp:197-206).
+int clamped_spline_solve(int N, float* bspline_coeff, const float* values) {
+    int n = N - 2;
+    if (n < 2) return 1;
+    std::vector<double> a(size_t(n), 1. / 6.), b(size_t(n), 2. / 3.), c(size_t(n), 1. / 6.), d(values, values + n);
+    c[0] *= 2.;
+    a[size_t(n - 1)] *= 2.;
+    for (int k = 1; k < n; ++k) {  // Thomas algorithm
+        double m = a[size_t(k)] / b[size_t(k - 1)];
+        b[size_t(k)] -= m * c[size_t(k - 1)];
+        d[size_t(k)] -= m * d[size_t(k - 1)];
+    }
+    d[size_t(n - 1)] /= b[size_t(n - 1)];
+    for (int k = n - 2; k >= 0; --k) d[size_t(k)] = (d[size_t(k)] - c[size_t(k)] * d[size_t(k + 1)]) / b[size_t(k)];
+    for (int k = 0; k < n; ++k) bspline_coeff[k + 1] = float(d[size_t(k)]);
+    bspline_coeff[0] = bspline_coeff[2];
+    bspline_coeff[N - 1] = bspline_coeff[N - 3];
+    return 0;
+}
+
+int clamped_spline_value(int N, float* result, const float* bspline_coeff, int nx, float* x) {
+    for (int i = 0; i < nx; ++i) {
+        float v, d;
+        clamped_h(bspline_coeff, x[i], N, v, d);
+        result[i] = v;
+    }
+    return 0;
+}
+
+int get_clamped_value_and_deriv(int N, float* result, const float* bspline_coeff, int nx, float* x) {
+    for (int i = 0; i < nx; ++i) clamped_h(bspline_coeff, x[i], N, result[2 * i], result[2 * i + 1]);
+    return 0;
+}
+
+int get_clamped_coeff_deriv(int N, float* result, const float* bspline_coeff, float x) {
+    (void)bspline_coeff;
+    for (int i = 0; i < N; ++i) result[i] = 0.f;
+    if (x <= 1.f) { result[0] = 1.f / 6.f; result[1] = 2.f / 3.f; result[2] = 1.f / 6.f; return 0; }
+    if (x >= float(N - 2)) { result[N - 3] = 1.f / 6.f; result[N - 2] = 2.f / 3.f; result[N - 1] = 1.f / 6.f; return 0; }
+    int xb = int(x);
+    float b[4];
+    bsp4h(x - float(xb), b);
+    for (int k = 0; k < 4; ++k) result[xb - 1 + k] = b[k];
+    return 0;
+}
+
+// ============================================================== batch API ===
+const char* ug_last_error(void) { return g_err.c_str(); }
+
+UgBatch* ug_create(int n_sys, const char* const* paths, const int* n_atom) {
+    GUARD_BEGIN
+    std::vector<std::string> p(paths, paths + n_sys);
+    std::vector<int> na(n_atom, n_atom + n_sys);
+    auto* b = new UgBatch;
+    b->e.reset(new Engine(p, na));
+    return b;
+    GUARD_END(nullptr)
+}
+
+void ug_free(UgBatch* b) { delete b; }
+int ug_atom_total(UgBatch* b) { return b->e->atom_total; }
+
+int ug_set_pos(UgBatch* b, const float* pos) {
+    GUARD_BEGIN
+    b->e->set_pos(pos);
+    return 0;
+    GUARD_END(1)
+}
+int ug_get_pos(UgBatch* b, float* pos) {
+    GUARD_BEGIN
+    b->e->get_pos(pos);
+    return 0;
+    GUARD_END(1)
+}
+int ug_set_mom(UgBatch* b, const float* mom) {
+    GUARD_BEGIN
+    UG_CK(cudaMemcpyAsync(b->e->d_mom, mom, sizeof(float) * 3 * size_t(b->e->atom_total), cudaMemcpyHostToDevice, b->e->st));
+    b->e->sync();
+    return 0;
+    GUARD_END(1)
+}
+int ug_get_mom(UgBatch* b, float* mom) {
+    GUARD_BEGIN
+    UG_CK(cudaMemcpyAsync(mom, b->e->d_mom, sizeof(float) * 3 * size_t(b->e->atom_total), cudaMemcpyDeviceToHost, b->e->st));
+    b->e->sync();
+    return 0;
+    GUARD_END(1)
+}
+
+int ug_evaluate(UgBatch* b, double* energy, float* deriv) {
+    GUARD_BEGIN
+    b->e->compute_checked(true);
+    if (energy) b->e->energies(energy);
+    if (deriv) b->e->get_deriv(deriv);
+    return 0;
+    GUARD_END(1)
+}
+
+int ug_set_thermostat(UgBatch* b, const float* temperature, const uint32_t* seed) {
+    GUARD_BEGIN
+    UG_CK(cudaMemcpyAsync(b->e->d_temp, temperature, sizeof(float) * size_t(b->e->n_sys), cudaMemcpyHostToDevice, b->e->st));
+    UG_CK(cudaMemcpyAsync(b->e->d_seed, seed, sizeof(uint32_t) * size_t(b->e->n_sys), cudaMemcpyHostToDevice, b->e->st));
+    b->e->sync();
+    return 0;
+    GUARD_END(1)
+}
+
+int ug_set_round(UgBatch* b, const uint64_t* round) {
+    GUARD_BEGIN
+    UG_CK(cudaMemcpyAsync(b->e->d_round, round, sizeof(uint64_t) * size_t(b->e->n_sys), cudaMemcpyHostToDevice, b->e->st));
+    b->e->sync();
+    return 0;
+    GUARD_END(1)
+}
+
+int ug_run(UgBatch* b, int n_round, float dt, float timescale, int use_graph, int graph_rounds) {
+    GUARD_BEGIN
+    Engine& e = *b->e;
+    if (!use_graph) {
+        for (int r = 0; r < n_round; ++r) e.round(dt, timescale, true);
+        e.sync();
+        return 0;
+    }
+    if (graph_rounds < 1) graph_rounds = 1;
+    if (!e.graph_exec || e.graph_rounds != graph_rounds) e.capture(dt, timescale, graph_rounds);
+    int full = n_round / graph_rounds;
+    for (int k = 0; k < full; ++k) e.launch_graph();
+    for (int r = full * graph_rounds; r < n_round; ++r) e.round(dt, timescale, true);
+    e.sync();
+    return 0;
+    GUARD_END(1)
+}
+
+int ug_node_dims(UgBatch* b, const char* node, int* n_elem, int* width) {
+    GUARD_BEGIN
+    auto& nd = b->e->node(node);
+    *n_elem = nd.potential ? 1 : nd.total;
+    *width = nd.potential ? 1 : nd.width;
+    return 0;
+    GUARD_END(1)
+}
+int ug_node_output(UgBatch* b, const char* node, float* out, int n) {
+    GUARD_BEGIN
+    return node_copy(*b->e, node, out, n, false);
+    GUARD_END(1)
+}
+int ug_node_sens(UgBatch* b, const char* node, float* out, int n) {
+    GUARD_BEGIN
+    return node_copy(*b->e, node, out, n, true);
+    GUARD_END(1)
+}
+int ug_node_edges(UgBatch* b, const char* node, int32_t* pairs, int cap) {
+    GUARD_BEGIN
+    auto* g = b->e->node(node).graph();
+    if (!g) throw ug::Error("node has no pair list");
+    b->e->sync();
+    int ne = 0;
+    UG_CK(cudaMemcpy(&ne, g->n_edge, 4, cudaMemcpyDeviceToHost));
+    int k = std::min(ne, cap);
+    if (k > 0) UG_CK(cudaMemcpy(pairs, g->edges, sizeof(int2) * size_t(k), cudaMemcpyDeviceToHost));
+    return ne;
+    GUARD_END(-1)
+}
+int ug_value_by_name(UgBatch* b, const char* node, const char* what, float* out, int n) {
+    GUARD_BEGIN
+    auto v = b->e->node(node).value_by_name(*b->e, what);
+    if (n != int(v.size())) throw ug::Error("size mismatch: " + std::to_string(v.size()));
+    std::copy(v.begin(), v.end(), out);
+    return 0;
+    GUARD_END(1)
+}
+int ug_node_potential(UgBatch* b, const char* node, double* out) {
+    GUARD_BEGIN
+    auto& nd = b->e->node(node);
+    if (!nd.potential) throw ug::Error("not a potential node");
+    b->e->sync();
+    UG_CK(cudaMemcpy(out, b->e->d_pot + size_t(nd.pot_slot) * b->e->n_sys, sizeof(double) * size_t(b->e->n_sys),
+                     cudaMemcpyDeviceToHost));
+    return 0;
+    GUARD_END(1)
+}
+
+// Replica exchange, criterion 0 of the reference (src/main.cpp:270-294):
+// energies at the current coordinates, swap the coordinates of every pair of
+// the set, energies again, then undo each swap that fails the Metropolis test
+// on the change of the log Boltzmann factors.  Energies are FP64 sums and the
+// acceptance arithmetic is FP64; the uniform draws come from the replica
+// exchange Threefry stream keyed by (seed, stream 1) at counter (round, 0, 0, k).
+namespace {
+void threefry_host(const uint32_t c[4], const uint32_t k[4], uint32_t out[4]) {
+    static const int R[8][2] = {{10, 26}, {11, 21}, {13, 27}, {23, 5}, {6, 20}, {17, 11}, {25, 10}, {18, 20}};
+    uint32_t ks[5] = {k[0], k[1], k[2], k[3], 0x1BD11BDAu ^ k[0] ^ k[1] ^ k[2] ^ k[3]};
+    uint32_t x[4];
+    for (int i = 0; i < 4; ++i) x[i] = c[i] + ks[i];
+    auto rotl = [](uint32_t v, int r) { return (v << r) | (v >> (32 - r)); };
+    for (int r = 0; r < 20; ++r) {
+        if (r % 2 == 0) {
+            x[0] += x[1]; x[1] = rotl(x[1], R[r % 8][0]); x[1] ^= x[0];
+            x[2] += x[3]; x[3] = rotl(x[3], R[r % 8][1]); x[3] ^= x[2];
+        } else {
+            x[0] += x[3]; x[3] = rotl(x[3], R[r % 8][0]); x[3] ^= x[0];
+            x[2] += x[1]; x[1] = rotl(x[1], R[r % 8][1]); x[1] ^= x[2];
+        }
+        if (r % 4 == 3) {
+            uint32_t s = uint32_t(r / 4 + 1);
+            for (int i = 0; i < 4; ++i) x[i] += ks[(s + uint32_t(i)) % 5];
+            x[3] += s;
+        }
+    }
+    for (int i = 0; i < 4; ++i) out[i] = x[i];
+}
+void swap_coords(Engine& e, int s1, int s2, float* tmp) {
+    if (e.n_atom[size_t(s1)] != e.n_atom[size_t(s2)]) throw ug::Error("replica exchange needs equal atom counts");
+    size_t n = sizeof(float) * 3 * size_t(e.n_atom[size_t(s1)]);
+    float* a = e.d_pos + 3 * size_t(e.atom_off[size_t(s1)]);
+    float* b = e.d_pos + 3 * size_t(e.atom_off[size_t(s2)]);
+    UG_CK(cudaMemcpyAsync(tmp, a, n, cudaMemcpyDeviceToDevice, e.st));
+    UG_CK(cudaMemcpyAsync(a, b, n, cudaMemcpyDeviceToDevice, e.st));
+    UG_CK(cudaMemcpyAsync(b, tmp, n, cudaMemcpyDeviceToDevice, e.st));
+}
+}  // namespace
+
+int ug_replica_exchange(UgBatch* b, int n_pairs, const int* pairs, uint32_t seed, uint64_t round, int* accepted) {
+    GUARD_BEGIN
+    Engine& e = *b->e;
+    int S = e.n_sys;
+    std::vector<float> temp(static_cast<size_t>(S));
+    UG_CK(cudaMemcpy(temp.data(), e.d_temp, sizeof(float) * size_t(S), cudaMemcpyDeviceToHost));
+    std::vector<double> e_old(static_cast<size_t>(S)), e_new(static_cast<size_t>(S));
+    e.compute_checked(true);
+    e.energies(e_old.data());
+    float* tmp = nullptr;
+    int max_atom = *std::max_element(e.n_atom.begin(), e.n_atom.end());
+    UG_CK(cudaMalloc(&tmp, sizeof(float) * 3 * size_t(max_atom)));
+    for (int k = 0; k < n_pairs; ++k) swap_coords(e, pairs[2 * k], pairs[2 * k + 1], tmp);
+    e.compute_checked(true);
+    e.energies(e_new.data());
+    uint32_t key[4] = {seed, 1u, 0u, 0u};
+    uint32_t ctr[4] = {uint32_t(round & 0xffffffffu), uint32_t(round >> 32), 0u, 0u};
+    for (int k = 0; k < n_pairs; ++k) {
+        int s1 = pairs[2 * k], s2 = pairs[2 * k + 1];
+        double b1 = 1.0 / temp[size_t(s1)], b2 = 1.0 / temp[size_t(s2)];
+        double diff = (-b1 * e_new[size_t(s1)] - b2 * e_new[size_t(s2)]) - (-b1 * e_old[size_t(s1)] - b2 * e_old[size_t(s2)]);
+        bool reject = false;
+        if (diff < 0.0) {
+            uint32_t bits[4];
+            threefry_host(ctr, key, bits);
+            ctr[3]++;
+            double u = double(float(bits[0]) * (1.f / 4294967296.f) + (0.5f / 4294967296.f));
+            reject = std::exp(diff) < u;
+        }
+        if (reject) swap_coords(e, s1, s2, tmp);
+        if (accepted) accepted[k] = reject ? 0 : 1;
+    }
+    e.sync();
+    cudaFree(tmp);
+    return 0;
+    GUARD_END(1)
+}
+
+int ug_status(UgBatch* b, int clear) {
+    GUARD_BEGIN
+    return b->e->status(clear != 0);
+    GUARD_END(-1)
+}
+
+int ug_info(UgBatch* b, int* launches, int64_t* bytes) {
+    if (launches) *launches = b->e->launches_per_compute;
+    if (bytes) *bytes = int64_t(b->e->device_bytes);
+    return 0;
+}
+
+}  // extern "C"

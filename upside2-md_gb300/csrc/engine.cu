@@ -1,0 +1,2071 @@
+// GB300 Upside engine: force-field nodes as batched sm_103a kernels, the
+// integrator with the Ornstein-Uhlenbeck thermostat, CUDA-graph capture.
+//
+// Each node restates one reference node type (registered by name prefix as
+// src/deriv_engine.cpp:353-437 does); the citation is beside each class.
+// Data layout: a node's output is a dense (elements x width) FP32 array over
+// the whole batch, systems concatenated; index arrays are global.
+#include "engine.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+#include <set>
+#include <unordered_map>
+
+#include "dev_math.cuh"
+
+namespace ug {
+
+void cuda_check(cudaError_t e, const char* what) {
+    if (e != cudaSuccess) throw Error(std::string("CUDA error ") + cudaGetErrorString(e) + " at " + what);
+}
+
+template <class T> T* Engine::alloc(size_t n) {
+    void* p = nullptr;
+    size_t bytes = std::max<size_t>(1, n) * sizeof(T);
+    UG_CK(cudaMalloc(&p, bytes));
+    UG_CK(cudaMemsetAsync(p, 0, bytes, st));
+    allocations_.push_back(p);
+    device_bytes += bytes;
+    return static_cast<T*>(p);
+}
+template <class T> T* Engine::upload(const std::vector<T>& v) {
+    T* p = alloc<T>(v.size());
+    if (!v.empty()) UG_CK(cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, st));
+    return p;
+}
+void Engine::free_all() {
+    for (void* p : allocations_) cudaFree(p);
+    allocations_.clear();
+}
+
+namespace {
+
+inline int nblk(long long n, int bs = 256) { return int(std::max(1LL, std::min<long long>((n + bs - 1) / bs, 8 * 152))); }
+
+// --------------------------------------------------------- host helpers ---
+std::vector<int> read_i(h5lite::File& f, const std::string& p) {
+    auto v = f.read<int32_t>(p);
+    return std::vector<int>(v.begin(), v.end());
+}
+std::vector<float> read_f(h5lite::File& f, const std::string& p) { return f.read<float>(p); }
+double attr_d(h5lite::File& f, const std::string& p, const std::string& a, double def = NAN) {
+    if (!f.has_attr(p, a)) {
+        if (std::isnan(def)) throw Error("missing attribute '" + a + "' on " + p);
+        return def;
+    }
+    return f.attr_values<double>(p, a).at(0);
+}
+
+// concatenate an index dataset over systems, adding the per-system offset of
+// the node the indices refer to (negative indices are kept as -1)
+std::vector<int> cat_idx(const Groups& g, const std::string& ds, const std::vector<int>* target_off, int stride = 1) {
+    std::vector<int> out;
+    (void)stride;
+    for (size_t s = 0; s < g.size(); ++s) {
+        auto v = read_i(g.f(s), g.p(ds));
+        int o = target_off ? (*target_off)[s] : 0;
+        // every index is checked against the referenced node's range here, so
+        // no kernel ever receives an out-of-range gather/scatter index
+        int lim = target_off ? (*target_off)[s + 1] - o : 0;
+        for (size_t i = 0; i < v.size(); ++i) {
+            if (target_off && (v[i] >= lim || v[i] < -1))
+                throw Error("index " + std::to_string(v[i]) + " in '" + g.p(ds) + "' is out of range [0," +
+                            std::to_string(lim) + ")");
+            out.push_back(v[i] < 0 ? -1 : v[i] + o);
+        }
+    }
+    return out;
+}
+std::vector<float> cat_f(const Groups& g, const std::string& ds) {
+    std::vector<float> out;
+    for (size_t s = 0; s < g.size(); ++s) {
+        auto v = read_f(g.f(s), g.p(ds));
+        out.insert(out.end(), v.begin(), v.end());
+    }
+    return out;
+}
+// one table for all systems; differing tables are an error (a batch shares
+// one force field)
+std::vector<float> shared_f(const Groups& g, const std::string& ds) {
+    auto a = read_f(g.f(0), g.p(ds));
+    for (size_t s = 1; s < g.size(); ++s)
+        if (read_f(g.f(s), g.p(ds)) != a) throw Error("'" + g.p(ds) + "' differs between systems of one batch");
+    return a;
+}
+double shared_attr(const Groups& g, const std::string& a, double def = NAN, const std::string& sub = "") {
+    double v = attr_d(g.f(0), sub.empty() ? g.path : g.p(sub), a, def);
+    for (size_t s = 1; s < g.size(); ++s)
+        if (attr_d(g.f(s), sub.empty() ? g.path : g.p(sub), a, def) != v)
+            throw Error("attribute '" + a + "' of " + g.path + " differs between systems of one batch");
+    return v;
+}
+std::vector<int> counts(const Groups& g, const std::string& ds) {
+    std::vector<int> c;
+    for (size_t s = 0; s < g.size(); ++s) c.push_back(int(g.f(s).dims(g.p(ds)).at(0)));
+    return c;
+}
+std::vector<int> offsets(const std::vector<int>& c) {
+    std::vector<int> o(c.size() + 1, 0);
+    for (size_t i = 0; i < c.size(); ++i) o[i + 1] = o[i] + c[i];
+    return o;
+}
+std::vector<int> sys_of(const std::vector<int>& off) {
+    std::vector<int> s;
+    for (size_t i = 0; i + 1 < off.size(); ++i)
+        for (int k = off[i]; k < off[i + 1]; ++k) s.push_back(int(i));
+    return s;
+}
+
+// periodic interpolating cubic B-spline coefficients (cyclic tridiagonal
+// (1/6, 2/3, 1/6) solve by Sherman-Morrison), in double
+void cyclic_solve(int n, const double* d, double* c) {
+    const double a = 1. / 6., b = 2. / 3., cc = 1. / 6., gamma = -b;
+    std::vector<double> bb(size_t(n), b), u(size_t(n), 0.), y(d, d + n), ys(static_cast<size_t>(n)), z(static_cast<size_t>(n)), cp(static_cast<size_t>(n));
+    bb[0] = b - gamma;
+    bb[size_t(n - 1)] = b - a * cc / gamma;
+    u[0] = gamma;
+    u[size_t(n - 1)] = cc;
+    auto tri = [&](std::vector<double>& rhs, std::vector<double>& x) {
+        cp[0] = cc / bb[0];
+        x[0] = rhs[0] / bb[0];
+        for (int i = 1; i < n; ++i) {
+            double m = bb[size_t(i)] - a * cp[size_t(i - 1)];
+            cp[size_t(i)] = cc / m;
+            x[size_t(i)] = (rhs[size_t(i)] - a * x[size_t(i - 1)]) / m;
+        }
+        for (int i = n - 2; i >= 0; --i) x[size_t(i)] -= cp[size_t(i)] * x[size_t(i + 1)];
+    };
+    tri(y, ys);
+    tri(u, z);
+    double f = (ys[0] + a / gamma * ys[size_t(n - 1)]) / (1. + z[0] + a / gamma * z[size_t(n - 1)]);
+    for (int i = 0; i < n; ++i) c[i] = ys[size_t(i)] - f * z[size_t(i)];
+}
+// fit one nx x ny periodic layer, emit the (nx+3) x (ny+3) padded coefficients
+void fit_periodic_layer(int nx, int ny, const double* data, std::vector<float>& out) {
+    std::vector<double> tmp(size_t(nx) * ny), row(size_t(std::max(nx, ny))), res(size_t(std::max(nx, ny)));
+    for (int ix = 0; ix < nx; ++ix) {
+        cyclic_solve(ny, data + size_t(ix) * ny, res.data());
+        for (int iy = 0; iy < ny; ++iy) tmp[size_t(ix) * ny + iy] = res[size_t(iy)];
+    }
+    std::vector<double> C(size_t(nx) * ny);
+    for (int iy = 0; iy < ny; ++iy) {
+        for (int ix = 0; ix < nx; ++ix) row[size_t(ix)] = tmp[size_t(ix) * ny + iy];
+        cyclic_solve(nx, row.data(), res.data());
+        for (int ix = 0; ix < nx; ++ix) C[size_t(ix) * ny + iy] = res[size_t(ix)];
+    }
+    int nxp = nx + 3, nyp = ny + 3;
+    for (int i = 0; i < nxp; ++i)
+        for (int j = 0; j < nyp; ++j)
+            out.push_back(float(C[size_t(((i - 1) % nx + nx) % nx) * ny + size_t(((j - 1) % ny + ny) % ny)]));
+}
+
+// Pool of periodic spline layers shared across systems: identical layers
+// (same data) are fitted and stored once.
+struct LayerPool {
+    int nx = 0, ny = 0;
+    std::vector<float> coeff;
+    std::map<std::vector<double>, int> seen;
+    int add(const double* d) {
+        std::vector<double> key(d, d + size_t(nx) * ny);
+        auto it = seen.find(key);
+        if (it != seen.end()) return it->second;
+        int id = int(seen.size());
+        fit_periodic_layer(nx, ny, d, coeff);
+        seen.emplace(std::move(key), id);
+        return id;
+    }
+};
+
+// energy accumulation (FP64 on device)
+__device__ __forceinline__ void add_energy(double* slot, int sys, float e) {
+    if (slot) atomicAdd(slot + sys, double(e));
+}
+
+// ============================================================ pos node ===
+struct PosNode : GNode {
+    void forward(Engine&, bool) override {}
+};
+
+// ========================================================= Distance3D ===
+// |x1 - x2| (DistCoord, src/coord_basic.cpp:13-66)
+__global__ void dist_fwd(int n, const int2* __restrict__ id, const float* __restrict__ p1, const float* __restrict__ p2,
+                         float* __restrict__ out, float* __restrict__ der) {
+    for (int i = grid_stride_start(); i < n; i += grid_stride()) {
+        int2 a = id[i];
+        f3 d = ld3(p1 + 3 * size_t(a.x)) - ld3(p2 + 3 * size_t(a.y));
+        float r = sqrtf(mag2(d));
+        out[i] = r;
+        st3(der + 3 * size_t(i), r != 0.f ? d * (1.f / r) : mk(0, 0, 0));
+    }
+}
+__global__ void dist_bwd(int n, const int2* __restrict__ id, const float* __restrict__ sens, const float* __restrict__ der,
+                         float* s1, float* s2) {
+    for (int i = grid_stride_start(); i < n; i += grid_stride()) {
+        float s = sens[i];
+        f3 d = ld3(der + 3 * size_t(i)) * s;
+        atomic_add3(s1 + 3 * size_t(id[i].x), d);
+        atomic_add3(s2 + 3 * size_t(id[i].y), -d);
+    }
+}
+struct DistNode : GNode {
+    int2* id = nullptr;
+    float* der = nullptr;
+    DistNode(Engine& e, const Groups& g, const std::vector<int>& o1, const std::vector<int>& o2) {
+        std::vector<int2> v;
+        for (size_t s = 0; s < g.size(); ++s) {
+            auto a = read_i(g.f(s), g.p("id"));
+            for (size_t i = 0; i + 1 < a.size(); i += 2) v.push_back(make_int2(a[i] + o1[s], a[i + 1] + o2[s]));
+            off.push_back(int(v.size()) - int(a.size() / 2));
+        }
+        off.push_back(int(v.size()));
+        width = 1;
+        total = int(v.size());
+        id = e.upload(v);
+        der = e.alloc<float>(size_t(total) * 3);
+    }
+    void forward(Engine& e, bool) override {
+        dist_fwd<<<nblk(total), 256, 0, e.st>>>(total, id, e.arg(*this, 0).out, e.arg(*this, 1).out, out, der);
+    }
+    void backward(Engine& e) override {
+        dist_bwd<<<nblk(total), 256, 0, e.st>>>(total, id, sens, der, e.arg(*this, 0).sens, e.arg(*this, 1).sens);
+    }
+};
+
+// ============================================================== Angle ===
+// cosine of the angle at the third atom (AngleCoord, src/coord_basic.cpp:183-243)
+__global__ void angle_fwd(int n, const int* __restrict__ id, const float* __restrict__ p, float* __restrict__ out,
+                          float* __restrict__ der) {
+    for (int i = grid_stride_start(); i < n; i += grid_stride()) {
+        f3 a = ld3(p + 3 * size_t(id[3 * i])), b = ld3(p + 3 * size_t(id[3 * i + 1])), c = ld3(p + 3 * size_t(id[3 * i + 2]));
+        f3 x1 = a - c, x2 = b - c;
+        float i1 = rsqrtf(mag2(x1)), i2 = rsqrtf(mag2(x2));
+        f3 h1 = x1 * i1, h2 = x2 * i2;
+        float dp = dot(h1, h2);
+        out[i] = dp;
+        st3(der + 6 * size_t(i), (h2 - h1 * dp) * i1);
+        st3(der + 6 * size_t(i) + 3, (h1 - h2 * dp) * i2);
+    }
+}
+__global__ void angle_bwd(int n, const int* __restrict__ id, const float* __restrict__ sens, const float* __restrict__ der,
+                          float* ps) {
+    for (int i = grid_stride_start(); i < n; i += grid_stride()) {
+        float s = sens[i];
+        f3 d1 = ld3(der + 6 * size_t(i)) * s, d2 = ld3(der + 6 * size_t(i) + 3) * s;
+        atomic_add3(ps + 3 * size_t(id[3 * i]), d1);
+        atomic_add3(ps + 3 * size_t(id[3 * i + 1]), d2);
+        atomic_add3(ps + 3 * size_t(id[3 * i + 2]), -(d1 + d2));
+    }
+}
+struct AngleNode : GNode {
+    int* id = nullptr;
+    float* der = nullptr;
+    AngleNode(Engine& e, const Groups& g, const std::vector<int>& o) {
+        std::vector<int> v;
+        off.push_back(0);
+        for (size_t s = 0; s < g.size(); ++s) {
+            auto a = read_i(g.f(s), g.p("id"));
+            for (int x : a) v.push_back(x + o[s]);
+            off.push_back(int(v.size() / 3));
+        }
+        width = 1;
+        total = int(v.size() / 3);
+        id = e.upload(v);
+        der = e.alloc<float>(size_t(total) * 6);
+    }
+    void forward(Engine& e, bool) override {
+        angle_fwd<<<nblk(total), 256, 0, e.st>>>(total, id, e.arg(*this, 0).out, out, der);
+    }
+    void backward(Engine& e) override {
+        angle_bwd<<<nblk(total), 256, 0, e.st>>>(total, id, sens, der, e.arg(*this, 0).sens);
+    }
+};
+
+// =========================================================== Dihedral ===
+// dihedral angle, -80 degrees when a terminal atom is missing
+// (DihedralCoord, src/coord_basic.cpp:311-374; dihedral_germ src/vector_math.h:766-800)
+__global__ void dihedral_fwd(int n, const int4* __restrict__ id, const float* __restrict__ p, float* __restrict__ out,
+                             float* __restrict__ jac) {
+    for (int i = grid_stride_start(); i < n; i += grid_stride()) {
+        int4 a = id[i];
+        if (a.x < 0 || a.w < 0) {
+            out[i] = -1.3963f;
+            continue;
+        }
+        f3 r1 = ld3(p + 3 * size_t(a.x)), r2 = ld3(p + 3 * size_t(a.y)), r3 = ld3(p + 3 * size_t(a.z)),
+           r4 = ld3(p + 3 * size_t(a.w));
+        f3 F = r1 - r2, G = r2 - r3, H = r4 - r3;
+        f3 A = cross(F, G), B = cross(H, G), C = cross(B, A);
+        float iA = 1.f / mag2(A), iB = 1.f / mag2(B);
+        float G2 = mag2(G), iG = rsqrtf(G2), Gm = G2 * iG;
+        f3 d1 = A * (-Gm * iA), d4 = B * (Gm * iB);
+        f3 fm = A * (dot(F, G) * iA * iG) - B * (dot(H, G) * iB * iG);
+        float* j = jac + 12 * size_t(i);
+        st3(j, d1);
+        st3(j + 3, fm - d1);
+        st3(j + 6, -d4 - fm);
+        st3(j + 9, d4);
+        out[i] = atan2f(dot(C, G), dot(A, B) * Gm);
+    }
+}
+__global__ void dihedral_bwd(int n, const int4* __restrict__ id, const float* __restrict__ sens,
+                             const float* __restrict__ jac, float* ps) {
+    for (int i = grid_stride_start(); i < n; i += grid_stride()) {
+        int4 a = id[i];
+        if (a.x < 0 || a.w < 0) continue;
+        float s = sens[i];
+        const float* j = jac + 12 * size_t(i);
+        atomic_add3(ps + 3 * size_t(a.x), ld3(j) * s);
+        atomic_add3(ps + 3 * size_t(a.y), ld3(j + 3) * s);
+        atomic_add3(ps + 3 * size_t(a.z), ld3(j + 6) * s);
+        atomic_add3(ps + 3 * size_t(a.w), ld3(j + 9) * s);
+    }
+}
+struct DihedralNode : GNode {
+    int4* id = nullptr;
+    float* jac = nullptr;
+    DihedralNode(Engine& e, const Groups& g, const std::vector<int>& o) {
+        std::vector<int4> v;
+        off.push_back(0);
+        for (size_t s = 0; s < g.size(); ++s) {
+            auto a = read_i(g.f(s), g.p("id"));
+            auto m = [&](int x) { return x < 0 ? -1 : x + o[s]; };
+            for (size_t i = 0; i + 3 < a.size(); i += 4) v.push_back(make_int4(m(a[i]), m(a[i + 1]), m(a[i + 2]), m(a[i + 3])));
+            off.push_back(int(v.size()));
+        }
+        width = 1;
+        total = int(v.size());
+        id = e.upload(v);
+        jac = e.alloc<float>(size_t(total) * 12);
+    }
+    void forward(Engine& e, bool) override {
+        dihedral_fwd<<<nblk(total), 256, 0, e.st>>>(total, id, e.arg(*this, 0).out, out, jac);
+    }
+    void backward(Engine& e) override {
+        dihedral_bwd<<<nblk(total), 256, 0, e.st>>>(total, id, sens, jac, e.arg(*this, 0).sens);
+    }
+};
+
+// ============================================================= Spring ===
+// harmonic spring on one component, periodic option (Spring, src/spring.cpp:9-81)
+__global__ void spring_kernel(int n, const int* __restrict__ id, const float* __restrict__ eq, const float* __restrict__ k,
+                              const int* __restrict__ sys, int w, int dim1, int pbc, float box, const float* __restrict__ x,
+                              float* xs, double* pot) {
+    for (int i = grid_stride_start(); i < n; i += grid_stride()) {
+        int r = id[i] * w + dim1;
+        float v = x[r];
+        float ex = v - eq[i], s2 = ex * ex;
+        if (ex == 0.f) continue;
+        if (pbc) {
+            float e1 = v - eq[i] - box, e2 = v - eq[i] + box;
+            if (e1 * e1 < s2) { s2 = e1 * e1; ex = e1; }
+            if (e2 * e2 < s2) { s2 = e2 * e2; ex = e2; }
+        }
+        add_energy(pot, sys[i], 0.5f * k[i] * s2);
+        atomicAdd(xs + r, k[i] * ex);
+    }
+}
+struct SpringNode : GNode {
+    int *id = nullptr, *sysv = nullptr;
+    float *eq = nullptr, *kk = nullptr;
+    int n = 0, dim1 = 0, pbc = 0;
+    float box = 0;
+    SpringNode(Engine& e, const Groups& g, const std::vector<int>& o) {
+        potential = true;
+        auto c = counts(g, "id");
+        auto so = offsets(c);
+        n = so.back();
+        id = e.upload(cat_idx(g, "id", &o));
+        eq = e.upload(cat_f(g, "equil_dist"));
+        kk = e.upload(cat_f(g, "spring_const"));
+        sysv = e.upload(sys_of(so));
+        dim1 = int(shared_attr(g, "dim1"));
+        pbc = int(shared_attr(g, "pbc"));
+        box = float(shared_attr(g, "box_len"));
+    }
+    void forward(Engine& e, bool energy) override {
+        auto& a = e.arg(*this, 0);
+        spring_kernel<<<nblk(n), 256, 0, e.st>>>(n, id, eq, kk, sysv, a.width, dim1, pbc, box, a.out, a.sens,
+                                                 energy ? e.d_pot + size_t(pot_slot) * e.n_sys : nullptr);
+    }
+};
+
+// ========================================================= rama_coord ===
+// paste (phi, psi) (PasteRama, src/coord_map.cpp:69-110) and cat_pos (CatPos, :112-161)
+__global__ void paste_fwd(int n1, int n2, const int* __restrict__ i1, const int* __restrict__ i2,
+                          const int* __restrict__ dst1, const int* __restrict__ dst2, int w, int wa, int wb, int col_b,
+                          const float* __restrict__ a, const float* __restrict__ b, float* __restrict__ out) {
+    for (int i = grid_stride_start(); i < n1; i += grid_stride())
+        for (int d = 0; d < wa; ++d) out[size_t(dst1[i]) * w + d] = a[size_t(i1[i]) * wa + d];
+    for (int i = grid_stride_start(); i < n2; i += grid_stride())
+        for (int d = 0; d < wb; ++d) out[size_t(dst2[i]) * w + col_b + d] = b[size_t(i2[i]) * wb + d];
+}
+__global__ void paste_bwd(int n1, int n2, const int* __restrict__ i1, const int* __restrict__ i2,
+                          const int* __restrict__ dst1, const int* __restrict__ dst2, int w, int wa, int wb, int col_b,
+                          const float* __restrict__ sens, float* as, float* bs) {
+    for (int i = grid_stride_start(); i < n1; i += grid_stride())
+        for (int d = 0; d < wa; ++d) atomicAdd(as + size_t(i1[i]) * wa + d, sens[size_t(dst1[i]) * w + d]);
+    for (int i = grid_stride_start(); i < n2; i += grid_stride())
+        for (int d = 0; d < wb; ++d) atomicAdd(bs + size_t(i2[i]) * wb + d, sens[size_t(dst2[i]) * w + col_b + d]);
+}
+// rama_coord: output row i = (phi[i1[i]], psi[i2[i]]); cat_pos: rows of a then rows of b
+struct PasteNode : GNode {
+    int *i1 = nullptr, *i2 = nullptr, *d1 = nullptr, *d2 = nullptr;
+    int n1 = 0, n2 = 0, col_b = 0, wa = 1, wb = 1;
+    PasteNode(Engine& e, const Groups& g, bool cat, const std::vector<int>& oa, const std::vector<int>& ob) {
+        auto c1 = counts(g, "index_pos1"), c2 = counts(g, "index_pos2");
+        std::vector<int> dst1, dst2;
+        off.push_back(0);
+        for (size_t s = 0; s < g.size(); ++s) {
+            int base = off.back();
+            for (int i = 0; i < c1[s]; ++i) dst1.push_back(base + i);
+            for (int i = 0; i < c2[s]; ++i) dst2.push_back(base + (cat ? c1[s] : 0) + i);
+            off.push_back(base + (cat ? c1[s] + c2[s] : c1[s]));
+        }
+        if (cat) {
+            width = int(shared_attr(g, "n_dim"));
+            wa = wb = width;
+            col_b = 0;
+        } else {
+            width = 2;
+            col_b = 1;
+        }
+        total = off.back();
+        i1 = e.upload(cat_idx(g, "index_pos1", &oa));
+        i2 = e.upload(cat_idx(g, "index_pos2", &ob));
+        d1 = e.upload(dst1);
+        d2 = e.upload(dst2);
+        n1 = int(dst1.size());
+        n2 = int(dst2.size());
+    }
+    void forward(Engine& e, bool) override {
+        auto &a = e.arg(*this, 0), &b = e.arg(*this, 1);
+        paste_fwd<<<nblk(std::max(n1, n2)), 256, 0, e.st>>>(n1, n2, i1, i2, d1, d2, width, a.width, b.width, col_b,
+                                                             a.out, b.out, out);
+    }
+    void backward(Engine& e) override {
+        auto &a = e.arg(*this, 0), &b = e.arg(*this, 1);
+        paste_bwd<<<nblk(std::max(n1, n2)), 256, 0, e.st>>>(n1, n2, i1, i2, d1, d2, width, a.width, b.width, col_b,
+                                                             sens, a.sens, b.sens);
+    }
+};
+
+// ========================================================= rama maps ===
+// per-residue periodic bicubic potential over (phi, psi)
+// (RamaMapPot, src/rama_map_pot.cpp:15-94; LayeredPeriodicSpline2D src/spline.h:444-499)
+__global__ void rama_map_kernel(int n, const int* __restrict__ res, const int* __restrict__ layer,
+                                const int* __restrict__ sys, const float* __restrict__ coeff, int nxp, int nyp,
+                                float scale, const float* __restrict__ rama, float* rs, double* pot) {
+    for (int i = grid_stride_start(); i < n; i += grid_stride()) {
+        int r = res[i];
+        float x = (rama[2 * r] + 3.14159265358979f) * scale, y = (rama[2 * r + 1] + 3.14159265358979f) * scale;
+        float v, dx, dy;
+        periodic2d(coeff + size_t(layer[i]) * nxp * nyp, nyp, x, y, v, dx, dy);
+        add_energy(pot, sys[i], v);
+        atomicAdd(rs + 2 * r, dx * scale);
+        atomicAdd(rs + 2 * r + 1, dy * scale);
+    }
+}
+struct RamaMapNode : GNode {
+    int *res = nullptr, *layer = nullptr, *sysv = nullptr;
+    float* coeff = nullptr;
+    int n = 0, nxp = 0, nyp = 0;
+    float scale = 0;
+    RamaMapNode(Engine& e, const Groups& g, const std::vector<int>& o) {
+        potential = true;
+        LayerPool pool;
+        std::vector<int> lay;
+        auto c = counts(g, "residue_id");
+        for (size_t s = 0; s < g.size(); ++s) {
+            auto d = g.f(s).dims(g.p("rama_pot"));
+            if (d.size() != 3 || d[1] != d[2]) throw Error("must have same x and y grid spacing for Rama maps");
+            if (s == 0) { pool.nx = int(d[1]); pool.ny = int(d[2]); }
+            if (int(d[1]) != pool.nx) throw Error("Rama map sizes differ between systems of one batch");
+            auto data = g.f(s).read<double>(g.p("rama_pot"));
+            std::vector<int> local(d[0]);
+            for (size_t l = 0; l < d[0]; ++l) local[l] = pool.add(data.data() + l * pool.nx * pool.ny);
+            for (int id : read_i(g.f(s), g.p("rama_map_id"))) lay.push_back(local.at(size_t(id)));
+        }
+        nxp = pool.nx + 3;
+        nyp = pool.ny + 3;
+        scale = float(pool.nx) * (0.5f / 3.14159265358979f - 1e-7f);
+        n = int(lay.size());
+        res = e.upload(cat_idx(g, "residue_id", &o));
+        layer = e.upload(lay);
+        sysv = e.upload(sys_of(offsets(c)));
+        coeff = e.upload(pool.coeff);
+    }
+    void forward(Engine& e, bool energy) override {
+        auto& a = e.arg(*this, 0);
+        rama_map_kernel<<<nblk(n), 256, 0, e.st>>>(n, res, layer, sysv, coeff, nxp, nyp, scale, a.out, a.sens,
+                                                   energy ? e.d_pot + size_t(pot_slot) * e.n_sys : nullptr);
+    }
+};
+
+// ===================================================== affine frames ===
+// Rigid frame (centroid, quaternion) per residue: the quaternion is the top
+// eigenvector of the 4x4 key matrix of the N/CA/C fit, found by cyclic
+// Jacobi rotations; the adjoint is first-order eigenvector perturbation
+// (AffineAlignment, src/eig.cpp:277-470).
+__device__ void jacobi4(float A[4][4], float V[4][4]) {
+    for (int i = 0; i < 4; ++i)
+        for (int j = 0; j < 4; ++j) V[i][j] = (i == j) ? 1.f : 0.f;
+    for (int sweep = 0; sweep < 12; ++sweep) {
+        float off = fabsf(A[0][1]) + fabsf(A[0][2]) + fabsf(A[0][3]) + fabsf(A[1][2]) + fabsf(A[1][3]) + fabsf(A[2][3]);
+        if (off == 0.f) break;
+#pragma unroll
+        for (int p = 0; p < 3; ++p)
+#pragma unroll
+            for (int q = p + 1; q < 4; ++q) {
+                float apq = A[p][q];
+                if (apq == 0.f) continue;
+                float theta = (A[q][q] - A[p][p]) / (2.f * apq);
+                float t = copysignf(1.f, theta) / (fabsf(theta) + sqrtf(theta * theta + 1.f));
+                float c = rsqrtf(t * t + 1.f), s = t * c;
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    float akp = A[k][p], akq = A[k][q];
+                    A[k][p] = c * akp - s * akq;
+                    A[k][q] = s * akp + c * akq;
+                }
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    float apk = A[p][k], aqk = A[q][k];
+                    A[p][k] = c * apk - s * aqk;
+                    A[q][k] = s * apk + c * aqk;
+                }
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    float vkp = V[k][p], vkq = V[k][q];
+                    V[k][p] = c * vkp - s * vkq;
+                    V[k][q] = s * vkp + c * vkq;
+                }
+            }
+    }
+}
+__global__ void affine_fwd(int n, const int* __restrict__ atoms, const float* __restrict__ ref,
+                           const float* __restrict__ pos, float* __restrict__ out, float* __restrict__ eig) {
+    for (int r = grid_stride_start(); r < n; r += grid_stride()) {
+        f3 x[3];
+        for (int a = 0; a < 3; ++a) x[a] = ld3(pos + 3 * size_t(atoms[3 * r + a]));
+        f3 c = (x[0] + x[1] + x[2]) * (1.f / 3.f);
+        for (int a = 0; a < 3; ++a) x[a] = x[a] - c;
+        const float* g = ref + 9 * size_t(r);
+        float R[3][3];
+        for (int i = 0; i < 3; ++i) {
+            R[i][0] = x[0].x * g[i] + x[1].x * g[3 + i] + x[2].x * g[6 + i];
+            R[i][1] = x[0].y * g[i] + x[1].y * g[3 + i] + x[2].y * g[6 + i];
+            R[i][2] = x[0].z * g[i] + x[1].z * g[3 + i] + x[2].z * g[6 + i];
+        }
+        float F[4][4];
+        F[0][0] = R[0][0] + R[1][1] + R[2][2];
+        F[0][1] = R[1][2] - R[2][1];
+        F[0][2] = R[2][0] - R[0][2];
+        F[0][3] = R[0][1] - R[1][0];
+        F[1][1] = R[0][0] - R[1][1] - R[2][2];
+        F[1][2] = R[0][1] + R[1][0];
+        F[1][3] = R[0][2] + R[2][0];
+        F[2][2] = -R[0][0] + R[1][1] - R[2][2];
+        F[2][3] = R[1][2] + R[2][1];
+        F[3][3] = -R[0][0] - R[1][1] + R[2][2];
+        F[1][0] = F[0][1]; F[2][0] = F[0][2]; F[3][0] = F[0][3];
+        F[2][1] = F[1][2]; F[3][1] = F[1][3]; F[3][2] = F[2][3];
+        float V[4][4];
+        jacobi4(F, V);
+        // sort eigenpairs by decreasing eigenvalue
+        int ord[4] = {0, 1, 2, 3};
+        for (int i = 0; i < 4; ++i)
+            for (int j = i + 1; j < 4; ++j)
+                if (F[ord[j]][ord[j]] > F[ord[i]][ord[i]]) { int t = ord[i]; ord[i] = ord[j]; ord[j] = t; }
+        float* E = eig + 20 * size_t(r);
+        for (int k = 0; k < 4; ++k) {
+            E[k] = F[ord[k]][ord[k]];
+            for (int i = 0; i < 4; ++i) E[4 + 4 * k + i] = V[i][ord[k]];
+        }
+        float* o = out + 7 * size_t(r);
+        o[0] = c.x; o[1] = c.y; o[2] = c.z;
+        for (int i = 0; i < 4; ++i) o[3 + i] = E[4 + i];
+    }
+}
+__global__ void affine_bwd(int n, const int* __restrict__ atoms, const float* __restrict__ ref,
+                           const float* __restrict__ eig, const float* __restrict__ sens, float* ps) {
+    for (int r = grid_stride_start(); r < n; r += grid_stride()) {
+        const float* s = sens + 7 * size_t(r);
+        const float* E = eig + 20 * size_t(r);
+        const float* q = E + 4;
+        float tx = s[3], ty = s[4], tz = s[5];
+        // torque -> gradient along the quaternion tangent
+        float qs[4] = {2.f * (-tx * q[1] - ty * q[2] - tz * q[3]), 2.f * (tx * q[0] + ty * q[3] - tz * q[2]),
+                       2.f * (ty * q[0] + tz * q[1] - tx * q[3]), 2.f * (tz * q[0] + tx * q[2] - ty * q[1])};
+        float proj[4] = {0, 0, 0, 0};
+        for (int k = 1; k < 4; ++k) {
+            const float* v = E + 4 + 4 * k;
+            proj[k] = (qs[0] * v[0] + qs[1] * v[1] + qs[2] * v[2] + qs[3] * v[3]) / (E[0] - E[k]);
+        }
+        // w[u][v] = sum_k proj_k (v_k[u] q[v] + v_k[v] q[u]) / 2 -> contraction with dF
+        float W[4][4];
+        for (int u = 0; u < 4; ++u)
+            for (int v = 0; v < 4; ++v) {
+                float acc = 0.f;
+                for (int k = 1; k < 4; ++k) acc += proj[k] * E[4 + 4 * k + u] * q[v];
+                W[u][v] = acc;
+            }
+        // dE/dR(i,j) = sum_uv W[u][v] dF[u][v]/dR(i,j)
+        float S[4][4];
+        for (int u = 0; u < 4; ++u)
+            for (int v = 0; v < 4; ++v) S[u][v] = W[u][v] + W[v][u];
+        float dR[3][3];
+        dR[0][0] = 0.5f * (S[0][0] + S[1][1] - S[2][2] - S[3][3]);
+        dR[1][1] = 0.5f * (S[0][0] - S[1][1] + S[2][2] - S[3][3]);
+        dR[2][2] = 0.5f * (S[0][0] - S[1][1] - S[2][2] + S[3][3]);
+        dR[1][2] = S[0][1] + S[2][3];
+        dR[2][1] = -S[0][1] + S[2][3];
+        dR[2][0] = S[0][2] + S[1][3];
+        dR[0][2] = -S[0][2] + S[1][3];
+        dR[0][1] = S[0][3] + S[1][2];
+        dR[1][0] = -S[0][3] + S[1][2];
+        const float* g = ref + 9 * size_t(r);
+        for (int a = 0; a < 3; ++a) {
+            f3 d = mk(s[0], s[1], s[2]) * (1.f / 3.f);
+            d.x += dR[0][0] * g[3 * a] + dR[1][0] * g[3 * a + 1] + dR[2][0] * g[3 * a + 2];
+            d.y += dR[0][1] * g[3 * a] + dR[1][1] * g[3 * a + 1] + dR[2][1] * g[3 * a + 2];
+            d.z += dR[0][2] * g[3 * a] + dR[1][2] * g[3 * a + 1] + dR[2][2] * g[3 * a + 2];
+            atomic_add3(ps + 3 * size_t(atoms[3 * r + a]), d);
+        }
+    }
+}
+struct AffineNode : GNode {
+    int* atoms = nullptr;
+    float *ref = nullptr, *eig = nullptr;
+    AffineNode(Engine& e, const Groups& g, const std::vector<int>& o) {
+        auto c = counts(g, "atoms");
+        off = offsets(c);
+        total = off.back();
+        width = 7;
+        atoms = e.upload(cat_idx(g, "atoms", &o));
+        ref = e.upload(cat_f(g, "ref_geom"));
+        eig = e.alloc<float>(size_t(total) * 20);
+    }
+    void forward(Engine& e, bool) override {
+        affine_fwd<<<nblk(total, 128), 128, 0, e.st>>>(total, atoms, ref, e.arg(*this, 0).out, out, eig);
+    }
+    void backward(Engine& e) override {
+        affine_bwd<<<nblk(total, 128), 128, 0, e.st>>>(total, atoms, ref, eig, sens, e.arg(*this, 0).sens);
+    }
+};
+
+// ========================================================== placement ===
+// rigid-body placement of points / vectors / scalars
+// (PlacementNode src/placement.cpp:233-314, FixedPlacement :102-167, RamaPlacement :20-99)
+// sig bits: per 3-block 'P'=point, 'V'=vector; trailing scalar when has_scalar
+template <int NB, bool SCALAR>
+__global__ void place_fixed_fwd(int n, const int* __restrict__ aff, const int* __restrict__ layer, const float* __restrict__ data,
+                                const float* __restrict__ af, float* __restrict__ out) {
+    constexpr int W = 3 * NB + (SCALAR ? 1 : 0);
+    for (int i = grid_stride_start(); i < n; i += grid_stride()) {
+        const float* a = af + 7 * size_t(aff[i]);
+        float U[9];
+        quat_to_rot(a + 3, U);
+        const float* v = data + size_t(layer[i]) * W;
+        float* o = out + size_t(i) * W;
+        f3 p = rot(U, ld3(v)) + mk(a[0], a[1], a[2]);
+        st3(o, p);
+        if (NB > 1) st3(o + 3, rot(U, ld3(v + 3)));
+        if (SCALAR) o[W - 1] = v[W - 1];
+    }
+}
+template <int NB, bool SCALAR>
+__global__ void place_fixed_bwd(int n, const int* __restrict__ aff, const float* __restrict__ af, const float* __restrict__ out,
+                                const float* __restrict__ sens, float* as) {
+    constexpr int W = 3 * NB + (SCALAR ? 1 : 0);
+    for (int i = grid_stride_start(); i < n; i += grid_stride()) {
+        const float* a = af + 7 * size_t(aff[i]);
+        f3 t = mk(a[0], a[1], a[2]);
+        const float* s = sens + size_t(i) * W;
+        const float* o = out + size_t(i) * W;
+        f3 sp = ld3(s);
+        f3 torque = cross(ld3(o) - t, sp);
+        if (NB > 1) torque += cross(ld3(o + 3), ld3(s + 3));
+        float* d = as + 7 * size_t(aff[i]);
+        atomic_add3(d, sp);
+        atomic_add3(d + 3, torque);
+    }
+}
+__global__ void place_rama_fwd(int n, const int* __restrict__ rres, const int* __restrict__ layer, const float* __restrict__ coeff,
+                               int nxp, int nyp, float sx, float sy, const float* __restrict__ rama, float* __restrict__ out,
+                               float* __restrict__ der) {
+    for (int i = grid_stride_start(); i < n; i += grid_stride()) {
+        const float* r = rama + 2 * size_t(rres[i]);
+        float v, dx, dy;
+        periodic2d(coeff + size_t(layer[i]) * nxp * nyp, nyp, (r[0] + 3.14159265358979f) * sx,
+                   (r[1] + 3.14159265358979f) * sy, v, dx, dy);
+        out[i] = v;
+        der[2 * size_t(i)] = dx;
+        der[2 * size_t(i) + 1] = dy;
+    }
+}
+__global__ void place_rama_bwd(int n, const int* __restrict__ rres, float sx, float sy, const float* __restrict__ der,
+                               const float* __restrict__ sens, float* rs) {
+    for (int i = grid_stride_start(); i < n; i += grid_stride()) {
+        float s = sens[i];
+        atomicAdd(rs + 2 * size_t(rres[i]), sx * s * der[2 * size_t(i)]);
+        atomicAdd(rs + 2 * size_t(rres[i]) + 1, sy * s * der[2 * size_t(i) + 1]);
+    }
+}
+struct PlacementNode : GNode {
+    int nb = 0;
+    bool scalar = false, rama = false;
+    int *aff = nullptr, *layer = nullptr, *rres = nullptr;
+    float *data = nullptr, *der = nullptr;
+    int nxp = 0, nyp = 0;
+    float sx = 0, sy = 0;
+    PlacementNode(Engine& e, const Groups& g, int nb_, bool scalar_, bool rama_, const std::vector<int>& oaff,
+                  const std::vector<int>* orama)
+        : nb(nb_), scalar(scalar_), rama(rama_) {
+        auto c = counts(g, "layer_index");
+        off = offsets(c);
+        total = off.back();
+        width = 3 * nb + (scalar ? 1 : 0);
+        aff = e.upload(cat_idx(g, "affine_residue", &oaff));
+        if (rama) {
+            LayerPool pool;
+            std::vector<int> lay;
+            for (size_t s = 0; s < g.size(); ++s) {
+                auto d = g.f(s).dims(g.p("placement_data"));
+                if (d.size() != 4 || d[3] != 1) throw Error("only scalar Rama placement is supported");
+                if (s == 0) { pool.nx = int(d[1]); pool.ny = int(d[2]); }
+                auto data_s = g.f(s).read<double>(g.p("placement_data"));
+                std::vector<int> local(d[0]);
+                for (size_t l = 0; l < d[0]; ++l) local[l] = pool.add(data_s.data() + l * pool.nx * pool.ny);
+                for (int x : read_i(g.f(s), g.p("layer_index"))) lay.push_back(local.at(size_t(x)));
+            }
+            nxp = pool.nx + 3;
+            nyp = pool.ny + 3;
+            sx = float(pool.nx) * (0.5f / 3.14159265358979f - 1e-7f);
+            sy = float(pool.ny) * (0.5f / 3.14159265358979f - 1e-7f);
+            layer = e.upload(lay);
+            data = e.upload(pool.coeff);
+            rres = e.upload(cat_idx(g, "rama_residue", orama));
+            der = e.alloc<float>(size_t(total) * 2);
+        } else {
+            auto table = shared_f(g, "placement_data");
+            auto d = g.f(0).dims(g.p("placement_data"));
+            if (int(d.at(1)) != width) throw Error("placement_data width does not match the node type");
+            data = e.upload(table);
+            layer = e.upload(cat_idx(g, "layer_index", nullptr));
+        }
+    }
+    void forward(Engine& e, bool) override {
+        if (rama) {
+            place_rama_fwd<<<nblk(total), 256, 0, e.st>>>(total, rres, layer, data, nxp, nyp, sx, sy, e.arg(*this, 1).out, out, der);
+            return;
+        }
+        const float* af = e.arg(*this, 0).out;
+        if (nb == 2 && !scalar) place_fixed_fwd<2, false><<<nblk(total), 256, 0, e.st>>>(total, aff, layer, data, af, out);
+        else if (nb == 2 && scalar) place_fixed_fwd<2, true><<<nblk(total), 256, 0, e.st>>>(total, aff, layer, data, af, out);
+        else if (nb == 1 && !scalar) place_fixed_fwd<1, false><<<nblk(total), 256, 0, e.st>>>(total, aff, layer, data, af, out);
+        else throw Error("unsupported placement signature");
+    }
+    void backward(Engine& e) override {
+        if (rama) {
+            place_rama_bwd<<<nblk(total), 256, 0, e.st>>>(total, rres, sx, sy, der, sens, e.arg(*this, 1).sens);
+            return;
+        }
+        auto& a = e.arg(*this, 0);
+        if (nb == 2 && !scalar) place_fixed_bwd<2, false><<<nblk(total), 256, 0, e.st>>>(total, aff, a.out, out, sens, a.sens);
+        else if (nb == 2 && scalar) place_fixed_bwd<2, true><<<nblk(total), 256, 0, e.st>>>(total, aff, a.out, out, sens, a.sens);
+        else place_fixed_bwd<1, false><<<nblk(total), 256, 0, e.st>>>(total, aff, a.out, out, sens, a.sens);
+    }
+};
+
+// ======================================================= weighted_pos ===
+// (bead xyz, exp(-E_1body)) (WeightedPos, src/environment.cpp:489-533)
+__global__ void wpos_fwd(int n, const int* __restrict__ ip, const int* __restrict__ iw, const float* __restrict__ p, int wp,
+                         const float* __restrict__ en, int we, float* __restrict__ out) {
+    for (int i = grid_stride_start(); i < n; i += grid_stride()) {
+        const float* x = p + size_t(ip[i]) * wp;
+        out[4 * i] = x[0];
+        out[4 * i + 1] = x[1];
+        out[4 * i + 2] = x[2];
+        out[4 * i + 3] = expf(-en[size_t(iw[i]) * we]);
+    }
+}
+__global__ void wpos_bwd(int n, const int* __restrict__ ip, const int* __restrict__ iw, int wp, int we,
+                         const float* __restrict__ out, const float* __restrict__ sens, float* ps, float* es) {
+    for (int i = grid_stride_start(); i < n; i += grid_stride()) {
+        atomic_add3(ps + size_t(ip[i]) * wp, ld3(sens + 4 * i));
+        atomicAdd(es + size_t(iw[i]) * we, -out[4 * i + 3] * sens[4 * i + 3]);
+    }
+}
+struct WeightedPosNode : GNode {
+    int *ip = nullptr, *iw = nullptr;
+    WeightedPosNode(Engine& e, const Groups& g, const std::vector<int>& op, const std::vector<int>& ow) {
+        off = offsets(counts(g, "index_pos"));
+        total = off.back();
+        width = 4;
+        ip = e.upload(cat_idx(g, "index_pos", &op));
+        iw = e.upload(cat_idx(g, "index_weight", &ow));
+    }
+    void forward(Engine& e, bool) override {
+        auto &p = e.arg(*this, 0), &w = e.arg(*this, 1);
+        wpos_fwd<<<nblk(total), 256, 0, e.st>>>(total, ip, iw, p.out, p.width, w.out, w.width, out);
+    }
+    void backward(Engine& e) override {
+        auto &p = e.arg(*this, 0), &w = e.arg(*this, 1);
+        wpos_bwd<<<nblk(total), 256, 0, e.st>>>(total, ip, iw, p.width, w.width, out, sens, p.sens, w.sens);
+    }
+};
+
+// ========================================================== infer_H_O ===
+// virtual H / O positions and bond directions (Infer_H_O, src/hbond.cpp:20-127)
+__global__ void infer_fwd(int n, const int* __restrict__ id, const float* __restrict__ bl, const float* __restrict__ p,
+                          float* __restrict__ out, float* __restrict__ cache) {
+    for (int i = grid_stride_start(); i < n; i += grid_stride()) {
+        f3 pc = ld3(p + 3 * size_t(id[3 * i])), cc = ld3(p + 3 * size_t(id[3 * i + 1])), nc = ld3(p + 3 * size_t(id[3 * i + 2]));
+        f3 pv = pc - cc; float pi = rsqrtf(mag2(pv)); pv = pv * pi;
+        f3 nv = nc - cc; float ni = rsqrtf(mag2(nv)); nv = nv * ni;
+        f3 dv = pv + nv; float di = rsqrtf(mag2(dv)); dv = dv * di;
+        float* c = cache + 12 * size_t(i);
+        st3(c, pv); c[3] = pi; st3(c + 4, nv); c[7] = ni; st3(c + 8, dv); c[11] = di;
+        st3(out + 6 * size_t(i), cc + dv * (-bl[i]));
+        st3(out + 6 * size_t(i) + 3, -dv);
+    }
+}
+__global__ void infer_bwd(int n, const int* __restrict__ id, const float* __restrict__ bl, const float* __restrict__ cache,
+                          const float* __restrict__ sens, float* ps) {
+    for (int i = grid_stride_start(); i < n; i += grid_stride()) {
+        const float* s = sens + 6 * size_t(i);
+        const float* c = cache + 12 * size_t(i);
+        f3 sp = ld3(s), sd = ld3(s + 3);
+        f3 sneg = sd + sp * bl[i];
+        f3 pv = ld3(c), nv = ld3(c + 4), dv = ld3(c + 8);
+        f3 snd = (dv * dot(dv, sneg) - sneg) * c[11];
+        f3 snp = (pv * dot(pv, snd) - snd) * (-c[3]);
+        f3 snn = (nv * dot(nv, snd) - snd) * (-c[7]);
+        atomic_add3(ps + 3 * size_t(id[3 * i]), snp);
+        atomic_add3(ps + 3 * size_t(id[3 * i + 1]), sp - snp - snn);
+        atomic_add3(ps + 3 * size_t(id[3 * i + 2]), snn);
+    }
+}
+struct InferHONode : GNode {
+    int* id = nullptr;
+    float *bl = nullptr, *cache = nullptr;
+    std::vector<int> n_don;
+    InferHONode(Engine& e, const Groups& g, const std::vector<int>& o) {
+        auto cd = counts(g, "donors/id"), ca = counts(g, "acceptors/id");
+        std::vector<int> ids;
+        std::vector<float> b;
+        off.push_back(0);
+        for (size_t s = 0; s < g.size(); ++s) {
+            for (auto grp : {"donors", "acceptors"}) {
+                for (int x : read_i(g.f(s), g.p(std::string(grp) + "/id"))) ids.push_back(x + o[s]);
+                auto bb = read_f(g.f(s), g.p(std::string(grp) + "/bond_length"));
+                b.insert(b.end(), bb.begin(), bb.end());
+            }
+            n_don.push_back(cd[s]);
+            off.push_back(off.back() + cd[s] + ca[s]);
+        }
+        total = off.back();
+        width = 6;
+        id = e.upload(ids);
+        bl = e.upload(b);
+        cache = e.alloc<float>(size_t(total) * 12);
+    }
+    void forward(Engine& e, bool) override {
+        infer_fwd<<<nblk(total), 256, 0, e.st>>>(total, id, bl, e.arg(*this, 0).out, out, cache);
+    }
+    void backward(Engine& e) override {
+        infer_bwd<<<nblk(total), 256, 0, e.st>>>(total, id, bl, cache, sens, e.arg(*this, 0).sens);
+    }
+};
+
+// ================================================ interaction graphs ===
+// Host wrapper of one DGraph: set membership, pair-search rows, buffers.
+struct HGraph {
+    DGraph g{};
+    std::vector<int> sys_first_row;
+    int *d_sys_start = nullptr, *d_sys_end = nullptr;
+    int per_elem_cap = 64;
+    Engine* eng = nullptr;
+    int* edge_bufs_int = nullptr;
+    void* bufs[4] = {nullptr, nullptr, nullptr, nullptr};
+
+    ~HGraph() { release(); }
+    void release() {
+        for (auto& p : bufs) {
+            if (p) cudaFree(p);
+            p = nullptr;
+        }
+    }
+    void alloc_edges(int cap) {
+        release();
+        g.cap = cap;
+        size_t dw = size_t(g.d1 + g.d2);
+        UG_CK(cudaMalloc(&bufs[0], sizeof(int2) * size_t(cap)));
+        UG_CK(cudaMalloc(&bufs[1], sizeof(float) * size_t(cap)));
+        UG_CK(cudaMalloc(&bufs[2], sizeof(float) * size_t(cap) * dw));
+        UG_CK(cudaMalloc(&bufs[3], sizeof(float) * size_t(cap)));
+        g.edges = static_cast<int2*>(bufs[0]);
+        g.value = static_cast<float*>(bufs[1]);
+        g.deriv = static_cast<float*>(bufs[2]);
+        g.esens = static_cast<float*>(bufs[3]);
+        UG_CK(cudaMemsetAsync(g.esens, 0, sizeof(float) * size_t(cap), eng->st));
+    }
+    // kind, sets: per-system counts n1/n2 and global element lists
+    void setup(Engine& e, int kind, int excl, bool sym, int d1, int d2, int n_param, const Groups& grp,
+               const std::string& base, const std::vector<int>& o_in1, const std::vector<int>& o_in2, int cap_per_elem) {
+        eng = &e;
+        g.kind = kind;
+        g.excl = excl;
+        g.symmetric = sym;
+        g.d1 = d1;
+        g.d2 = d2;
+        g.n_param = n_param;
+        g.n_sys = e.n_sys;
+        g.status = e.d_status;
+        std::string sfx = sym ? "" : "1";
+        auto bp = [&](const std::string& n) { return (base.empty() ? "" : base + "/") + n; };
+        auto c1 = counts(grp, bp("index" + sfx));
+        auto c2 = sym ? c1 : counts(grp, bp("index2"));
+        auto of1 = offsets(c1), of2 = offsets(c2);
+        g.n1 = of1.back();
+        g.n2 = of2.back();
+        std::vector<int> type1, type2, id1, id2;
+        for (size_t s = 0; s < grp.size(); ++s) {
+            auto t1 = read_i(grp.f(s), grp.p(bp("type" + sfx)));
+            auto i1 = read_i(grp.f(s), grp.p(bp("id" + sfx)));
+            type1.insert(type1.end(), t1.begin(), t1.end());
+            id1.insert(id1.end(), i1.begin(), i1.end());
+            if (!sym) {
+                auto t2 = read_i(grp.f(s), grp.p(bp("type2")));
+                auto i2 = read_i(grp.f(s), grp.p(bp("id2")));
+                type2.insert(type2.end(), t2.begin(), t2.end());
+                id2.insert(id2.end(), i2.begin(), i2.end());
+            }
+        }
+        // parameters: one table for the batch
+        auto dm = grp.f(0).dims(grp.p(bp("interaction_param")));
+        if (dm.size() != 3 || int(dm[2]) != n_param) throw Error("interaction_param shape mismatch in " + grp.path);
+        g.n_type1 = int(dm[0]);
+        g.n_type2 = int(dm[1]);
+        param_host = shared_f(grp, bp("interaction_param"));
+        g.param = e.upload(param_host);
+        g.loc1 = e.upload(cat_idx(grp, bp("index" + sfx), &o_in1));
+        g.type1 = e.upload(type1);
+        g.id1 = e.upload(id1);
+        g.sys1 = e.upload(sys_of(of1));
+        if (sym) {
+            g.loc2 = g.loc1; g.type2 = g.type1; g.id2 = g.id1;
+        } else {
+            g.loc2 = e.upload(cat_idx(grp, bp("index2"), &o_in2));
+            g.type2 = e.upload(type2);
+            g.id2 = e.upload(id2);
+        }
+        // rows
+        std::vector<int> ri1, ri1e, ri2, ri2e;
+        for (size_t s = 0; s < grp.size(); ++s) {
+            sys_first_row.push_back(int(ri1.size()));
+            for (int b = 0; b < c1[s]; b += 4) {
+                ri1.push_back(of1[s] + b);
+                ri1e.push_back(of1[s] + c1[s]);
+                ri2.push_back(sym ? of1[s] + b + 1 : of2[s]);
+                ri2e.push_back(sym ? of1[s] + c1[s] : of2[s] + c2[s]);
+            }
+        }
+        sys_first_row.push_back(int(ri1.size()));
+        g.n_rows = int(ri1.size());
+        g.row_i1 = e.upload(ri1);
+        g.row_i1_end = e.upload(ri1e);
+        g.row_i2 = e.upload(ri2);
+        g.row_i2_end = e.upload(ri2e);
+        g.row_count = e.alloc<int>(size_t(g.n_rows) + 1);
+        g.row_off = e.alloc<int>(size_t(g.n_rows) + 1);
+        g.sys_first_row = e.upload(sys_first_row);
+        g.n_edge = e.alloc<int>(1);
+        g.x1 = e.alloc<float4>(size_t(g.n1));
+        g.x2 = sym ? g.x1 : e.alloc<float4>(size_t(g.n2));
+        d_sys_start = e.alloc<int>(size_t(e.n_sys));
+        d_sys_end = e.alloc<int>(size_t(e.n_sys));
+        long long full = sym ? (long long)g.n1 * (g.n1 - 1) / 2 : (long long)g.n1 * g.n2;
+        long long cap = std::min<long long>(std::max<long long>(full, 1), (long long)cap_per_elem * std::max(g.n1, 1) + 1024);
+        per_elem_cap = cap_per_elem;
+        alloc_edges(int(std::min<long long>(cap, 1LL << 30)));
+        update_cutoff();
+    }
+    std::vector<float> param_host;
+    void update_cutoff() {
+        float c = 0.f;
+        for (int a = 0; a < g.n_type1 * g.n_type2; ++a) {
+            const float* p = &param_host[size_t(a) * g.n_param];
+            float ci = 0.f;
+            switch (g.kind) {
+                case IK_ROTAMER: ci = float((12 - 2 - 1e-6) / double(1.f / 0.7f)); break;
+                case IK_HBCOV: ci = float((10 - 2 - 1e-6) / double(1.f / 0.625f)); break;
+                case IK_PHB: ci = sqrtf(3.5f * 3.5f); break;
+                case IK_ENVCOV:
+                case IK_HBENV: ci = p[0] + 1.f / p[1]; break;
+                default: break;
+            }
+            c = std::max(c, ci);
+        }
+        g.cutoff = c;
+    }
+    void set_param(const std::vector<float>& p) {
+        if (p.size() != param_host.size()) throw Error("Bad param size, got " + std::to_string(p.size()) +
+                                                       " params, but expected " + std::to_string(param_host.size()));
+        param_host = p;
+        UG_CK(cudaMemcpyAsync(const_cast<float*>(g.param), p.data(), p.size() * 4, cudaMemcpyHostToDevice, eng->st));
+        update_cutoff();
+    }
+    void bind(const GNode& n1, const GNode& n2) {
+        g.in1 = n1.out; g.in2 = n2.out; g.sens1 = n1.sens; g.sens2 = n2.sens;
+        g.w1 = n1.width; g.w2 = n2.width;
+    }
+    void search_and_eval(cudaStream_t st) {
+        launch_pairs(g, st);
+        launch_edge_eval(g, d_sys_start, d_sys_end, st);
+    }
+    bool grow_if_full() {
+        int ne = 0;
+        UG_CK(cudaMemcpy(&ne, g.n_edge, 4, cudaMemcpyDeviceToHost));
+        if (ne < g.cap) return false;
+        alloc_edges(int(std::min<long long>(2LL * g.cap, 1LL << 30)));
+        return true;
+    }
+    std::vector<float> count_edges_by_type() {
+        int ne = 0;
+        UG_CK(cudaMemcpy(&ne, g.n_edge, 4, cudaMemcpyDeviceToHost));
+        std::vector<int2> ed(static_cast<size_t>(ne));
+        if (ne) UG_CK(cudaMemcpy(ed.data(), g.edges, sizeof(int2) * size_t(ne), cudaMemcpyDeviceToHost));
+        std::vector<int> t1(size_t(g.n1)), t2(size_t(g.n2));
+        UG_CK(cudaMemcpy(t1.data(), g.type1, 4 * size_t(g.n1), cudaMemcpyDeviceToHost));
+        UG_CK(cudaMemcpy(t2.data(), g.type2, 4 * size_t(g.n2), cudaMemcpyDeviceToHost));
+        std::vector<float> r(size_t(g.n_type1 * g.n_type2), 0.f);
+        for (auto& x : ed) r[size_t(t1[size_t(x.x)] * g.n_type2 + t2[size_t(x.y)])] += 1.f;
+        return r;
+    }
+};
+
+// ====================================================== protein_hbond ===
+// hbond score per donor / acceptor in multiplicative space (ProteinHBond, src/hbond.cpp:357-435)
+__global__ void phb_init(int n, const int* __restrict__ src_row, const float* __restrict__ in, float* __restrict__ out) {
+    for (int i = grid_stride_start(); i < n; i += grid_stride()) {
+        const float* x = in + 6 * size_t(src_row[i]);
+        float* o = out + 7 * size_t(i);
+        for (int d = 0; d < 6; ++d) o[d] = x[d];
+        o[6] = 0.f;
+    }
+}
+__global__ void phb_accum(DGraph g, const int* __restrict__ row1, const int* __restrict__ row2, float* out) {
+    int ne = *g.n_edge;
+    for (int e = grid_stride_start(); e < ne; e += grid_stride()) {
+        int2 ij = g.edges[e];
+        float v = g.value[e];
+        atomicAdd(out + 7 * size_t(row1[ij.x]) + 6, v);
+        atomicAdd(out + 7 * size_t(row2[ij.y]) + 6, v);
+    }
+}
+__global__ void phb_final(int n, float* out) {
+    for (int i = grid_stride_start(); i < n; i += grid_stride()) out[7 * size_t(i) + 6] = 1.f - expf(-out[7 * size_t(i) + 6]);
+}
+__global__ void phb_esens(DGraph g, const int* __restrict__ row1, const int* __restrict__ row2, const float* __restrict__ out,
+                          const float* __restrict__ sens) {
+    int ne = *g.n_edge;
+    for (int e = grid_stride_start(); e < ne; e += grid_stride()) {
+        int2 ij = g.edges[e];
+        size_t a = 7 * size_t(row1[ij.x]) + 6, b = 7 * size_t(row2[ij.y]) + 6;
+        g.esens[e] = sens[a] * (1.f - out[a]) + sens[b] * (1.f - out[b]);
+    }
+}
+__global__ void phb_pass(int n, const int* __restrict__ src_row, const float* __restrict__ sens, float* in_sens) {
+    for (int i = grid_stride_start(); i < n; i += grid_stride()) {
+        const float* s = sens + 7 * size_t(i);
+        float* d = in_sens + 6 * size_t(src_row[i]);
+        for (int k = 0; k < 6; ++k) atomicAdd(d + k, s[k]);
+    }
+}
+struct ProteinHBondNode : GNode {
+    HGraph hg;
+    int *row1 = nullptr, *row2 = nullptr, *src = nullptr;
+    ProteinHBondNode(Engine& e, const Groups& g, const std::vector<int>& oin) {
+        auto c1 = counts(g, "index1"), c2 = counts(g, "index2");
+        std::vector<int> r1, r2, sr;
+        off.push_back(0);
+        for (size_t s = 0; s < g.size(); ++s) {
+            int base = off.back();
+            auto l1 = read_i(g.f(s), g.p("index1")), l2 = read_i(g.f(s), g.p("index2"));
+            for (int i = 0; i < c1[s]; ++i) { r1.push_back(base + i); sr.push_back(l1[size_t(i)] + oin[s]); }
+            for (int i = 0; i < c2[s]; ++i) { r2.push_back(base + c1[s] + i); sr.push_back(l2[size_t(i)] + oin[s]); }
+            off.push_back(base + c1[s] + c2[s]);
+        }
+        total = off.back();
+        width = 7;
+        hg.setup(e, IK_PHB, EX_SEQ1, false, 6, 6, 8, g, "", oin, oin, 8);
+        row1 = e.upload(r1);
+        row2 = e.upload(r2);
+        src = e.upload(sr);
+    }
+    void forward(Engine& e, bool) override {
+        auto& in = e.arg(*this, 0);
+        hg.bind(in, in);
+        phb_init<<<nblk(total), 256, 0, e.st>>>(total, src, in.out, out);
+        hg.search_and_eval(e.st);
+        phb_accum<<<nblk(hg.g.cap), 256, 0, e.st>>>(hg.g, row1, row2, out);
+        phb_final<<<nblk(total), 256, 0, e.st>>>(total, out);
+    }
+    void backward(Engine& e) override {
+        auto& in = e.arg(*this, 0);
+        phb_esens<<<nblk(hg.g.cap), 256, 0, e.st>>>(hg.g, row1, row2, out, sens);
+        launch_edge_scatter(hg.g, e.st);
+        phb_pass<<<nblk(total), 256, 0, e.st>>>(total, src, sens, in.sens);
+    }
+    DGraph* graph() override { return &hg.g; }
+    bool grow(Engine&) override { return hg.grow_if_full(); }
+    std::vector<float> value_by_name(Engine& e, const std::string& w) override {
+        if (w == "count_edges_by_type") return hg.count_edges_by_type();
+        return GNode::value_by_name(e, w);
+    }
+};
+
+// ======================================================= hbond_energy ===
+// helix/sheet/turn hbond energies (HBondEnergy, src/hbond.cpp:487-739)
+__global__ void hbe_kernel(int n, const float* __restrict__ prm, const int* __restrict__ rama_row,
+                           const int* __restrict__ don_row, const int* __restrict__ acc_row,
+                           const int* __restrict__ next_don_row, const int* __restrict__ sys, const float* __restrict__ pp,
+                           float* ps, const float* __restrict__ ra, float* rs, double* pot) {
+    for (int i = grid_stride_start(); i < n; i += grid_stride()) {
+        float phi = ra[2 * size_t(rama_row[i])], psi = ra[2 * size_t(rama_row[i]) + 1];
+        float p1v, p1d, p2v, p2d, s1v, s1d, s2v, s2d;
+        csig(phi - prm[4], prm[5], p1v, p1d);
+        csig(phi - prm[6], prm[7], p2v, p2d);
+        csig(psi - prm[8], prm[9], s1v, s1d);
+        csig(psi - prm[10], prm[11], s2v, s2d);
+        float turn = (1.f - p1v) * p2v, psis = (1.f - s1v) * s2v;
+        float nturn = 1.f - turn, npsi = 1.f - psis;
+        float dturn = p2d - (p1d * p2v + p1v * p2d);
+        float dpsis = s2d - (s1d * s2v + s1v * s2d);
+        float E = prm[0] * nturn * psis + prm[1] * nturn * npsi + prm[2] * turn;
+        float dphi = prm[0] * (-dturn * psis) + prm[1] * (-dturn * npsi) + prm[2] * dturn;
+        float dpsi = prm[0] * (nturn * dpsis) + prm[1] * (nturn * -dpsis);
+        int dr = don_row[i], ar = acc_row[i];
+        float hb1 = (dr >= 0 ? pp[7 * size_t(dr) + 6] : 0.f) + (ar >= 0 ? pp[7 * size_t(ar) + 6] : 0.f);
+        float en = 0.f;
+        if (hb1 != 0.f) {
+            en += hb1 * E;
+            if (dr >= 0) atomicAdd(ps + 7 * size_t(dr) + 6, E);
+            if (ar >= 0) atomicAdd(ps + 7 * size_t(ar) + 6, E);
+            atomicAdd(rs + 2 * size_t(rama_row[i]), hb1 * dphi);
+            atomicAdd(rs + 2 * size_t(rama_row[i]) + 1, hb1 * dpsi);
+        }
+        // peptide i (between residue i and i+1): donor of i+1 plus acceptor of i
+        int nd = next_don_row[i];
+        if (nd != -2) {
+            float hb2 = (nd >= 0 ? pp[7 * size_t(nd) + 6] : 0.f) + (ar >= 0 ? pp[7 * size_t(ar) + 6] : 0.f);
+            if (hb2 > 1.f) {
+                float v, d;
+                csig(1.5f - hb2, 2.f, v, d);
+                en += v * prm[3];
+                float dE = -d * prm[3];
+                if (nd >= 0) atomicAdd(ps + 7 * size_t(nd) + 6, dE);
+                if (ar >= 0) atomicAdd(ps + 7 * size_t(ar) + 6, dE);
+            }
+        }
+        add_energy(pot, sys[i], en);
+    }
+}
+struct HBondEnergyNode : GNode {
+    float* prm = nullptr;
+    int *rama_row = nullptr, *don_row = nullptr, *acc_row = nullptr, *next_don = nullptr, *sysv = nullptr;
+    int n = 0;
+    HBondEnergyNode(Engine& e, const Groups& g, const GNode& phb, const std::vector<int>& orama) {
+        potential = true;
+        prm = e.upload(shared_f(g, "parameters"));
+        std::vector<int> rr, dr, ar, nd, sy;
+        for (size_t s = 0; s < g.size(); ++s) {
+            int nres = int(g.f(s).dims(g.p("rama_resid")).at(0));
+            auto d = read_i(g.f(s), g.p("donor_resid")), a = read_i(g.f(s), g.p("acceptor_resid"));
+            std::vector<int> drow(size_t(nres), -1), arow(size_t(nres), -1);
+            int base = phb.off[s];
+            for (size_t k = 0; k < d.size(); ++k) if (drow[size_t(d[k])] < 0) drow[size_t(d[k])] = base + int(k);
+            for (size_t k = 0; k < a.size(); ++k) if (arow[size_t(a[k])] < 0) arow[size_t(a[k])] = base + int(d.size() + k);
+            for (int i = 0; i < nres; ++i) {
+                rr.push_back(orama[s] + i);
+                dr.push_back(drow[size_t(i)]);
+                ar.push_back(arow[size_t(i)]);
+                nd.push_back(i < nres - 1 ? drow[size_t(i + 1)] : -2);
+                sy.push_back(int(s));
+            }
+        }
+        n = int(rr.size());
+        rama_row = e.upload(rr);
+        don_row = e.upload(dr);
+        acc_row = e.upload(ar);
+        next_don = e.upload(nd);
+        sysv = e.upload(sy);
+    }
+    void forward(Engine& e, bool energy) override {
+        auto &pp = e.arg(*this, 0), &ra = e.arg(*this, 1);
+        hbe_kernel<<<nblk(n), 256, 0, e.st>>>(n, prm, rama_row, don_row, acc_row, next_don, sysv, pp.out, pp.sens, ra.out,
+                                              ra.sens, energy ? e.d_pot + size_t(pot_slot) * e.n_sys : nullptr);
+    }
+};
+
+// ===================================================== hbond_coverage ===
+// coverage of side-chain beads by backbone H/O or hydrophobe points
+// (HBondCoverage, src/hbond.cpp:438-484)
+__global__ void zero_kernel(float* p, int n) {
+    for (int i = grid_stride_start(); i < n; i += grid_stride()) p[i] = 0.f;
+}
+__global__ void cov_accum(DGraph g, float* out, int by_first, int n_aa, const int* __restrict__ aa2) {
+    int ne = *g.n_edge;
+    for (int e = grid_stride_start(); e < ne; e += grid_stride()) {
+        int2 ij = g.edges[e];
+        int row = by_first ? (aa2 ? ij.x * n_aa + aa2[ij.y] : ij.x) : ij.y;
+        atomicAdd(out + row, g.value[e]);
+    }
+}
+__global__ void cov_esens(DGraph g, const float* __restrict__ sens, int by_first, int n_aa, const int* __restrict__ aa2) {
+    int ne = *g.n_edge;
+    for (int e = grid_stride_start(); e < ne; e += grid_stride()) {
+        int2 ij = g.edges[e];
+        int row = by_first ? (aa2 ? ij.x * n_aa + aa2[ij.y] : ij.x) : ij.y;
+        g.esens[e] = sens[row];
+    }
+}
+// one node class for hbond_coverage (rows = set 2), environment_coverage
+// (rows = set-1 element x amino-acid type of the bead's residue) and
+// hb_environment_coverage (rows = set 1)
+struct CoverageNode : GNode {
+    HGraph hg;
+    int by_first = 0, n_aa = 0;
+    int* aa2 = nullptr;
+    CoverageNode(Engine& e, const Groups& g, int kind, const std::vector<int>& o1, const std::vector<int>& o2) {
+        auto c1 = counts(g, "index1"), c2 = counts(g, "index2");
+        if (kind == IK_HBCOV) {
+            off = offsets(c2);
+            hg.setup(e, IK_HBCOV, EX_SEQ2, false, 7, 6, 50, g, "", o1, o2, 64);
+        } else if (kind == IK_ENVCOV) {
+            by_first = 1;
+            n_aa = int(shared_attr(g, "num_aa_types"));
+            std::vector<int> c1a(c1);
+            for (auto& x : c1a) x *= n_aa;
+            off = offsets(c1a);
+            hg.setup(e, IK_ENVCOV, EX_SEQ2, false, 6, 4, 4, g, "", o1, o2, 192);
+            // amino-acid type of each set-2 element (aa_types indexed by id2)
+            std::vector<int> a2;
+            for (size_t s = 0; s < g.size(); ++s) {
+                auto aa = read_i(g.f(s), g.p("aa_types"));
+                for (int id : read_i(g.f(s), g.p("id2"))) {
+                    if (id < 0 || size_t(id) >= aa.size()) throw Error("environment_coverage id2 out of range of aa_types");
+                    a2.push_back(aa[size_t(id)]);
+                }
+            }
+            aa2 = e.upload(a2);
+        } else {
+            by_first = 1;
+            off = offsets(c1);
+            hg.setup(e, IK_HBENV, EX_SEQ2, false, 6, 6, 4, g, "", o1, o2, 24);
+        }
+        total = off.back();
+        width = 1;
+    }
+    void forward(Engine& e, bool) override {
+        hg.bind(e.arg(*this, 0), e.arg(*this, 1));
+        hg.search_and_eval(e.st);
+        zero_kernel<<<nblk(total), 256, 0, e.st>>>(out, total);
+        cov_accum<<<nblk(hg.g.cap), 256, 0, e.st>>>(hg.g, out, by_first, n_aa, aa2);
+    }
+    void backward(Engine& e) override {
+        cov_esens<<<nblk(hg.g.cap), 256, 0, e.st>>>(hg.g, sens, by_first, n_aa, aa2);
+        launch_edge_scatter(hg.g, e.st);
+    }
+    std::vector<float> get_param(Engine&) override { return hg.param_host; }
+    void set_param(Engine&, const std::vector<float>& p) override { hg.set_param(p); }
+    std::vector<float> param_deriv(Engine& e) override {
+        size_t n = hg.param_host.size();
+        std::vector<float> r(n, 0.f);
+        if (hg.g.kind != IK_HBCOV) return r;  // environment coverage: not implemented in the reference either
+        float* d = nullptr;
+        UG_CK(cudaMalloc(&d, n * 4));
+        UG_CK(cudaMemsetAsync(d, 0, n * 4, e.st));
+        launch_param_deriv(hg.g, d, e.st);
+        UG_CK(cudaMemcpyAsync(r.data(), d, n * 4, cudaMemcpyDeviceToHost, e.st));
+        UG_CK(cudaStreamSynchronize(e.st));
+        cudaFree(d);
+        return r;
+    }
+    DGraph* graph() override { return &hg.g; }
+    bool grow(Engine&) override { return hg.grow_if_full(); }
+    std::vector<float> value_by_name(Engine& e, const std::string& w) override {
+        if (w == "count_edges_by_type") return hg.count_edges_by_type();
+        return GNode::value_by_name(e, w);
+    }
+};
+
+// ===================================================== couplings ===
+// sigmoid_coupling (src/environment.cpp:851-1003), nonlinear_coupling (:701-849),
+// bb_sigmoid_coupling (:1054-1138)
+__global__ void sig_coupling_kernel(int n, int n_rt, const int* __restrict__ ctype, const int* __restrict__ sys,
+                                    const float* __restrict__ w, const float* __restrict__ scale,
+                                    const float* __restrict__ center, const float* __restrict__ sharp,
+                                    const float* __restrict__ in, float* is, double* pot) {
+    for (int r = grid_stride_start(); r < n; r += grid_stride()) {
+        int c = ctype[r];
+        const float* wr = w + size_t(c) * n_rt;
+        const float* x = in + size_t(r) * n_rt;
+        float wn = 0.f;
+        for (int a = 0; a < n_rt; ++a) wn += wr[a] * x[a];
+        float v, d;
+        csig(wn - center[c], sharp[c], v, d);
+        add_energy(pot, sys[r], scale[c] * v);
+        for (int a = 0; a < n_rt; ++a) atomicAdd(is + size_t(r) * n_rt + a, wr[a] * scale[c] * d);
+    }
+}
+__global__ void nl_coupling_kernel(int n, int n_rt, int n_coeff, float offset, float inv_dx, const int* __restrict__ ctype,
+                                   const int* __restrict__ sys, const float* __restrict__ w, const float* __restrict__ coeff,
+                                   const float* __restrict__ in, float* is, double* pot) {
+    for (int r = grid_stride_start(); r < n; r += grid_stride()) {
+        int c = ctype[r];
+        const float* wr = w + size_t(c) * n_rt;
+        const float* x = in + size_t(r) * n_rt;
+        float wn = 0.f;
+        for (int a = 0; a < n_rt; ++a) wn += wr[a] * x[a];
+        float v, d;
+        clamped(coeff + size_t(c) * n_coeff, (wn - offset) * inv_dx, n_coeff, v, d);
+        add_energy(pot, sys[r], v);
+        // the reference assigns (not accumulates) this sensitivity
+        for (int a = 0; a < n_rt; ++a) is[size_t(r) * n_rt + a] = wr[a] * inv_dx * d;
+    }
+}
+__global__ void nl_param_deriv_kernel(int n, int n_rt, int n_coeff, int n_indep, float offset, float inv_dx,
+                                      const int* __restrict__ ctype, const float* __restrict__ w,
+                                      const float* __restrict__ coeff, const float* __restrict__ in, float* out) {
+    for (int r = grid_stride_start(); r < n; r += grid_stride()) {
+        int c = ctype[r];
+        const float* wr = w + size_t(c) * n_rt;
+        const float* x = in + size_t(r) * n_rt;
+        float wn = 0.f;
+        for (int a = 0; a < n_rt; ++a) wn += wr[a] * x[a];
+        float xc = (wn - offset) * inv_dx, res[4];
+        int sb = clamped_coeff_deriv(xc, n_coeff, res);
+        for (int i = 0; i < 4; ++i) atomicAdd(out + size_t(c) * n_coeff + sb + i, res[i]);
+        if (n_indep > 1) {
+            float v, d;
+            clamped(coeff + size_t(c) * n_coeff, xc, n_coeff, v, d);
+            float sn = inv_dx * d;
+            float* wd = out + size_t(n_rt) * n_coeff;
+            for (int a = 0; a < n_rt; ++a) {
+                float da = sn * x[a];
+                if (n_indep == 400) atomicAdd(wd + size_t(c) * n_rt + a, da);
+                else
+                    for (int a2 = 0; a2 < n_rt; ++a2) atomicAdd(wd + size_t(a2) * n_rt + a, da);
+            }
+        }
+    }
+}
+__global__ void bb_coupling_kernel(int n, int n_rt, float scale, float center, float sharp, float hbw,
+                                   const int* __restrict__ sys, const float* __restrict__ w, const float* __restrict__ sc,
+                                   const float* __restrict__ hb, float* scs, float* hbs, double* pot) {
+    for (int r = grid_stride_start(); r < n; r += grid_stride()) {
+        const float* x = sc + size_t(r) * n_rt;
+        float bl = 0.f;
+        for (int a = 0; a < n_rt; ++a) bl += w[a] * x[a];
+        bl += hbw * hb[r];
+        float v, d;
+        csig(bl - center, sharp, v, d);
+        add_energy(pot, sys[r], scale * v);
+        float dp = scale * d;
+        for (int a = 0; a < n_rt; ++a) atomicAdd(scs + size_t(r) * n_rt + a, w[a] * dp);
+        atomicAdd(hbs + r, hbw * dp);
+    }
+}
+struct CouplingNode : GNode {
+    enum Kind { SIGMOID, NONLINEAR, BB } kind;
+    int n = 0, n_rt = 0, n_coeff = 0, n_indep = 0;
+    int *ctype = nullptr, *sysv = nullptr;
+    float *w = nullptr, *scale = nullptr, *center = nullptr, *sharp = nullptr, *coeff = nullptr;
+    std::vector<float> h_w, h_a, h_b, h_c, h_coeff;
+    float offset = 0, inv_dx = 0, s_scale = 0, s_center = 0, s_sharp = 0, s_hbw = 0;
+    CouplingNode(Engine& e, const Groups& g, Kind k, const GNode& in) : kind(k) {
+        potential = true;
+        h_w = shared_f(g, "weights");
+        if (k == BB) {
+            n_rt = int(shared_attr(g, "num_aa_types"));
+            s_scale = float(shared_attr(g, "scale"));
+            s_center = float(shared_attr(g, "center"));
+            s_sharp = float(shared_attr(g, "sharpness"));
+            s_hbw = float(shared_attr(g, "hbond_weight"));
+            n = in.total / n_rt;
+            std::vector<int> sy;
+            for (size_t s = 0; s < g.size(); ++s)
+                for (int i = in.off[s] / n_rt; i < in.off[s + 1] / n_rt; ++i) sy.push_back(int(s));
+            sysv = e.upload(sy);
+        } else {
+            auto ct = cat_idx(g, "coupling_types", nullptr);
+            n = int(ct.size());
+            ctype = e.upload(ct);
+            sysv = e.upload(sys_of(offsets(counts(g, "coupling_types"))));
+            n_indep = int(shared_attr(g, "number_independent_weights"));
+            if (k == SIGMOID) {
+                h_a = shared_f(g, "scale");
+                h_b = shared_f(g, "center");
+                h_c = shared_f(g, "sharpness");
+                n_rt = int(h_a.size());
+                scale = e.upload(h_a);
+                center = e.upload(h_b);
+                sharp = e.upload(h_c);
+            } else {
+                h_coeff = shared_f(g, "coeff");
+                auto d = g.f(0).dims(g.p("coeff"));
+                n_rt = int(d[0]);
+                n_coeff = int(d[1]);
+                offset = float(shared_attr(g, "spline_offset", NAN, "coeff"));
+                inv_dx = float(shared_attr(g, "spline_inv_dx", NAN, "coeff"));
+                coeff = e.upload(h_coeff);
+            }
+            if (in.total != n * n_rt) throw Error("coupling input size does not match coupling_types");
+        }
+        w = e.upload(h_w);
+    }
+    void forward(Engine& e, bool energy) override {
+        double* pot = energy ? e.d_pot + size_t(pot_slot) * e.n_sys : nullptr;
+        auto& a = e.arg(*this, 0);
+        if (kind == SIGMOID)
+            sig_coupling_kernel<<<nblk(n), 256, 0, e.st>>>(n, n_rt, ctype, sysv, w, scale, center, sharp, a.out, a.sens, pot);
+        else if (kind == NONLINEAR)
+            nl_coupling_kernel<<<nblk(n), 256, 0, e.st>>>(n, n_rt, n_coeff, offset, inv_dx, ctype, sysv, w, coeff, a.out,
+                                                          a.sens, pot);
+        else {
+            auto& b = e.arg(*this, 1);
+            bb_coupling_kernel<<<nblk(n), 256, 0, e.st>>>(n, n_rt, s_scale, s_center, s_sharp, s_hbw, sysv, w, a.out, b.out,
+                                                          a.sens, b.sens, pot);
+        }
+    }
+    std::vector<float> get_param(Engine&) override {
+        std::vector<float> p;
+        if (kind == SIGMOID) {
+            p = h_a;
+            p.insert(p.end(), h_b.begin(), h_b.end());
+            p.insert(p.end(), h_c.begin(), h_c.end());
+        } else if (kind == NONLINEAR) {
+            p = h_coeff;
+        } else {
+            return {s_scale, s_center, s_sharp, s_hbw};
+        }
+        p.insert(p.end(), h_w.begin(), h_w.end());
+        return p;
+    }
+    void set_param(Engine& e, const std::vector<float>& p) override {
+        if (kind == BB) {
+            if (p.size() < 4) throw Error("bb_sigmoid_coupling takes 4 parameters");
+            s_scale = p[0]; s_center = p[1]; s_sharp = p[2]; s_hbw = p[3];
+            return;
+        }
+        size_t head = kind == SIGMOID ? 3 * size_t(n_rt) : h_coeff.size();
+        if (p.size() != head + h_w.size()) throw Error("the size of parameters should be " + std::to_string(head + h_w.size()));
+        if (kind == SIGMOID) {
+            h_a.assign(p.begin(), p.begin() + n_rt);
+            h_b.assign(p.begin() + n_rt, p.begin() + 2 * n_rt);
+            h_c.assign(p.begin() + 2 * n_rt, p.begin() + 3 * n_rt);
+            UG_CK(cudaMemcpyAsync(scale, h_a.data(), 4 * size_t(n_rt), cudaMemcpyHostToDevice, e.st));
+            UG_CK(cudaMemcpyAsync(center, h_b.data(), 4 * size_t(n_rt), cudaMemcpyHostToDevice, e.st));
+            UG_CK(cudaMemcpyAsync(sharp, h_c.data(), 4 * size_t(n_rt), cudaMemcpyHostToDevice, e.st));
+        } else {
+            h_coeff.assign(p.begin(), p.begin() + long(head));
+            UG_CK(cudaMemcpyAsync(coeff, h_coeff.data(), 4 * head, cudaMemcpyHostToDevice, e.st));
+        }
+        h_w.assign(p.begin() + long(head), p.end());
+        UG_CK(cudaMemcpyAsync(w, h_w.data(), 4 * h_w.size(), cudaMemcpyHostToDevice, e.st));
+        UG_CK(cudaStreamSynchronize(e.st));
+    }
+    std::vector<float> param_deriv(Engine& e) override {
+        if (kind != NONLINEAR) return std::vector<float>(get_param(e).size(), 0.f);
+        size_t np = h_coeff.size() + h_w.size();
+        std::vector<float> r(np, 0.f);
+        float* d = nullptr;
+        UG_CK(cudaMalloc(&d, np * 4));
+        UG_CK(cudaMemsetAsync(d, 0, np * 4, e.st));
+        nl_param_deriv_kernel<<<nblk(n), 256, 0, e.st>>>(n, n_rt, n_coeff, n_indep, offset, inv_dx, ctype, w, coeff,
+                                                         e.arg(*this, 0).out, d);
+        UG_CK(cudaMemcpyAsync(r.data(), d, np * 4, cudaMemcpyDeviceToHost, e.st));
+        UG_CK(cudaStreamSynchronize(e.st));
+        cudaFree(d);
+        if (n_indep == 1) std::fill(r.begin() + long(h_coeff.size()), r.end(), 0.f);
+        return r;
+    }
+};
+
+// ===================================================== backbone_pairs ===
+// rigid-body backbone steric repulsion (BackbonePairs, src/backbone_steric.cpp:38-147)
+__global__ void bb_pairs_kernel(DGraph g, const int* __restrict__ res_row, const int* __restrict__ nat,
+                                const float* __restrict__ refp, const int* __restrict__ sys, const float* __restrict__ af,
+                                float* as, double* pot) {
+    int ne = *g.n_edge;
+    const float c2 = 3.f * 3.f + 0.1f * 3.f;
+    const float sharp = 1.f / (3.0f * 0.10f);
+    for (int e = grid_stride_start(); e < ne; e += grid_stride()) {
+        int2 ij = g.edges[e];
+        int ra = res_row[ij.x], rb = res_row[ij.y];
+        const float* A = af + 7 * size_t(ra);
+        const float* B = af + 7 * size_t(rb);
+        float Ua[9], Ub[9];
+        quat_to_rot(A + 3, Ua);
+        quat_to_rot(B + 3, Ub);
+        f3 ta = mk(A[0], A[1], A[2]), tb = mk(B[0], B[1], B[2]);
+        int na = nat[ij.x], nb = nat[ij.y];
+        f3 xa[4], xb[4];
+        for (int k = 0; k < na; ++k) xa[k] = rot(Ua, ld3(refp + 12 * size_t(ij.x) + 3 * k)) + ta;
+        for (int k = 0; k < nb; ++k) xb[k] = rot(Ub, ld3(refp + 12 * size_t(ij.y) + 3 * k)) + tb;
+        f3 da = mk(0, 0, 0), db = mk(0, 0, 0), qa = mk(0, 0, 0), qb = mk(0, 0, 0);
+        float en = 0.f;
+        bool hit = false;
+        for (int i = 0; i < na; ++i)
+            for (int j = 0; j < nb; ++j) {
+                f3 r = xa[i] - xb[j];
+                float m2 = mag2(r);
+                if (m2 > c2) continue;
+                hit = true;
+                float v, d;
+                csig(m2 - 9.f, sharp, v, d);
+                en += 4.f * v;
+                f3 gg = r * (2.f * 4.f * d);
+                da += gg;
+                qa += cross(xa[i] - ta, gg);
+                db += -gg;
+                qb += cross(xb[j] - tb, -gg);
+            }
+        if (hit) {
+            atomic_add3(as + 7 * size_t(ra), da);
+            atomic_add3(as + 7 * size_t(ra) + 3, qa);
+            atomic_add3(as + 7 * size_t(rb), db);
+            atomic_add3(as + 7 * size_t(rb) + 3, qb);
+            add_energy(pot, sys[ij.x], en);
+        }
+    }
+}
+struct BackbonePairsNode : GNode {
+    HGraph hg;
+    int *res_row = nullptr, *nat = nullptr;
+    float* refp = nullptr;
+    BackbonePairsNode(Engine& e, const Groups& g, const std::vector<int>& oaff) {
+        potential = true;
+        // residues are the set of a symmetric graph on the frame centres
+        hg.eng = &e;
+        DGraph& d = hg.g;
+        d.kind = IK_BACKBONE; d.excl = EX_SEQ1; d.symmetric = 1; d.d1 = 0; d.d2 = 0; d.n_param = 1;
+        d.n_type1 = d.n_type2 = 1;
+        d.n_sys = e.n_sys;
+        d.status = e.d_status;
+        auto c = counts(g, "id");
+        auto of = offsets(c);
+        d.n1 = d.n2 = of.back();
+        std::vector<int> rr, ids, na, zeros(size_t(d.n1), 0);
+        std::vector<float> rp;
+        float max_dev = 0.f;
+        for (size_t s = 0; s < g.size(); ++s) {
+            auto id = read_i(g.f(s), g.p("id"));
+            auto n_at = read_i(g.f(s), g.p("n_atom"));
+            auto ref = g.f(s).read<float>(g.p("ref_pos"));
+            for (size_t i = 0; i < id.size(); ++i) {
+                rr.push_back(id[i] + oaff[s]);
+                ids.push_back(id[i]);
+                na.push_back(n_at[i]);
+                for (int k = 0; k < 12; ++k) {
+                    float x = ref[i * 12 + size_t(k)];
+                    rp.push_back(std::isfinite(x) ? x : 0.f);
+                }
+                for (int k = 0; k < n_at[i]; ++k) {
+                    const float* q = &ref[i * 12 + size_t(3 * k)];
+                    max_dev = std::max(max_dev, std::sqrt(q[0] * q[0] + q[1] * q[1] + q[2] * q[2]));
+                }
+            }
+        }
+        res_row = e.upload(rr);
+        nat = e.upload(na);
+        refp = e.upload(rp);
+        d.loc1 = d.loc2 = res_row;
+        d.id1 = d.id2 = e.upload(ids);
+        d.type1 = d.type2 = e.upload(zeros);
+        d.sys1 = e.upload(sys_of(of));
+        d.cutoff = 2.f * max_dev + sqrtf(3.f * 3.f + 0.1f * 3.f);
+        std::vector<int> ri1, ri1e, ri2, ri2e;
+        for (size_t s = 0; s < g.size(); ++s) {
+            hg.sys_first_row.push_back(int(ri1.size()));
+            for (int b = 0; b < c[s]; b += 4) {
+                ri1.push_back(of[s] + b); ri1e.push_back(of[s] + c[s]);
+                ri2.push_back(of[s] + b + 1); ri2e.push_back(of[s] + c[s]);
+            }
+        }
+        hg.sys_first_row.push_back(int(ri1.size()));
+        d.n_rows = int(ri1.size());
+        d.row_i1 = e.upload(ri1); d.row_i1_end = e.upload(ri1e);
+        d.row_i2 = e.upload(ri2); d.row_i2_end = e.upload(ri2e);
+        d.row_count = e.alloc<int>(size_t(d.n_rows) + 1);
+        d.row_off = e.alloc<int>(size_t(d.n_rows) + 1);
+        d.sys_first_row = e.upload(hg.sys_first_row);
+        d.n_edge = e.alloc<int>(1);
+        d.x1 = d.x2 = e.alloc<float4>(size_t(d.n1));
+        long long full = (long long)d.n1 * (d.n1 - 1) / 2;
+        hg.alloc_edges(int(std::max(1LL, std::min<long long>(full, 48LL * d.n1 + 1024))));
+    }
+    void forward(Engine& e, bool energy) override {
+        auto& a = e.arg(*this, 0);
+        hg.bind(a, a);
+        launch_pairs(hg.g, e.st);
+        bb_pairs_kernel<<<nblk(hg.g.cap), 256, 0, e.st>>>(hg.g, res_row, nat, refp, hg.g.sys1, a.out, a.sens,
+                                                          energy ? e.d_pot + size_t(pot_slot) * e.n_sys : nullptr);
+    }
+    DGraph* graph() override { return &hg.g; }
+    bool grow(Engine&) override { return hg.grow_if_full(); }
+};
+
+// ============================================================ rotamer ===
+// side-chain rotamer free energy by loopy belief propagation
+// (RotamerSidechain, src/rotamer.cpp:628-1169)
+struct RotamerNode : GNode {
+    HGraph hg;
+    DBP b{};
+    std::vector<int> n_res_sys;
+    int n_prob = 0;
+    double* d_energy = nullptr;
+    int prev_n_ent = 0;
+    RotamerNode(Engine& e, const Groups& g, const std::vector<int>& obead) {
+        potential = true;
+        hg.setup(e, IK_ROTAMER, EX_ROTAMER, true, 6, 6, 54, g, "pair_interaction", obead, obead, 96);
+        b.damping = float(shared_attr(g, "damping"));
+        b.max_iter = int(shared_attr(g, "max_iter"));
+        b.tol = float(shared_attr(g, "tol"));
+        b.chunk = int(shared_attr(g, "iteration_chunk_size"));
+        b.n_sys = e.n_sys;
+        b.status = e.d_status;
+        // decode bead ids: (local index within its rotamer-count class, n_rot, rot)
+        std::vector<int> bead_res, bead_rot, nrot, res_off{0}, resN, rsys, rlocal;
+        std::vector<long long> slot_off{0};
+        for (size_t s = 0; s < g.size(); ++s) {
+            auto id = read_i(g.f(s), g.p("pair_interaction/id"));
+            std::map<std::pair<int, int>, int> res_of;  // (n_rot, local) -> residue index
+            std::vector<std::pair<int, int>> order;
+            for (int x : id) {
+                int rot = x & 15, nr = (x >> 4) & 15, loc = x >> 8;
+                if (rot >= nr) throw Error("invalid rotamer number");
+                if (nr != 1 && nr != 3 && nr != 6) throw Error("invalid rotamer count " + std::to_string(nr));
+                auto key = std::make_pair(nr, loc);
+                if (!res_of.count(key)) {
+                    res_of[key] = int(order.size());
+                    order.push_back(key);
+                }
+            }
+            int base = res_off.back();
+            int N = int(order.size());
+            for (int x : id) {
+                bead_res.push_back(base + res_of[std::make_pair((x >> 4) & 15, x >> 8)]);
+                bead_rot.push_back(x & 15);
+            }
+            for (int i = 0; i < N; ++i) {
+                nrot.push_back(order[size_t(i)].first);
+                resN.push_back(N);
+                rsys.push_back(int(s));
+                rlocal.push_back(i);
+            }
+            res_off.push_back(base + N);
+            slot_off.push_back(slot_off.back() + (long long)N * N);
+            n_res_sys.push_back(N);
+        }
+        b.n_res = res_off.back();
+        b.n_bead = int(bead_res.size());
+        b.res_off = e.upload(res_off);
+        b.nrot = e.upload(nrot);
+        b.res_N = e.upload(resN);
+        b.res_sys = e.upload(rsys);
+        b.res_local = e.upload(rlocal);
+        b.slot_off = e.upload(slot_off);
+        std::vector<int> minus1(size_t(slot_off.back()), -1);
+        b.slot = e.upload(minus1);
+        b.row_count = e.alloc<int>(size_t(b.n_res) + 1);
+        b.row_ptr = e.alloc<int>(size_t(b.n_res) + 1);
+        b.bead_res = e.upload(bead_res);
+        b.bead_rot = e.upload(bead_rot);
+        b.bead_loc = hg.g.loc1;
+        b.n_ent = e.alloc<int>(1);
+        alloc_entries(e, std::max(1024, 48 * b.n_res));
+        b.E1 = e.alloc<float>(size_t(b.n_res) * 8);
+        b.E1x = e.alloc<float>(size_t(b.n_res) * 8);
+        b.prob = e.alloc<float>(size_t(b.n_res) * 8);
+        b.eoff = e.alloc<float>(size_t(b.n_res));
+        b.belief = e.alloc<float>(size_t(b.n_res) * 16);
+        b.marg = e.alloc<float>(size_t(b.n_res) * 8);
+        b.n_iter = e.alloc<int>(size_t(e.n_sys));
+        b.e11 = e.alloc<double>(size_t(e.n_sys));
+        d_energy = e.alloc<double>(size_t(e.n_sys));
+    }
+    void alloc_entries(Engine& e, int cap) {
+        b.ent_cap = cap;
+        b.col = e.alloc<int>(size_t(cap));
+        b.erow = e.alloc<int>(size_t(cap));
+        b.rev = e.alloc<int>(size_t(cap));
+        b.esum = e.alloc<float>(size_t(cap) * 36);
+        b.P = e.alloc<float>(size_t(cap) * 36);
+        b.emarg = e.alloc<float>(size_t(cap) * 36);
+        b.msg = e.alloc<float>(size_t(cap) * 16);
+    }
+    void forward(Engine& e, bool energy) override {
+        auto& beads = e.arg(*this, 0);
+        hg.bind(beads, beads);
+        hg.search_and_eval(e.st);
+        n_prob = int(args.size()) - 1;
+        if (n_prob < 1 || n_prob > 4) throw Error("rotamer node needs 1 to 4 one-body energy inputs");
+        const float* in[4] = {nullptr, nullptr, nullptr, nullptr};
+        float* ins[4] = {nullptr, nullptr, nullptr, nullptr};
+        int w[4] = {1, 1, 1, 1};
+        for (int k = 0; k < n_prob; ++k) {
+            auto& pn = e.arg(*this, 1 + k);
+            in[k] = pn.out;
+            ins[k] = pn.sens;
+            w[k] = pn.width;
+        }
+        for (int k = n_prob; k < 4; ++k) { in[k] = in[0]; ins[k] = ins[0]; w[k] = w[0]; }
+        launch_bp(b, hg.g, in, ins, w, n_prob, prev_n_ent, nullptr, energy ? 1 : 0, d_energy, e.st);
+        if (energy) add_pot(e);
+    }
+    void add_pot(Engine& e);
+    void backward(Engine& e) override { launch_edge_scatter(hg.g, e.st); }
+    std::vector<float> get_param(Engine&) override { return hg.param_host; }
+    void set_param(Engine&, const std::vector<float>& p) override { hg.set_param(p); }
+    std::vector<float> param_deriv(Engine& e) override {
+        size_t n = hg.param_host.size();
+        std::vector<float> r(n, 0.f);
+        float* d = nullptr;
+        UG_CK(cudaMalloc(&d, n * 4));
+        UG_CK(cudaMemsetAsync(d, 0, n * 4, e.st));
+        launch_param_deriv(hg.g, d, e.st);
+        UG_CK(cudaMemcpyAsync(r.data(), d, n * 4, cudaMemcpyDeviceToHost, e.st));
+        UG_CK(cudaStreamSynchronize(e.st));
+        cudaFree(d);
+        return r;
+    }
+    DGraph* graph() override { return &hg.g; }
+    bool grow(Engine& e) override {
+        bool g1 = hg.grow_if_full();
+        int ne = 0;
+        UG_CK(cudaMemcpy(&ne, b.n_ent, 4, cudaMemcpyDeviceToHost));
+        if (ne >= b.ent_cap) {
+            // the residue map still holds entry numbers of the old storage:
+            // clear it so the next evaluation starts from an empty map
+            std::vector<long long> so(size_t(e.n_sys) + 1);
+            UG_CK(cudaMemcpy(so.data(), b.slot_off, so.size() * 8, cudaMemcpyDeviceToHost));
+            UG_CK(cudaMemset(b.slot, 0xff, size_t(so.back()) * 4));
+            UG_CK(cudaMemset(b.n_ent, 0, 4));
+            alloc_entries(e, 2 * b.ent_cap);
+            return true;
+        }
+        return g1;
+    }
+    std::vector<float> value_by_name(Engine& e, const std::string& w) override {
+        if (w == "count_edges_by_type") return hg.count_edges_by_type();
+        if (w == "n_node") return {float(n_res_sys.at(0))};
+        if (w == "n_iter") {
+            std::vector<int> it(size_t(e.n_sys));
+            UG_CK(cudaMemcpy(it.data(), b.n_iter, 4 * it.size(), cudaMemcpyDeviceToHost));
+            return std::vector<float>(it.begin(), it.end());
+        }
+        if (w == "node_marginal") {
+            std::vector<float> m(size_t(b.n_res) * 8);
+            std::vector<int> nr(size_t(b.n_res));
+            UG_CK(cudaMemcpy(m.data(), b.marg, 4 * m.size(), cudaMemcpyDeviceToHost));
+            UG_CK(cudaMemcpy(nr.data(), b.nrot, 4 * nr.size(), cudaMemcpyDeviceToHost));
+            // ordered by rotamer class (1, 3, 6), then residue order, padded to 6
+            std::vector<float> out;
+            for (int cls : {1, 3, 6})
+                for (int r = 0; r < b.n_res; ++r)
+                    if (nr[size_t(r)] == cls)
+                        for (int k = 0; k < 6; ++k) out.push_back(m[size_t(r) * 8 + size_t(k)]);
+            return out;
+        }
+        return GNode::value_by_name(e, w);
+    }
+};
+
+__global__ void add_pot_kernel(int n, const double* __restrict__ src, double* dst) {
+    for (int s = grid_stride_start(); s < n; s += grid_stride()) dst[s] = src[s];
+}
+void RotamerNode::add_pot(Engine& e) {
+    add_pot_kernel<<<1, 256, 0, e.st>>>(e.n_sys, d_energy, e.d_pot + size_t(pot_slot) * e.n_sys);
+}
+
+bool is_prefix(const std::string& p, const std::string& s) { return s.compare(0, p.size(), p) == 0; }
+
+// ----------------------------------------------------------------- misc ---
+__global__ void sum_energy_kernel(int n_sys, int n_slots, const double* __restrict__ pot, double* __restrict__ out) {
+    for (int s = grid_stride_start(); s < n_sys; s += grid_stride()) {
+        double t = 0.0;
+        for (int k = 0; k < n_slots; ++k) t += pot[size_t(k) * n_sys + s];
+        out[s] = t;
+    }
+}
+
+// p -= dt F ; x += dt p   (integration_cycle, src/deriv_engine.cpp:317-331)
+__global__ void integrate_kernel(int n, float dt, const float* __restrict__ f, float* __restrict__ mom, float* __restrict__ pos) {
+    for (int i = grid_stride_start(); i < n; i += grid_stride()) {
+        float p = mom[i] - dt * f[i];
+        mom[i] = p;
+        pos[i] += dt * p;
+    }
+}
+
+// Threefry-4x32-20 (Salmon et al. 2011) keyed by (seed, stream 0), counter
+// (invocation, atom): the reference thermostat's random stream (src/random.h:19-67)
+__device__ __forceinline__ uint32_t rotl32(uint32_t x, int r) { return (x << r) | (x >> (32 - r)); }
+__device__ void threefry4x32(const uint32_t c[4], const uint32_t k[4], uint32_t out[4]) {
+    const int R[8][2] = {{10, 26}, {11, 21}, {13, 27}, {23, 5}, {6, 20}, {17, 11}, {25, 10}, {18, 20}};
+    uint32_t ks[5] = {k[0], k[1], k[2], k[3], 0x1BD11BDAu ^ k[0] ^ k[1] ^ k[2] ^ k[3]};
+    uint32_t x[4];
+    for (int i = 0; i < 4; ++i) x[i] = c[i] + ks[i];
+#pragma unroll
+    for (int r = 0; r < 20; ++r) {
+        if (r % 2 == 0) {
+            x[0] += x[1]; x[1] = rotl32(x[1], R[r % 8][0]); x[1] ^= x[0];
+            x[2] += x[3]; x[3] = rotl32(x[3], R[r % 8][1]); x[3] ^= x[2];
+        } else {
+            x[0] += x[3]; x[3] = rotl32(x[3], R[r % 8][0]); x[3] ^= x[0];
+            x[2] += x[1]; x[1] = rotl32(x[1], R[r % 8][1]); x[1] ^= x[2];
+        }
+        if (r % 4 == 3) {
+            uint32_t s = uint32_t(r / 4 + 1);
+            for (int i = 0; i < 4; ++i) x[i] += ks[(s + uint32_t(i)) % 5];
+            x[3] += s;
+        }
+    }
+    for (int i = 0; i < 4; ++i) out[i] = x[i];
+}
+// OU thermostat p <- e^{-dt/tau} p + sqrt(T (1 - e^{-2dt/tau})) N(0,1)
+// (OrnsteinUhlenbeckThermostat::apply, src/thermostat.cpp:9-18)
+__global__ void thermostat_kernel(int n_sys, const int* __restrict__ atom_off, const int* __restrict__ atom_sys,
+                                  int n_atom, float delta_t, float timescale, const float* __restrict__ temp,
+                                  const unsigned* __restrict__ seed, unsigned long long* round, float* mom) {
+    for (int a = grid_stride_start(); a < n_atom; a += grid_stride()) {
+        int s = atom_sys[a];
+        float ms = expf(-delta_t / timescale);
+        float ns = sqrtf(temp[s] * (1.f - ms * ms));
+        unsigned long long inv = round[s];
+        uint32_t key[4] = {seed[s], 0u, 0u, 0u};
+        uint32_t ctr[4] = {uint32_t(inv & 0xffffffffu), uint32_t(inv >> 32), uint32_t(a - atom_off[s]), 0u};
+        uint32_t bits[4];
+        threefry4x32(ctr, key, bits);
+        const float PIf = 3.1415926535897932f;
+        float a0 = PIf * (float(int32_t(bits[0])) * (1.f / 2147483648.f) + (0.5f / 2147483648.f));
+        float r0 = sqrtf(-2.f * logf(float(bits[1]) * (1.f / 4294967296.f) + (0.5f / 4294967296.f)));
+        float a1 = PIf * (float(int32_t(bits[2])) * (1.f / 2147483648.f) + (0.5f / 2147483648.f));
+        float r1 = sqrtf(-2.f * logf(float(bits[3]) * (1.f / 4294967296.f) + (0.5f / 4294967296.f)));
+        float z[3] = {sinf(a0) * r0, cosf(a0) * r0, sinf(a1) * r1};
+        for (int d = 0; d < 3; ++d) mom[3 * size_t(a) + d] = ms * mom[3 * size_t(a) + d] + ns * z[d];
+    }
+}
+__global__ void round_advance_kernel(int n_sys, unsigned long long* round) {
+    for (int s = grid_stride_start(); s < n_sys; s += grid_stride()) round[s] += 1;
+}
+
+}  // namespace
+
+// ================================================================ Engine ===
+Engine::Engine(const std::vector<std::string>& paths, const std::vector<int>& n_atom_) {
+    if (paths.empty()) throw Error("no systems given");
+    n_sys = int(paths.size());
+    n_atom = n_atom_;
+    atom_off = offsets(n_atom);
+    atom_total = atom_off.back();
+    UG_CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    for (auto& p : paths) files_.push_back(std::make_unique<h5lite::File>(p));
+    // graph structure from the first system; all systems must agree
+    auto names = files_[0]->list("/input/potential");
+    std::map<std::string, std::vector<std::string>> deps;
+    for (auto& nm : names) deps[nm] = files_[0]->attr_strings("/input/potential/" + nm, "arguments");
+    for (size_t s = 1; s < files_.size(); ++s) {
+        if (files_[s]->list("/input/potential") != names) throw Error("systems of one batch must share one node graph");
+        for (auto& nm : names)
+            if (files_[s]->attr_strings("/input/potential/" + nm, "arguments") != deps[nm])
+                throw Error("node '" + nm + "' has different arguments between systems of one batch");
+    }
+    std::set<std::string> done{"pos"};
+    std::vector<std::string> order;
+    for (size_t round = 0; round <= deps.size(); ++round)
+        for (auto& kv : deps) {
+            if (done.count(kv.first)) continue;
+            bool ok = true;
+            for (auto& a : kv.second) ok = ok && done.count(a);
+            if (ok) { order.push_back(kv.first); done.insert(kv.first); }
+        }
+    if (order.size() != deps.size()) throw Error("Unsatisfiable dependency in potential computation");
+
+    d_status = alloc<int>(1);
+    auto pos = std::make_unique<PosNode>();
+    pos->name = "pos";
+    pos->width = 3;
+    pos->total = atom_total;
+    pos->off = atom_off;
+    index["pos"] = 0;
+    nodes.push_back(std::move(pos));
+
+    for (auto& nm : order) {
+        Groups g;
+        for (auto& f : files_) g.files.push_back(f.get());
+        g.path = "/input/potential/" + nm;
+        std::vector<int> a;
+        for (auto& x : deps[nm]) a.push_back(index.at(x));
+        auto O = [&](int i) -> const std::vector<int>& { return nodes[size_t(a.at(size_t(i)))]->off; };
+        std::unique_ptr<GNode> n;
+        try {
+            if (is_prefix("Distance3D", nm)) n.reset(new DistNode(*this, g, O(0), O(1)));
+            else if (is_prefix("Angle", nm)) n.reset(new AngleNode(*this, g, O(0)));
+            else if (is_prefix("Dihedral", nm)) n.reset(new DihedralNode(*this, g, O(0)));
+            else if (is_prefix("Spring", nm)) n.reset(new SpringNode(*this, g, O(0)));
+            else if (is_prefix("rama_coord", nm)) n.reset(new PasteNode(*this, g, false, O(0), O(1)));
+            else if (is_prefix("cat_pos", nm)) n.reset(new PasteNode(*this, g, true, O(0), O(1)));
+            else if (is_prefix("rama_map_pot", nm)) n.reset(new RamaMapNode(*this, g, O(0)));
+            else if (is_prefix("affine_alignment", nm)) n.reset(new AffineNode(*this, g, O(0)));
+            else if (is_prefix("backbone_pairs", nm)) n.reset(new BackbonePairsNode(*this, g, O(0)));
+            else if (is_prefix("infer_H_O", nm)) n.reset(new InferHONode(*this, g, O(0)));
+            else if (is_prefix("protein_hbond", nm)) n.reset(new ProteinHBondNode(*this, g, O(0)));
+            else if (is_prefix("hbond_energy", nm)) n.reset(new HBondEnergyNode(*this, g, *nodes[size_t(a[0])], O(1)));
+            else if (is_prefix("hbond_coverage", nm)) n.reset(new CoverageNode(*this, g, IK_HBCOV, O(0), O(1)));
+            else if (is_prefix("placement_fixed_point_vector_scalar", nm)) n.reset(new PlacementNode(*this, g, 2, true, false, O(0), nullptr));
+            else if (is_prefix("placement_fixed_point_vector_only", nm)) n.reset(new PlacementNode(*this, g, 2, false, false, O(0), nullptr));
+            else if (is_prefix("placement_fixed_point_only", nm)) n.reset(new PlacementNode(*this, g, 1, false, false, O(0), nullptr));
+            else if (is_prefix("placement_scalar", nm)) n.reset(new PlacementNode(*this, g, 0, true, true, O(0), &O(1)));
+            else if (is_prefix("rotamer", nm)) n.reset(new RotamerNode(*this, g, O(0)));
+            else if (is_prefix("weighted_pos", nm)) n.reset(new WeightedPosNode(*this, g, O(0), O(1)));
+            else if (is_prefix("environment_coverage", nm)) n.reset(new CoverageNode(*this, g, IK_ENVCOV, O(0), O(1)));
+            else if (is_prefix("hb_environment_coverage", nm)) n.reset(new CoverageNode(*this, g, IK_HBENV, O(0), O(1)));
+            else if (is_prefix("sigmoid_coupling", nm)) n.reset(new CouplingNode(*this, g, CouplingNode::SIGMOID, *nodes[size_t(a[0])]));
+            else if (is_prefix("nonlinear_coupling", nm)) n.reset(new CouplingNode(*this, g, CouplingNode::NONLINEAR, *nodes[size_t(a[0])]));
+            else if (is_prefix("bb_sigmoid_coupling", nm)) n.reset(new CouplingNode(*this, g, CouplingNode::BB, *nodes[size_t(a[0])]));
+            else throw Error("No node type found for name '" + nm + "'");
+        } catch (const h5lite::Error& ex) {
+            throw Error("while adding '" + nm + "', " + ex.what());
+        } catch (const Error& ex) {
+            throw Error("while adding '" + nm + "', " + ex.what());
+        }
+        n->name = nm;
+        n->args = a;
+        if (n->potential) n->pot_slot = n_pot_slots++;
+        index[nm] = int(nodes.size());
+        nodes.push_back(std::move(n));
+    }
+    // node output / sensitivity arenas
+    size_t tot = 0;
+    for (auto& n : nodes) tot += size_t(n->total) * size_t(n->width);
+    float* out_arena = alloc<float>(tot);
+    d_sens_arena = alloc<float>(tot);
+    sens_arena_floats = tot;
+    size_t o = 0;
+    for (auto& n : nodes) {
+        if (n->name == "pos") {
+            d_pos = out_arena + o;
+        }
+        n->out = out_arena + o;
+        n->sens = d_sens_arena + o;
+        o += size_t(n->total) * size_t(n->width);
+    }
+    d_mom = alloc<float>(size_t(atom_total) * 3);
+    d_pot = alloc<double>(size_t(std::max(1, n_pot_slots)) * size_t(n_sys));
+    d_energy = alloc<double>(size_t(n_sys));
+    d_round = alloc<unsigned long long>(size_t(n_sys));
+    d_temp = alloc<float>(size_t(n_sys));
+    d_seed = alloc<unsigned>(size_t(n_sys));
+    atom_sys_d = upload(sys_of(atom_off));
+    atom_off_d = upload(atom_off);
+    UG_CK(cudaStreamSynchronize(st));
+}
+
+Engine::~Engine() {
+    if (graph_exec) cudaGraphExecDestroy(graph_exec);
+    if (graph) cudaGraphDestroy(graph);
+    nodes.clear();
+    free_all();
+    if (st) cudaStreamDestroy(st);
+}
+
+GNode& Engine::node(const std::string& name) {
+    auto it = index.find(name);
+    if (it == index.end()) throw Error("name not found");
+    return *nodes[size_t(it->second)];
+}
+
+void Engine::compute(bool energy) {
+    UG_CK(cudaMemsetAsync(d_sens_arena, 0, sens_arena_floats * sizeof(float), st));
+    if (energy) UG_CK(cudaMemsetAsync(d_pot, 0, sizeof(double) * size_t(std::max(1, n_pot_slots)) * n_sys, st));
+    for (auto& n : nodes) n->forward(*this, energy);
+    for (size_t i = nodes.size(); i-- > 0;) nodes[i]->backward(*this);
+    if (energy) sum_energy_kernel<<<1, 256, 0, st>>>(n_sys, n_pot_slots, d_pot, d_energy);
+    UG_CK(cudaGetLastError());
+}
+
+void Engine::round(float dt, float timescale, bool thermostat) {
+    if (thermostat) {
+        thermostat_kernel<<<nblk(atom_total), 256, 0, st>>>(n_sys, atom_off_d, atom_sys_d, atom_total, 3.f * dt, timescale,
+                                                            d_temp, d_seed, d_round, d_mom);
+        round_advance_kernel<<<1, 256, 0, st>>>(n_sys, d_round);
+    }
+    for (int stage = 0; stage < 3; ++stage) {
+        compute(false);
+        integrate_kernel<<<nblk(3LL * atom_total), 256, 0, st>>>(3 * atom_total, dt, nodes[0]->sens, d_mom, d_pos);
+    }
+    UG_CK(cudaGetLastError());
+}
+
+void Engine::compute_checked(bool energy) {
+    for (int attempt = 0; attempt < 8; ++attempt) {
+        compute(energy);
+        int s = status(true);
+        if (!(s & (ST_EDGE_OVERFLOW | ST_RES_EDGE_OVERFLOW))) return;
+        bool grew = false;
+        for (auto& n : nodes) grew |= n->grow(*this);
+        if (!grew) throw Error("pair-list storage overflow that could not be grown");
+        if (graph_exec) {  // buffers moved: the captured graph is stale
+            cudaGraphExecDestroy(graph_exec);
+            graph_exec = nullptr;
+            cudaGraphDestroy(graph);
+            graph = nullptr;
+        }
+    }
+    throw Error("pair-list storage kept overflowing");
+}
+
+void Engine::set_pos(const float* p) {
+    UG_CK(cudaMemcpyAsync(d_pos, p, sizeof(float) * 3 * size_t(atom_total), cudaMemcpyHostToDevice, st));
+}
+void Engine::get_pos(float* p) {
+    UG_CK(cudaMemcpyAsync(p, d_pos, sizeof(float) * 3 * size_t(atom_total), cudaMemcpyDeviceToHost, st));
+    UG_CK(cudaStreamSynchronize(st));
+}
+void Engine::get_deriv(float* p) {
+    UG_CK(cudaMemcpyAsync(p, nodes[0]->sens, sizeof(float) * 3 * size_t(atom_total), cudaMemcpyDeviceToHost, st));
+    UG_CK(cudaStreamSynchronize(st));
+}
+void Engine::energies(double* e) {
+    UG_CK(cudaMemcpyAsync(e, d_energy, sizeof(double) * size_t(n_sys), cudaMemcpyDeviceToHost, st));
+    UG_CK(cudaStreamSynchronize(st));
+}
+int Engine::status(bool clear) {
+    int s = 0;
+    UG_CK(cudaMemcpyAsync(&s, d_status, sizeof(int), cudaMemcpyDeviceToHost, st));
+    UG_CK(cudaStreamSynchronize(st));
+    if (clear && s) UG_CK(cudaMemsetAsync(d_status, 0, sizeof(int), st));
+    return s;
+}
+void Engine::sync() { UG_CK(cudaStreamSynchronize(st)); }
+
+void Engine::capture(float dt, float timescale, int rounds) {
+    if (graph_exec) { cudaGraphExecDestroy(graph_exec); graph_exec = nullptr; }
+    if (graph) { cudaGraphDestroy(graph); graph = nullptr; }
+    UG_CK(cudaStreamSynchronize(st));
+    UG_CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    for (int r = 0; r < rounds; ++r) round(dt, timescale, true);
+    UG_CK(cudaStreamEndCapture(st, &graph));
+    UG_CK(cudaGraphInstantiate(&graph_exec, graph, 0));
+    graph_rounds = rounds;
+}
+void Engine::launch_graph() { UG_CK(cudaGraphLaunch(graph_exec, st)); }
+
+}  // namespace ug

@@ -1,0 +1,124 @@
+// GB300 Upside engine: host-side graph of force-field nodes over a batch of
+// systems, device buffers, and the integrator.  Every node's compute runs as
+// sm_103a kernels over all systems of the batch at once.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <map>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "graph.h"
+#include "h5lite.h"
+
+namespace ug {
+
+struct Error : std::runtime_error {
+    explicit Error(const std::string& s) : std::runtime_error(s) {}
+};
+
+void cuda_check(cudaError_t e, const char* what);
+#define UG_CK(x) ::ug::cuda_check((x), #x)
+
+class Engine;
+
+// One `/input/potential/<node>` group of every system of the batch.
+struct Groups {
+    std::vector<h5lite::File*> files;
+    std::string path;
+    size_t size() const { return files.size(); }
+    h5lite::File& f(size_t s) const { return *files[s]; }
+    std::string p(const std::string& n) const { return path + "/" + n; }
+};
+
+struct GNode {
+    std::string name;
+    std::vector<int> args;
+    bool potential = false;
+    int width = 0, total = 0;
+    std::vector<int> off;  // per-system element offsets (n_sys+1)
+    float* out = nullptr;  // total*width
+    float* sens = nullptr;
+    int pot_slot = -1;
+    virtual ~GNode() {}
+    virtual void forward(Engine& e, bool energy) = 0;
+    virtual void backward(Engine&) {}
+    virtual std::vector<float> get_param(Engine&) { return {}; }
+    virtual void set_param(Engine&, const std::vector<float>&) { throw Error("set_param not supported for this node"); }
+    virtual std::vector<float> param_deriv(Engine&) { return {}; }
+    virtual std::vector<float> value_by_name(Engine&, const std::string& w) {
+        throw Error("Value " + w + " not implemented");
+    }
+    virtual DGraph* graph() { return nullptr; }
+    // enlarge edge storage after an overflow; returns true if anything grew
+    virtual bool grow(Engine&) { return false; }
+};
+
+class Engine {
+public:
+    Engine(const std::vector<std::string>& paths, const std::vector<int>& n_atom);
+    ~Engine();
+
+    int n_sys = 0;
+    std::vector<int> n_atom, atom_off;
+    int atom_total = 0;
+    cudaStream_t st = nullptr;
+
+    std::vector<std::unique_ptr<GNode>> nodes;
+    std::map<std::string, int> index;
+    int n_pot_slots = 0;
+
+    // device state
+    float* d_pos = nullptr;   // atom_total*3
+    float* d_mom = nullptr;   // atom_total*3
+    double* d_pot = nullptr;  // n_pot_slots*n_sys
+    double* d_energy = nullptr;  // n_sys
+    int* d_status = nullptr;
+    unsigned long long* d_round = nullptr;  // per-system thermostat invocation counters
+    float* d_temp = nullptr;   // per-system temperature
+    unsigned* d_seed = nullptr;  // per-system thermostat seed
+    float* d_sens_arena = nullptr;
+    size_t sens_arena_floats = 0;
+    int* atom_sys_d = nullptr;
+    int* atom_off_d = nullptr;
+
+    // allocation helpers (engine owns every device buffer)
+    template <class T> T* alloc(size_t n);
+    template <class T> T* upload(const std::vector<T>& v);
+    void free_all();
+
+    GNode& node(const std::string& name);
+    GNode& arg(const GNode& n, int i) { return *nodes[size_t(n.args.at(size_t(i)))]; }
+
+    // enqueue one force evaluation (forward + adjoint) on the stream
+    void compute(bool energy);
+    // one integration round: thermostat, then 3 x {compute; p -= dt F; x += dt p}
+    void round(float dt, float timescale, bool thermostat);
+    // host helpers
+    void set_pos(const float* pos_all);     // atom_total*3
+    void get_pos(float* pos_all);
+    void get_deriv(float* d_all);
+    void energies(double* e);               // n_sys, valid after compute(true)
+    int status(bool clear);
+    // evaluate with automatic growth of pair-list storage on overflow
+    void compute_checked(bool energy);
+    void sync();
+
+    // CUDA graph of `rounds_per_graph` integration rounds
+    void capture(float dt, float timescale, int rounds_per_graph);
+    void launch_graph();
+    cudaGraphExec_t graph_exec = nullptr;
+    cudaGraph_t graph = nullptr;
+    int graph_rounds = 0;
+
+    size_t device_bytes = 0;
+    int launches_per_compute = 0;
+
+private:
+    std::vector<void*> allocations_;
+    std::vector<std::unique_ptr<h5lite::File>> files_;
+};
+
+}  // namespace ug

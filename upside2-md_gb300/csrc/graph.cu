@@ -1,0 +1,797 @@
+// Interaction-graph kernels (pair search in the reference's edge order, edge
+// evaluation, sensitivity scatter), the batch prefix scan, and the rotamer
+// belief-propagation kernels.  sm_103a, FP32 arithmetic, FP64 energy sums.
+//
+// Reference behaviour restated here:
+//   pair search / edge order   src/interaction_graph.h:51-258
+//   edge values / adjoint      src/interaction_graph.h:445-564
+//   quadspline                 src/bead_interaction.h:31-85
+//   protein hbond edge         src/hbond.cpp:158-246
+//   hbond coverage edge        src/hbond.cpp:249-294
+//   environment coverage edges src/environment.cpp:114-228
+//   rotamer BP                 src/rotamer.cpp:239-302, :425-569, :854-1162
+#include <cstdio>
+
+#include "dev_math.cuh"
+#include "graph.h"
+
+namespace ug {
+
+// ---------------------------------------------------------------- scan ---
+// Exclusive scan of n ints into out[0..n] (out[n] = total) by one 1024-thread
+// block: each thread owns a contiguous chunk, then a block-level scan of the
+// chunk sums.
+__global__ void __launch_bounds__(1024) scan_kernel(const int* __restrict__ in, int* __restrict__ out, int n,
+                                                    int* total_out) {
+    __shared__ int warp_sums[32];
+    int t = threadIdx.x;
+    int per = (n + blockDim.x - 1) / blockDim.x;
+    int lo = min(n, t * per), hi = min(n, lo + per);
+    int s = 0;
+    for (int i = lo; i < hi; ++i) s += in[i];
+    // block exclusive scan of s
+    int lane = t & 31, w = t >> 5;
+    int v = s;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int y = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += y;
+    }
+    if (lane == 31) warp_sums[w] = v;
+    __syncthreads();
+    if (w == 0) {
+        int ws = warp_sums[lane];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            int y = __shfl_up_sync(0xffffffffu, ws, o);
+            if (lane >= o) ws += y;
+        }
+        warp_sums[lane] = ws;
+    }
+    __syncthreads();
+    int excl = v - s + (w ? warp_sums[w - 1] : 0);
+    for (int i = lo; i < hi; ++i) {
+        out[i] = excl;
+        excl += in[i];
+    }
+    if (t == blockDim.x - 1) {
+        out[n] = excl;
+        if (total_out) *total_out = excl;
+    }
+    if (n == 0 && t == 0) {
+        out[0] = 0;
+        if (total_out) *total_out = 0;
+    }
+}
+
+void launch_scan(const int* in, int* out, int n, int* total_out, cudaStream_t st) {
+    scan_kernel<<<1, 1024, 0, st>>>(in, out, n, total_out);
+}
+
+// --------------------------------------------------------- pair search ---
+__global__ void pack_kernel(const int* __restrict__ loc, const float* __restrict__ in, int w, int n,
+                            float4* __restrict__ x) {
+    for (int i = grid_stride_start(); i < n; i += grid_stride()) {
+        const float* p = in + size_t(loc[i]) * w;
+        x[i] = make_float4(p[0], p[1], p[2], 0.f);
+    }
+}
+
+void launch_pack_positions(const DGraph& g, cudaStream_t st) {
+    if (g.n1) pack_kernel<<<min(1024, (g.n1 + 255) / 256), 256, 0, st>>>(g.loc1, g.in1, g.w1, g.n1, g.x1);
+    if (!g.symmetric && g.n2) pack_kernel<<<min(1024, (g.n2 + 255) / 256), 256, 0, st>>>(g.loc2, g.in2, g.w2, g.n2, g.x2);
+}
+
+// One warp per row (4 consecutive set-1 elements of one system).  Pass 0
+// counts hits; pass 1 writes them in (i2, lane) order at the row's scanned
+// offset, which reproduces the reference's edge order exactly.
+template <int PASS>
+__global__ void pair_kernel(DGraph g) {
+    int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    int lane = threadIdx.x & 31;
+    int n_warps = (gridDim.x * blockDim.x) >> 5;
+    const float c2 = g.cutoff * g.cutoff;
+    const float4* X2 = g.symmetric ? g.x1 : g.x2;
+    const int* ID2 = g.symmetric ? g.id1 : g.id2;
+    for (int r = warp; r < g.n_rows; r += n_warps) {
+        int i1s = g.row_i1[r], i1e = g.row_i1_end[r];
+        int i2s = g.row_i2[r], i2e = g.row_i2_end[r];
+        float4 a[4];
+        int ida[4];
+        int nl = min(4, i1e - i1s);
+#pragma unroll
+        for (int l = 0; l < 4; ++l) {
+            a[l] = l < nl ? g.x1[i1s + l] : make_float4(1e20f, 1e20f, 1e20f, 0.f);
+            ida[l] = l < nl ? g.id1[i1s + l] : 0;
+        }
+        int base = PASS ? g.row_off[r] : 0;
+        int count = 0;
+        for (int j0 = i2s; j0 < i2e; j0 += 32) {
+            int j = j0 + lane;
+            unsigned mask = 0;
+            if (j < i2e) {
+                float4 b = X2[j];
+                int idb = ID2[j];
+#pragma unroll
+                for (int l = 0; l < 4; ++l) {
+                    if (l >= nl) break;
+                    if (g.symmetric && !(i1s + l < j)) continue;
+                    float dx = a[l].x - b.x, dy = a[l].y - b.y, dz = a[l].z - b.z;
+                    float d2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+                    if (d2 < c2 && acceptable_ids(g.excl, ida[l], idb)) mask |= 1u << l;
+                }
+            }
+            int c = __popc(mask);
+            if (PASS == 0) {
+                count += c;
+            } else {
+                int incl = c;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    int y = __shfl_up_sync(0xffffffffu, incl, o);
+                    if (lane >= o) incl += y;
+                }
+                int pos = base + incl - c;
+                for (int l = 0; l < 4; ++l)
+                    if (mask & (1u << l)) {
+                        if (pos < g.cap) g.edges[pos] = make_int2(i1s + l, j);
+                        ++pos;
+                    }
+                base += __shfl_sync(0xffffffffu, incl, 31);
+            }
+        }
+        if (PASS == 0) {
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) count += __shfl_xor_sync(0xffffffffu, count, o);
+            if (lane == 0) g.row_count[r] = count;
+        }
+    }
+}
+
+__global__ void cap_check_kernel(int* n_edge, int cap, int* status) {
+    if (*n_edge > cap) {
+        atomicOr(status, ST_EDGE_OVERFLOW);
+        *n_edge = cap;
+    }
+}
+
+void launch_pairs(const DGraph& g, cudaStream_t st) {
+    launch_pack_positions(g, st);
+    if (g.n_rows == 0) {
+        cudaMemsetAsync(g.n_edge, 0, sizeof(int), st);
+        cudaMemsetAsync(g.row_off, 0, sizeof(int), st);
+        return;
+    }
+    int blocks = min(4 * 152, (g.n_rows * 32 + 255) / 256);
+    pair_kernel<0><<<blocks, 256, 0, st>>>(g);
+    launch_scan(g.row_count, g.row_off, g.n_rows, g.n_edge, st);
+    pair_kernel<1><<<blocks, 256, 0, st>>>(g);
+    cap_check_kernel<<<1, 1, 0, st>>>(g.n_edge, g.cap, g.status);
+}
+
+// ------------------------------------------------------ edge evaluation ---
+__device__ float quadspline(int n_ka, int n_k, float inv_dtheta, float inv_dx, const float* p, const float* x1,
+                            const float* x2, float* d1, float* d2) {
+    f3 disp = ld3(x2) - ld3(x1), r1 = ld3(x1 + 3), r2 = ld3(x2 + 3);
+    float dist2 = mag2(disp), inv_dist = rsqrtf(dist2);
+    float dc = dist2 * (inv_dist * inv_dx);
+    f3 u = disp * inv_dist;
+    float c1 = dot(r1, u), c2 = -dot(r2, u);
+    float a1v, a1d, a2v, a2d, wv, wd, nv, nd;
+    deboor(p, (c1 + 1.f) * inv_dtheta + 1.f, a1v, a1d);
+    deboor(p + n_ka, (c2 + 1.f) * inv_dtheta + 1.f, a2v, a2d);
+    clamped(p + 2 * n_ka, dc, n_k, wv, wd);
+    clamped(p + 2 * n_ka + n_k, dc, n_k, nv, nd);
+    float aw = a1v * a2v;
+    float rad = inv_dx * (wd + aw * nd);
+    float ad1 = inv_dtheta * a1d * a2v * nv;
+    float ad2 = inv_dtheta * a1v * a2d * nv;
+    f3 rXX = r1 * ad1 - r2 * ad2;
+    f3 ddir = (rXX - u * dot(u, rXX)) * inv_dist;
+    f3 dd = u * rad + ddir;
+    st3(d1, -dd);
+    st3(d1 + 3, u * ad1);
+    st3(d2, dd);
+    st3(d2 + 3, u * (-ad2));
+    return wv + aw * nv;
+}
+
+__device__ __forceinline__ bool phb_in_angle(const float* H, const float* O) {
+    f3 HO = ld3(H) - ld3(O);
+    float m2 = mag2(HO) + 1e-6f;
+    f3 rHO = HO * rsqrtf(m2);
+    return (dot(rHO, ld3(O + 3)) > 0.f) && (-dot(rHO, ld3(H + 3)) > 0.f);
+}
+
+template <int KIND>
+__device__ float edge_value(const DGraph& g, const float* p, const float* a, const float* b, float* da, float* db,
+                            bool active) {
+    if (KIND == IK_ROTAMER) return quadspline(15, 12, 6.f, 1.f / 0.7f, p, a, b, da, db);
+    if (KIND == IK_HBCOV) {
+        float cov = quadspline(15, 10, 6.f, 1.f / 0.625f, p, a, b, da, db);
+        float om = 1.f - a[6];
+        float pre = om * om;
+#pragma unroll
+        for (int i = 0; i < 6; ++i) { da[i] *= pre; db[i] *= pre; }
+        da[6] = -cov * om * 2.f;
+        return pre * cov;
+    }
+    if (KIND == IK_PHB) {
+        f3 H = ld3(a), O = ld3(b), rHN = ld3(a + 3), rOC = ld3(b + 3);
+        f3 HO = H - O;
+        float m2 = mag2(HO) + 1e-6f, inv = rsqrtf(m2), mg = m2 * inv;
+        f3 rHO = HO * inv;
+        float dHOC = dot(rHO, rOC), dOHN = -dot(rHO, rHN);
+        float hb = 0.f;
+        f3 dH = mk(0, 0, 0), drHN = mk(0, 0, 0), drOC = mk(0, 0, 0);
+        if (active) {
+            float ov, od, iv, id_, a1v, a1d, a2v, a2d;
+            logistic((p[2] - mg) * p[3], ov, od);
+            logistic((mg - p[0]) * p[1], iv, id_);
+            float rv = ov * iv, rd = -p[3] * od * iv + p[1] * id_ * ov;
+            logistic((dHOC - p[4]) * p[5], a1v, a1d);
+            a1d *= p[5];
+            logistic((dOHN - p[4]) * p[5], a2v, a2d);
+            a2d *= p[5];
+            hb = rv * a1v * a2v;
+            float c0 = rd * a1v * a2v, c1 = rv * a1d * a2v, c2 = -rv * a1v * a2d;
+            drOC = rHO * c1;
+            drHN = rHO * c2;
+            dH = rHO * c0 + (rOC - rHO * dHOC) * (c1 * inv) + (rHN + rHO * dOHN) * (c2 * inv);
+        }
+        float hb_log = (1.f <= hb) ? 100.f : -logf(1.f - hb);
+        float pre = fminf(1.f / (1.f - hb), 1e5f);
+        st3(da, dH * pre);
+        st3(da + 3, drHN * pre);
+        st3(db, dH * (-pre));
+        st3(db + 3, drOC * pre);
+        return hb_log;
+    }
+    if (KIND == IK_ENVCOV || KIND == IK_HBENV) {
+        f3 disp = ld3(b) - ld3(a), r1 = ld3(a + 3);
+        float prob = KIND == IK_ENVCOV ? b[3] : 1.f;
+        float d2 = mag2(disp), inv = rsqrtf(d2), dist = d2 * inv;
+        f3 u = disp * inv;
+        float dp = dot(u, r1), rv, rd, av, ad;
+        csig(dist - p[0], p[1], rv, rd);
+        csig(p[2] - dp, p[3], av, ad);
+        f3 dd = (u * (rd * av) - (r1 - u * dp) * (rv * ad * inv)) * prob;
+        st3(da + 3, u * (-prob * rv * ad));
+        st3(da, -dd);
+        st3(db, dd);
+        float score = rv * av;
+        if (KIND == IK_ENVCOV) {
+            db[3] = score;
+            return prob * score;
+        }
+        db[3] = db[4] = db[5] = 0.f;
+        return score;
+    }
+    return 0.f;
+}
+
+template <int KIND>
+__global__ void edge_eval_kernel(DGraph g, const int* __restrict__ edge_sys_start, const int* __restrict__ edge_sys_end) {
+    int ne = *g.n_edge;
+    int dw = g.d1 + g.d2;
+    for (int e = grid_stride_start(); e < ne; e += grid_stride()) {
+        int2 ij = g.edges[e];
+        const float* a = g.in1 + size_t(g.loc1[ij.x]) * g.w1;
+        const float* b = g.in2 + size_t(g.loc2[ij.y]) * g.w2;
+        const float* p = g.param + (size_t(g.type1[ij.x]) * g.n_type2 + g.type2[ij.y]) * g.n_param;
+        bool active = true;
+        if (KIND == IK_PHB) {
+            // lanes of a group of 4 consecutive edges of one system are
+            // evaluated together; a group with no edge inside the angular
+            // cutoff gives zero for all its edges (src/hbond.cpp:207-213)
+            int s = g.sys1[ij.x];
+            int st = edge_sys_start[s], en = edge_sys_end[s];
+            int g0 = st + ((e - st) & ~3);
+            active = false;
+            for (int k = g0; k < min(g0 + 4, en); ++k) {
+                int2 q = g.edges[k];
+                active |= phb_in_angle(g.in1 + size_t(g.loc1[q.x]) * g.w1, g.in2 + size_t(g.loc2[q.y]) * g.w2);
+            }
+        }
+        float* da = g.deriv + size_t(e) * dw;
+        g.value[e] = edge_value<KIND>(g, p, a, b, da, da + g.d1, active);
+    }
+}
+
+__global__ void edge_sys_range_kernel(DGraph g, int* start, int* end) {
+    for (int s = grid_stride_start(); s < g.n_sys; s += grid_stride()) {
+        start[s] = min(g.row_off[g.sys_first_row[s]], g.cap);
+        end[s] = min(g.row_off[g.sys_first_row[s + 1]], g.cap);
+    }
+}
+
+void launch_edge_eval(const DGraph& g, int* sys_start, int* sys_end, cudaStream_t st) {
+    int blocks = 2 * 152;
+    if (g.kind == IK_PHB) edge_sys_range_kernel<<<1, 256, 0, st>>>(g, sys_start, sys_end);
+    switch (g.kind) {
+        case IK_ROTAMER: edge_eval_kernel<IK_ROTAMER><<<blocks, 256, 0, st>>>(g, sys_start, sys_end); break;
+        case IK_HBCOV: edge_eval_kernel<IK_HBCOV><<<blocks, 256, 0, st>>>(g, sys_start, sys_end); break;
+        case IK_PHB: edge_eval_kernel<IK_PHB><<<blocks, 256, 0, st>>>(g, sys_start, sys_end); break;
+        case IK_ENVCOV: edge_eval_kernel<IK_ENVCOV><<<blocks, 256, 0, st>>>(g, sys_start, sys_end); break;
+        case IK_HBENV: edge_eval_kernel<IK_HBENV><<<blocks, 256, 0, st>>>(g, sys_start, sys_end); break;
+        default: break;
+    }
+}
+
+__global__ void edge_scatter_kernel(DGraph g) {
+    int ne = *g.n_edge;
+    int dw = g.d1 + g.d2;
+    for (int e = grid_stride_start(); e < ne; e += grid_stride()) {
+        float s = g.esens[e];
+        if (s == 0.f) continue;
+        int2 ij = g.edges[e];
+        const float* da = g.deriv + size_t(e) * dw;
+        float* s1 = g.sens1 + size_t(g.loc1[ij.x]) * g.w1;
+        float* s2 = g.sens2 + size_t(g.loc2[ij.y]) * g.w2;
+        for (int d = 0; d < g.d1; ++d) atomicAdd(s1 + d, s * da[d]);
+        for (int d = 0; d < g.d2; ++d) atomicAdd(s2 + d, s * da[g.d1 + d]);
+    }
+}
+
+void launch_edge_scatter(const DGraph& g, cudaStream_t st) {
+    edge_scatter_kernel<<<2 * 152, 256, 0, st>>>(g);
+}
+
+// dE/dparam for the quadspline graphs, accumulated per type pair with the
+// current edge sensitivities (src/interaction_graph.h:406-416, :498-550,
+// src/bead_interaction.h:87-131)
+__global__ void param_deriv_kernel(DGraph g, float* __restrict__ out) {
+    int ne = *g.n_edge;
+    for (int e = grid_stride_start(); e < ne; e += grid_stride()) {
+        float s = g.esens[e];
+        if (s == 0.f) continue;
+        int2 ij = g.edges[e];
+        const float* a = g.in1 + size_t(g.loc1[ij.x]) * g.w1;
+        const float* b = g.in2 + size_t(g.loc2[ij.y]) * g.w2;
+        int t1 = g.type1[ij.x], t2 = g.type2[ij.y];
+        const float* p = g.param + (size_t(t1) * g.n_type2 + t2) * g.n_param;
+        int n_ka = 15, n_k = g.kind == IK_ROTAMER ? 12 : 10;
+        float inv_dx = g.kind == IK_ROTAMER ? 1.f / 0.7f : 1.f / 0.625f;
+        float pre = 1.f;
+        if (g.kind == IK_HBCOV) pre = (1.f - a[6]) * (1.f - a[6]);
+        f3 disp = ld3(b) - ld3(a), r1 = ld3(a + 3), r2 = ld3(b + 3);
+        float dist2 = mag2(disp), inv_dist = rsqrtf(dist2);
+        float dc = dist2 * (inv_dist * inv_dx);
+        f3 u = disp * inv_dist;
+        float x1s = (dot(r1, u) + 1.f) * 6.f + 1.f, x2s = (-dot(r2, u) + 1.f) * 6.f + 1.f;
+        float a1v, a1d, a2v, a2d, nv, nd, r[4];
+        deboor(p, x1s, a1v, a1d);
+        deboor(p + n_ka, x2s, a2v, a2d);
+        clamped(p + 2 * n_ka + n_k, dc, n_k, nv, nd);
+        float w = s * pre;
+        float* o1 = out + (size_t(t1) * g.n_type2 + t2) * g.n_param;
+        float* o2 = out + (size_t(t2) * g.n_type1 + t1) * g.n_param;
+        int sb = clamped_coeff_deriv(dc, n_k, r);
+        for (int i = 0; i < 4; ++i) {
+            atomicAdd(o1 + 2 * n_ka + sb + i, w * r[i]);
+            atomicAdd(o1 + 2 * n_ka + n_k + sb + i, w * a1v * a2v * r[i]);
+            if (g.symmetric) {
+                atomicAdd(o2 + 2 * n_ka + sb + i, w * r[i]);
+                atomicAdd(o2 + 2 * n_ka + n_k + sb + i, w * a1v * a2v * r[i]);
+            }
+        }
+        sb = coeff_deriv(x1s, r);
+        for (int i = 0; i < 4; ++i) {
+            atomicAdd(o1 + sb + i, w * a2v * nv * r[i]);
+            if (g.symmetric) atomicAdd(o2 + sb + i, w * a2v * nv * r[i]);
+        }
+        sb = coeff_deriv(x2s, r);
+        for (int i = 0; i < 4; ++i) {
+            atomicAdd(o1 + n_ka + sb + i, w * a1v * nv * r[i]);
+            if (g.symmetric) atomicAdd(o2 + n_ka + sb + i, w * a1v * nv * r[i]);
+        }
+    }
+}
+
+void launch_param_deriv(const DGraph& g, float* out, cudaStream_t st) {
+    param_deriv_kernel<<<2 * 152, 256, 0, st>>>(g, out);
+}
+
+// ------------------------------------------------------------ rotamer BP ---
+__device__ __forceinline__ long long slot_index(const DBP& b, int r1, int r2) {
+    int s = b.res_sys[r1];
+    return b.slot_off[s] + (long long)b.res_local[r1] * b.res_N[r1] + b.res_local[r2];
+}
+
+// reset the residue-pair map entries of the previous evaluation and the
+// per-residue accumulators
+__global__ void bp_reset_kernel(DBP b) {
+    int prev_n_ent = min(*b.n_ent, b.ent_cap);  // entries of the previous evaluation
+    for (int e = grid_stride_start(); e < prev_n_ent; e += grid_stride())
+        b.slot[slot_index(b, b.erow[e], b.col[e])] = -1;
+    for (int r = grid_stride_start(); r < b.n_res * 8; r += grid_stride()) {
+        b.E1[r] = 0.f;
+        b.E1x[r] = 0.f;
+    }
+    for (int s = grid_stride_start(); s < b.n_sys; s += grid_stride()) b.e11[s] = 0.0;
+}
+
+// 1-body energy per (residue, rotamer) from up to 4 input nodes (src/rotamer.cpp:862-884)
+__global__ void bp_bead_energy_kernel(DBP b, const float* p0, const float* p1, const float* p2, const float* p3,
+                                      int n_in, int w0, int w1, int w2, int w3) {
+    for (int i = grid_stride_start(); i < b.n_bead; i += grid_stride()) {
+        int l = b.bead_loc[i];
+        float e = p0[size_t(l) * w0];
+        if (n_in > 1) e += p1[size_t(l) * w1];
+        if (n_in > 2) e += p2[size_t(l) * w2];
+        if (n_in > 3) e += p3[size_t(l) * w3];
+        atomicAdd(&b.E1[b.bead_res[i] * 8 + b.bead_rot[i]], e);
+    }
+}
+
+// classify bead edges: mark multi-rotamer residue pairs; fold 1-rotamer
+// partners into node energies; sum 1-1 edges (src/rotamer.cpp:886-912)
+__global__ void bp_mark_kernel(DBP b, DGraph g) {
+    int ne = *g.n_edge;
+    for (int e = grid_stride_start(); e < ne; e += grid_stride()) {
+        int2 ij = g.edges[e];
+        int r1 = b.bead_res[ij.x], r2 = b.bead_res[ij.y];
+        int n1 = b.nrot[r1], n2 = b.nrot[r2];
+        float v = g.value[e];
+        if (n1 > 1 && n2 > 1) {
+            b.slot[slot_index(b, r1, r2)] = -2;
+            b.slot[slot_index(b, r2, r1)] = -2;
+        } else if (n1 == 1 && n2 == 1) {
+            atomicAdd(&b.e11[b.res_sys[r1]], double(v));
+        } else if (n1 == 1) {
+            atomicAdd(&b.E1x[r2 * 8 + b.bead_rot[ij.y]], v);
+        } else {
+            atomicAdd(&b.E1x[r1 * 8 + b.bead_rot[ij.x]], v);
+        }
+    }
+}
+
+// warp per residue row of the dense map: count (PASS 0) or emit (PASS 1) the
+// marked neighbours in increasing order
+template <int PASS>
+__global__ void bp_rows_kernel(DBP b) {
+    int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    int lane = threadIdx.x & 31;
+    int n_warps = (gridDim.x * blockDim.x) >> 5;
+    for (int r = warp; r < b.n_res; r += n_warps) {
+        int N = b.res_N[r];
+        int s = b.res_sys[r];
+        int rbase = b.res_off[s];
+        long long row = b.slot_off[s] + (long long)b.res_local[r] * N;
+        int pos = PASS ? b.row_ptr[r] : 0;
+        int cnt = 0;
+        for (int c0 = 0; c0 < N; c0 += 32) {
+            int c = c0 + lane;
+            bool hit = c < N && b.slot[row + c] == -2;
+            unsigned m = __ballot_sync(0xffffffffu, hit);
+            if (PASS == 0) {
+                cnt += __popc(m);
+            } else {
+                if (hit) {
+                    int p = pos + __popc(m & ((1u << lane) - 1u));
+                    if (p < b.ent_cap) {
+                        b.col[p] = rbase + c;
+                        b.erow[p] = r;
+                        b.slot[row + c] = p;
+                    } else {
+                        b.slot[row + c] = -1;
+                    }
+                }
+                pos += __popc(m);
+            }
+        }
+        if (PASS == 0 && lane == 0) b.row_count[r] = cnt;
+    }
+}
+
+__global__ void bp_entry_init_kernel(DBP b) {
+    int n = min(*b.n_ent, b.ent_cap);
+    for (int e = grid_stride_start(); e < n; e += grid_stride()) {
+        int rv = b.slot[slot_index(b, b.col[e], b.erow[e])];
+        if (rv < 0) {  // partner entry lost to overflow: point at itself, flag it
+            atomicOr(b.status, ST_RES_EDGE_OVERFLOW);
+            rv = e;
+        }
+        b.rev[e] = rv;
+    }
+    for (int i = grid_stride_start(); i < n * 36; i += grid_stride()) b.esum[i] = 0.f;
+}
+
+__global__ void bp_cap_check_kernel(DBP b) {
+    if (*b.n_ent > b.ent_cap) {
+        atomicOr(b.status, ST_RES_EDGE_OVERFLOW);
+        *b.n_ent = b.ent_cap;
+    }
+}
+
+__global__ void bp_edge_energy_kernel(DBP b, DGraph g) {
+    int ne = *g.n_edge;
+    for (int e = grid_stride_start(); e < ne; e += grid_stride()) {
+        int2 ij = g.edges[e];
+        int r1 = b.bead_res[ij.x], r2 = b.bead_res[ij.y];
+        if (b.nrot[r1] == 1 || b.nrot[r2] == 1) continue;
+        int e12 = b.slot[slot_index(b, r1, r2)], e21 = b.slot[slot_index(b, r2, r1)];
+        if (e12 < 0 || e21 < 0) continue;
+        int k1 = b.bead_rot[ij.x], k2 = b.bead_rot[ij.y];
+        float v = g.value[e];
+        atomicAdd(&b.esum[size_t(e12) * 36 + k1 * 6 + k2], v);
+        atomicAdd(&b.esum[size_t(e21) * 36 + k2 * 6 + k1], v);
+    }
+}
+
+// node probabilities (src/rotamer.cpp:239-256, :398-405) and edge matrices
+__global__ void bp_prob_kernel(DBP b) {
+    for (int r = grid_stride_start(); r < b.n_res; r += grid_stride()) {
+        int n = b.nrot[r];
+        float m = b.E1[r * 8];
+        for (int k = 1; k < n; ++k) m = fminf(m, b.E1[r * 8 + k]);
+        for (int k = 0; k < 8; ++k)
+            b.prob[r * 8 + k] = k < n ? expf(m - b.E1[r * 8 + k]) * expf(-b.E1x[r * 8 + k]) : 0.f;
+        b.eoff[r] = m;
+    }
+    int n_ent = *b.n_ent;
+    for (int i = grid_stride_start(); i < n_ent * 36; i += grid_stride()) {
+        int e = i / 36, k = i - e * 36;
+        int a = k / 6, c = k - a * 6;
+        b.P[i] = (a < b.nrot[b.erow[e]] && c < b.nrot[b.col[e]]) ? expf(-b.esum[i]) : 0.f;
+    }
+}
+
+// One block per system: damped loopy BP to convergence, then marginals and
+// (optionally) the Bethe free energy.  The iteration structure (undamped
+// first sweep with swap, chunks of `chunk` damped sweeps, one-sided maximum
+// deviation test) follows src/rotamer.cpp:1106-1162.
+__global__ void __launch_bounds__(1024) bp_solve_kernel(DBP b, int want_energy, double* energy_out) {
+    __shared__ float red[32];
+    __shared__ double dred[32];
+    int s = blockIdx.x;
+    int r0 = b.res_off[s], r1 = b.res_off[s + 1];
+    int e0 = b.row_ptr[r0], e1 = min(b.row_ptr[r1], b.ent_cap);
+    float* NB[2] = {b.belief, b.belief + size_t(b.n_res) * 8};
+    float* EM[2] = {b.msg, b.msg + size_t(b.ent_cap) * 8};
+    const int tid = threadIdx.x, nt = blockDim.x;
+
+    auto edge_phase = [&](const float* Nold, const float* Eold, float* Ecur) {
+        for (int e = e0 + tid; e < e1; e += nt) {
+            int u = b.erow[e], v = b.col[e];
+            int nu = b.nrot[u], nv = b.nrot[v];
+            const float* ob = Nold + v * 8;
+            const float* om = Eold + b.rev[e] * 8;
+            float v2[6];
+#pragma unroll
+            for (int j = 0; j < 6; ++j) v2[j] = j < nv ? ob[j] / (1e-10f + om[j]) : 0.f;
+            const float* P = b.P + size_t(e) * 36;
+            float m[6], sum = 0.f;
+#pragma unroll
+            for (int i = 0; i < 6; ++i) {
+                float acc = 0.f;
+#pragma unroll
+                for (int j = 0; j < 6; ++j) acc += P[i * 6 + j] * v2[j];
+                m[i] = i < nu ? acc : 0.f;
+                sum += m[i];
+            }
+            float inv = 1.f / sum;
+#pragma unroll
+            for (int i = 0; i < 6; ++i) Ecur[e * 8 + i] = m[i] * inv;
+        }
+    };
+    // product of prob and incoming messages, renormalised after each factor;
+    // then (mode 1) damped max-normalisation against Nold, returning the
+    // largest increase over Nold
+    auto node_phase = [&](const float* Ecur, float* Ncur, const float* Nold, int mode, float damp) -> float {
+        float dev = 0.f;
+        for (int u = r0 + tid; u < r1; u += nt) {
+            int n = b.nrot[u];
+            if (n == 1) continue;
+            float bl[6];
+#pragma unroll
+            for (int k = 0; k < 6; ++k) bl[k] = k < n ? b.prob[u * 8 + k] : 0.f;
+            for (int e = b.row_ptr[u]; e < min(b.row_ptr[u + 1], e1); ++e) {
+                float sum = 0.f;
+#pragma unroll
+                for (int k = 0; k < 6; ++k) {
+                    bl[k] *= Ecur[e * 8 + k];
+                    sum += bl[k];
+                }
+                float inv = 1.f / sum;
+#pragma unroll
+                for (int k = 0; k < 6; ++k) bl[k] *= inv;
+            }
+            if (mode == 1) {
+                float mx = bl[0];
+                for (int k = 1; k < n; ++k) mx = fmaxf(mx, bl[k]);
+                float inv = 1.f / mx;
+#pragma unroll
+                for (int k = 0; k < 6; ++k) {
+                    float o = Nold[u * 8 + k];
+                    bl[k] = damp != 0.f ? (1.f - damp) * inv * bl[k] + damp * o : inv * bl[k];
+                    if (k < n) dev = fmaxf(dev, bl[k] - o);
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < 6; ++k) Ncur[u * 8 + k] = bl[k];
+        }
+        return dev;
+    };
+    auto block_max = [&](float v) -> float {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+        if ((tid & 31) == 0) red[tid >> 5] = v;
+        __syncthreads();
+        float r = -1e30f;
+        for (int w = 0; w < (nt + 31) / 32; ++w) r = fmaxf(r, red[w]);
+        __syncthreads();
+        return r;
+    };
+
+    // initial state: N.old = prob, E.old = 1
+    for (int u = r0 + tid; u < r1; u += nt)
+        for (int k = 0; k < 8; ++k) {
+            NB[1][u * 8 + k] = b.prob[u * 8 + k];
+            NB[0][u * 8 + k] = b.prob[u * 8 + k];
+        }
+    for (int e = e0 + tid; e < e1; e += nt)
+        for (int k = 0; k < 8; ++k) EM[1][e * 8 + k] = 1.f;
+    __syncthreads();
+    // first sweep, undamped, with the swap of the initial beliefs
+    edge_phase(NB[1], EM[1], EM[0]);
+    __syncthreads();
+    node_phase(EM[0], NB[0], NB[1], 0, 0.f);
+    __syncthreads();
+    for (int u = r0 + tid; u < r1; u += nt) {
+        int n = b.nrot[u];
+        if (n == 1) continue;
+        float mx = NB[1][u * 8];
+        for (int k = 1; k < n; ++k) mx = fmaxf(mx, NB[1][u * 8 + k]);
+        float inv = 1.f / mx;
+        for (int k = 0; k < 6; ++k) NB[1][u * 8 + k] *= inv;
+    }
+    __syncthreads();
+    int nc = 1, ec = 0;
+    float dev = 1e10f;
+    int iter = 0;
+    for (; dev > b.tol && iter < b.max_iter; iter += b.chunk) {
+        float d = 0.f;
+        for (int j = 0; j < b.chunk; ++j) {
+            nc ^= 1;
+            ec ^= 1;
+            edge_phase(NB[nc ^ 1], EM[ec ^ 1], EM[ec]);
+            __syncthreads();
+            d = node_phase(EM[ec], NB[nc], NB[nc ^ 1], 1, b.damping);
+            __syncthreads();
+        }
+        dev = block_max(d);
+        dev = fmaxf(dev, 0.f);
+    }
+    if (tid == 0) {
+        b.n_iter[s] = iter;
+        if (iter >= b.max_iter - b.chunk - 1) atomicOr(b.status, ST_BP_NOT_CONVERGED);
+    }
+    // node marginals (src/rotamer.cpp:283-290)
+    const float* Nf = NB[nc];
+    for (int u = r0 + tid; u < r1; u += nt) {
+        int n = b.nrot[u];
+        if (n == 1) {
+            b.marg[u * 8] = 1.f;
+            for (int k = 1; k < 8; ++k) b.marg[u * 8 + k] = 0.f;
+            continue;
+        }
+        float sum = 0.f;
+        for (int k = 0; k < n; ++k) sum += Nf[u * 8 + k];
+        float inv = 1.f / sum;
+        for (int k = 0; k < 8; ++k) b.marg[u * 8 + k] = k < n ? Nf[u * 8 + k] * inv : 0.f;
+    }
+    __syncthreads();
+    // edge marginals (src/rotamer.cpp:425-449)
+    const float* Ef = EM[ec];
+    for (int e = e0 + tid; e < e1; e += nt) {
+        int u = b.erow[e], v = b.col[e];
+        int nu = b.nrot[u], nv = b.nrot[v];
+        const float* mu = Ef + e * 8;
+        const float* mv = Ef + b.rev[e] * 8;
+        float bu[6], bv[6];
+        for (int i = 0; i < 6; ++i) bu[i] = i < nu ? b.marg[u * 8 + i] / (1e-10f + mu[i]) : 0.f;
+        for (int j = 0; j < 6; ++j) bv[j] = j < nv ? b.marg[v * 8 + j] / (1e-10f + mv[j]) : 0.f;
+        const float* P = b.P + size_t(e) * 36;
+        float* mg = b.emarg + size_t(e) * 36;
+        float sum = 0.f;
+        for (int i = 0; i < 6; ++i)
+            for (int j = 0; j < 6; ++j) {
+                float x = P[i * 6 + j] * bu[i] * bv[j];
+                mg[i * 6 + j] = x;
+                sum += x;
+            }
+        float inv = 1.f / sum;
+        for (int k = 0; k < 36; ++k) mg[k] *= inv;
+    }
+    if (!want_energy) return;
+    __syncthreads();
+    // Bethe free energy (src/rotamer.cpp:292-302, :451-471, :915-927)
+    double en = 0.0;
+    for (int u = r0 + tid; u < r1; u += nt) {
+        int n = b.nrot[u];
+        float f = b.eoff[u];
+        for (int k = 0; k < n; ++k) {
+            float bk = b.marg[u * 8 + k];
+            f += bk * logf((1e-10f + bk) / (1e-10f + b.prob[u * 8 + k]));
+        }
+        en += double(f);
+    }
+    for (int e = e0 + tid; e < e1; e += nt) {
+        int u = b.erow[e], v = b.col[e];
+        if (!(u < v)) continue;
+        int nu = b.nrot[u], nv = b.nrot[v];
+        const float* p = b.emarg + size_t(e) * 36;
+        const float* P = b.P + size_t(e) * 36;
+        float f = 0.f;
+        for (int i = 0; i < nu; ++i)
+            for (int j = 0; j < nv; ++j) {
+                float x = p[i * 6 + j];
+                f += x * logf((1e-10f + x) / (1e-10f + P[i * 6 + j] * b.marg[u * 8 + i] * b.marg[v * 8 + j]));
+            }
+        en += double(f);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) en += __shfl_xor_sync(0xffffffffu, en, o);
+    if ((tid & 31) == 0) dred[tid >> 5] = en;
+    __syncthreads();
+    if (tid == 0) {
+        double t = b.e11[s];
+        for (int w = 0; w < (nt + 31) / 32; ++w) t += dred[w];
+        energy_out[s] = t;
+    }
+}
+
+// bead-edge sensitivities from the marginals and 1-body sensitivities
+// (src/rotamer.cpp:1057-1086)
+__global__ void bp_sens_kernel(DBP b, DGraph g, float* s0, float* s1, float* s2, float* s3, int n_in, int w0,
+                               int w1, int w2, int w3) {
+    int ne = *g.n_edge;
+    for (int e = grid_stride_start(); e < ne; e += grid_stride()) {
+        int2 ij = g.edges[e];
+        int r1 = b.bead_res[ij.x], r2 = b.bead_res[ij.y];
+        int n1 = b.nrot[r1], n2 = b.nrot[r2];
+        int k1 = b.bead_rot[ij.x], k2 = b.bead_rot[ij.y];
+        float s;
+        if (n1 == 1 && n2 == 1) s = 1.f;
+        else if (n1 == 1) s = b.marg[r2 * 8 + k2];
+        else if (n2 == 1) s = b.marg[r1 * 8 + k1];
+        else {
+            int en = b.slot[slot_index(b, r1, r2)];
+            s = en >= 0 ? b.emarg[size_t(en) * 36 + k1 * 6 + k2] : 0.f;
+        }
+        g.esens[e] = s;
+    }
+    for (int i = grid_stride_start(); i < b.n_bead; i += grid_stride()) {
+        float m = b.marg[b.bead_res[i] * 8 + b.bead_rot[i]];
+        int l = b.bead_loc[i];
+        atomicAdd(s0 + size_t(l) * w0, m);
+        if (n_in > 1) atomicAdd(s1 + size_t(l) * w1, m);
+        if (n_in > 2) atomicAdd(s2 + size_t(l) * w2, m);
+        if (n_in > 3) atomicAdd(s3 + size_t(l) * w3, m);
+    }
+}
+
+void launch_bp(DBP& b, const DGraph& g, const float* const* in, float* const* in_sens, const int* w, int n_in,
+               int prev_n_ent, int* scan_total, int want_energy, double* energy_out, cudaStream_t st) {
+    int blocks = 2 * 152;
+    // one block: the reset must finish reading n_ent before anything rewrites it
+    bp_reset_kernel<<<1, 1024, 0, st>>>(b);
+    (void)prev_n_ent;
+    bp_bead_energy_kernel<<<blocks, 256, 0, st>>>(b, in[0], in[1], in[2], in[3], n_in, w[0], w[1], w[2], w[3]);
+    bp_mark_kernel<<<blocks, 256, 0, st>>>(b, g);
+    int rb = min(4 * 152, (b.n_res * 32 + 255) / 256);
+    bp_rows_kernel<0><<<rb, 256, 0, st>>>(b);
+    launch_scan(b.row_count, b.row_ptr, b.n_res, b.n_ent, st);
+    bp_rows_kernel<1><<<rb, 256, 0, st>>>(b);
+    bp_cap_check_kernel<<<1, 1, 0, st>>>(b);
+    bp_entry_init_kernel<<<blocks, 256, 0, st>>>(b);
+    bp_edge_energy_kernel<<<blocks, 256, 0, st>>>(b, g);
+    bp_prob_kernel<<<blocks, 256, 0, st>>>(b);
+    bp_solve_kernel<<<b.n_sys, 1024, 0, st>>>(b, want_energy, energy_out);
+    bp_sens_kernel<<<blocks, 256, 0, st>>>(b, g, in_sens[0], in_sens[1], in_sens[2], in_sens[3], n_in, w[0], w[1],
+                                           w[2], w[3]);
+    (void)scan_total;
+}
+
+}  // namespace ug

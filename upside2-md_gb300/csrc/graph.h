@@ -1,0 +1,114 @@
+// Plain structs shared by the host engine (engine.cu) and the sm_103a kernels
+// (graph.cu, nodes.cu).  All pointers are device pointers.  Arrays are flattened over
+// the batch: every system's elements are concatenated and all stored indices
+// are global (already offset by the owning system's start).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace ug {
+
+// status bits written by kernels into Engine::d_status
+enum StatusBits : int {
+    ST_EDGE_OVERFLOW = 1,   // a pair list exceeded its capacity
+    ST_BP_NOT_CONVERGED = 2,  // a BP solve hit max_iter
+    ST_RES_EDGE_OVERFLOW = 4, // residue-pair edge storage exceeded
+};
+
+enum IKind : int { IK_ROTAMER = 0, IK_HBCOV = 1, IK_PHB = 2, IK_ENVCOV = 3, IK_HBENV = 4, IK_BACKBONE = 5 };
+enum Excl : int { EX_ROTAMER = 0, EX_SEQ1 = 1, EX_SEQ2 = 2 };
+
+// Pair list + per-edge values for one interaction graph over the whole batch.
+struct DGraph {
+    int kind, excl, symmetric;
+    int d1, d2, n_param, n_type1, n_type2;
+    float cutoff;
+    // element sets (set2 == set1 when symmetric)
+    int n1, n2;                 // total elements over the batch
+    const int* loc1;            // element -> row in the arg node output
+    const int* loc2;
+    const int* type1;
+    const int* type2;
+    const int* id1;
+    const int* id2;
+    const int* sys1;            // element -> system
+    const float* param;         // (n_type1*n_type2, n_param)
+    int w1, w2;                 // row widths of the arg node outputs
+    const float* in1;           // arg node outputs
+    const float* in2;
+    float* sens1;               // arg node sensitivities
+    float* sens2;
+    // pair search rows: one row = one block of 4 set-1 elements of one system
+    int n_rows;
+    const int* row_i1;          // first set-1 element of the row
+    const int* row_i1_end;      // end of the system's set-1 range
+    const int* row_i2;          // first candidate set-2 element
+    const int* row_i2_end;      // end of the system's set-2 range
+    int* row_count;
+    int* row_off;               // exclusive scan of row_count (n_rows+1)
+    const int* sys_first_row;   // per system: first row (n_sys+1)
+    int n_sys;
+    // edges
+    int cap;
+    int2* edges;                // (i1, i2) set indices
+    int* n_edge;                // device scalar
+    float* value;
+    float* deriv;               // cap * (d1+d2)
+    float* esens;
+    float4* x1;                 // packed positions (xyz) of set 1 for the search
+    float4* x2;
+    int* status;
+};
+
+// One system-batched rotamer belief-propagation problem.
+struct DBP {
+    int n_sys;
+    int n_res;                  // residues over the batch
+    const int* res_off;         // per system residue start (n_sys+1)
+    const int* nrot;            // residue -> 1, 3 or 6
+    const int* res_N;           // residue -> number of residues of its system
+    const int* res_sys;         // residue -> system
+    const int* res_local;       // residue -> index within its system
+    const long long* slot_off;  // per system offset into the dense slot map
+    int* slot;                  // dense (N_s x N_s) residue-pair map, -1 = none
+    int* row_count;             // per residue number of neighbours
+    int* row_ptr;               // n_res+1
+    int* col;                   // entry -> neighbour residue (global)
+    int* erow;                  // entry -> row residue
+    int* rev;                   // entry -> reverse entry
+    int ent_cap;
+    int* n_ent;
+    float* esum;                // entry * 36: summed bead energies (row rot, col rot)
+    float* P;                   // entry * 36: exp(-esum)
+    float* msg;                 // 2 * ent_cap * 8
+    float* emarg;               // entry * 36
+    float* E1;                  // res * 8: 1-body energy per rotamer
+    float* E1x;                 // res * 8: folded 1-rotamer-partner edge energies
+    float* prob;                // res * 8
+    float* eoff;                // res
+    float* belief;              // 2 * n_res * 8
+    float* marg;                // res * 8
+    int* n_iter;                // per system
+    float damping, tol;
+    int max_iter, chunk;
+    // bead level
+    int n_bead;
+    const int* bead_res;        // bead -> residue (global)
+    const int* bead_rot;        // bead -> rotamer
+    const int* bead_loc;        // bead -> row in the bead node output
+    double* e11;                // per system sum of energies of 1-1 bead edges
+    int* status;
+};
+
+// --------------------------------------------------------------- launchers --
+void launch_scan(const int* in, int* out, int n, int* total_out, cudaStream_t st);
+void launch_pack_positions(const DGraph& g, cudaStream_t st);
+void launch_pairs(const DGraph& g, cudaStream_t st);
+void launch_edge_eval(const DGraph& g, int* sys_start, int* sys_end, cudaStream_t st);
+void launch_edge_scatter(const DGraph& g, cudaStream_t st);
+void launch_param_deriv(const DGraph& g, float* out, cudaStream_t st);
+// in: up to 4 one-body energy inputs (bead rows), in_sens their sensitivities
+void launch_bp(DBP& b, const DGraph& g, const float* const* in, float* const* in_sens, const int* w, int n_in,
+               int prev_n_ent, int* scan_total, int want_energy, double* energy_out, cudaStream_t st);
+
+}  // namespace ug
