@@ -1,0 +1,262 @@
+"""Benchmark: residue-steps/s of the batched GB300 Upside engine.
+
+python bench.py [--gpus N] [--steps K] [--warmup W] [--workload C4] [--impl gpu|reference]
+
+A step is the reference's unit: one force evaluation plus one integrator
+stage (src/main.cpp:1009-1012); a timed iteration is one integration round of
+the whole batch (thermostat + 3 x {force, p -= dt F, x += dt p}), i.e. 3 steps
+for every system.  residue-steps/s = sum over systems of residues x 3 x rounds
+/ time.  The default workload is C4 (64 chains, lengths uniform in [40,400]).
+
+Multi-GPU: one process per GPU (torchrun); each rank advances its own batch of
+independently seeded systems ("replicas only", weak scaling); ranks only meet
+for a barrier and the max-over-ranks timing reduction.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "upside2-md_gb300"))
+
+METRIC = "residue-steps/s on 1 GB300: batched+learned-BP vs plain GPU at same force error"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--workload", default="C4")
+    ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile", action="store_true", help="print per-node device times to stderr")
+    return ap.parse_args()
+
+
+class Dist:
+    def __init__(self):
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as dist
+            dist.init_process_group("gloo")
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, x):
+        if not self.pg:
+            return x
+        import torch
+        t = torch.tensor([float(x)], dtype=torch.float64)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, x):
+        if not self.pg:
+            return x
+        import torch
+        t = torch.tensor([float(x)], dtype=torch.float64)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.SUM)
+        return float(t.item())
+
+
+class Clocks:
+    """nvidia-smi samples every 200 ms while the timed region runs."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.rows = []
+        self.proc = None
+        self.gpu = gpu_index
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=2)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            try:
+                sm.append(float(r[1]))
+                mx.append(float(r[2]))
+                for k, nm in enumerate(names):
+                    if r[5 + k].lower().startswith("active"):
+                        reasons.add(nm)
+            except Exception:
+                pass
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return p["hbm_gbs"], "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+# ------------------------------------------------------------ CPU oracle ---
+def _cpu_worker(args):
+    path, n_atom, seconds, seed = args
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    sys.path.insert(0, os.path.join(ROOT, "upside2-md_gb300"))
+    import numpy as np
+    import oracle_py
+    from h5lite import H5File
+    with H5File(path) as f:
+        pos = f.read("/input/pos")[:, :, 0].astype(np.float32)
+    o = oracle_py.Oracle(path, n_atom)
+    mom = np.zeros_like(pos)
+    t0 = time.perf_counter()
+    rounds = 0
+    while time.perf_counter() - t0 < seconds:
+        pos, mom = o.run(pos, mom, 1, seed=seed, round_start=rounds)
+        rounds += 1
+    return rounds, time.perf_counter() - t0, n_atom // 3
+
+
+def cpu_port_rate(configs, seconds, max_procs=None):
+    """Oracle port (the CPU restatement) timed on the host cores: one process
+    per system (the reference parallelises across systems only), each running
+    whole integration rounds for `seconds`.  Returns (residue-steps/s, cores, sample)."""
+    import multiprocessing as mp
+    from workloads import n_res_of
+    procs = min(len(configs), max_procs or os.cpu_count() or 1)
+    jobs = [(configs[i], 3 * n_res_of(configs[i]), seconds, 1 + i) for i in range(procs)]
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(procs) as pool:
+        res = pool.map(_cpu_worker, jobs)
+    rate = sum(r * 3 * n / t for r, t, n in res)
+    sample = "%d systems (%s residues), %.0f s of whole integration rounds each, %d rounds total" % (
+        procs, ",".join(str(n) for _, _, n in res[:8]) + ("..." if procs > 8 else ""), seconds,
+        sum(r for r, _, _ in res))
+    return rate, procs, sample
+
+
+# ----------------------------------------------------------------- main ---
+def main():
+    a = parse()
+    d = Dist()
+    if a.gpus != d.world and d.world > 1:
+        print("warning: --gpus %d but WORLD_SIZE %d" % (a.gpus, d.world), file=sys.stderr)
+    import numpy as np
+    import workloads
+
+    W = workloads.workload(a.workload, seed=1 + d.rank)
+    n_res_total = sum(W["n_res"])
+
+    if a.impl == "reference":
+        if d.rank != 0:
+            return
+        rate, cores, sample = cpu_port_rate(W["configs"], a.cpu_seconds)
+        line = {"impl": "reference", "metric": METRIC, "value": rate, "unit": "residue-steps/s",
+                "n_gpus": a.gpus, "steps": a.steps, "warmup": a.warmup,
+                "ms_per_step": 1e3 * n_res_total * 3 / rate, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded ff_2.1 proteins)",
+                "config": {"workload": a.workload, "systems": len(W["configs"]), "residues": n_res_total},
+                "cpu_baseline": {"value": rate, "unit": "residue-steps/s", "cores": cores, "kind": "port",
+                                 "sample": sample},
+                "e2e": {"value": rate, "unit": "residue-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    import upside_gb300 as U
+    U.lib().ug_set_device(d.local)
+    b = U.Batch(W["configs"])
+    b.set_pos(workloads.initial_positions(W["configs"]))
+    b.set_thermostat(W["temps"], np.array(W["seeds"], np.uint32))
+    b.run(a.warmup, use_graph=True, graph_rounds=1)
+    launches, dev_bytes = b.info()
+    if a.profile:
+        for nm, ms in sorted(b.profile(5), key=lambda x: -x[1])[:25]:
+            print("%-48s %8.3f ms" % (nm, ms), file=sys.stderr)
+    d.barrier()
+    with Clocks(d.local) as clk:
+        ms = b.bench(a.steps, flush_l2=True)
+    d.barrier()
+    t_dev = d.max(float(ms.sum()) / 1e3)
+    units = d.sum(n_res_total * 3 * a.steps)
+    value = units / t_dev
+    # end to end: the same rounds with the state round-tripped through pinned host memory
+    ms_e2e = b.bench(a.steps, flush_l2=True, e2e=True)
+    t_e2e = d.max(float(ms_e2e.sum()) / 1e3)
+    e2e_value = units / t_e2e
+    st = b.status()
+    cpu = None
+    if d.rank == 0 and d.world == 1 and not a.no_cpu_baseline:
+        rate, cores, sample = cpu_port_rate(W["configs"], a.cpu_seconds)
+        cpu = {"value": rate, "unit": "residue-steps/s", "cores": cores, "kind": "port", "sample": sample}
+    peak, peak_kind = measured_peaks()
+    roof = roofline(b, W, a, peak, peak_kind)
+    if d.rank != 0:
+        return
+    state_bytes = 2 * 12 * b.atom_total
+    line = {
+        "metric": METRIC, "value": value, "unit": "residue-steps/s", "n_gpus": d.world, "steps": a.steps,
+        "warmup": a.warmup, "ms_per_step": 1e3 * t_dev / a.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded ff_2.1 proteins, random initial chains)",
+        "config": {"workload": a.workload, "systems": len(W["configs"]), "residues": n_res_total,
+                   "step": "one integration round = 3 force evaluations + integrator stages per system",
+                   "l2": "256 MiB buffer rewritten before every timed round", "bp_init": "uniform messages"},
+        "e2e": {"value": e2e_value, "unit": "residue-steps/s", "h2d_bytes_per_step": state_bytes,
+                "d2h_bytes_per_step": state_bytes},
+        "gpu_launches": int(a.steps * (3 * launches + 5)),
+        "clocks": clk.summary(),
+        "roofline": roof,
+        "cpu_baseline": cpu,
+        "status_bits": st,
+        "device_bytes": dev_bytes,
+    }
+    print(json.dumps(line))
+
+
+def roofline(b, W, a, peak, peak_kind):
+    """Dominant kernel against the HBM roofline (filled in by kernel_roofline)."""
+    try:
+        from roofline import kernel_roofline
+        return kernel_roofline(b, W, peak, peak_kind)
+    except Exception as ex:  # reported, never silently dropped
+        return {"error": str(ex)}
+
+
+if __name__ == "__main__":
+    main()

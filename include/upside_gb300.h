@@ -20,6 +20,9 @@ typedef struct UgBatch UgBatch;
 
 const char* ug_last_error(void);
 
+/* Select the CUDA device used by engines created afterwards on this thread. */
+int ug_set_device(int device);
+
 /* Build one engine over n_sys `.up` files (identical node graphs). */
 UgBatch* ug_create(int n_sys, const char* const* paths, const int* n_atom);
 void ug_free(UgBatch* b);
@@ -64,6 +67,20 @@ int ug_replica_exchange(UgBatch* b, int n_pairs, const int* pairs, uint32_t seed
 int ug_status(UgBatch* b, int clear);
 /* kernel launches per force evaluation and device bytes held */
 int ug_info(UgBatch* b, int* launches_per_eval, int64_t* device_bytes);
+
+/* Timed integration rounds for benchmarking: n_round replays of a captured
+ * one-round CUDA graph, each bracketed by CUDA events on the engine stream;
+ * with flush_l2 a 256 MiB buffer is rewritten before every round (outside
+ * the events) so no round starts with a warm L2.  ms[n_round] receives the
+ * device time of each round.  With e2e != 0 each timed region also holds the
+ * host->device copy of positions and momenta from pinned host memory and the
+ * device->host copy of them back (the state a caller round-trips per round). */
+int ug_bench(UgBatch* b, int n_round, float dt, float timescale, int flush_l2, int e2e, float* ms);
+
+/* Per-node device time of n_eval eager force evaluations (CUDA events on the
+ * engine stream): names '\n'-separated "<node>:fwd" / "<node>:bwd", ms[k] the
+ * mean time of entry k.  Returns the number of entries (or -1). */
+int ug_profile(UgBatch* b, int n_eval, char* names, int names_cap, float* ms, int cap);
 
 #ifdef __cplusplus
 }

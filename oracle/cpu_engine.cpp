@@ -2155,3 +2155,7 @@ void ocpu_thermostat_normals(uint32_t seed, uint64_t invocation, int n_atom, flo
 }
 
 }  // extern "C"
+
+extern "C" void ocpu_threefry4x32(const uint32_t* ctr, const uint32_t* key, uint32_t* out) {
+    threefry4x32(ctr, key, out);
+}

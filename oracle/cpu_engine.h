@@ -49,3 +49,12 @@ void ocpu_thermostat_normals(uint32_t seed, uint64_t invocation, int n_atom, flo
 #ifdef __cplusplus
 }
 #endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+// raw Threefry-4x32-20 block (known-answer tests)
+void ocpu_threefry4x32(const uint32_t* ctr, const uint32_t* key, uint32_t* out);
+#ifdef __cplusplus
+}
+#endif

@@ -1,0 +1,48 @@
+import os
+import sys
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+GOLDEN = os.path.join(ROOT, "tests", "golden")
+for p in (os.path.join(ROOT, "upside2-md_gb300"), os.path.join(ROOT, "oracle")):
+    if p not in sys.path:
+        sys.path.insert(0, p)
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a)")
+
+
+@pytest.fixture(scope="session")
+def built():
+    """Compile the in-tree libraries once per session."""
+    sys.path.insert(0, ROOT)
+    import __graft_entry__
+    __graft_entry__.build()
+    return True
+
+
+@pytest.fixture(scope="session")
+def syn_configs(tmp_path_factory, built):
+    """The synthetic fixture configs regenerated from their sequence and seed."""
+    import config_gen
+    d = tmp_path_factory.mktemp("cfg")
+    out = {}
+    for n in (60, 150):
+        z = np.load(os.path.join(GOLDEN, "syn%d_ref.npz" % n))
+        path = str(d / ("syn%d.up" % n))
+        config_gen.write_config(path, [s.decode() for s in z["seq"]], int(z["seed"]), pos=z["pos"][0])
+        out[n] = (path, z)
+    return out
+
+
+def quat_align(a, ref):
+    """Flip the quaternion columns (3:7) of affine outputs to the sign of ref
+    (q and -q are the same rotation)."""
+    a = np.array(a, copy=True)
+    s = np.sign((a[:, 3:] * ref[:, 3:]).sum(1))
+    s[s == 0] = 1
+    a[:, 3:] *= s[:, None]
+    return a

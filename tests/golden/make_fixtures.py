@@ -136,7 +136,37 @@ def synthetic(L, n_res, seed, n_frames=3, tmpdir="/tmp"):
     np.savez_compressed(os.path.join(HERE, "syn%d_ref.npz" % n_res), **out)
 
 
+KAT_SRC = r"""
+#include <cstdio>
+#include <cstdint>
+#include <Random123/threefry.h>
+int main() {
+  for (uint32_t seed : {1u, 12345u, 4294967290u}) for (unsigned long long step : {0ull, 1ull, 4294967298ull})
+  for (uint32_t stream : {0u, 1u}) for (uint32_t atom : {0u, 7u}) {
+    threefry4x32_key_t k = {{seed, stream, 0u, 0u}};
+    threefry4x32_ctr_t c = {{uint32_t(step & 0xffffffffu), uint32_t(step >> 32), atom, 0u}};
+    threefry4x32_ctr_t r = threefry4x32(c, k);
+    printf("%u %u %llu %u %u %u %u %u\n", seed, stream, step, atom, r.v[0], r.v[1], r.v[2], r.v[3]);
+  }
+}
+"""
+
+
+def threefry_kat():
+    """Known answers of the reference's vendored Threefry-4x32-20 (src/include/Random123)."""
+    import subprocess
+    import tempfile
+    d = tempfile.mkdtemp()
+    src, exe = os.path.join(d, "kat.cpp"), os.path.join(d, "kat")
+    open(src, "w").write(KAT_SRC)
+    subprocess.check_call(["g++", "-O1", "-I", os.path.join(REF, "src", "include"), src, "-o", exe])
+    out = subprocess.check_output([exe], text=True)
+    with open(os.path.join(HERE, "threefry_kat.txt"), "w") as f:
+        f.write("# seed stream counter_lo_hi(step) atom out0 out1 out2 out3\n" + out)
+
+
 def main():
+    threefry_kat()
     L = load_ref()
     chig(L)
     synthetic(L, 60, 1)

@@ -217,6 +217,13 @@ int get_clamped_coeff_deriv(int N, float* result, const float* bspline_coeff, fl
 // ============================================================== batch API ===
 const char* ug_last_error(void) { return g_err.c_str(); }
 
+int ug_set_device(int device) {
+    GUARD_BEGIN
+    UG_CK(cudaSetDevice(device));
+    return 0;
+    GUARD_END(1)
+}
+
 UgBatch* ug_create(int n_sys, const char* const* paths, const int* n_atom) {
     GUARD_BEGIN
     std::vector<std::string> p(paths, paths + n_sys);
@@ -435,9 +442,72 @@ int ug_status(UgBatch* b, int clear) {
 }
 
 int ug_info(UgBatch* b, int* launches, int64_t* bytes) {
-    if (launches) *launches = b->e->launches_per_compute;
+    GUARD_BEGIN
+    if (launches) *launches = b->e->launches_per_compute ? b->e->launches_per_compute : b->e->count_launches();
     if (bytes) *bytes = int64_t(b->e->device_bytes);
     return 0;
+    GUARD_END(1)
+}
+
+int ug_bench(UgBatch* b, int n_round, float dt, float timescale, int flush_l2, int e2e, float* ms) {
+    GUARD_BEGIN
+    Engine& e = *b->e;
+    if (!e.graph_exec || e.graph_rounds != 1) e.capture(dt, timescale, 1);
+    const size_t flush_bytes = size_t(256) << 20;
+    void* flush = nullptr;
+    if (flush_l2) UG_CK(cudaMalloc(&flush, flush_bytes));
+    size_t state = sizeof(float) * 3 * size_t(e.atom_total);
+    float *hpos = nullptr, *hmom = nullptr;
+    if (e2e) {
+        UG_CK(cudaMallocHost(&hpos, state));
+        UG_CK(cudaMallocHost(&hmom, state));
+        UG_CK(cudaMemcpyAsync(hpos, e.d_pos, state, cudaMemcpyDeviceToHost, e.st));
+        UG_CK(cudaMemcpyAsync(hmom, e.d_mom, state, cudaMemcpyDeviceToHost, e.st));
+    }
+    std::vector<cudaEvent_t> ev(2 * size_t(n_round));
+    for (auto& x : ev) UG_CK(cudaEventCreate(&x));
+    for (int r = 0; r < n_round; ++r) {
+        if (flush) UG_CK(cudaMemsetAsync(flush, r & 0xff, flush_bytes, e.st));
+        UG_CK(cudaEventRecord(ev[2 * size_t(r)], e.st));
+        if (e2e) {
+            UG_CK(cudaMemcpyAsync(e.d_pos, hpos, state, cudaMemcpyHostToDevice, e.st));
+            UG_CK(cudaMemcpyAsync(e.d_mom, hmom, state, cudaMemcpyHostToDevice, e.st));
+        }
+        e.launch_graph();
+        if (e2e) {
+            UG_CK(cudaMemcpyAsync(hpos, e.d_pos, state, cudaMemcpyDeviceToHost, e.st));
+            UG_CK(cudaMemcpyAsync(hmom, e.d_mom, state, cudaMemcpyDeviceToHost, e.st));
+        }
+        UG_CK(cudaEventRecord(ev[2 * size_t(r) + 1], e.st));
+    }
+    UG_CK(cudaStreamSynchronize(e.st));
+    for (int r = 0; r < n_round; ++r) UG_CK(cudaEventElapsedTime(&ms[r], ev[2 * size_t(r)], ev[2 * size_t(r) + 1]));
+    for (auto& x : ev) cudaEventDestroy(x);
+    if (flush) cudaFree(flush);
+    if (hpos) cudaFreeHost(hpos);
+    if (hmom) cudaFreeHost(hmom);
+    int s = e.status(true);
+    if (s & (ug::ST_EDGE_OVERFLOW | ug::ST_RES_EDGE_OVERFLOW)) {
+        // storage grew mid-run: results of this run are invalid, report it
+        for (auto& n : e.nodes) n->grow(e);
+        throw ug::Error("pair-list storage overflowed during the timed rounds; rerun");
+    }
+    return 0;
+    GUARD_END(1)
+}
+
+int ug_profile(UgBatch* b, int n_eval, char* names, int names_cap, float* ms, int cap) {
+    GUARD_BEGIN
+    auto p = b->e->profile_nodes(n_eval);
+    std::string s;
+    for (size_t k = 0; k < p.size(); ++k) {
+        s += p[k].first + "\n";
+        if (int(k) < cap) ms[k] = p[k].second;
+    }
+    if (int(s.size()) + 1 > names_cap) throw ug::Error("names buffer too small");
+    memcpy(names, s.c_str(), s.size() + 1);
+    return int(p.size());
+    GUARD_END(-1)
 }
 
 }  // extern "C"

@@ -2068,4 +2068,60 @@ void Engine::capture(float dt, float timescale, int rounds) {
 }
 void Engine::launch_graph() { UG_CK(cudaGraphLaunch(graph_exec, st)); }
 
+int Engine::count_launches() {
+    UG_CK(cudaStreamSynchronize(st));
+    cudaGraph_t g = nullptr;
+    UG_CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    compute(false);
+    UG_CK(cudaStreamEndCapture(st, &g));
+    size_t n = 0;
+    UG_CK(cudaGraphGetNodes(g, nullptr, &n));
+    std::vector<cudaGraphNode_t> nodes_v(n);
+    UG_CK(cudaGraphGetNodes(g, nodes_v.data(), &n));
+    int k = 0;
+    for (auto nd : nodes_v) {
+        cudaGraphNodeType t;
+        UG_CK(cudaGraphNodeGetType(nd, &t));
+        if (t == cudaGraphNodeTypeKernel) ++k;
+    }
+    cudaGraphDestroy(g);
+    launches_per_compute = k;
+    return k;
+}
+
+std::vector<std::pair<std::string, float>> Engine::profile_nodes(int n) {
+    std::vector<std::pair<std::string, float>> acc;
+    for (auto& nd : nodes) acc.emplace_back(nd->name + ":fwd", 0.f);
+    for (auto& nd : nodes) acc.emplace_back(nd->name + ":bwd", 0.f);
+    std::vector<cudaEvent_t> ev(2 * nodes.size() + 1);
+    for (auto& e : ev) UG_CK(cudaEventCreate(&e));
+    for (int it = 0; it < n; ++it) {
+        UG_CK(cudaMemsetAsync(d_sens_arena, 0, sens_arena_floats * sizeof(float), st));
+        size_t k = 0;
+        UG_CK(cudaEventRecord(ev[k++], st));
+        for (auto& nd : nodes) {
+            nd->forward(*this, false);
+            UG_CK(cudaEventRecord(ev[k++], st));
+        }
+        for (size_t i = nodes.size(); i-- > 0;) {
+            nodes[i]->backward(*this);
+            UG_CK(cudaEventRecord(ev[k++], st));
+        }
+        UG_CK(cudaStreamSynchronize(st));
+        for (size_t j = 0; j < nodes.size(); ++j) {
+            float ms = 0;
+            UG_CK(cudaEventElapsedTime(&ms, ev[j], ev[j + 1]));
+            acc[j].second += ms;
+        }
+        for (size_t j = 0; j < nodes.size(); ++j) {
+            float ms = 0;
+            UG_CK(cudaEventElapsedTime(&ms, ev[nodes.size() + j], ev[nodes.size() + j + 1]));
+            acc[nodes.size() + (nodes.size() - 1 - j)].second += ms;
+        }
+    }
+    for (auto& e : ev) cudaEventDestroy(e);
+    for (auto& a : acc) a.second /= float(std::max(1, n));
+    return acc;
+}
+
 }  // namespace ug

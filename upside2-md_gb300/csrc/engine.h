@@ -115,6 +115,10 @@ public:
 
     size_t device_bytes = 0;
     int launches_per_compute = 0;
+    // number of kernel nodes in one captured force evaluation
+    int count_launches();
+    // per-node device time (ms) of n eager evaluations, CUDA events on the stream
+    std::vector<std::pair<std::string, float>> profile_nodes(int n);
 
 private:
     std::vector<void*> allocations_;

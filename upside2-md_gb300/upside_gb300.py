@@ -57,6 +57,9 @@ def lib():
         L.ug_replica_exchange.argtypes = [vp, ip, vp, ctypes.c_uint32, ctypes.c_uint64, vp]
         L.ug_status.argtypes = [vp, ip]
         L.ug_info.argtypes = [vp, vp, vp]
+        L.ug_profile.argtypes = [vp, ip, ctypes.c_char_p, ip, vp, ip]
+        L.ug_bench.argtypes = [vp, ip, ctypes.c_float, ctypes.c_float, ip, ip, vp]
+        L.ug_set_device.argtypes = [ip]
         _lib = L
     return _lib
 
@@ -257,5 +260,20 @@ class Batch:
 
     def info(self):
         l, b = ctypes.c_int(), ctypes.c_int64()
-        lib().ug_info(self.h, ctypes.byref(l), ctypes.byref(b))
+        self._chk(lib().ug_info(self.h, ctypes.byref(l), ctypes.byref(b)))
         return l.value, b.value
+
+    def bench(self, n_round, dt=0.009, timescale=5.0, flush_l2=True, e2e=False):
+        """Device time (ms) of each of n_round timed integration rounds."""
+        ms = np.zeros(n_round, np.float32)
+        self._chk(lib().ug_bench(self.h, int(n_round), float(dt), float(timescale), int(flush_l2), int(e2e),
+                                 ms.ctypes.data))
+        return ms
+
+    def profile(self, n_eval=5):
+        names = ctypes.create_string_buffer(1 << 16)
+        ms = np.zeros(256, np.float32)
+        n = lib().ug_profile(self.h, n_eval, names, 1 << 16, ms.ctypes.data, 256)
+        if n < 0:
+            raise RuntimeError(lib().ug_last_error().decode())
+        return list(zip(names.value.decode().split("\n")[:n], ms[:n].tolist()))

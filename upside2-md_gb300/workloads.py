@@ -1,0 +1,81 @@
+"""Seeded synthetic workloads (the five benchmark configurations).
+
+  C1  1 chain of 60 residues, T=0.85
+  C2  1 chain of 300 residues, T=0.85
+  C3  48 replicas of one 150-residue chain, T geometric 0.80 -> 1.00, replica
+      exchange between alternating even/odd neighbour pairs every 20 steps
+  C4  64 independent chains, lengths uniform in [40, 400], T uniform in [0.80, 0.95]
+  C5  8 chains of 250 residues in one system (2000 residues), spaced apart
+
+Sequences are drawn uniformly over the 20 amino acids from the seed; initial
+structures are random (phi, psi) chains (py/upside_config.py:186-201).  Files
+are cached under a work directory keyed by the configuration and seed.
+"""
+import os
+
+import numpy as np
+
+import config_gen
+
+WORK = os.environ.get("UPSIDE_GB300_WORK", "/tmp/upside_gb300_work")
+
+
+def _cfg(name, seed, n_res, **kw):
+    os.makedirs(WORK, exist_ok=True)
+    path = os.path.join(WORK, "%s_s%d_n%d.up" % (name, seed, n_res if isinstance(n_res, int) else sum(n_res)))
+    if not os.path.exists(path):
+        rng = np.random.RandomState(seed)
+        seq = config_gen.random_sequence(int(n_res) if isinstance(n_res, int) else int(sum(n_res)), rng)
+        tmp = path + ".tmp%d" % os.getpid()
+        config_gen.write_config(tmp, seq, seed, **kw)
+        os.replace(tmp, path)
+    return path
+
+
+def n_res_of(path):
+    from h5lite import H5File
+    with H5File(path) as f:
+        return f.read("/input/pos").shape[0] // 3
+
+
+def workload(name, seed=1):
+    """Returns dict(configs=[...], n_res=[...], temps=[...], seeds=[...], swap_sets=None|[...])."""
+    if name == "C1":
+        cfgs = [_cfg("C1", seed, 60)]
+        temps = [0.85]
+    elif name == "C2":
+        cfgs = [_cfg("C2", seed, 300)]
+        temps = [0.85]
+    elif name == "C3":
+        c = _cfg("C3", seed, 150)
+        cfgs = [c] * 48
+        temps = list(0.80 * (1.00 / 0.80) ** (np.arange(48) / 47.))
+    elif name == "C4":
+        rng = np.random.RandomState(1000 + seed)
+        lengths = rng.randint(40, 401, size=64)
+        cfgs = [_cfg("C4c%02d" % i, seed * 100 + i, int(n)) for i, n in enumerate(lengths)]
+        temps = list(rng.uniform(0.80, 0.95, size=64))
+    elif name == "C5":
+        starts = [250 * k for k in range(1, 8)]
+        offsets = np.array([[60.0 * (k % 4) - 90.0, 60.0 * (k // 4) - 30.0, 0.0] for k in range(8)])
+        cfgs = [_cfg("C5", seed, 2000, chain_first_residue=starts, chain_offsets=offsets)]
+        temps = [0.85]
+    else:
+        raise ValueError("unknown workload " + name)
+    n_res = [n_res_of(c) for c in cfgs]
+    swap_sets = None
+    if name == "C3":
+        even = [(i, i + 1) for i in range(0, 47, 2)]
+        odd = [(i, i + 1) for i in range(1, 47, 2)]
+        swap_sets = [even, odd]
+    return dict(configs=cfgs, n_res=n_res, temps=temps, seeds=[seed + i for i in range(len(cfgs))],
+                swap_sets=swap_sets)
+
+
+def initial_positions(configs):
+    from h5lite import H5File
+    out = []
+    for c in configs:
+        with H5File(c) as f:
+            out.append(f.read("/input/pos")[:, :, 0].astype(np.float32))
+    return np.concatenate(out)
