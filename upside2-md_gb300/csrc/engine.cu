@@ -1675,6 +1675,8 @@ struct RotamerNode : GNode {
         }
         b.n_res = res_off.back();
         b.n_bead = int(bead_res.size());
+        b.max_res_sys = *std::max_element(n_res_sys.begin(), n_res_sys.end());
+        if (b.max_res_sys * 64 > 220 * 1024) throw Error("system too large for the shared-memory BP solver");
         b.res_off = e.upload(res_off);
         b.nrot = e.upload(nrot);
         b.res_N = e.upload(resN);

@@ -742,6 +742,240 @@ __global__ void __launch_bounds__(1024) bp_solve_kernel(DBP b, int want_energy, 
     }
 }
 
+// ---------------------------------------------------------------------------
+// BP solve, warp-per-node form.  One block per system; the system's node
+// beliefs (both ping-pong buffers) live in shared memory.  A sweep is one
+// pass over the nodes: the warp that owns node u computes, one lane per
+// incoming entry (u <- v), the new message from v's old belief divided by the
+// old reverse message, stores it, and folds it into u's new belief with a
+// butterfly product across lanes (renormalised at every level, which only
+// rescales).  Sweeps are Jacobi updates (all reads from the old buffers), as
+// in the reference, so one barrier per sweep suffices.
+__device__ __forceinline__ void renorm6(float* x, int n) {
+    float s = 0.f;
+#pragma unroll
+    for (int k = 0; k < 6; ++k) s += k < n ? x[k] : 0.f;
+    float inv = 1.f / s;
+#pragma unroll
+    for (int k = 0; k < 6; ++k) x[k] *= inv;
+}
+
+__device__ __forceinline__ float bp_node_sweep(const DBP& b, int u, int r0, int e1, const float* __restrict__ Nold,
+                                               float* __restrict__ Ncur, const float* __restrict__ Eold,
+                                               float* __restrict__ Ecur, int mode, float damp, int lane) {
+    int n = b.nrot[u];
+    if (n == 1) return 0.f;
+    int eb = b.row_ptr[u], ee = min(b.row_ptr[u + 1], e1);
+    float prod[6] = {1.f, 1.f, 1.f, 1.f, 1.f, 1.f};
+    for (int base = eb; base < ee; base += 32) {
+        int e = base + lane;
+        float m[6] = {1.f, 1.f, 1.f, 1.f, 1.f, 1.f};
+        if (e < ee) {
+            int v = b.col[e];
+            int rv = b.rev[e];
+            int nv = b.nrot[v];
+            const float* ob = Nold + (v - r0) * 8;
+            const float4* om = reinterpret_cast<const float4*>(Eold + size_t(rv) * 8);
+            float4 o0 = om[0], o1 = om[1];
+            float omv[6] = {o0.x, o0.y, o0.z, o0.w, o1.x, o1.y};
+            float cav[6];
+#pragma unroll
+            for (int k = 0; k < 6; ++k) cav[k] = k < nv ? ob[k] / (1e-10f + omv[k]) : 0.f;
+            const float4* P4 = reinterpret_cast<const float4*>(b.P + size_t(e) * 36);
+            float P[36];
+#pragma unroll
+            for (int q = 0; q < 9; ++q) {
+                float4 t = P4[q];
+                P[4 * q] = t.x; P[4 * q + 1] = t.y; P[4 * q + 2] = t.z; P[4 * q + 3] = t.w;
+            }
+            float mm[6], sum = 0.f;
+#pragma unroll
+            for (int i = 0; i < 6; ++i) {
+                float acc = 0.f;
+#pragma unroll
+                for (int k = 0; k < 6; ++k) acc += P[i * 6 + k] * cav[k];
+                mm[i] = i < n ? acc : 0.f;
+                sum += mm[i];
+            }
+            float inv = 1.f / sum;
+            float4* out = reinterpret_cast<float4*>(Ecur + size_t(e) * 8);
+            out[0] = make_float4(mm[0] * inv, mm[1] * inv, mm[2] * inv, mm[3] * inv);
+            out[1] = make_float4(mm[4] * inv, mm[5] * inv, 0.f, 0.f);
+#pragma unroll
+            for (int i = 0; i < 6; ++i) m[i] = i < n ? mm[i] * inv : 1.f;
+        }
+#pragma unroll
+        for (int i = 0; i < 6; ++i) prod[i] *= m[i];
+        renorm6(prod, n);
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+#pragma unroll
+        for (int i = 0; i < 6; ++i) prod[i] *= __shfl_xor_sync(0xffffffffu, prod[i], off);
+        renorm6(prod, n);
+    }
+    float dev = 0.f;
+    if (lane == 0) {
+        float bl[6];
+#pragma unroll
+        for (int k = 0; k < 6; ++k) bl[k] = k < n ? b.prob[u * 8 + k] * prod[k] : 0.f;
+        renorm6(bl, n);
+        const float* o = Nold + (u - r0) * 8;
+        if (mode == 1) {
+            float mx = bl[0];
+            for (int k = 1; k < n; ++k) mx = fmaxf(mx, bl[k]);
+            float inv = 1.f / mx;
+#pragma unroll
+            for (int k = 0; k < 6; ++k) {
+                bl[k] = damp != 0.f ? (1.f - damp) * inv * bl[k] + damp * o[k] : inv * bl[k];
+                if (k < n) dev = fmaxf(dev, bl[k] - o[k]);
+            }
+        }
+        float* c = Ncur + (u - r0) * 8;
+#pragma unroll
+        for (int k = 0; k < 6; ++k) c[k] = bl[k];
+        c[6] = c[7] = 0.f;
+    }
+    return dev;
+}
+
+__global__ void __launch_bounds__(1024) bp_solve2_kernel(DBP b, int want_energy, double* energy_out) {
+    extern __shared__ float smem[];
+    __shared__ float red[32];
+    __shared__ double dred[32];
+    const int s = blockIdx.x;
+    const int r0 = b.res_off[s], r1 = b.res_off[s + 1], N = r1 - r0;
+    const int e0 = b.row_ptr[r0], e1 = min(b.row_ptr[r1], b.ent_cap);
+    float* NB[2] = {smem, smem + N * 8};
+    float* EM[2] = {b.msg, b.msg + size_t(b.ent_cap) * 8};
+    const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
+
+    auto sweep = [&](const float* Nold, float* Ncur, const float* Eold, float* Ecur, int mode, float damp) {
+        float dev = 0.f;
+        for (int u = r0 + warp; u < r1; u += nw) dev = fmaxf(dev, bp_node_sweep(b, u, r0, e1, Nold, Ncur, Eold, Ecur,
+                                                                               mode, damp, lane));
+        return dev;
+    };
+    auto block_max = [&](float v) -> float {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+        if (lane == 0) red[warp] = v;
+        __syncthreads();
+        float r = 0.f;
+        for (int w = 0; w < nw; ++w) r = fmaxf(r, red[w]);
+        __syncthreads();
+        return r;
+    };
+
+    // N.old = N.cur = prob; E.old = 1
+    for (int i = tid; i < N * 8; i += nt) NB[0][i] = NB[1][i] = b.prob[r0 * 8 + i];
+    for (int i = e0 * 8 + tid; i < e1 * 8; i += nt) EM[1][i] = 1.f;
+    __syncthreads();
+    // first sweep, undamped: new beliefs go to the buffer that then becomes
+    // "old"; the other (prob) is max-normalised (src/rotamer.cpp:1135)
+    sweep(NB[1], NB[0], EM[1], EM[0], 0, 0.f);
+    __syncthreads();
+    for (int u = r0 + tid; u < r1; u += nt) {
+        int n = b.nrot[u];
+        if (n == 1) continue;
+        float* c = NB[1] + (u - r0) * 8;
+        float mx = c[0];
+        for (int k = 1; k < n; ++k) mx = fmaxf(mx, c[k]);
+        float inv = 1.f / mx;
+        for (int k = 0; k < 6; ++k) c[k] *= inv;
+    }
+    __syncthreads();
+    int nc = 1, ec = 0;
+    float dev = 1e10f;
+    int iter = 0;
+    for (; dev > b.tol && iter < b.max_iter; iter += b.chunk) {
+        float d = 0.f;
+        for (int j = 0; j < b.chunk; ++j) {
+            nc ^= 1;
+            ec ^= 1;
+            d = sweep(NB[nc ^ 1], NB[nc], EM[ec ^ 1], EM[ec], 1, b.damping);
+            __syncthreads();
+        }
+        dev = block_max(d);
+    }
+    if (tid == 0) {
+        b.n_iter[s] = iter;
+        if (iter >= b.max_iter - b.chunk - 1) atomicOr(b.status, ST_BP_NOT_CONVERGED);
+    }
+    // node marginals
+    const float* Nf = NB[nc];
+    for (int u = r0 + tid; u < r1; u += nt) {
+        int n = b.nrot[u];
+        if (n == 1) {
+            b.marg[u * 8] = 1.f;
+            for (int k = 1; k < 8; ++k) b.marg[u * 8 + k] = 0.f;
+            continue;
+        }
+        float sum = 0.f;
+        for (int k = 0; k < n; ++k) sum += Nf[(u - r0) * 8 + k];
+        float inv = 1.f / sum;
+        for (int k = 0; k < 8; ++k) b.marg[u * 8 + k] = k < n ? Nf[(u - r0) * 8 + k] * inv : 0.f;
+    }
+    __syncthreads();
+    // edge marginals
+    const float* Ef = EM[ec];
+    for (int e = e0 + tid; e < e1; e += nt) {
+        int u = b.erow[e], v = b.col[e];
+        int nu = b.nrot[u], nv = b.nrot[v];
+        const float* mu = Ef + size_t(e) * 8;
+        const float* mv = Ef + size_t(b.rev[e]) * 8;
+        float bu[6], bv[6];
+        for (int i = 0; i < 6; ++i) bu[i] = i < nu ? b.marg[u * 8 + i] / (1e-10f + mu[i]) : 0.f;
+        for (int j = 0; j < 6; ++j) bv[j] = j < nv ? b.marg[v * 8 + j] / (1e-10f + mv[j]) : 0.f;
+        const float* P = b.P + size_t(e) * 36;
+        float* mg = b.emarg + size_t(e) * 36;
+        float sum = 0.f;
+        for (int i = 0; i < 6; ++i)
+            for (int j = 0; j < 6; ++j) {
+                float x = P[i * 6 + j] * bu[i] * bv[j];
+                mg[i * 6 + j] = x;
+                sum += x;
+            }
+        float inv = 1.f / sum;
+        for (int k = 0; k < 36; ++k) mg[k] *= inv;
+    }
+    if (!want_energy) return;
+    __syncthreads();
+    double en = 0.0;
+    for (int u = r0 + tid; u < r1; u += nt) {
+        int n = b.nrot[u];
+        float f = b.eoff[u];
+        for (int k = 0; k < n; ++k) {
+            float bk = b.marg[u * 8 + k];
+            f += bk * logf((1e-10f + bk) / (1e-10f + b.prob[u * 8 + k]));
+        }
+        en += double(f);
+    }
+    for (int e = e0 + tid; e < e1; e += nt) {
+        int u = b.erow[e], v = b.col[e];
+        if (!(u < v)) continue;
+        int nu = b.nrot[u], nv = b.nrot[v];
+        const float* p = b.emarg + size_t(e) * 36;
+        const float* P = b.P + size_t(e) * 36;
+        float f = 0.f;
+        for (int i = 0; i < nu; ++i)
+            for (int j = 0; j < nv; ++j) {
+                float x = p[i * 6 + j];
+                f += x * logf((1e-10f + x) / (1e-10f + P[i * 6 + j] * b.marg[u * 8 + i] * b.marg[v * 8 + j]));
+            }
+        en += double(f);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) en += __shfl_xor_sync(0xffffffffu, en, o);
+    if (lane == 0) dred[warp] = en;
+    __syncthreads();
+    if (tid == 0) {
+        double t = b.e11[s];
+        for (int w = 0; w < nw; ++w) t += dred[w];
+        energy_out[s] = t;
+    }
+}
+
 // bead-edge sensitivities from the marginals and 1-body sensitivities
 // (src/rotamer.cpp:1057-1086)
 __global__ void bp_sens_kernel(DBP b, DGraph g, float* s0, float* s1, float* s2, float* s3, int n_in, int w0,
@@ -775,8 +1009,8 @@ __global__ void bp_sens_kernel(DBP b, DGraph g, float* s0, float* s1, float* s2,
 void launch_bp(DBP& b, const DGraph& g, const float* const* in, float* const* in_sens, const int* w, int n_in,
                int prev_n_ent, int* scan_total, int want_energy, double* energy_out, cudaStream_t st) {
     int blocks = 2 * 152;
-    // one block: the reset must finish reading n_ent before anything rewrites it
-    bp_reset_kernel<<<1, 1024, 0, st>>>(b);
+    // n_ent is rewritten only by the scan below, after this kernel completes
+    bp_reset_kernel<<<blocks, 256, 0, st>>>(b);
     (void)prev_n_ent;
     bp_bead_energy_kernel<<<blocks, 256, 0, st>>>(b, in[0], in[1], in[2], in[3], n_in, w[0], w[1], w[2], w[3]);
     bp_mark_kernel<<<blocks, 256, 0, st>>>(b, g);
@@ -788,7 +1022,13 @@ void launch_bp(DBP& b, const DGraph& g, const float* const* in, float* const* in
     bp_entry_init_kernel<<<blocks, 256, 0, st>>>(b);
     bp_edge_energy_kernel<<<blocks, 256, 0, st>>>(b, g);
     bp_prob_kernel<<<blocks, 256, 0, st>>>(b);
-    bp_solve_kernel<<<b.n_sys, 1024, 0, st>>>(b, want_energy, energy_out);
+    size_t smem = size_t(b.max_res_sys) * 8 * 2 * sizeof(float);
+    static size_t configured = 0;
+    if (smem > 48 * 1024 && smem > configured) {
+        cudaFuncSetAttribute(bp_solve2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+        configured = smem;
+    }
+    bp_solve2_kernel<<<b.n_sys, 1024, smem, st>>>(b, want_energy, energy_out);
     bp_sens_kernel<<<blocks, 256, 0, st>>>(b, g, in_sens[0], in_sens[1], in_sens[2], in_sens[3], n_in, w[0], w[1],
                                            w[2], w[3]);
     (void)scan_total;

@@ -91,6 +91,7 @@ struct DBP {
     int* n_iter;                // per system
     float damping, tol;
     int max_iter, chunk;
+    int max_res_sys;            // largest residue count of one system (shared-memory sizing)
     // bead level
     int n_bead;
     const int* bead_res;        // bead -> residue (global)
