@@ -76,11 +76,29 @@ int ug_info(UgBatch* b, int* launches_per_eval, int64_t* device_bytes);
  * host->device copy of positions and momenta from pinned host memory and the
  * device->host copy of them back (the state a caller round-trips per round). */
 int ug_bench(UgBatch* b, int n_round, float dt, float timescale, int flush_l2, int e2e, float* ms);
+/* The rotamer BP solve kernel over the last ug_bench: stats[0] its summed
+ * device time in ms (CUDA events recorded around each launch inside the
+ * replayed graph, on the engine stream), stats[1] its number of launches,
+ * stats[2] its summed algorithmic bytes (P, messages, beliefs and indices
+ * each sweep touches; the count is kept by the kernel itself). */
+int ug_bench_kernel(UgBatch* b, double* stats);
 
 /* Per-node device time of n_eval eager force evaluations (CUDA events on the
  * engine stream): names '\n'-separated "<node>:fwd" / "<node>:bwd", ms[k] the
  * mean time of entry k.  Returns the number of entries (or -1). */
 int ug_profile(UgBatch* b, int n_eval, char* names, int names_cap, float* ms, int cap);
+
+/* Pair list of one point set held in device memory: every (i, j), i < j, with
+ * |x_i - x_j| < cutoff, the interaction-graph pair search of the engine
+ * (replaces PairlistComputation's cache pass, src/interaction_graph.h:122-157,
+ * for callers without an engine).  pos: n x 3 floats on the device; pairs:
+ * device int32 (i, j) x cap; *n_pairs (device int32) receives the total number
+ * of pairs, which may exceed cap (pairs past cap are not written).  Pair order:
+ * i / 4, then j, then i % 4.  stream: a cudaStream_t or NULL.  Allocates its
+ * scratch (2 ceil(n/4) + 1 ints) with cudaMalloc and synchronises the stream
+ * before returning. */
+int ug_pair_list(const float* pos, int n, float cutoff, int32_t* pairs, int cap, int32_t* n_pairs, void* stream);
+
 
 #ifdef __cplusplus
 }

@@ -18,7 +18,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC = os.environ.get("NVCC", "nvcc")
 CXX = os.environ.get("CXX", "g++")
 
-CU_SOURCES = ["engine.cu", "graph.cu", "capi.cu"]
+CU_SOURCES = ["engine.cu", "graph.cu", "pairlist.cu", "capi.cu"]
 HEADERS = ["engine.h", "graph.h", "dev_math.cuh", "h5lite.h"]
 
 

@@ -44,6 +44,9 @@ struct DerivEngine {
 };
 struct UgBatch {
     std::unique_ptr<Engine> e;
+    // measured kernel over the last ug_bench: device ms, launches, algorithmic bytes
+    double kt_ms = 0.0, kt_bytes = 0.0;
+    long long kt_launches = 0;
 };
 
 #define GUARD_BEGIN try {
@@ -452,7 +455,10 @@ int ug_info(UgBatch* b, int* launches, int64_t* bytes) {
 int ug_bench(UgBatch* b, int n_round, float dt, float timescale, int flush_l2, int e2e, float* ms) {
     GUARD_BEGIN
     Engine& e = *b->e;
-    if (!e.graph_exec || e.graph_rounds != 1) e.capture(dt, timescale, 1);
+    if (!e.graph_exec || e.graph_rounds != 1 || !e.graph_timed) e.capture_timed(dt, timescale);
+    b->kt_ms = b->kt_bytes = 0.0;
+    b->kt_launches = 0;
+    double bytes0 = e.kernel_bytes();
     const size_t flush_bytes = size_t(256) << 20;
     void* flush = nullptr;
     if (flush_l2) UG_CK(cudaMalloc(&flush, flush_bytes));
@@ -479,8 +485,28 @@ int ug_bench(UgBatch* b, int n_round, float dt, float timescale, int flush_l2, i
             UG_CK(cudaMemcpyAsync(hmom, e.d_mom, state, cudaMemcpyDeviceToHost, e.st));
         }
         UG_CK(cudaEventRecord(ev[2 * size_t(r) + 1], e.st));
+        if (e.graph_timed) {
+            // the graph's event-record nodes are re-recorded by the next
+            // replay: read this round's kernel brackets now
+            UG_CK(cudaStreamSynchronize(e.st));
+            for (int k = 0; k + 1 < e.kt_used; k += 2) {
+                float t = 0.f;
+                if (cudaEventElapsedTime(&t, e.kt_ev[size_t(k)], e.kt_ev[size_t(k) + 1]) != cudaSuccess) {
+                    // no timing for this kernel (reported as zero launches);
+                    // the round times above are unaffected
+                    cudaGetLastError();
+                    b->kt_launches = 0;
+                    b->kt_ms = 0.0;
+                    e.graph_timed = false;
+                    break;
+                }
+                b->kt_ms += t;
+                b->kt_launches += 1;
+            }
+        }
     }
     UG_CK(cudaStreamSynchronize(e.st));
+    b->kt_bytes = e.kernel_bytes() - bytes0;
     for (int r = 0; r < n_round; ++r) UG_CK(cudaEventElapsedTime(&ms[r], ev[2 * size_t(r)], ev[2 * size_t(r) + 1]));
     for (auto& x : ev) cudaEventDestroy(x);
     if (flush) cudaFree(flush);
@@ -492,6 +518,15 @@ int ug_bench(UgBatch* b, int n_round, float dt, float timescale, int flush_l2, i
         for (auto& n : e.nodes) n->grow(e);
         throw ug::Error("pair-list storage overflowed during the timed rounds; rerun");
     }
+    return 0;
+    GUARD_END(1)
+}
+
+int ug_bench_kernel(UgBatch* b, double* stats) {
+    GUARD_BEGIN
+    stats[0] = b->kt_ms;
+    stats[1] = double(b->kt_launches);
+    stats[2] = b->kt_bytes;
     return 0;
     GUARD_END(1)
 }
@@ -508,6 +543,24 @@ int ug_profile(UgBatch* b, int n_eval, char* names, int names_cap, float* ms, in
     memcpy(names, s.c_str(), s.size() + 1);
     return int(p.size());
     GUARD_END(-1)
+}
+
+int ug_pair_list(const float* pos, int n, float cutoff, int32_t* pairs, int cap, int32_t* n_pairs, void* stream) {
+    GUARD_BEGIN
+    if (n < 0 || cap < 0 || !(cutoff > 0.f)) throw ug::Error("ug_pair_list: need n >= 0, cap >= 0, cutoff > 0");
+    if ((n > 0 && !pos) || (cap > 0 && !pairs) || !n_pairs) throw ug::Error("ug_pair_list: null device pointer");
+    auto st = static_cast<cudaStream_t>(stream);
+    size_t n_rows = (size_t(n) + 3) / 4;
+    int* scratch = nullptr;
+    UG_CK(cudaMalloc(&scratch, sizeof(int) * (2 * n_rows + 1)));
+    cudaError_t e1 = ug::launch_point_pairs(pos, n, cutoff, pairs, cap, n_pairs, scratch, scratch + n_rows, st);
+    cudaError_t e2 = cudaStreamSynchronize(st);
+    cudaError_t e3 = cudaFree(scratch);
+    UG_CK(e1);
+    UG_CK(e2);
+    UG_CK(e3);
+    return 0;
+    GUARD_END(1)
 }
 
 }  // extern "C"

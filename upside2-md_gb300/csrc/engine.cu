@@ -1700,6 +1700,7 @@ struct RotamerNode : GNode {
         b.marg = e.alloc<float>(size_t(b.n_res) * 8);
         b.n_iter = e.alloc<int>(size_t(e.n_sys));
         b.e11 = e.alloc<double>(size_t(e.n_sys));
+        b.alg_bytes = e.alloc<unsigned long long>(size_t(e.n_sys));
         d_energy = e.alloc<double>(size_t(e.n_sys));
     }
     void alloc_entries(Engine& e, int cap) {
@@ -1748,6 +1749,19 @@ struct RotamerNode : GNode {
         return r;
     }
     DGraph* graph() override { return &hg.g; }
+    bool set_kernel_timer(cudaEvent_t* ev, int* used, int cap) override {
+        b.kt_ev = ev;
+        b.kt_used = used;
+        b.kt_cap = cap;
+        return true;
+    }
+    double kernel_bytes(Engine& e) override {
+        std::vector<unsigned long long> v(size_t(e.n_sys));
+        UG_CK(cudaMemcpy(v.data(), b.alg_bytes, 8 * v.size(), cudaMemcpyDeviceToHost));
+        double t = 0;
+        for (auto x : v) t += double(x);
+        return t;
+    }
     bool grow(Engine& e) override {
         bool g1 = hg.grow_if_full();
         int ne = 0;
@@ -1983,6 +1997,7 @@ Engine::Engine(const std::vector<std::string>& paths, const std::vector<int>& n_
 Engine::~Engine() {
     if (graph_exec) cudaGraphExecDestroy(graph_exec);
     if (graph) cudaGraphDestroy(graph);
+    for (auto& x : kt_ev) cudaEventDestroy(x);
     nodes.clear();
     free_all();
     if (st) cudaStreamDestroy(st);
@@ -2067,8 +2082,35 @@ void Engine::capture(float dt, float timescale, int rounds) {
     UG_CK(cudaStreamEndCapture(st, &graph));
     UG_CK(cudaGraphInstantiate(&graph_exec, graph, 0));
     graph_rounds = rounds;
+    graph_timed = false;
 }
 void Engine::launch_graph() { UG_CK(cudaGraphLaunch(graph_exec, st)); }
+
+// One-round graph whose measured-kernel launches are bracketed by event-record
+// nodes (kt_ev[0..kt_used)); each replay re-records them.
+void Engine::capture_timed(float dt, float timescale) {
+    if (kt_ev.empty()) {
+        kt_ev.resize(16);
+        for (auto& x : kt_ev) UG_CK(cudaEventCreate(&x));
+    }
+    kt_used = 0;
+    bool any = false;
+    for (auto& n : nodes) any |= n->set_kernel_timer(kt_ev.data(), &kt_used, int(kt_ev.size()));
+    try {
+        capture(dt, timescale, 1);
+    } catch (...) {
+        for (auto& n : nodes) n->set_kernel_timer(nullptr, nullptr, 0);
+        throw;
+    }
+    for (auto& n : nodes) n->set_kernel_timer(nullptr, nullptr, 0);
+    graph_timed = any;
+}
+
+double Engine::kernel_bytes() {
+    double t = 0;
+    for (auto& n : nodes) t += n->kernel_bytes(*this);
+    return t;
+}
 
 int Engine::count_launches() {
     UG_CK(cudaStreamSynchronize(st));

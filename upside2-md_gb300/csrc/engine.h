@@ -54,6 +54,11 @@ struct GNode {
     virtual DGraph* graph() { return nullptr; }
     // enlarge edge storage after an overflow; returns true if anything grew
     virtual bool grow(Engine&) { return false; }
+    // measured kernel of this node: bracket its launches with events from
+    // ev[*used..cap) (ev null: stop), and the running total of its
+    // algorithmic bytes; nodes without one return false / 0
+    virtual bool set_kernel_timer(cudaEvent_t*, int*, int) { return false; }
+    virtual double kernel_bytes(Engine&) { return 0.0; }
 };
 
 class Engine {
@@ -112,6 +117,13 @@ public:
     cudaGraphExec_t graph_exec = nullptr;
     cudaGraph_t graph = nullptr;
     int graph_rounds = 0;
+    // kernel timing of the measured kernel (the rotamer BP solve): with
+    // timed != 0 the captured graph records kt_ev around each of its launches
+    bool graph_timed = false;
+    std::vector<cudaEvent_t> kt_ev;
+    int kt_used = 0;
+    void capture_timed(float dt, float timescale);
+    double kernel_bytes();
 
     size_t device_bytes = 0;
     int launches_per_compute = 0;

@@ -537,211 +537,6 @@ __global__ void bp_prob_kernel(DBP b) {
     }
 }
 
-// One block per system: damped loopy BP to convergence, then marginals and
-// (optionally) the Bethe free energy.  The iteration structure (undamped
-// first sweep with swap, chunks of `chunk` damped sweeps, one-sided maximum
-// deviation test) follows src/rotamer.cpp:1106-1162.
-__global__ void __launch_bounds__(1024) bp_solve_kernel(DBP b, int want_energy, double* energy_out) {
-    __shared__ float red[32];
-    __shared__ double dred[32];
-    int s = blockIdx.x;
-    int r0 = b.res_off[s], r1 = b.res_off[s + 1];
-    int e0 = b.row_ptr[r0], e1 = min(b.row_ptr[r1], b.ent_cap);
-    float* NB[2] = {b.belief, b.belief + size_t(b.n_res) * 8};
-    float* EM[2] = {b.msg, b.msg + size_t(b.ent_cap) * 8};
-    const int tid = threadIdx.x, nt = blockDim.x;
-
-    auto edge_phase = [&](const float* Nold, const float* Eold, float* Ecur) {
-        for (int e = e0 + tid; e < e1; e += nt) {
-            int u = b.erow[e], v = b.col[e];
-            int nu = b.nrot[u], nv = b.nrot[v];
-            const float* ob = Nold + v * 8;
-            const float* om = Eold + b.rev[e] * 8;
-            float v2[6];
-#pragma unroll
-            for (int j = 0; j < 6; ++j) v2[j] = j < nv ? ob[j] / (1e-10f + om[j]) : 0.f;
-            const float* P = b.P + size_t(e) * 36;
-            float m[6], sum = 0.f;
-#pragma unroll
-            for (int i = 0; i < 6; ++i) {
-                float acc = 0.f;
-#pragma unroll
-                for (int j = 0; j < 6; ++j) acc += P[i * 6 + j] * v2[j];
-                m[i] = i < nu ? acc : 0.f;
-                sum += m[i];
-            }
-            float inv = 1.f / sum;
-#pragma unroll
-            for (int i = 0; i < 6; ++i) Ecur[e * 8 + i] = m[i] * inv;
-        }
-    };
-    // product of prob and incoming messages, renormalised after each factor;
-    // then (mode 1) damped max-normalisation against Nold, returning the
-    // largest increase over Nold
-    auto node_phase = [&](const float* Ecur, float* Ncur, const float* Nold, int mode, float damp) -> float {
-        float dev = 0.f;
-        for (int u = r0 + tid; u < r1; u += nt) {
-            int n = b.nrot[u];
-            if (n == 1) continue;
-            float bl[6];
-#pragma unroll
-            for (int k = 0; k < 6; ++k) bl[k] = k < n ? b.prob[u * 8 + k] : 0.f;
-            for (int e = b.row_ptr[u]; e < min(b.row_ptr[u + 1], e1); ++e) {
-                float sum = 0.f;
-#pragma unroll
-                for (int k = 0; k < 6; ++k) {
-                    bl[k] *= Ecur[e * 8 + k];
-                    sum += bl[k];
-                }
-                float inv = 1.f / sum;
-#pragma unroll
-                for (int k = 0; k < 6; ++k) bl[k] *= inv;
-            }
-            if (mode == 1) {
-                float mx = bl[0];
-                for (int k = 1; k < n; ++k) mx = fmaxf(mx, bl[k]);
-                float inv = 1.f / mx;
-#pragma unroll
-                for (int k = 0; k < 6; ++k) {
-                    float o = Nold[u * 8 + k];
-                    bl[k] = damp != 0.f ? (1.f - damp) * inv * bl[k] + damp * o : inv * bl[k];
-                    if (k < n) dev = fmaxf(dev, bl[k] - o);
-                }
-            }
-#pragma unroll
-            for (int k = 0; k < 6; ++k) Ncur[u * 8 + k] = bl[k];
-        }
-        return dev;
-    };
-    auto block_max = [&](float v) -> float {
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
-        if ((tid & 31) == 0) red[tid >> 5] = v;
-        __syncthreads();
-        float r = -1e30f;
-        for (int w = 0; w < (nt + 31) / 32; ++w) r = fmaxf(r, red[w]);
-        __syncthreads();
-        return r;
-    };
-
-    // initial state: N.old = prob, E.old = 1
-    for (int u = r0 + tid; u < r1; u += nt)
-        for (int k = 0; k < 8; ++k) {
-            NB[1][u * 8 + k] = b.prob[u * 8 + k];
-            NB[0][u * 8 + k] = b.prob[u * 8 + k];
-        }
-    for (int e = e0 + tid; e < e1; e += nt)
-        for (int k = 0; k < 8; ++k) EM[1][e * 8 + k] = 1.f;
-    __syncthreads();
-    // first sweep, undamped, with the swap of the initial beliefs
-    edge_phase(NB[1], EM[1], EM[0]);
-    __syncthreads();
-    node_phase(EM[0], NB[0], NB[1], 0, 0.f);
-    __syncthreads();
-    for (int u = r0 + tid; u < r1; u += nt) {
-        int n = b.nrot[u];
-        if (n == 1) continue;
-        float mx = NB[1][u * 8];
-        for (int k = 1; k < n; ++k) mx = fmaxf(mx, NB[1][u * 8 + k]);
-        float inv = 1.f / mx;
-        for (int k = 0; k < 6; ++k) NB[1][u * 8 + k] *= inv;
-    }
-    __syncthreads();
-    int nc = 1, ec = 0;
-    float dev = 1e10f;
-    int iter = 0;
-    for (; dev > b.tol && iter < b.max_iter; iter += b.chunk) {
-        float d = 0.f;
-        for (int j = 0; j < b.chunk; ++j) {
-            nc ^= 1;
-            ec ^= 1;
-            edge_phase(NB[nc ^ 1], EM[ec ^ 1], EM[ec]);
-            __syncthreads();
-            d = node_phase(EM[ec], NB[nc], NB[nc ^ 1], 1, b.damping);
-            __syncthreads();
-        }
-        dev = block_max(d);
-        dev = fmaxf(dev, 0.f);
-    }
-    if (tid == 0) {
-        b.n_iter[s] = iter;
-        if (iter >= b.max_iter - b.chunk - 1) atomicOr(b.status, ST_BP_NOT_CONVERGED);
-    }
-    // node marginals (src/rotamer.cpp:283-290)
-    const float* Nf = NB[nc];
-    for (int u = r0 + tid; u < r1; u += nt) {
-        int n = b.nrot[u];
-        if (n == 1) {
-            b.marg[u * 8] = 1.f;
-            for (int k = 1; k < 8; ++k) b.marg[u * 8 + k] = 0.f;
-            continue;
-        }
-        float sum = 0.f;
-        for (int k = 0; k < n; ++k) sum += Nf[u * 8 + k];
-        float inv = 1.f / sum;
-        for (int k = 0; k < 8; ++k) b.marg[u * 8 + k] = k < n ? Nf[u * 8 + k] * inv : 0.f;
-    }
-    __syncthreads();
-    // edge marginals (src/rotamer.cpp:425-449)
-    const float* Ef = EM[ec];
-    for (int e = e0 + tid; e < e1; e += nt) {
-        int u = b.erow[e], v = b.col[e];
-        int nu = b.nrot[u], nv = b.nrot[v];
-        const float* mu = Ef + e * 8;
-        const float* mv = Ef + b.rev[e] * 8;
-        float bu[6], bv[6];
-        for (int i = 0; i < 6; ++i) bu[i] = i < nu ? b.marg[u * 8 + i] / (1e-10f + mu[i]) : 0.f;
-        for (int j = 0; j < 6; ++j) bv[j] = j < nv ? b.marg[v * 8 + j] / (1e-10f + mv[j]) : 0.f;
-        const float* P = b.P + size_t(e) * 36;
-        float* mg = b.emarg + size_t(e) * 36;
-        float sum = 0.f;
-        for (int i = 0; i < 6; ++i)
-            for (int j = 0; j < 6; ++j) {
-                float x = P[i * 6 + j] * bu[i] * bv[j];
-                mg[i * 6 + j] = x;
-                sum += x;
-            }
-        float inv = 1.f / sum;
-        for (int k = 0; k < 36; ++k) mg[k] *= inv;
-    }
-    if (!want_energy) return;
-    __syncthreads();
-    // Bethe free energy (src/rotamer.cpp:292-302, :451-471, :915-927)
-    double en = 0.0;
-    for (int u = r0 + tid; u < r1; u += nt) {
-        int n = b.nrot[u];
-        float f = b.eoff[u];
-        for (int k = 0; k < n; ++k) {
-            float bk = b.marg[u * 8 + k];
-            f += bk * logf((1e-10f + bk) / (1e-10f + b.prob[u * 8 + k]));
-        }
-        en += double(f);
-    }
-    for (int e = e0 + tid; e < e1; e += nt) {
-        int u = b.erow[e], v = b.col[e];
-        if (!(u < v)) continue;
-        int nu = b.nrot[u], nv = b.nrot[v];
-        const float* p = b.emarg + size_t(e) * 36;
-        const float* P = b.P + size_t(e) * 36;
-        float f = 0.f;
-        for (int i = 0; i < nu; ++i)
-            for (int j = 0; j < nv; ++j) {
-                float x = p[i * 6 + j];
-                f += x * logf((1e-10f + x) / (1e-10f + P[i * 6 + j] * b.marg[u * 8 + i] * b.marg[v * 8 + j]));
-            }
-        en += double(f);
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) en += __shfl_xor_sync(0xffffffffu, en, o);
-    if ((tid & 31) == 0) dred[tid >> 5] = en;
-    __syncthreads();
-    if (tid == 0) {
-        double t = b.e11[s];
-        for (int w = 0; w < (nt + 31) / 32; ++w) t += dred[w];
-        energy_out[s] = t;
-    }
-}
-
 // ---------------------------------------------------------------------------
 // BP solve, warp-per-node form.  One block per system; the system's node
 // beliefs (both ping-pong buffers) live in shared memory.  A sweep is one
@@ -750,7 +545,10 @@ __global__ void __launch_bounds__(1024) bp_solve_kernel(DBP b, int want_energy, 
 // old reverse message, stores it, and folds it into u's new belief with a
 // butterfly product across lanes (renormalised at every level, which only
 // rescales).  Sweeps are Jacobi updates (all reads from the old buffers), as
-// in the reference, so one barrier per sweep suffices.
+// in the reference, so one barrier per sweep suffices.  The iteration
+// structure (undamped first sweep with swap, chunks of `chunk` damped sweeps,
+// one-sided maximum deviation test) follows src/rotamer.cpp:1106-1162; the
+// marginals and Bethe free energy follow src/rotamer.cpp:425-569.
 __device__ __forceinline__ void renorm6(float* x, int n) {
     float s = 0.f;
 #pragma unroll
@@ -868,9 +666,18 @@ __global__ void __launch_bounds__(1024) bp_solve2_kernel(DBP b, int want_energy,
     };
 
     // N.old = N.cur = prob; E.old = 1
+    __shared__ int s_multi;
+    if (tid == 0) s_multi = 0;
     for (int i = tid; i < N * 8; i += nt) NB[0][i] = NB[1][i] = b.prob[r0 * 8 + i];
     for (int i = e0 * 8 + tid; i < e1 * 8; i += nt) EM[1][i] = 1.f;
     __syncthreads();
+    {  // multi-rotamer node count, for the algorithmic-byte tally at the end
+        int m = 0;
+        for (int u = r0 + tid; u < r1; u += nt) m += b.nrot[u] > 1;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) m += __shfl_xor_sync(0xffffffffu, m, o);
+        if (lane == 0 && m) atomicAdd(&s_multi, m);
+    }
     // first sweep, undamped: new beliefs go to the buffer that then becomes
     // "old"; the other (prob) is max-normalised (src/rotamer.cpp:1135)
     sweep(NB[1], NB[0], EM[1], EM[0], 0, 0.f);
@@ -901,6 +708,17 @@ __global__ void __launch_bounds__(1024) bp_solve2_kernel(DBP b, int want_energy,
     if (tid == 0) {
         b.n_iter[s] = iter;
         if (iter >= b.max_iter - b.chunk - 1) atomicOr(b.status, ST_BP_NOT_CONVERGED);
+        // algorithmic bytes of this launch for system s.  Per sweep, each
+        // directed entry reads its 6x6 P (144 B), the old reverse message
+        // (32 B) and col/rev/n_rot of the neighbour (12 B) and writes its new
+        // message (32 B); each multi-rotamer node reads row_ptr[u..u+1], n_rot
+        // and prob (44 B), a 1-rotamer node its n_rot (4 B).  Set-up reads
+        // prob and writes the initial messages (32 B per node and entry); the
+        // marginals write 36 B per node and touch 420 B per entry.
+        unsigned long long E = (unsigned long long)(e1 - e0), Nm = s_multi, N1 = N - s_multi;
+        unsigned long long sweep = E * 220ull + Nm * 44ull + N1 * 4ull;
+        b.alg_bytes[s] += (unsigned long long)(1 + iter) * sweep + (unsigned long long)N * 32ull + E * 32ull +
+                          (unsigned long long)N * 36ull + E * 420ull;
     }
     // node marginals
     const float* Nf = NB[nc];
@@ -1028,7 +846,13 @@ void launch_bp(DBP& b, const DGraph& g, const float* const* in, float* const* in
         cudaFuncSetAttribute(bp_solve2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
         configured = smem;
     }
+    // external records: under stream capture they become event-record nodes
+    // that every replay of the graph re-records (a plain record would only
+    // order the capture)
+    bool timed = b.kt_ev && *b.kt_used + 2 <= b.kt_cap;
+    if (timed) cudaEventRecordWithFlags(b.kt_ev[(*b.kt_used)++], st, cudaEventRecordExternal);
     bp_solve2_kernel<<<b.n_sys, 1024, smem, st>>>(b, want_energy, energy_out);
+    if (timed) cudaEventRecordWithFlags(b.kt_ev[(*b.kt_used)++], st, cudaEventRecordExternal);
     bp_sens_kernel<<<blocks, 256, 0, st>>>(b, g, in_sens[0], in_sens[1], in_sens[2], in_sens[3], n_in, w[0], w[1],
                                            w[2], w[3]);
     (void)scan_total;

@@ -99,6 +99,13 @@ struct DBP {
     const int* bead_loc;        // bead -> row in the bead node output
     double* e11;                // per system sum of energies of 1-1 bead edges
     int* status;
+    // measurement: running per-system total of the solve kernel's algorithmic
+    // bytes (the formula is in bp_solve2_kernel), and optional host-side CUDA
+    // events bracketing each solve launch (kt_ev null: no events recorded)
+    unsigned long long* alg_bytes;
+    cudaEvent_t* kt_ev;
+    int* kt_used;
+    int kt_cap;
 };
 
 // --------------------------------------------------------------- launchers --
@@ -111,5 +118,9 @@ void launch_param_deriv(const DGraph& g, float* out, cudaStream_t st);
 // in: up to 4 one-body energy inputs (bead rows), in_sens their sensitivities
 void launch_bp(DBP& b, const DGraph& g, const float* const* in, float* const* in_sens, const int* w, int n_in,
                int prev_n_ent, int* scan_total, int want_energy, double* energy_out, cudaStream_t st);
+// standalone pair list of one point set (pairlist.cu); row_count and row_off
+// each hold ceil(n/4) ints, row_off one more
+cudaError_t launch_point_pairs(const float* pos, int n, float cutoff, int* pairs, int cap, int* n_pairs,
+                               int* row_count, int* row_off, cudaStream_t st);
 
 }  // namespace ug

@@ -1,0 +1,95 @@
+// Standalone pair list of one point set on the device: every (i, j), i < j,
+// with |x_i - x_j| < cutoff.  This is the interaction-graph pair search of the
+// engine (the reference's PairlistComputation, src/interaction_graph.h:122-157:
+// blocks of four set-1 points against all later points) exposed on its own, for callers
+// that hold positions in device memory and want the list without building an
+// engine.
+//
+// Layout: positions are n x 3 floats (x, y, z per point), pairs are written
+// as int32 (i, j).  The order is the engine's (and the reference's): by
+// i / 4, then j, then i % 4.
+//
+// Two passes with a scan between them: one warp per row of four points counts
+// its hits, a single-block scan turns counts into row offsets and the total,
+// and the second pass writes each row's pairs at its offset.  The scratch is
+// the row counts and row offsets (2 * ceil(n/4) + 1 ints).
+#include <cuda_runtime.h>
+
+#include "graph.h"
+
+namespace ug {
+
+template <int PASS>
+__global__ void point_pair_kernel(const float* __restrict__ pos, int n, float c2, int* __restrict__ row_count,
+                                  const int* __restrict__ row_off, int2* __restrict__ pairs, int cap) {
+    int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    int lane = threadIdx.x & 31;
+    int n_warps = (gridDim.x * blockDim.x) >> 5;
+    int n_rows = (n + 3) >> 2;
+    for (int r = warp; r < n_rows; r += n_warps) {
+        int i1s = 4 * r;
+        int nl = min(4, n - i1s);
+        float ax[4], ay[4], az[4];
+#pragma unroll
+        for (int l = 0; l < 4; ++l) {
+            bool ok = l < nl;
+            ax[l] = ok ? pos[3 * (i1s + l)] : 1e20f;
+            ay[l] = ok ? pos[3 * (i1s + l) + 1] : 1e20f;
+            az[l] = ok ? pos[3 * (i1s + l) + 2] : 1e20f;
+        }
+        int base = PASS ? row_off[r] : 0;
+        int count = 0;
+        for (int j0 = i1s + 1; j0 < n; j0 += 32) {
+            int j = j0 + lane;
+            unsigned mask = 0;
+            if (j < n) {
+                float bx = pos[3 * j], by = pos[3 * j + 1], bz = pos[3 * j + 2];
+#pragma unroll
+                for (int l = 0; l < 4; ++l) {
+                    if (l >= nl || !(i1s + l < j)) continue;
+                    float dx = ax[l] - bx, dy = ay[l] - by, dz = az[l] - bz;
+                    float d2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+                    if (d2 < c2) mask |= 1u << l;
+                }
+            }
+            int c = __popc(mask);
+            if (PASS == 0) {
+                count += c;
+            } else {
+                int incl = c;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    int y = __shfl_up_sync(0xffffffffu, incl, o);
+                    if (lane >= o) incl += y;
+                }
+                int p = base + incl - c;
+                for (int l = 0; l < 4; ++l)
+                    if (mask & (1u << l)) {
+                        if (p < cap) pairs[p] = make_int2(i1s + l, j);
+                        ++p;
+                    }
+                base += __shfl_sync(0xffffffffu, incl, 31);
+            }
+        }
+        if (PASS == 0) {
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) count += __shfl_xor_sync(0xffffffffu, count, o);
+            if (lane == 0) row_count[r] = count;
+        }
+    }
+}
+
+cudaError_t launch_point_pairs(const float* pos, int n, float cutoff, int* pairs, int cap, int* n_pairs,
+                               int* row_count, int* row_off, cudaStream_t st) {
+    int n_rows = (n + 3) / 4;
+    if (n_rows == 0) return cudaMemsetAsync(n_pairs, 0, sizeof(int), st);
+    int blocks = min(8 * 152, (n_rows * 32 + 255) / 256);
+    float c2 = cutoff * cutoff;
+    int2* p2 = reinterpret_cast<int2*>(pairs);
+    point_pair_kernel<0><<<blocks, 256, 0, st>>>(pos, n, c2, row_count, row_off, p2, cap);
+    launch_scan(row_count, row_off, n_rows, n_pairs, st);
+    point_pair_kernel<1><<<blocks, 256, 0, st>>>(pos, n, c2, row_count, row_off, p2, cap);
+    return cudaGetLastError();
+}
+
+}  // namespace ug

@@ -60,8 +60,16 @@ def lib():
         L.ug_profile.argtypes = [vp, ip, ctypes.c_char_p, ip, vp, ip]
         L.ug_bench.argtypes = [vp, ip, ctypes.c_float, ctypes.c_float, ip, ip, vp]
         L.ug_set_device.argtypes = [ip]
+        L.ug_bench_kernel.argtypes = [vp, vp]
+        L.ug_pair_list.argtypes = [vp, ip, ctypes.c_float, vp, ip, vp, vp]
         _lib = L
     return _lib
+
+
+def pair_list(pos_ptr, n, cutoff, pairs_ptr, cap, n_pairs_ptr, stream=0):
+    """ug_pair_list on device pointers (ints): pairs (i, j), i < j, closer than cutoff."""
+    if lib().ug_pair_list(pos_ptr, n, cutoff, pairs_ptr, cap, n_pairs_ptr, stream):
+        raise RuntimeError(lib().ug_last_error().decode())
 
 
 def _f32(a):
@@ -269,6 +277,13 @@ class Batch:
         self._chk(lib().ug_bench(self.h, int(n_round), float(dt), float(timescale), int(flush_l2), int(e2e),
                                  ms.ctypes.data))
         return ms
+
+    def bench_kernel(self):
+        """The BP solve kernel over the last bench(): summed device ms, launches,
+        summed algorithmic bytes."""
+        s = np.zeros(3, np.float64)
+        self._chk(lib().ug_bench_kernel(self.h, s.ctypes.data))
+        return {"ms": float(s[0]), "launches": int(s[1]), "bytes": float(s[2])}
 
     def profile(self, n_eval=5):
         names = ctypes.create_string_buffer(1 << 16)
