@@ -99,6 +99,20 @@ int ug_profile(UgBatch* b, int n_eval, char* names, int names_cap, float* ms, in
  * before returning. */
 int ug_pair_list(const float* pos, int n, float cutoff, int32_t* pairs, int cap, int32_t* n_pairs, void* stream);
 
+/* ug_pair_list without any device allocation (no counterpart in the
+ * reference).  For callers that cannot allocate device memory when they need
+ * the list: services whose device memory is reserved up front, code that must
+ * not synchronise the device the way cudaMalloc/cudaFree can, hosts without an
+ * allocator of their own.  The scratch is a fixed device array built into the
+ * library, so n is limited to 262144 points; larger n is rejected with an
+ * error naming the limit.  The first call on each device looks up that array's
+ * address (make it before any stream capture); later calls only enqueue work
+ * on `stream` and return without synchronising.  Nothing has to be zeroed
+ * beforehand.  Calls that can run at the same time on one device (two streams,
+ * two host threads) share the array and race: order them on one stream.
+ * Output, order and arguments as ug_pair_list. */
+int ug_pair_list_noalloc(const float* pos, int n, float cutoff, int32_t* pairs, int cap, int32_t* n_pairs,
+                         void* stream);
 
 #ifdef __cplusplus
 }

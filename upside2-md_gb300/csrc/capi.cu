@@ -563,4 +563,23 @@ int ug_pair_list(const float* pos, int n, float cutoff, int32_t* pairs, int cap,
     GUARD_END(1)
 }
 
+int ug_pair_list_noalloc(const float* pos, int n, float cutoff, int32_t* pairs, int cap, int32_t* n_pairs,
+                         void* stream) {
+    GUARD_BEGIN
+    if (n < 0 || cap < 0 || !(cutoff > 0.f))
+        throw ug::Error("ug_pair_list_noalloc: need n >= 0, cap >= 0, cutoff > 0");
+    if (n > ug::point_pairs_noalloc_max())
+        throw ug::Error("ug_pair_list_noalloc: n = " + std::to_string(n) + " points exceeds the fixed scratch limit of " +
+                        std::to_string(ug::point_pairs_noalloc_max()) + " points (use ug_pair_list)");
+    if ((n > 0 && !pos) || (cap > 0 && !pairs) || !n_pairs)
+        throw ug::Error("ug_pair_list_noalloc: null device pointer");
+    int* scratch = nullptr;
+    UG_CK(ug::point_pairs_noalloc_scratch(&scratch));
+    int n_rows = (n + 3) / 4;
+    UG_CK(ug::launch_point_pairs(pos, n, cutoff, pairs, cap, n_pairs, scratch, scratch + n_rows,
+                                 static_cast<cudaStream_t>(stream)));
+    return 0;
+    GUARD_END(1)
+}
+
 }  // extern "C"

@@ -122,5 +122,9 @@ void launch_bp(DBP& b, const DGraph& g, const float* const* in, float* const* in
 // each hold ceil(n/4) ints, row_off one more
 cudaError_t launch_point_pairs(const float* pos, int n, float cutoff, int* pairs, int cap, int* n_pairs,
                                int* row_count, int* row_off, cudaStream_t st);
+// fixed device scratch for the no-allocation pair list: the largest point
+// count it holds, and its address on the current device
+int point_pairs_noalloc_max();
+cudaError_t point_pairs_noalloc_scratch(int** out);
 
 }  // namespace ug

@@ -15,6 +15,8 @@
 // the row counts and row offsets (2 * ceil(n/4) + 1 ints).
 #include <cuda_runtime.h>
 
+#include <mutex>
+
 #include "graph.h"
 
 namespace ug {
@@ -90,6 +92,47 @@ cudaError_t launch_point_pairs(const float* pos, int n, float cutoff, int* pairs
     launch_scan(row_count, row_off, n_rows, n_pairs, st);
     point_pair_kernel<1><<<blocks, 256, 0, st>>>(pos, n, c2, row_count, row_off, p2, cap);
     return cudaGetLastError();
+}
+
+// ------------------------------------------------------ no-allocation form --
+// Some callers cannot allocate device memory at the moment they need a pair
+// list: code running inside a real-time or memory-capped service whose device
+// memory is fully reserved up front, callers that must not synchronise the
+// device (cudaMalloc/cudaFree can), and host code that owns no allocator of
+// its own.  For them the scratch lives in a fixed file-scope device array
+// instead of being allocated per call.  Its size bounds the problem: at most
+// kNoAllocMaxPoints points (2 * 65536 + 1 ints = 512 KiB of scratch).
+//
+// Nothing in the scratch needs to start at zero: the counting pass writes
+// every row count, and the scan writes every row offset and the total.
+// Calls whose kernels can run at the same time on one device (two streams,
+// two host threads) share this one array and race; order them on one stream.
+constexpr int kNoAllocMaxPoints = 262144;
+constexpr int kNoAllocRows = kNoAllocMaxPoints / 4;
+static __device__ __align__(256) int g_point_pair_scratch[2 * kNoAllocRows + 1];
+
+int point_pairs_noalloc_max() { return kNoAllocMaxPoints; }
+
+// Device address of the fixed scratch on the current device, looked up once
+// per device (the first call on a device does this setup; later calls only
+// read the cached pointer).
+cudaError_t point_pairs_noalloc_scratch(int** out) {
+    constexpr int kMaxDevices = 64;
+    static std::mutex mu;
+    static int* addr[kMaxDevices] = {};
+    int dev = -1;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lock(mu);
+    if (!addr[dev]) {
+        void* p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_point_pair_scratch);
+        if (e != cudaSuccess) return e;
+        addr[dev] = static_cast<int*>(p);
+    }
+    *out = addr[dev];
+    return cudaSuccess;
 }
 
 }  // namespace ug

@@ -62,6 +62,7 @@ def lib():
         L.ug_set_device.argtypes = [ip]
         L.ug_bench_kernel.argtypes = [vp, vp]
         L.ug_pair_list.argtypes = [vp, ip, ctypes.c_float, vp, ip, vp, vp]
+        L.ug_pair_list_noalloc.argtypes = [vp, ip, ctypes.c_float, vp, ip, vp, vp]
         _lib = L
     return _lib
 
@@ -69,6 +70,13 @@ def lib():
 def pair_list(pos_ptr, n, cutoff, pairs_ptr, cap, n_pairs_ptr, stream=0):
     """ug_pair_list on device pointers (ints): pairs (i, j), i < j, closer than cutoff."""
     if lib().ug_pair_list(pos_ptr, n, cutoff, pairs_ptr, cap, n_pairs_ptr, stream):
+        raise RuntimeError(lib().ug_last_error().decode())
+
+
+def pair_list_noalloc(pos_ptr, n, cutoff, pairs_ptr, cap, n_pairs_ptr, stream=0):
+    """ug_pair_list_noalloc: as pair_list, scratch in a fixed device array
+    (n <= 262144), asynchronous on `stream`."""
+    if lib().ug_pair_list_noalloc(pos_ptr, n, cutoff, pairs_ptr, cap, n_pairs_ptr, stream):
         raise RuntimeError(lib().ug_last_error().decode())
 
 
