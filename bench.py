@@ -36,6 +36,7 @@ def parse():
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-plain", action="store_true", help="skip the plain single-system GPU comparison")
     ap.add_argument("--profile", action="store_true", help="print per-node device times to stderr")
     return ap.parse_args()
 
@@ -223,6 +224,7 @@ def main():
     t_e2e = d.max(float(ms_e2e.sum()) / 1e3)
     e2e_value = units / t_e2e
     st = b.status()
+    plain = plain_single_rate(W, a) if not a.no_plain else None
     cpu = None
     if d.rank == 0 and d.world == 1 and not a.no_cpu_baseline:
         rate, cores, sample = cpu_port_rate(W["configs"], a.cpu_seconds)
@@ -243,17 +245,43 @@ def main():
         "clocks": clk.summary(),
         "roofline": roof,
         "cpu_baseline": cpu,
+        "plain_single_replica": plain,
         "status_bits": st,
         "device_bytes": dev_bytes,
     }
     print(json.dumps(line))
 
 
+def plain_single_rate(W, a, n_sample=6, rounds=8):
+    """The plain single-replica GPU path on a sample of the same workload:
+    each sampled system in an engine of its own (one system per launch, the
+    same kernels and one-round CUDA graph), timed like the batch.  Returns
+    residue-steps/s of running the sample one system after another."""
+    import numpy as np
+    import upside_gb300 as U
+    import workloads
+    idx = list(range(min(n_sample, len(W["configs"]))))
+    units = t = 0.0
+    for i in idx:
+        c = W["configs"][i]
+        s = U.Batch([c])
+        s.set_pos(workloads.initial_positions([c]))
+        s.set_thermostat([W["temps"][i]], np.array([W["seeds"][i]], np.uint32))
+        s.run(3, use_graph=True, graph_rounds=1)
+        ms = s.bench(rounds, flush_l2=True)
+        units += W["n_res"][i] * 3 * rounds
+        t += float(ms.sum()) / 1e3
+        del s
+    return {"value": units / t, "unit": "residue-steps/s",
+            "sample": "systems %s of the workload (%s residues), %d rounds each, one system per engine" % (
+                ",".join(map(str, idx)), ",".join(str(W["n_res"][i]) for i in idx), rounds)}
+
+
 def ncu_traffic(workload):
     """DRAM bytes per launch of the BP solve kernel from the committed ncu
-    summary of this workload (profiles/bp_solve2_kernel_<workload>.md, line
+    summary of this workload (profiles/bp_solve_kernel_<workload>.md, line
     'dram_bytes_per_launch: N'), or None when no capture was summarised."""
-    path = os.path.join(ROOT, "profiles", "bp_solve2_kernel_%s.md" % workload)
+    path = os.path.join(ROOT, "profiles", "bp_solve_kernel_%s.md" % workload)
     try:
         with open(path) as f:
             for line in f:
@@ -265,7 +293,7 @@ def ncu_traffic(workload):
 
 
 def roofline(b, W, a, peak, peak_kind):
-    """The dominant kernel (the rotamer BP solve, bp_solve2_kernel) against the
+    """The dominant kernel (the rotamer BP solve, bp_solve_kernel) against the
     HBM roofline: algorithmic bytes per launch (tallied by the kernel) over its
     mean launch time, both from the timed rounds (CUDA events recorded around
     every launch inside the replayed graph on the engine stream)."""
@@ -275,7 +303,7 @@ def roofline(b, W, a, peak, peak_kind):
     per_launch_s = k["ms"] / 1e3 / k["launches"]
     bytes_per_launch = k["bytes"] / k["launches"]
     achieved = bytes_per_launch / per_launch_s / 1e9
-    return {"kernel": "bp_solve2_kernel", "bound": "hbm", "achieved": achieved, "peak": peak,
+    return {"kernel": "bp_solve_kernel", "bound": "hbm", "achieved": achieved, "peak": peak,
             "peak_kind": "of " + peak_kind, "unit": "GB/s", "frac": achieved / peak,
             "traffic": ncu_traffic(a.workload), "algorithmic_bytes_per_launch": bytes_per_launch,
             "ms_per_launch": 1e3 * per_launch_s, "launches": k["launches"]}

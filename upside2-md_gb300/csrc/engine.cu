@@ -1676,7 +1676,9 @@ struct RotamerNode : GNode {
         b.n_res = res_off.back();
         b.n_bead = int(bead_res.size());
         b.max_res_sys = *std::max_element(n_res_sys.begin(), n_res_sys.end());
-        if (b.max_res_sys * 64 > 220 * 1024) throw Error("system too large for the shared-memory BP solver");
+        if (bp_solve_smem_bytes(b.max_res_sys) > size_t(220) * 1024)
+            throw Error("system too large for the shared-memory BP solver (" + std::to_string(b.max_res_sys) +
+                        " residues)");
         b.res_off = e.upload(res_off);
         b.nrot = e.upload(nrot);
         b.res_N = e.upload(resN);
@@ -1708,6 +1710,7 @@ struct RotamerNode : GNode {
         b.col = e.alloc<int>(size_t(cap));
         b.erow = e.alloc<int>(size_t(cap));
         b.rev = e.alloc<int>(size_t(cap));
+        b.einfo = e.alloc<int4>(size_t(cap));
         b.esum = e.alloc<float>(size_t(cap) * 36);
         b.P = e.alloc<float>(size_t(cap) * 36);
         b.emarg = e.alloc<float>(size_t(cap) * 36);

@@ -10,12 +10,18 @@
 //   hbond coverage edge        src/hbond.cpp:249-294
 //   environment coverage edges src/environment.cpp:114-228
 //   rotamer BP                 src/rotamer.cpp:239-302, :425-569, :854-1162
+#include <cooperative_groups.h>
 #include <cstdio>
 
 #include "dev_math.cuh"
 #include "graph.h"
 
 namespace ug {
+
+namespace cg = cooperative_groups;
+
+// blocks (SMs) per system in the BP solve
+constexpr int BP_CLUSTER = 2;
 
 // ---------------------------------------------------------------- scan ---
 // Exclusive scan of n ints into out[0..n] (out[n] = total) by one 1024-thread
@@ -493,6 +499,7 @@ __global__ void bp_entry_init_kernel(DBP b) {
             rv = e;
         }
         b.rev[e] = rv;
+        b.einfo[e] = make_int4(b.res_local[b.erow[e]], rv, b.res_local[b.col[e]], 0);
     }
     for (int i = grid_stride_start(); i < n * 36; i += grid_stride()) b.esum[i] = 0.f;
 }
@@ -538,17 +545,23 @@ __global__ void bp_prob_kernel(DBP b) {
 }
 
 // ---------------------------------------------------------------------------
-// BP solve, warp-per-node form.  One block per system; the system's node
-// beliefs (both ping-pong buffers) live in shared memory.  A sweep is one
-// pass over the nodes: the warp that owns node u computes, one lane per
-// incoming entry (u <- v), the new message from v's old belief divided by the
-// old reverse message, stores it, and folds it into u's new belief with a
-// butterfly product across lanes (renormalised at every level, which only
-// rescales).  Sweeps are Jacobi updates (all reads from the old buffers), as
-// in the reference, so one barrier per sweep suffices.  The iteration
-// structure (undamped first sweep with swap, chunks of `chunk` damped sweeps,
-// one-sided maximum deviation test) follows src/rotamer.cpp:1106-1162; the
-// marginals and Bethe free energy follow src/rotamer.cpp:425-569.
+// BP solve.  One block per system.  A sweep has two phases separated by a
+// block barrier:
+//   messages: one thread per directed entry f = (v <- u) of the system.  From
+//     v's old belief divided by the old message into v along f, and f's
+//     matrix P_f(x_v, x_u), it forms the new message from v to u and stores
+//     it in the reverse entry (u <- v), the slot u reads;
+//   beliefs: one thread per node u multiplies its incoming new messages into
+//     prob_u and applies the reference's normalisation, damping and
+//     one-sided deviation.
+// This is the reference's Jacobi sweep (every read from the old buffers)
+// with the message computed by the sending node, so each thread's loads are
+// independent of the others'.  The iteration structure (undamped first sweep
+// with swap, chunks of `chunk` damped sweeps, one-sided maximum deviation
+// test) follows src/rotamer.cpp:1106-1162; the messages and beliefs follow
+// src/rotamer.cpp:259-281, :500-569; the marginals and Bethe free energy
+// src/rotamer.cpp:425-471.  Node beliefs (both buffers) and rotamer counts
+// live in shared memory; P and messages stay in global memory (L2-resident).
 __device__ __forceinline__ void renorm6(float* x, int n) {
     float s = 0.f;
 #pragma unroll
@@ -558,67 +571,80 @@ __device__ __forceinline__ void renorm6(float* x, int n) {
     for (int k = 0; k < 6; ++k) x[k] *= inv;
 }
 
-__device__ __forceinline__ float bp_node_sweep(const DBP& b, int u, int r0, int e1, const float* __restrict__ Nold,
-                                               float* __restrict__ Ncur, const float* __restrict__ Eold,
-                                               float* __restrict__ Ecur, int mode, float damp, int lane) {
-    int n = b.nrot[u];
-    if (n == 1) return 0.f;
-    int eb = b.row_ptr[u], ee = min(b.row_ptr[u + 1], e1);
-    float prod[6] = {1.f, 1.f, 1.f, 1.f, 1.f, 1.f};
-    for (int base = eb; base < ee; base += 32) {
-        int e = base + lane;
-        float m[6] = {1.f, 1.f, 1.f, 1.f, 1.f, 1.f};
-        if (e < ee) {
-            int v = b.col[e];
-            int rv = b.rev[e];
-            int nv = b.nrot[v];
-            const float* ob = Nold + (v - r0) * 8;
-            const float4* om = reinterpret_cast<const float4*>(Eold + size_t(rv) * 8);
-            float4 o0 = om[0], o1 = om[1];
-            float omv[6] = {o0.x, o0.y, o0.z, o0.w, o1.x, o1.y};
-            float cav[6];
+// new message along every entry of [e0, e1): einfo[f] = (local index of the
+// row node v, reverse entry, local index of the column node u, 0)
+__device__ __forceinline__ void bp_messages(const DBP& b, int e0, int e1, const float* __restrict__ Nold,
+                                            const int* __restrict__ s_nrot, const float* __restrict__ Eold,
+                                            float* __restrict__ Ecur, int tid, int nt) {
+    for (int f = e0 + tid; f < e1; f += nt) {
+        int4 inf = b.einfo[f];
+        int nv = s_nrot[inf.x], nu = s_nrot[inf.z];
+        const float* ob = Nold + inf.x * 8;
+        const float4* om = reinterpret_cast<const float4*>(Eold + size_t(f) * 8);
+        float4 o0 = om[0], o1 = om[1];
+        float omv[6] = {o0.x, o0.y, o0.z, o0.w, o1.x, o1.y};
+        float cav[6];
 #pragma unroll
-            for (int k = 0; k < 6; ++k) cav[k] = k < nv ? ob[k] / (1e-10f + omv[k]) : 0.f;
-            const float4* P4 = reinterpret_cast<const float4*>(b.P + size_t(e) * 36);
-            float P[36];
+        for (int k = 0; k < 6; ++k) cav[k] = k < nv ? ob[k] / (1e-10f + omv[k]) : 0.f;
+        const float4* P4 = reinterpret_cast<const float4*>(b.P + size_t(f) * 36);
+        float P[36];
 #pragma unroll
-            for (int q = 0; q < 9; ++q) {
-                float4 t = P4[q];
-                P[4 * q] = t.x; P[4 * q + 1] = t.y; P[4 * q + 2] = t.z; P[4 * q + 3] = t.w;
-            }
-            float mm[6], sum = 0.f;
-#pragma unroll
-            for (int i = 0; i < 6; ++i) {
-                float acc = 0.f;
-#pragma unroll
-                for (int k = 0; k < 6; ++k) acc += P[i * 6 + k] * cav[k];
-                mm[i] = i < n ? acc : 0.f;
-                sum += mm[i];
-            }
-            float inv = 1.f / sum;
-            float4* out = reinterpret_cast<float4*>(Ecur + size_t(e) * 8);
-            out[0] = make_float4(mm[0] * inv, mm[1] * inv, mm[2] * inv, mm[3] * inv);
-            out[1] = make_float4(mm[4] * inv, mm[5] * inv, 0.f, 0.f);
-#pragma unroll
-            for (int i = 0; i < 6; ++i) m[i] = i < n ? mm[i] * inv : 1.f;
+        for (int q = 0; q < 9; ++q) {
+            float4 t = P4[q];
+            P[4 * q] = t.x; P[4 * q + 1] = t.y; P[4 * q + 2] = t.z; P[4 * q + 3] = t.w;
         }
+        float mm[6], sum = 0.f;
 #pragma unroll
-        for (int i = 0; i < 6; ++i) prod[i] *= m[i];
-        renorm6(prod, n);
+        for (int i = 0; i < 6; ++i) {
+            float acc = 0.f;
+#pragma unroll
+            for (int k = 0; k < 6; ++k) acc += P[k * 6 + i] * cav[k];
+            mm[i] = i < nu ? acc : 0.f;
+            sum += mm[i];
+        }
+        float inv = 1.f / sum;
+        float4* out = reinterpret_cast<float4*>(Ecur + size_t(inf.y) * 8);
+        out[0] = make_float4(mm[0] * inv, mm[1] * inv, mm[2] * inv, mm[3] * inv);
+        out[1] = make_float4(mm[4] * inv, mm[5] * inv, 0.f, 0.f);
     }
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) {
-#pragma unroll
-        for (int i = 0; i < 6; ++i) prod[i] *= __shfl_xor_sync(0xffffffffu, prod[i], off);
-        renorm6(prod, n);
-    }
+}
+
+// new beliefs of the system's nodes; returns this thread's largest one-sided
+// deviation (mode 1)
+__device__ __forceinline__ float bp_beliefs(const DBP& b, int r0, int lo, int hi, int e1, const float* __restrict__ Nold,
+                                            float* __restrict__ Ncur, const int* __restrict__ s_nrot,
+                                            const float* __restrict__ Ecur, int mode, float damp, int tid,
+                                            int nt) {
     float dev = 0.f;
-    if (lane == 0) {
+    for (int ul = lo + tid; ul < hi; ul += nt) {
+        int n = s_nrot[ul];
+        if (n == 1) continue;
+        int u = r0 + ul;
+        int eb = b.row_ptr[u], ee = min(b.row_ptr[u + 1], e1);
+        float prod[6] = {1.f, 1.f, 1.f, 1.f, 1.f, 1.f};
+        const float4* m4 = reinterpret_cast<const float4*>(Ecur);
+        int e = eb;
+        // four messages per step with their loads issued together; the
+        // running product is renormalised after every factor, so it never
+        // underflows (each message sums to 1)
+        auto fold = [&](float4 a, float4 c) {
+            prod[0] *= a.x; prod[1] *= a.y; prod[2] *= a.z; prod[3] *= a.w; prod[4] *= c.x; prod[5] *= c.y;
+            renorm6(prod, n);
+        };
+        for (; e + 4 <= ee; e += 4) {
+            float4 a0 = m4[2 * e], c0 = m4[2 * e + 1], a1 = m4[2 * e + 2], c1 = m4[2 * e + 3];
+            float4 a2 = m4[2 * e + 4], c2 = m4[2 * e + 5], a3 = m4[2 * e + 6], c3 = m4[2 * e + 7];
+            fold(a0, c0);
+            fold(a1, c1);
+            fold(a2, c2);
+            fold(a3, c3);
+        }
+        for (; e < ee; ++e) fold(m4[2 * e], m4[2 * e + 1]);
         float bl[6];
 #pragma unroll
         for (int k = 0; k < 6; ++k) bl[k] = k < n ? b.prob[u * 8 + k] * prod[k] : 0.f;
         renorm6(bl, n);
-        const float* o = Nold + (u - r0) * 8;
+        const float* o = Nold + ul * 8;
         if (mode == 1) {
             float mx = bl[0];
             for (int k = 1; k < n; ++k) mx = fmaxf(mx, bl[k]);
@@ -629,7 +655,7 @@ __device__ __forceinline__ float bp_node_sweep(const DBP& b, int u, int r0, int 
                 if (k < n) dev = fmaxf(dev, bl[k] - o[k]);
             }
         }
-        float* c = Ncur + (u - r0) * 8;
+        float* c = Ncur + ul * 8;
 #pragma unroll
         for (int k = 0; k < 6; ++k) c[k] = bl[k];
         c[6] = c[7] = 0.f;
@@ -637,22 +663,49 @@ __device__ __forceinline__ float bp_node_sweep(const DBP& b, int u, int r0, int 
     return dev;
 }
 
-__global__ void __launch_bounds__(1024) bp_solve2_kernel(DBP b, int want_energy, double* energy_out) {
+// One cluster of BP_CLUSTER blocks per system.  Block c of the cluster owns a
+// contiguous range of the system's nodes, split so that every block gets
+// about the same number of directed entries (the CSR rows of its nodes), and
+// runs both phases over its own entries and nodes.  Messages cross blocks
+// through global memory: a block writes the reverse entries of its rows, and
+// the cluster barrier between the phases (release/acquire at cluster scope)
+// makes them visible to their owners.  Beliefs never leave their block.
+__global__ void __launch_bounds__(1024) bp_solve_kernel(DBP b, int want_energy, double* energy_out) {
     extern __shared__ float smem[];
     __shared__ float red[32];
     __shared__ double dred[32];
-    const int s = blockIdx.x;
+    __shared__ float s_dev[BP_CLUSTER];
+    __shared__ double s_en[BP_CLUSTER];
+    __shared__ int s_multi;
+    cg::cluster_group cluster = cg::this_cluster();
+    const int crank = int(cluster.block_rank());
+    const int s = blockIdx.x / BP_CLUSTER;
     const int r0 = b.res_off[s], r1 = b.res_off[s + 1], N = r1 - r0;
     const int e0 = b.row_ptr[r0], e1 = min(b.row_ptr[r1], b.ent_cap);
+    // own nodes [lo, hi) (system-local): block c starts at the first node whose
+    // row begins at or after c/BP_CLUSTER of the system's entries
+    auto split = [&](int c) -> int {
+        if (c <= 0) return 0;
+        if (c >= BP_CLUSTER) return N;
+        long long target = e0 + (long long)(e1 - e0) * c / BP_CLUSTER;
+        int a = 0, z = N;  // first ul in [0, N] with row_ptr[r0 + ul] >= target
+        while (a < z) {
+            int m = (a + z) >> 1;
+            if (b.row_ptr[r0 + m] >= target) z = m; else a = m + 1;
+        }
+        return a;
+    };
+    const int lo = split(crank), hi = split(crank + 1);
+    const int eo0 = min(b.row_ptr[r0 + lo], e1), eo1 = min(b.row_ptr[r0 + hi], e1);
     float* NB[2] = {smem, smem + N * 8};
+    int* s_nrot = reinterpret_cast<int*>(smem + 2 * N * 8);
     float* EM[2] = {b.msg, b.msg + size_t(b.ent_cap) * 8};
     const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
 
     auto sweep = [&](const float* Nold, float* Ncur, const float* Eold, float* Ecur, int mode, float damp) {
-        float dev = 0.f;
-        for (int u = r0 + warp; u < r1; u += nw) dev = fmaxf(dev, bp_node_sweep(b, u, r0, e1, Nold, Ncur, Eold, Ecur,
-                                                                               mode, damp, lane));
-        return dev;
+        bp_messages(b, eo0, eo1, Nold, s_nrot, Eold, Ecur, tid, nt);
+        cluster.sync();
+        return bp_beliefs(b, r0, lo, hi, e1, Nold, Ncur, s_nrot, Ecur, mode, damp, tid, nt);
     };
     auto block_max = [&](float v) -> float {
 #pragma unroll
@@ -664,16 +717,27 @@ __global__ void __launch_bounds__(1024) bp_solve2_kernel(DBP b, int want_energy,
         __syncthreads();
         return r;
     };
+    // largest deviation over the cluster: every block posts its own maximum
+    // into slot crank of every block, then one cluster barrier
+    auto cluster_max = [&](float v) -> float {
+        v = block_max(v);
+        if (tid < BP_CLUSTER) *cluster.map_shared_rank(&s_dev[crank], tid) = v;
+        cluster.sync();
+        float r = 0.f;
+#pragma unroll
+        for (int c = 0; c < BP_CLUSTER; ++c) r = fmaxf(r, s_dev[c]);
+        return r;
+    };
 
-    // N.old = N.cur = prob; E.old = 1
-    __shared__ int s_multi;
+    // N.old = N.cur = prob; E.old = 1 (own entries)
     if (tid == 0) s_multi = 0;
     for (int i = tid; i < N * 8; i += nt) NB[0][i] = NB[1][i] = b.prob[r0 * 8 + i];
-    for (int i = e0 * 8 + tid; i < e1 * 8; i += nt) EM[1][i] = 1.f;
+    for (int i = tid; i < N; i += nt) s_nrot[i] = b.nrot[r0 + i];
+    for (int i = eo0 * 8 + tid; i < eo1 * 8; i += nt) EM[1][i] = 1.f;
     __syncthreads();
-    {  // multi-rotamer node count, for the algorithmic-byte tally at the end
+    {  // multi-rotamer node count of the system, for the algorithmic-byte tally
         int m = 0;
-        for (int u = r0 + tid; u < r1; u += nt) m += b.nrot[u] > 1;
+        for (int u = tid; u < N; u += nt) m += s_nrot[u] > 1;
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) m += __shfl_xor_sync(0xffffffffu, m, o);
         if (lane == 0 && m) atomicAdd(&s_multi, m);
@@ -682,10 +746,10 @@ __global__ void __launch_bounds__(1024) bp_solve2_kernel(DBP b, int want_energy,
     // "old"; the other (prob) is max-normalised (src/rotamer.cpp:1135)
     sweep(NB[1], NB[0], EM[1], EM[0], 0, 0.f);
     __syncthreads();
-    for (int u = r0 + tid; u < r1; u += nt) {
-        int n = b.nrot[u];
+    for (int ul = lo + tid; ul < hi; ul += nt) {
+        int n = s_nrot[ul];
         if (n == 1) continue;
-        float* c = NB[1] + (u - r0) * 8;
+        float* c = NB[1] + ul * 8;
         float mx = c[0];
         for (int k = 1; k < n; ++k) mx = fmaxf(mx, c[k]);
         float inv = 1.f / mx;
@@ -703,41 +767,42 @@ __global__ void __launch_bounds__(1024) bp_solve2_kernel(DBP b, int want_energy,
             d = sweep(NB[nc ^ 1], NB[nc], EM[ec ^ 1], EM[ec], 1, b.damping);
             __syncthreads();
         }
-        dev = block_max(d);
+        dev = cluster_max(d);
     }
-    if (tid == 0) {
+    if (tid == 0 && crank == 0) {
         b.n_iter[s] = iter;
         if (iter >= b.max_iter - b.chunk - 1) atomicOr(b.status, ST_BP_NOT_CONVERGED);
         // algorithmic bytes of this launch for system s.  Per sweep, each
-        // directed entry reads its 6x6 P (144 B), the old reverse message
-        // (32 B) and col/rev/n_rot of the neighbour (12 B) and writes its new
-        // message (32 B); each multi-rotamer node reads row_ptr[u..u+1], n_rot
-        // and prob (44 B), a 1-rotamer node its n_rot (4 B).  Set-up reads
-        // prob and writes the initial messages (32 B per node and entry); the
-        // marginals write 36 B per node and touch 420 B per entry.
-        unsigned long long E = (unsigned long long)(e1 - e0), Nm = s_multi, N1 = N - s_multi;
-        unsigned long long sweep = E * 220ull + Nm * 44ull + N1 * 4ull;
-        b.alg_bytes[s] += (unsigned long long)(1 + iter) * sweep + (unsigned long long)N * 32ull + E * 32ull +
+        // directed entry is read by the message phase (einfo 16 B, P 144 B,
+        // old message 32 B), written once (new message 32 B) and read by the
+        // belief phase (32 B); each multi-rotamer node reads row_ptr[u..u+1]
+        // and prob (40 B).  Set-up reads prob and n_rot and writes the
+        // initial messages (36 B per node, 32 B per entry); the marginals
+        // write 36 B per node and touch 420 B per entry.
+        unsigned long long E = (unsigned long long)(e1 - e0), Nm = s_multi;
+        unsigned long long sweep = E * 256ull + Nm * 40ull;
+        b.alg_bytes[s] += (unsigned long long)(1 + iter) * sweep + (unsigned long long)N * 36ull + E * 32ull +
                           (unsigned long long)N * 36ull + E * 420ull;
     }
-    // node marginals
+    // node marginals of own nodes
     const float* Nf = NB[nc];
-    for (int u = r0 + tid; u < r1; u += nt) {
-        int n = b.nrot[u];
+    for (int ul = lo + tid; ul < hi; ul += nt) {
+        int u = r0 + ul;
+        int n = s_nrot[ul];
         if (n == 1) {
             b.marg[u * 8] = 1.f;
             for (int k = 1; k < 8; ++k) b.marg[u * 8 + k] = 0.f;
             continue;
         }
         float sum = 0.f;
-        for (int k = 0; k < n; ++k) sum += Nf[(u - r0) * 8 + k];
+        for (int k = 0; k < n; ++k) sum += Nf[ul * 8 + k];
         float inv = 1.f / sum;
-        for (int k = 0; k < 8; ++k) b.marg[u * 8 + k] = k < n ? Nf[(u - r0) * 8 + k] * inv : 0.f;
+        for (int k = 0; k < 8; ++k) b.marg[u * 8 + k] = k < n ? Nf[ul * 8 + k] * inv : 0.f;
     }
-    __syncthreads();
-    // edge marginals
+    cluster.sync();  // every node marginal of the system is written
+    // edge marginals of own entries
     const float* Ef = EM[ec];
-    for (int e = e0 + tid; e < e1; e += nt) {
+    for (int e = eo0 + tid; e < eo1; e += nt) {
         int u = b.erow[e], v = b.col[e];
         int nu = b.nrot[u], nv = b.nrot[v];
         const float* mu = Ef + size_t(e) * 8;
@@ -757,11 +822,12 @@ __global__ void __launch_bounds__(1024) bp_solve2_kernel(DBP b, int want_energy,
         float inv = 1.f / sum;
         for (int k = 0; k < 36; ++k) mg[k] *= inv;
     }
-    if (!want_energy) return;
+    if (!want_energy) return;  // no shared-memory traffic between blocks after the last barrier
     __syncthreads();
     double en = 0.0;
-    for (int u = r0 + tid; u < r1; u += nt) {
-        int n = b.nrot[u];
+    for (int ul = lo + tid; ul < hi; ul += nt) {
+        int u = r0 + ul;
+        int n = s_nrot[ul];
         float f = b.eoff[u];
         for (int k = 0; k < n; ++k) {
             float bk = b.marg[u * 8 + k];
@@ -769,7 +835,7 @@ __global__ void __launch_bounds__(1024) bp_solve2_kernel(DBP b, int want_energy,
         }
         en += double(f);
     }
-    for (int e = e0 + tid; e < e1; e += nt) {
+    for (int e = eo0 + tid; e < eo1; e += nt) {
         int u = b.erow[e], v = b.col[e];
         if (!(u < v)) continue;
         int nu = b.nrot[u], nv = b.nrot[v];
@@ -788,8 +854,14 @@ __global__ void __launch_bounds__(1024) bp_solve2_kernel(DBP b, int want_energy,
     if (lane == 0) dred[warp] = en;
     __syncthreads();
     if (tid == 0) {
-        double t = b.e11[s];
+        double t = 0.0;
         for (int w = 0; w < nw; ++w) t += dred[w];
+        *cluster.map_shared_rank(&s_en[crank], 0) = t;
+    }
+    cluster.sync();
+    if (tid == 0 && crank == 0) {
+        double t = b.e11[s];
+        for (int c = 0; c < BP_CLUSTER; ++c) t += s_en[c];
         energy_out[s] = t;
     }
 }
@@ -840,10 +912,10 @@ void launch_bp(DBP& b, const DGraph& g, const float* const* in, float* const* in
     bp_entry_init_kernel<<<blocks, 256, 0, st>>>(b);
     bp_edge_energy_kernel<<<blocks, 256, 0, st>>>(b, g);
     bp_prob_kernel<<<blocks, 256, 0, st>>>(b);
-    size_t smem = size_t(b.max_res_sys) * 8 * 2 * sizeof(float);
+    size_t smem = bp_solve_smem_bytes(b.max_res_sys);
     static size_t configured = 0;
     if (smem > 48 * 1024 && smem > configured) {
-        cudaFuncSetAttribute(bp_solve2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+        cudaFuncSetAttribute(bp_solve_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
         configured = smem;
     }
     // external records: under stream capture they become event-record nodes
@@ -851,7 +923,21 @@ void launch_bp(DBP& b, const DGraph& g, const float* const* in, float* const* in
     // order the capture)
     bool timed = b.kt_ev && *b.kt_used + 2 <= b.kt_cap;
     if (timed) cudaEventRecordWithFlags(b.kt_ev[(*b.kt_used)++], st, cudaEventRecordExternal);
-    bp_solve2_kernel<<<b.n_sys, 1024, smem, st>>>(b, want_energy, energy_out);
+    {
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(unsigned(b.n_sys) * BP_CLUSTER);
+        cfg.blockDim = dim3(1024);
+        cfg.dynamicSmemBytes = smem;
+        cfg.stream = st;
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeClusterDimension;
+        at[0].val.clusterDim.x = BP_CLUSTER;
+        at[0].val.clusterDim.y = 1;
+        at[0].val.clusterDim.z = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        cudaLaunchKernelEx(&cfg, bp_solve_kernel, b, want_energy, energy_out);
+    }
     if (timed) cudaEventRecordWithFlags(b.kt_ev[(*b.kt_used)++], st, cudaEventRecordExternal);
     bp_sens_kernel<<<blocks, 256, 0, st>>>(b, g, in_sens[0], in_sens[1], in_sens[2], in_sens[3], n_in, w[0], w[1],
                                            w[2], w[3]);

@@ -76,6 +76,7 @@ struct DBP {
     int* col;                   // entry -> neighbour residue (global)
     int* erow;                  // entry -> row residue
     int* rev;                   // entry -> reverse entry
+    int4* einfo;                // entry -> (row node local index, reverse entry, column node local index, 0)
     int ent_cap;
     int* n_ent;
     float* esum;                // entry * 36: summed bead energies (row rot, col rot)
@@ -107,6 +108,10 @@ struct DBP {
     int* kt_used;
     int kt_cap;
 };
+
+// dynamic shared memory of the BP solve for a system of n residues: both
+// belief buffers (8 floats per node each) and the rotamer counts
+inline size_t bp_solve_smem_bytes(int n) { return size_t(n) * (2 * 8 * sizeof(float) + sizeof(int)); }
 
 // --------------------------------------------------------------- launchers --
 void launch_scan(const int* in, int* out, int n, int* total_out, cudaStream_t st);
