@@ -198,3 +198,26 @@ def test_error_codes(built, tmp_path):
     # the engine stays usable after the errors
     z = np.load(os.path.join(GOLDEN, "chig_frames.npz"))
     assert abs(eng.energy(z["pos"][0]) - z["ref_energy"][0]) < 1e-3
+
+
+def test_pair_cache_transparent(syn_configs):
+    """After many integration rounds (candidate caches reused and partly
+    rebuilt), every edge list equals the one a fresh engine finds from scratch
+    at the same coordinates, and so do energies and forces."""
+    import upside_gb300 as U
+    (p60, z60), (p150, z150) = syn_configs[60], syn_configs[150]
+    b = U.Batch([p60, p150])
+    b.set_pos(np.concatenate([z60["pos"][0], z150["pos"][0]]))
+    b.set_thermostat([0.85, 0.9], np.array([3, 4], np.uint32))
+    b.run(60, use_graph=True, graph_rounds=10)
+    x = b.get_pos()
+    e_run, d_run = b.evaluate()
+    fresh = U.Batch([p60, p150])
+    fresh.set_pos(x)
+    e_new, d_new = fresh.evaluate()
+    for node in ["rotamer", "hbond_coverage", "hbond_coverage_hydrophobe", "protein_hbond",
+                 "environment_coverage_sc", "environment_coverage_hb", "hb_environment_coverage_hn",
+                 "hb_environment_coverage_oc"]:
+        assert np.array_equal(b.node_edges(node), fresh.node_edges(node)), node
+    assert np.abs(e_run - e_new).max() < 1e-4 * max(1.0, np.abs(e_new).max())
+    assert rel_f(d_run, d_new) < 1e-4

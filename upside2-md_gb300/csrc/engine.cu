@@ -891,13 +891,50 @@ struct HGraph {
     Engine* eng = nullptr;
     int* edge_bufs_int = nullptr;
     void* bufs[4] = {nullptr, nullptr, nullptr, nullptr};
+    void* cbufs[4] = {nullptr, nullptr, nullptr, nullptr};
+    std::vector<int> cache_cap;  // per system candidate capacity (multiple of CACHE_TILE)
 
-    ~HGraph() { release(); }
+    ~HGraph() {
+        release();
+        release_cache();
+    }
     void release() {
         for (auto& p : bufs) {
             if (p) cudaFree(p);
             p = nullptr;
         }
+    }
+    void release_cache() {
+        for (auto& p : cbufs) {
+            if (p) cudaFree(p);
+            p = nullptr;
+        }
+    }
+    // (re)lay out the per-system candidate segments; every system is rebuilt
+    // at the next evaluation
+    void layout_cache() {
+        release_cache();
+        std::vector<int> off{0};
+        for (int c : cache_cap) off.push_back(off.back() + c);
+        g.max_tiles = off.back() / CACHE_TILE;
+        UG_CK(cudaMalloc(&cbufs[0], sizeof(int2) * size_t(off.back())));
+        UG_CK(cudaMalloc(&cbufs[1], sizeof(int) * off.size()));
+        UG_CK(cudaMalloc(&cbufs[2], sizeof(int) * (size_t(g.max_tiles) + 1)));
+        UG_CK(cudaMalloc(&cbufs[3], sizeof(int) * (size_t(g.max_tiles) + 1)));
+        UG_CK(cudaMemcpy(cbufs[1], off.data(), sizeof(int) * off.size(), cudaMemcpyHostToDevice));
+        g.cache_edges = static_cast<int2*>(cbufs[0]);
+        g.cache_off = static_cast<const int*>(cbufs[1]);
+        g.tile_count = static_cast<int*>(cbufs[2]);
+        g.tile_off = static_cast<int*>(cbufs[3]);
+        UG_CK(cudaMemset(g.cache_n, 0, sizeof(int) * size_t(g.n_sys)));
+        UG_CK(cudaMemset(g.sys_over, 0, sizeof(int) * size_t(g.n_sys)));
+        UG_CK(cudaMemset(g.active_off, 0, sizeof(int) * (size_t(g.n_sys) + 1)));
+        force_rebuild();
+    }
+    void force_rebuild() {
+        if (!g.cached) return;
+        const int one = 1;
+        UG_CK(cudaMemcpy(g.cache_force, &one, sizeof(int), cudaMemcpyHostToDevice));
     }
     void alloc_edges(int cap) {
         release();
@@ -992,6 +1029,24 @@ struct HGraph {
         long long cap = std::min<long long>(std::max<long long>(full, 1), (long long)cap_per_elem * std::max(g.n1, 1) + 1024);
         per_elem_cap = cap_per_elem;
         alloc_edges(int(std::min<long long>(cap, 1LL << 30)));
+        // candidate cache: per-system segments sized for twice the edge
+        // capacity per element (the buffer widens the cutoff), grown on overflow
+        g.cached = 1;
+        g.sys2 = sym ? g.sys1 : e.upload(sys_of(of2));
+        g.xc1 = e.alloc<float4>(size_t(g.n1));
+        g.xc2 = sym ? g.xc1 : e.alloc<float4>(size_t(g.n2));
+        g.sys_flag = e.alloc<int>(size_t(e.n_sys));
+        g.sys_over = e.alloc<int>(size_t(e.n_sys));
+        g.cache_n = e.alloc<int>(size_t(e.n_sys));
+        g.active_off = e.alloc<int>(size_t(e.n_sys) + 1);
+        g.cache_force = e.alloc<int>(1);
+        for (size_t s = 0; s < grp.size(); ++s) {
+            long long fs = sym ? (long long)c1[s] * (c1[s] - 1) / 2 : (long long)c1[s] * c2[s];
+            long long want = std::min<long long>(std::max<long long>(fs, 1), 2LL * cap_per_elem * c1[s]);
+            cache_cap.push_back(int(std::min<long long>((want + CACHE_TILE - 1) / CACHE_TILE * CACHE_TILE, 1LL << 28)));
+        }
+        UG_CK(cudaStreamSynchronize(e.st));
+        layout_cache();
         update_cutoff();
     }
     std::vector<float> param_host;
@@ -1010,7 +1065,9 @@ struct HGraph {
             }
             c = std::max(c, ci);
         }
+        if (c != g.cutoff) force_rebuild();
         g.cutoff = c;
+        g.buffer = 1.f + 0.2f * c;
     }
     void set_param(const std::vector<float>& p) {
         if (p.size() != param_host.size()) throw Error("Bad param size, got " + std::to_string(p.size()) +
@@ -1028,10 +1085,22 @@ struct HGraph {
         launch_edge_eval(g, d_sys_start, d_sys_end, st);
     }
     bool grow_if_full() {
+        bool grew = false;
+        if (g.cached) {
+            std::vector<int> over(size_t(g.n_sys));
+            UG_CK(cudaMemcpy(over.data(), g.sys_over, 4 * over.size(), cudaMemcpyDeviceToHost));
+            for (size_t s = 0; s < over.size(); ++s)
+                if (over[s]) {
+                    cache_cap[s] = int(std::min<long long>(2LL * cache_cap[s], 1LL << 28));
+                    grew = true;
+                }
+            if (grew) layout_cache();
+        }
         int ne = 0;
         UG_CK(cudaMemcpy(&ne, g.n_edge, 4, cudaMemcpyDeviceToHost));
-        if (ne < g.cap) return false;
+        if (ne < g.cap) return grew;
         alloc_edges(int(std::min<long long>(2LL * g.cap, 1LL << 30)));
+        force_rebuild();
         return true;
     }
     std::vector<float> count_edges_by_type() {

@@ -91,16 +91,32 @@ void launch_pack_positions(const DGraph& g, cudaStream_t st) {
 // One warp per row (4 consecutive set-1 elements of one system).  Pass 0
 // counts hits; pass 1 writes them in (i2, lane) order at the row's scanned
 // offset, which reproduces the reference's edge order exactly.
-template <int PASS>
+//
+// CACHED: the search fills the candidate cache instead of the edge list: it
+// runs only for the rows of systems flagged for a rebuild, with cutoff +
+// buffer, and writes each system's candidates into its own cache segment
+// (the reference's cache rebuild, src/interaction_graph.h:96-157).
+__device__ __forceinline__ float pair_d2(float4 a, float4 b) {
+    float dx = a.x - b.x, dy = a.y - b.y, dz = a.z - b.z;
+    return __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+}
+
+template <int PASS, bool CACHED>
 __global__ void pair_kernel(DGraph g) {
     int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     int lane = threadIdx.x & 31;
     int n_warps = (gridDim.x * blockDim.x) >> 5;
-    const float c2 = g.cutoff * g.cutoff;
+    const float rc = CACHED ? g.cutoff + g.buffer : g.cutoff;
+    const float c2 = rc * rc;
     const float4* X2 = g.symmetric ? g.x1 : g.x2;
     const int* ID2 = g.symmetric ? g.id1 : g.id2;
     for (int r = warp; r < g.n_rows; r += n_warps) {
         int i1s = g.row_i1[r], i1e = g.row_i1_end[r];
+        int sys = 0;
+        if (CACHED) {
+            sys = g.sys1[i1s];
+            if (!g.sys_flag[sys]) continue;  // warp-uniform
+        }
         int i2s = g.row_i2[r], i2e = g.row_i2_end[r];
         float4 a[4];
         int ida[4];
@@ -110,7 +126,18 @@ __global__ void pair_kernel(DGraph g) {
             a[l] = l < nl ? g.x1[i1s + l] : make_float4(1e20f, 1e20f, 1e20f, 0.f);
             ida[l] = l < nl ? g.id1[i1s + l] : 0;
         }
-        int base = PASS ? g.row_off[r] : 0;
+        int base = 0, lim = g.cap;
+        int2* out = g.edges;
+        if (PASS) {
+            if (CACHED) {
+                int seg = g.cache_off[sys];
+                base = seg + g.row_off[r] - g.row_off[g.sys_first_row[sys]];
+                lim = g.cache_off[sys + 1];
+                out = g.cache_edges;
+            } else {
+                base = g.row_off[r];
+            }
+        }
         int count = 0;
         for (int j0 = i2s; j0 < i2e; j0 += 32) {
             int j = j0 + lane;
@@ -122,9 +149,7 @@ __global__ void pair_kernel(DGraph g) {
                 for (int l = 0; l < 4; ++l) {
                     if (l >= nl) break;
                     if (g.symmetric && !(i1s + l < j)) continue;
-                    float dx = a[l].x - b.x, dy = a[l].y - b.y, dz = a[l].z - b.z;
-                    float d2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
-                    if (d2 < c2 && acceptable_ids(g.excl, ida[l], idb)) mask |= 1u << l;
+                    if (pair_d2(a[l], b) < c2 && acceptable_ids(g.excl, ida[l], idb)) mask |= 1u << l;
                 }
             }
             int c = __popc(mask);
@@ -140,7 +165,7 @@ __global__ void pair_kernel(DGraph g) {
                 int pos = base + incl - c;
                 for (int l = 0; l < 4; ++l)
                     if (mask & (1u << l)) {
-                        if (pos < g.cap) g.edges[pos] = make_int2(i1s + l, j);
+                        if (pos < lim) out[pos] = make_int2(i1s + l, j);
                         ++pos;
                     }
                 base += __shfl_sync(0xffffffffu, incl, 31);
@@ -161,6 +186,135 @@ __global__ void cap_check_kernel(int* n_edge, int cap, int* status) {
     }
 }
 
+// ----------------------------------------------------- candidate cache ---
+// A system's cache is rebuilt when any of its elements moved more than half
+// the buffer since its last rebuild, or when a rebuild of every system was
+// requested (src/interaction_graph.h:51-91: same bound, same comparison).
+__global__ void cache_flag_init_kernel(DGraph g) {
+    int f = *g.cache_force;
+    for (int s = grid_stride_start(); s < g.n_sys; s += grid_stride()) g.sys_flag[s] = f | g.sys_over[s];
+}
+
+__global__ void cache_check_kernel(DGraph g) {
+    float h = 0.5f * ((g.cutoff + g.buffer) - g.cutoff);
+    float lim = h * h;
+    int n = g.n1 + (g.symmetric ? 0 : g.n2);
+    for (int i = grid_stride_start(); i < n; i += grid_stride()) {
+        bool first = i < g.n1;
+        int k = first ? i : i - g.n1;
+        int sys = first ? g.sys1[k] : g.sys2[k];
+        float4 x = first ? g.x1[k] : g.x2[k];
+        float4 c = first ? g.xc1[k] : g.xc2[k];
+        float dx = x.x - c.x, dy = x.y - c.y, dz = x.z - c.z;
+        if (lim < dx * dx + dy * dy + dz * dz) g.sys_flag[sys] = 1;
+    }
+}
+
+// after the rebuild search: per system candidate counts (capped by the
+// segment, overflow flagged), and the refine pass's tile prefix over systems
+__global__ void cache_commit_kernel(DGraph g) {
+    for (int s = grid_stride_start(); s < g.n_sys; s += grid_stride()) {
+        if (!g.sys_flag[s]) continue;
+        int cnt = g.row_off[g.sys_first_row[s + 1]] - g.row_off[g.sys_first_row[s]];
+        int cap = g.cache_off[s + 1] - g.cache_off[s];
+        g.sys_over[s] = cnt > cap;
+        if (cnt > cap) {
+            atomicOr(g.status, ST_EDGE_OVERFLOW);
+            cnt = cap;
+        }
+        g.cache_n[s] = cnt;
+    }
+}
+
+// positions of the rebuilt systems become their new reference positions; the
+// first thread also clears the rebuild-everything request and recomputes the
+// per-system prefix of active refine tiles
+__global__ void cache_positions_kernel(DGraph g) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        *g.cache_force = 0;
+        int t = 0;
+        for (int s = 0; s < g.n_sys; ++s) {
+            g.active_off[s] = t;
+            t += (g.cache_n[s] + CACHE_TILE - 1) / CACHE_TILE;
+        }
+        g.active_off[g.n_sys] = t;
+    }
+    int n = g.n1 + (g.symmetric ? 0 : g.n2);
+    for (int i = grid_stride_start(); i < n; i += grid_stride()) {
+        bool first = i < g.n1;
+        int k = first ? i : i - g.n1;
+        int sys = first ? g.sys1[k] : g.sys2[k];
+        if (!g.sys_flag[sys]) continue;
+        if (first) g.xc1[k] = g.x1[k];
+        else g.xc2[k] = g.x2[k];
+    }
+}
+
+// Refine: the edges are the cached candidates now within the cutoff, in
+// cache order (src/interaction_graph.h:203-258).  One block per active tile
+// of CACHE_TILE candidates (4 per thread); pass 0 counts each tile's hits,
+// a scan over tiles gives offsets, pass 1 writes them in order.
+template <int PASS>
+__global__ void __launch_bounds__(256) cache_refine_kernel(DGraph g) {
+    __shared__ int warp_sum[8];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int n_active = g.active_off[g.n_sys];
+    const float c2 = g.cutoff * g.cutoff;
+    const float4* X2 = g.symmetric ? g.x1 : g.x2;
+    for (int t = blockIdx.x; t < g.max_tiles; t += gridDim.x) {
+        if (t >= n_active) {  // block-uniform
+            if (PASS == 0 && tid == 0) g.tile_count[t] = 0;
+            continue;
+        }
+        int a = 0, z = g.n_sys;  // system s with active_off[s] <= t < active_off[s+1]
+        while (z - a > 1) {
+            int m = (a + z) >> 1;
+            if (g.active_off[m] <= t) a = m; else z = m;
+        }
+        const int s = a;
+        const int first = (t - g.active_off[s]) * CACHE_TILE + 4 * tid;  // within the segment
+        const int n = g.cache_n[s];
+        const int2* ce = g.cache_edges + g.cache_off[s];
+        unsigned mask = 0;
+        int2 ij[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            int k = first + q;
+            ij[q] = make_int2(0, 0);
+            if (k < n) {
+                ij[q] = ce[k];
+                if (pair_d2(g.x1[ij[q].x], X2[ij[q].y]) < c2) mask |= 1u << q;
+            }
+        }
+        int c = __popc(mask);
+        int incl = c;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            int y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += y;
+        }
+        if (lane == 31) warp_sum[warp] = incl;
+        __syncthreads();
+        if (PASS == 0) {
+            if (tid == 0) {
+                int tot = 0;
+                for (int w = 0; w < 8; ++w) tot += warp_sum[w];
+                g.tile_count[t] = tot;
+            }
+        } else {
+            int pos = g.tile_off[t] + incl - c;
+            for (int w = 0; w < warp; ++w) pos += warp_sum[w];
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+                if (mask & (1u << q)) {
+                    if (pos < g.cap) g.edges[pos] = ij[q];
+                    ++pos;
+                }
+        }
+        __syncthreads();  // warp_sum is reused by the next tile
+    }
+}
+
 void launch_pairs(const DGraph& g, cudaStream_t st) {
     launch_pack_positions(g, st);
     if (g.n_rows == 0) {
@@ -169,9 +323,26 @@ void launch_pairs(const DGraph& g, cudaStream_t st) {
         return;
     }
     int blocks = min(4 * 152, (g.n_rows * 32 + 255) / 256);
-    pair_kernel<0><<<blocks, 256, 0, st>>>(g);
-    launch_scan(g.row_count, g.row_off, g.n_rows, g.n_edge, st);
-    pair_kernel<1><<<blocks, 256, 0, st>>>(g);
+    if (!g.cached) {
+        pair_kernel<0, false><<<blocks, 256, 0, st>>>(g);
+        launch_scan(g.row_count, g.row_off, g.n_rows, g.n_edge, st);
+        pair_kernel<1, false><<<blocks, 256, 0, st>>>(g);
+        cap_check_kernel<<<1, 1, 0, st>>>(g.n_edge, g.cap, g.status);
+        return;
+    }
+    int ne = g.n1 + (g.symmetric ? 0 : g.n2);
+    int eb = min(1024, (ne + 255) / 256);
+    cache_flag_init_kernel<<<1, 256, 0, st>>>(g);
+    cache_check_kernel<<<eb, 256, 0, st>>>(g);
+    pair_kernel<0, true><<<blocks, 256, 0, st>>>(g);
+    launch_scan(g.row_count, g.row_off, g.n_rows, nullptr, st);
+    pair_kernel<1, true><<<blocks, 256, 0, st>>>(g);
+    cache_commit_kernel<<<1, 256, 0, st>>>(g);
+    cache_positions_kernel<<<eb, 256, 0, st>>>(g);
+    int rblocks = min(8 * 152, g.max_tiles);
+    cache_refine_kernel<0><<<rblocks, 256, 0, st>>>(g);
+    launch_scan(g.tile_count, g.tile_off, g.max_tiles, g.n_edge, st);
+    cache_refine_kernel<1><<<rblocks, 256, 0, st>>>(g);
     cap_check_kernel<<<1, 1, 0, st>>>(g.n_edge, g.cap, g.status);
 }
 
@@ -311,9 +482,27 @@ __global__ void edge_sys_range_kernel(DGraph g, int* start, int* end) {
     }
 }
 
+// per-system edge ranges from the edge list itself (edges are in system order)
+__global__ void edge_sys_bounds_kernel(DGraph g, int* start, int* end) {
+    int n = min(*g.n_edge, g.cap);
+    for (int e = grid_stride_start(); e < n; e += grid_stride()) {
+        int s = g.sys1[g.edges[e].x];
+        if (e == 0 || g.sys1[g.edges[e - 1].x] != s) start[s] = e;
+        if (e == n - 1 || g.sys1[g.edges[e + 1].x] != s) end[s] = e + 1;
+    }
+}
+
 void launch_edge_eval(const DGraph& g, int* sys_start, int* sys_end, cudaStream_t st) {
     int blocks = 2 * 152;
-    if (g.kind == IK_PHB) edge_sys_range_kernel<<<1, 256, 0, st>>>(g, sys_start, sys_end);
+    if (g.kind == IK_PHB) {
+        if (g.cached) {
+            cudaMemsetAsync(sys_start, 0, sizeof(int) * size_t(g.n_sys), st);
+            cudaMemsetAsync(sys_end, 0, sizeof(int) * size_t(g.n_sys), st);
+            edge_sys_bounds_kernel<<<blocks, 256, 0, st>>>(g, sys_start, sys_end);
+        } else {
+            edge_sys_range_kernel<<<1, 256, 0, st>>>(g, sys_start, sys_end);
+        }
+    }
     switch (g.kind) {
         case IK_ROTAMER: edge_eval_kernel<IK_ROTAMER><<<blocks, 256, 0, st>>>(g, sys_start, sys_end); break;
         case IK_HBCOV: edge_eval_kernel<IK_HBCOV><<<blocks, 256, 0, st>>>(g, sys_start, sys_end); break;
@@ -609,37 +798,54 @@ __device__ __forceinline__ void bp_messages(const DBP& b, int e0, int e1, const 
     }
 }
 
-// new beliefs of the system's nodes; returns this thread's largest one-sided
-// deviation (mode 1)
+// new beliefs of nodes [lo, hi); returns this thread's largest one-sided
+// deviation (mode 1).  BP_LANES consecutive lanes share a node: each folds
+// every BP_LANES-th incoming message, then the partial products are combined
+// across the group with shuffles, so a node's latency chain is its degree /
+// BP_LANES loads.
+constexpr int BP_LANES = 8;
 __device__ __forceinline__ float bp_beliefs(const DBP& b, int r0, int lo, int hi, int e1, const float* __restrict__ Nold,
                                             float* __restrict__ Ncur, const int* __restrict__ s_nrot,
                                             const float* __restrict__ Ecur, int mode, float damp, int tid,
                                             int nt) {
     float dev = 0.f;
-    for (int ul = lo + tid; ul < hi; ul += nt) {
+    const int q = tid % BP_LANES, lane = tid & 31;
+    const unsigned gmask = ((1u << BP_LANES) - 1u) << (lane & ~(BP_LANES - 1));
+    const float4* m4 = reinterpret_cast<const float4*>(Ecur);
+    for (int ul = lo + tid / BP_LANES; ul < hi; ul += nt / BP_LANES) {  // group-uniform
         int n = s_nrot[ul];
         if (n == 1) continue;
         int u = r0 + ul;
         int eb = b.row_ptr[u], ee = min(b.row_ptr[u + 1], e1);
         float prod[6] = {1.f, 1.f, 1.f, 1.f, 1.f, 1.f};
-        const float4* m4 = reinterpret_cast<const float4*>(Ecur);
-        int e = eb;
-        // four messages per step with their loads issued together; the
-        // running product is renormalised after every factor, so it never
-        // underflows (each message sums to 1)
-        auto fold = [&](float4 a, float4 c) {
-            prod[0] *= a.x; prod[1] *= a.y; prod[2] *= a.z; prod[3] *= a.w; prod[4] *= c.x; prod[5] *= c.y;
+        // renormalised after every factor, so the product never underflows
+        // (each message sums to 1)
+        auto fold = [&](const float* a) {
+#pragma unroll
+            for (int k = 0; k < 6; ++k) prod[k] *= a[k];
             renorm6(prod, n);
         };
-        for (; e + 4 <= ee; e += 4) {
-            float4 a0 = m4[2 * e], c0 = m4[2 * e + 1], a1 = m4[2 * e + 2], c1 = m4[2 * e + 3];
-            float4 a2 = m4[2 * e + 4], c2 = m4[2 * e + 5], a3 = m4[2 * e + 6], c3 = m4[2 * e + 7];
-            fold(a0, c0);
-            fold(a1, c1);
-            fold(a2, c2);
-            fold(a3, c3);
+        int e = eb + q;
+        for (; e + BP_LANES < ee; e += 2 * BP_LANES) {  // two loads in flight
+            float4 a0 = m4[2 * e], c0 = m4[2 * e + 1];
+            float4 a1 = m4[2 * (e + BP_LANES)], c1 = m4[2 * (e + BP_LANES) + 1];
+            float x0[6] = {a0.x, a0.y, a0.z, a0.w, c0.x, c0.y}, x1[6] = {a1.x, a1.y, a1.z, a1.w, c1.x, c1.y};
+            fold(x0);
+            fold(x1);
         }
-        for (; e < ee; ++e) fold(m4[2 * e], m4[2 * e + 1]);
+        if (e < ee) {
+            float4 a0 = m4[2 * e], c0 = m4[2 * e + 1];
+            float x0[6] = {a0.x, a0.y, a0.z, a0.w, c0.x, c0.y};
+            fold(x0);
+        }
+#pragma unroll
+        for (int o = BP_LANES / 2; o > 0; o >>= 1) {
+            float y[6];
+#pragma unroll
+            for (int k = 0; k < 6; ++k) y[k] = __shfl_xor_sync(gmask, prod[k], o);
+            fold(y);
+        }
+        if (q != 0) continue;
         float bl[6];
 #pragma unroll
         for (int k = 0; k < 6; ++k) bl[k] = k < n ? b.prob[u * 8 + k] * prod[k] : 0.f;

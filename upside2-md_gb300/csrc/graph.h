@@ -58,7 +58,29 @@ struct DGraph {
     float4* x1;                 // packed positions (xyz) of set 1 for the search
     float4* x2;
     int* status;
+    // candidate cache (src/interaction_graph.h:51-258): per system, the pairs
+    // within cutoff + buffer at the positions of that system's last rebuild;
+    // every evaluation refines them to the cutoff.  cached == 0: full search
+    // every evaluation.
+    int cached;
+    float buffer;               // 1 + 0.2 * cutoff (src/interaction_graph.h:396)
+    float4* xc1;                // positions at each system's last rebuild
+    float4* xc2;
+    const int* sys2;            // set-2 element -> system
+    int* sys_flag;              // per system: rebuilt in this evaluation
+    int* cache_force;           // device scalar: rebuild every system next time
+    int* sys_over;              // per system: its segment overflowed at the last rebuild
+    int2* cache_edges;          // per-system segments of candidates
+    const int* cache_off;       // segment starts (n_sys+1)
+    int* cache_n;               // per system number of candidates
+    int* active_off;            // per system prefix of refine tiles (n_sys+1)
+    int max_tiles;              // refine tiles if every segment were full
+    int* tile_count;            // max_tiles + 1
+    int* tile_off;              // max_tiles + 1
 };
+
+// candidates per refine tile (one 256-thread block, 4 per thread)
+constexpr int CACHE_TILE = 1024;
 
 // One system-batched rotamer belief-propagation problem.
 struct DBP {
@@ -101,7 +123,7 @@ struct DBP {
     double* e11;                // per system sum of energies of 1-1 bead edges
     int* status;
     // measurement: running per-system total of the solve kernel's algorithmic
-    // bytes (the formula is in bp_solve2_kernel), and optional host-side CUDA
+    // bytes (the formula is in bp_solve_kernel), and optional host-side CUDA
     // events bracketing each solve launch (kt_ev null: no events recorded)
     unsigned long long* alg_bytes;
     cudaEvent_t* kt_ev;
