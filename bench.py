@@ -37,6 +37,8 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain single-system GPU comparison")
+    ap.add_argument("--bp-start", default="learned", choices=["uniform", "learned", "previous", "reuse"],
+                    help="BP initial state of the batched run")
     ap.add_argument("--profile", action="store_true", help="print per-node device times to stderr")
     return ap.parse_args()
 
@@ -205,6 +207,7 @@ def main():
     b = U.Batch(W["configs"])
     b.set_pos(workloads.initial_positions(W["configs"]))
     b.set_thermostat(W["temps"], np.array(W["seeds"], np.uint32))
+    bp_start = set_bp_start(b, a.bp_start)
     b.run(a.warmup, use_graph=True, graph_rounds=1)
     launches, dev_bytes = b.info()
     if a.profile:
@@ -238,7 +241,8 @@ def main():
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded ff_2.1 proteins, random initial chains)",
         "config": {"workload": a.workload, "systems": len(W["configs"]), "residues": n_res_total,
                    "step": "one integration round = 3 force evaluations + integrator stages per system",
-                   "l2": "256 MiB buffer rewritten before every timed round", "bp_init": "uniform messages"},
+                   "l2": "256 MiB buffer rewritten before every timed round", "bp_init": bp_start,
+                   "bp_sweeps_per_solve": bp_sweeps(b)},
         "e2e": {"value": e2e_value, "unit": "residue-steps/s", "h2d_bytes_per_step": state_bytes,
                 "d2h_bytes_per_step": state_bytes},
         "gpu_launches": int(a.steps * (3 * launches + 5)),
@@ -250,6 +254,34 @@ def main():
         "device_bytes": dev_bytes,
     }
     print(json.dumps(line))
+
+
+def set_bp_start(b, mode):
+    """BP initial state of the batched run: the learned warm start (with its
+    per-system fallback to the uniform start), the previous solve's marginals,
+    or the reference's uniform start."""
+    if mode == "uniform":
+        return "uniform messages (reference)"
+    if mode == "previous":
+        b.set_warm_start(None, 2)
+        return "previous solve's marginals"
+    if mode == "reuse":
+        b.set_warm_start(None, 3)
+        return "previous solve's messages and marginals"
+    import warm_start
+    if not os.path.exists(warm_start.WEIGHTS):
+        return "uniform messages (no trained warm-start weights)"
+    b.set_warm_start(warm_start.load(), 1)
+    return "learned warm start (bf16 MLP), per-system fallback to uniform"
+
+
+def bp_sweeps(b):
+    """BP sweeps of each system's last solve, averaged (first sweep included)."""
+    import numpy as np
+    try:
+        return float(np.mean(b.value_by_name("rotamer", "n_iter", b.n_sys))) + 1.0
+    except Exception:
+        return None
 
 
 def plain_single_rate(W, a, n_sample=6, rounds=8):

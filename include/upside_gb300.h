@@ -56,6 +56,15 @@ int ug_value_by_name(UgBatch* b, const char* node, const char* what, float* out,
 /* per-node potential of each system after ug_evaluate: out[n_sys] */
 int ug_node_potential(UgBatch* b, const char* node, double* out);
 
+/* Parameters of a node, shared by every system of the batch (set_param /
+ * get_param of the reference, src/engine_c_library.cpp:68-92), and
+ * dE/d(param) after ug_evaluate summed over all systems of the batch (the
+ * adjoint kernels behind get_param_deriv, src/engine_c_library.cpp:94-110);
+ * a batch of frames of one protein gives the frame sum in one call. */
+int ug_set_param(UgBatch* b, const char* node, const float* param, int n);
+int ug_get_param(UgBatch* b, const char* node, float* param, int n);
+int ug_param_deriv(UgBatch* b, const char* node, float* deriv, int n);
+
 /* Replica exchange over the batch: energies of all systems are evaluated,
  * then Metropolis swaps of coordinates between the neighbour pairs of the
  * given swap set (pairs[2*k], pairs[2*k+1]) with FP64 acceptance
@@ -113,6 +122,46 @@ int ug_pair_list(const float* pos, int n, float cutoff, int32_t* pairs, int cap,
  * Output, order and arguments as ug_pair_list. */
 int ug_pair_list_noalloc(const float* pos, int n, float cutoff, int32_t* pairs, int cap, int32_t* n_pairs,
                          void* stream);
+
+/* Learned BP warm start (no counterpart in the reference; it replaces the
+ * uniform initial state of the BP solve, src/rotamer.cpp:1110-1135).  A
+ * per-residue MLP, 64 features -> 128 -> 128 -> 8 rotamer logits with ReLU,
+ * predicts each residue's converged rotamer marginal; the solve starts from
+ * the prediction and still iterates to the configured tolerance.  Per system
+ * the engine tracks the sweeps needed from the learned and from the uniform
+ * start (every 16th solve tries the other one) and uses the learned start
+ * only while it needs no more sweeps.  Weights are FP32 row-major (W1 64x128,
+ * b1 128, W2 128x128, b2 128, W3 128x8, b3 8), stored as bf16; pass all six
+ * or none (none: keep the loaded weights, only switch).  enable selects the
+ * start: 0 uniform (the reference's), 1 learned, 2 the previous solve's
+ * marginals, 3 the previous solve's final messages and marginals (modes 2
+ * and 3 make a solve depend on the previous evaluation of the same system,
+ * to within the BP tolerance; the reference re-initialises every call).
+ * Training data: ug_value_by_name on the rotamer node with "warm_features"
+ * (n_node x 64), "bp_marginal" (n_node x 8), "bp_nrot", "bp_n_node". */
+int ug_set_warm_start(UgBatch* b, const float* w1, const float* b1, const float* w2, const float* b2, const float* w3,
+                      const float* b3, int enable);
+
+/* Kernels of the warm-start network, on caller-owned device memory, enqueued
+ * on `stream` (no counterpart in the reference).  bf16 operands are uint16
+ * bit patterns; accumulation is FP32.
+ *   gemm:   C[M x N] (row stride ldc) = (accumulate ? C : 0) + A[M x K] . B[K x N]
+ *           with A(i,k) = A[i*a_r + k*a_c], B(k,n) = B[k*b_r + n*b_c]
+ *   bias_act: H = bf16(act(Z + bias)) and/or Hf = act(Z + bias), act = ReLU if relu
+ *   to_bf16: Y = bf16(X); with relu_of (bf16) given, X and Y are zeroed where it is not positive
+ *   softmax_xent: softmax over the first nrot[i] of 8 logits, soft-target
+ *           cross-entropy; dZ = scale (p - T), *loss += scale * loss (rows with nrot < 2: 0)
+ *   colsum: out[N] = column sums of X[M x N]
+ *   adam:   Adam step `step` (1-based) on w with gradient g, moments m, v; wb = bf16(w) */
+int ug_mlp_gemm(const uint16_t* A, int64_t a_r, int64_t a_c, const uint16_t* B, int64_t b_r, int64_t b_c, float* C,
+                int ldc, int M, int N, int K, int accumulate, void* stream);
+int ug_mlp_bias_act(const float* Z, const float* bias, uint16_t* H, float* Hf, int M, int N, int relu, void* stream);
+int ug_mlp_to_bf16(float* X, const uint16_t* relu_of, uint16_t* Y, int64_t n, void* stream);
+int ug_mlp_softmax_xent(const float* Z, const float* T, const int32_t* nrot, float* dZ, float* loss, int M, float scale,
+                        void* stream);
+int ug_mlp_colsum(const float* X, float* out, int M, int N, void* stream);
+int ug_mlp_adam(float* w, const float* g, float* m, float* v, uint16_t* wb, int n, float lr, float b1, float b2,
+                float eps, int step, void* stream);
 
 #ifdef __cplusplus
 }

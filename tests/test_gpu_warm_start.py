@@ -1,0 +1,161 @@
+"""Learned BP warm start: the network's kernels against the CPU restatement
+(oracle/warm_mlp_ref.py), training, and what the trained network gains.
+
+Tolerances: the GEMM against an FP32 product of the same bf16 operands, 1e-3
+of the largest |entry|; weight gradients 2e-2 of each tensor's largest
+|entry| (FP32 accumulation order differs and bf16 rounding of intermediate
+gradients can flip by one unit).
+"""
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _dev(a, dtype=None):
+    import torch
+    return torch.tensor(a if dtype is None else np.asarray(a, dtype), device="cuda")
+
+
+@pytest.mark.parametrize("trans_a,trans_b", [(False, False), (True, False), (False, True)])
+def test_gemm_matches_numpy(built, trans_a, trans_b):
+    import ctypes
+    import torch
+    import warm_mlp_ref as R
+    from warm_start import _lib, _p, _stream, to_bf16_bits
+    rng = np.random.RandomState(3)
+    M, N, K = 301, 70, 97
+    A = rng.normal(size=(M, K)).astype(np.float32)
+    B = rng.normal(size=(K, N)).astype(np.float32)
+    As = A.T.copy() if trans_a else A
+    Bs = B.T.copy() if trans_b else B
+    a_r, a_c = (1, M) if trans_a else (K, 1)
+    b_r, b_c = (1, K) if trans_b else (N, 1)
+    dA, dB = _dev(to_bf16_bits(As)), _dev(to_bf16_bits(Bs))
+    C = torch.zeros((M, N), device="cuda")
+    assert _lib().ug_mlp_gemm(_p(dA), a_r, a_c, _p(dB), b_r, b_c, _p(C), N, M, N, K, 0, _stream()) == 0
+    ref = R.bf16(A) @ R.bf16(B)
+    got = C.cpu().numpy()
+    assert np.abs(got - ref).max() <= 1e-3 * np.abs(ref).max()
+    del ctypes
+
+
+def _random_problem(seed, M=700):
+    rng = np.random.RandomState(seed)
+    X = rng.normal(size=(M, 64)).astype(np.float32)
+    nrot = rng.choice([1, 3, 6], size=M).astype(np.int32)
+    T = np.zeros((M, 8), np.float32)
+    for i in range(M):
+        p = rng.dirichlet(np.ones(nrot[i]))
+        T[i, :nrot[i]] = p
+    w = {"W1": rng.normal(0, 0.2, (64, 128)), "b1": rng.normal(0, 0.1, 128), "W2": rng.normal(0, 0.1, (128, 128)),
+         "b2": rng.normal(0, 0.1, 128), "W3": rng.normal(0, 0.1, (128, 8)), "b3": rng.normal(0, 0.1, 8)}
+    return X, T, nrot, {k: v.astype(np.float32) for k, v in w.items()}
+
+
+def test_gradients_match_cpu_oracle(built):
+    import warm_mlp_ref as R
+    from warm_start import WarmNet, to_device
+    X, T, nrot, w = _random_problem(5)
+    net = WarmNet(weights=w)
+    loss, g = net.grads(*to_device(X, T, nrot))
+    loss_ref, g_ref = R.loss_and_grads(X, T, nrot, w)
+    assert abs(loss - loss_ref) <= 1e-3 * abs(loss_ref)
+    for k in g_ref:
+        a, b = g[k].cpu().numpy(), g_ref[k]
+        assert np.abs(a - b).max() <= 2e-2 * np.abs(b).max(), k
+
+
+def test_training_fits_a_teacher(built):
+    """Adam steps on the library's kernels fit targets made by a fixed teacher
+    network of the same shape."""
+    import warm_mlp_ref as R
+    from warm_start import WarmNet, to_device, train
+    X, _, nrot, teacher = _random_problem(7, M=8192)
+    Z = R.forward(X, teacher)[3]
+    T = np.zeros((X.shape[0], 8), np.float32)
+    for i in range(X.shape[0]):
+        z = Z[i, :nrot[i]]
+        p = np.exp(z - z.max())
+        T[i, :nrot[i]] = p / p.sum()
+    data = to_device(X, T, nrot)
+    # the loss cannot fall below the targets' own entropy: compare the excess
+    valid = nrot > 1
+    entropy = -np.mean([(T[i, :nrot[i]] * np.log(T[i, :nrot[i]])).sum() for i in np.nonzero(valid)[0]])
+    net = WarmNet(seed=1)
+    before = net.loss(*data)
+    hist = train(net, data, data, epochs=6, batch=1024, lr=3e-3)
+    assert hist[-1][1] - entropy < 0.3 * (before - entropy), (before, entropy, hist)
+
+
+def test_warm_start_sweeps_and_forces(built, capsys):
+    """What the starts gain on proteins the network never saw, at the same
+    coordinates and the reference tolerance: the learned start (with its
+    per-system fallback) needs no more sweeps than the uniform start; the
+    previous solve's marginals (a perfect belief prediction) need clearly
+    fewer; every start gives the uniform-start forces to BP's tolerance."""
+    import upside_gb300 as U
+    import workloads
+    from warm_start import WEIGHTS, load, sweeps_per_solve
+    if not os.path.exists(WEIGHTS):
+        pytest.skip("no trained weights in the package")
+    W = workloads.workload("C4", seed=205)
+    cfg = W["configs"][:16]
+    b = U.Batch(cfg)
+    b.set_pos(workloads.initial_positions(cfg))
+    b.set_thermostat(W["temps"][:16], np.array(W["seeds"][:16], np.uint32))
+    b.run(30, use_graph=True, graph_rounds=1)
+    _, f_uniform = b.evaluate()
+    uniform = sweeps_per_solve(b, 4)
+    b.set_warm_start(load(), 1)
+    learned = sweeps_per_solve(b, 4)
+    _, f_learned = b.evaluate()
+    b.set_warm_start(None, 2)
+    b.evaluate()
+    previous = sweeps_per_solve(b, 4)
+    _, f_previous = b.evaluate()
+    b.set_warm_start(None, 3)
+    b.evaluate()
+    reuse = sweeps_per_solve(b, 4)
+    _, f_reuse = b.evaluate()
+    with capsys.disabled():
+        print("\nBP sweeps per solve: uniform %.2f learned %.2f previous-marginals %.2f previous-messages %.2f"
+              % (uniform, learned, previous, reuse))
+    assert learned <= 1.05 * uniform, (learned, uniform)
+    assert previous < 0.85 * uniform, (previous, uniform)
+    assert reuse < 0.5 * uniform, (reuse, uniform)
+    for f in (f_learned, f_previous, f_reuse):
+        rel = np.abs(f - f_uniform).max() / np.abs(f_uniform).max()
+        assert rel < 5e-3, rel
+
+
+def test_previous_messages_along_a_trajectory(built, capsys):
+    """Along a trajectory advanced with the previous-solve start, every force
+    evaluation stays within BP's tolerance of a fresh uniform-start solve at
+    the same coordinates, and the sweep count stays low."""
+    import upside_gb300 as U
+    import workloads
+    W = workloads.workload("C4", seed=206)
+    cfg = W["configs"][:8]
+    b = U.Batch(cfg)
+    b.set_pos(workloads.initial_positions(cfg))
+    b.set_thermostat(W["temps"][:8], np.array(W["seeds"][:8], np.uint32))
+    b.set_warm_start(None, 3)
+    b.run(20, use_graph=True, graph_rounds=1)
+    fresh = U.Batch(cfg)
+    worst, sweeps = 0.0, []
+    for _ in range(5):
+        b.run(5, use_graph=True, graph_rounds=1)
+        sweeps.append(b.value_by_name("rotamer", "n_iter", 8).mean() + 1)
+        x = b.get_pos()
+        _, f_reuse = b.evaluate()
+        fresh.set_pos(x)
+        _, f_fresh = fresh.evaluate()
+        worst = max(worst, np.abs(f_reuse - f_fresh).max() / np.abs(f_fresh).max())
+    with capsys.disabled():
+        print("\nprevious-message start along a trajectory: sweeps %.2f, worst force deviation %.2e"
+              % (float(np.mean(sweeps)), worst))
+    assert worst < 5e-3, worst
+    assert np.mean(sweeps) < 16, sweeps

@@ -8,6 +8,7 @@
 #include <vector>
 
 #include "engine.h"
+#include "warm.h"
 #include "../../include/engine_c_library.h"
 #include "../../include/upside_gb300.h"
 
@@ -349,6 +350,44 @@ int ug_value_by_name(UgBatch* b, const char* node, const char* what, float* out,
     return 0;
     GUARD_END(1)
 }
+int ug_set_param(UgBatch* b, const char* node, const float* param, int n) {
+    GUARD_BEGIN
+    b->e->node(node).set_param(*b->e, std::vector<float>(param, param + n));
+    return 0;
+    GUARD_END(1)
+}
+int ug_get_param(UgBatch* b, const char* node, float* param, int n) {
+    GUARD_BEGIN
+    auto v = b->e->node(node).get_param(*b->e);
+    if (n != int(v.size())) throw ug::Error("parameter size mismatch: " + std::to_string(v.size()));
+    std::copy(v.begin(), v.end(), param);
+    return 0;
+    GUARD_END(1)
+}
+int ug_param_deriv(UgBatch* b, const char* node, float* deriv, int n) {
+    GUARD_BEGIN
+    auto v = b->e->node(node).param_deriv(*b->e);
+    if (n != int(v.size())) throw ug::Error("parameter size mismatch: " + std::to_string(v.size()));
+    std::copy(v.begin(), v.end(), deriv);
+    return 0;
+    GUARD_END(1)
+}
+
+int ug_set_warm_start(UgBatch* b, const float* w1, const float* b1, const float* w2, const float* b2, const float* w3,
+                      const float* b3, int enable) {
+    GUARD_BEGIN
+    const float* p[6] = {w1, b1, w2, b2, w3, b3};
+    bool given = w1 && b1 && w2 && b2 && w3 && b3;
+    if (!given && (w1 || b1 || w2 || b2 || w3 || b3)) throw ug::Error("ug_set_warm_start: give all six arrays or none");
+    bool found = false;
+    if (enable < 0 || enable > 3) throw ug::Error("ug_set_warm_start: mode must be 0, 1, 2 or 3");
+    for (auto& n : b->e->nodes) found |= n->set_warm(*b->e, given ? p : nullptr, enable);
+    if (!found) throw ug::Error("ug_set_warm_start: the node graph has no rotamer node");
+    b->e->drop_graph();
+    return 0;
+    GUARD_END(1)
+}
+
 int ug_node_potential(UgBatch* b, const char* node, double* out) {
     GUARD_BEGIN
     auto& nd = b->e->node(node);
@@ -543,6 +582,36 @@ int ug_profile(UgBatch* b, int n_eval, char* names, int names_cap, float* ms, in
     memcpy(names, s.c_str(), s.size() + 1);
     return int(p.size());
     GUARD_END(-1)
+}
+
+// ------------------------------------------- warm-start network kernels ---
+#define UG_MLP(call)                                        \
+    GUARD_BEGIN                                             \
+    UG_CK(call);                                            \
+    return 0;                                               \
+    GUARD_END(1)
+
+int ug_mlp_gemm(const uint16_t* A, int64_t a_r, int64_t a_c, const uint16_t* B, int64_t b_r, int64_t b_c, float* C,
+                int ldc, int M, int N, int K, int accumulate, void* stream) {
+    UG_MLP(ug::launch_gemm_bf16(A, a_r, a_c, B, b_r, b_c, C, ldc, M, N, K, accumulate,
+                                static_cast<cudaStream_t>(stream)))
+}
+int ug_mlp_bias_act(const float* Z, const float* bias, uint16_t* H, float* Hf, int M, int N, int relu, void* stream) {
+    UG_MLP(ug::launch_bias_act(Z, bias, H, Hf, M, N, relu, static_cast<cudaStream_t>(stream)))
+}
+int ug_mlp_to_bf16(float* X, const uint16_t* relu_of, uint16_t* Y, int64_t n, void* stream) {
+    UG_MLP(ug::launch_to_bf16(X, relu_of, Y, n, static_cast<cudaStream_t>(stream)))
+}
+int ug_mlp_softmax_xent(const float* Z, const float* T, const int32_t* nrot, float* dZ, float* loss, int M, float scale,
+                        void* stream) {
+    UG_MLP(ug::launch_softmax_xent(Z, T, nrot, dZ, loss, M, scale, static_cast<cudaStream_t>(stream)))
+}
+int ug_mlp_colsum(const float* X, float* out, int M, int N, void* stream) {
+    UG_MLP(ug::launch_colsum(X, out, M, N, static_cast<cudaStream_t>(stream)))
+}
+int ug_mlp_adam(float* w, const float* g, float* m, float* v, uint16_t* wb, int n, float lr, float b1, float b2,
+                float eps, int step, void* stream) {
+    UG_MLP(ug::launch_adam(w, g, m, v, wb, n, lr, b1, b2, eps, step, static_cast<cudaStream_t>(stream)))
 }
 
 int ug_pair_list(const float* pos, int n, float cutoff, int32_t* pairs, int cap, int32_t* n_pairs, void* stream) {

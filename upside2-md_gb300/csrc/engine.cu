@@ -15,6 +15,7 @@
 #include <unordered_map>
 
 #include "dev_math.cuh"
+#include "warm.h"
 
 namespace ug {
 
@@ -1700,7 +1701,12 @@ struct RotamerNode : GNode {
     int n_prob = 0;
     double* d_energy = nullptr;
     int prev_n_ent = 0;
-    RotamerNode(Engine& e, const Groups& g, const std::vector<int>& obead) {
+    // learned warm start: node -> chain residue and residue type (host copies
+    // kept for validation), device state once enabled
+    std::vector<int> h_node_res, h_node_aa;
+    WarmDev wd{};
+    bool warm_on = false, warm_alloc = false;
+    RotamerNode(Engine& e, const Groups& g, const std::vector<int>& obead, const std::string& bead_node) {
         potential = true;
         hg.setup(e, IK_ROTAMER, EX_ROTAMER, true, 6, 6, 54, g, "pair_interaction", obead, obead, 96);
         b.damping = float(shared_attr(g, "damping"));
@@ -1731,6 +1737,35 @@ struct RotamerNode : GNode {
             for (int x : id) {
                 bead_res.push_back(base + res_of[std::make_pair((x >> 4) & 15, x >> 8)]);
                 bead_rot.push_back(x & 15);
+            }
+            // chain residue of each node (the frame that places its first
+            // bead) and its residue type, for the warm-start features
+            {
+                std::vector<int> first(size_t(N), -1), node_res(size_t(N), -1), node_aa(size_t(N), -1);
+                auto bead_row = read_i(g.f(s), g.p("pair_interaction/index"));
+                std::string aff = "/input/potential/" + bead_node + "/affine_residue";
+                if (g.f(s).exists(aff) && bead_row.size() == id.size()) {
+                    auto ar = read_i(g.f(s), aff);
+                    for (size_t k = 0; k < id.size(); ++k) {
+                        int u = res_of[std::make_pair((id[k] >> 4) & 15, id[k] >> 8)];
+                        if (first[size_t(u)] < 0 && bead_row[k] >= 0 && size_t(bead_row[k]) < ar.size())
+                            first[size_t(u)] = ar[size_t(bead_row[k])];
+                    }
+                    node_res = first;
+                }
+                if (g.f(s).exists("/input/sequence")) {
+                    static const char* aa3[20] = {"ALA", "ARG", "ASN", "ASP", "CYS", "GLN", "GLU", "GLY", "HIS", "ILE",
+                                                  "LEU", "LYS", "MET", "PHE", "PRO", "SER", "THR", "TRP", "TYR", "VAL"};
+                    auto seq = g.f(s).read_strings("/input/sequence");
+                    for (int u = 0; u < N; ++u) {
+                        int r = node_res[size_t(u)];
+                        if (r < 0 || size_t(r) >= seq.size()) continue;
+                        for (int a = 0; a < 20; ++a)
+                            if (seq[size_t(r)].compare(0, 3, aa3[a]) == 0) node_aa[size_t(u)] = a;
+                    }
+                }
+                h_node_res.insert(h_node_res.end(), node_res.begin(), node_res.end());
+                h_node_aa.insert(h_node_aa.end(), node_aa.begin(), node_aa.end());
             }
             for (int i = 0; i < N; ++i) {
                 nrot.push_back(order[size_t(i)].first);
@@ -1772,6 +1807,9 @@ struct RotamerNode : GNode {
         b.n_iter = e.alloc<int>(size_t(e.n_sys));
         b.e11 = e.alloc<double>(size_t(e.n_sys));
         b.alg_bytes = e.alloc<unsigned long long>(size_t(e.n_sys));
+        b.parity = e.alloc<int>(1);
+        b.prev_valid = e.alloc<int>(size_t(e.n_sys) * 2);
+        b.prev_row_ptr = e.alloc<int>((size_t(b.n_res) + 1) * 2);
         d_energy = e.alloc<double>(size_t(e.n_sys));
     }
     void alloc_entries(Engine& e, int cap) {
@@ -1784,6 +1822,10 @@ struct RotamerNode : GNode {
         b.P = e.alloc<float>(size_t(cap) * 36);
         b.emarg = e.alloc<float>(size_t(cap) * 36);
         b.msg = e.alloc<float>(size_t(cap) * 16);
+        // previous-solve state (both halves); what the old storage held is gone
+        b.prev_col = e.alloc<int>(size_t(cap) * 2);
+        b.prev_msg = e.alloc<float>(size_t(cap) * 16);
+        if (b.prev_valid) UG_CK(cudaMemset(b.prev_valid, 0, sizeof(int) * 2 * size_t(e.n_sys)));
     }
     void forward(Engine& e, bool energy) override {
         auto& beads = e.arg(*this, 0);
@@ -1801,7 +1843,8 @@ struct RotamerNode : GNode {
             w[k] = pn.width;
         }
         for (int k = n_prob; k < 4; ++k) { in[k] = in[0]; ins[k] = ins[0]; w[k] = w[0]; }
-        launch_bp(b, hg.g, in, ins, w, n_prob, prev_n_ent, nullptr, energy ? 1 : 0, d_energy, e.st);
+        launch_bp(b, hg.g, in, ins, w, n_prob, prev_n_ent, nullptr, energy ? 1 : 0, d_energy, warm_on ? &wd : nullptr,
+                  e.d_pos, e.atom_off_d, e.st);
         if (energy) add_pot(e);
     }
     void add_pot(Engine& e);
@@ -1821,6 +1864,82 @@ struct RotamerNode : GNode {
         return r;
     }
     DGraph* graph() override { return &hg.g; }
+    // device buffers of the warm start, allocated on first use
+    void warm_buffers(Engine& e) {
+        if (warm_alloc) return;
+        std::vector<int> rsys(size_t(b.n_res));
+        UG_CK(cudaMemcpy(rsys.data(), b.res_sys, 4 * rsys.size(), cudaMemcpyDeviceToHost));
+        int max_chain = 0;
+        for (int na : e.n_atom) max_chain = std::max(max_chain, na / 3);
+        for (size_t u = 0; u < h_node_res.size(); ++u) {
+            int r = h_node_res[u];
+            if (r < 0 || r >= e.n_atom[size_t(rsys[u])] / 3)
+                throw Error("warm start needs the chain residue of every rotamer node (affine_residue of the bead "
+                            "placement and 3 backbone atoms per residue)");
+        }
+        if (size_t(max_chain) * 24 > size_t(200) * 1024) throw Error("chain too long for the warm-start features");
+        wd.node_res = e.upload(h_node_res);
+        wd.node_aa = e.upload(h_node_aa);
+        wd.max_chain = max_chain;
+        size_t n = size_t(b.n_res);
+        wd.X = e.alloc<uint16_t>(n * WARM_IN);
+        wd.Zh = e.alloc<float>(n * WARM_HID);
+        wd.H1 = e.alloc<uint16_t>(n * WARM_HID);
+        wd.H2 = e.alloc<uint16_t>(n * WARM_HID);
+        wd.Z = e.alloc<float>(n * WARM_OUT);
+        wd.belief = e.alloc<float>(n * 8);
+        wd.W1 = e.alloc<uint16_t>(size_t(WARM_IN) * WARM_HID);
+        wd.W2 = e.alloc<uint16_t>(size_t(WARM_HID) * WARM_HID);
+        wd.W3 = e.alloc<uint16_t>(size_t(WARM_HID) * WARM_OUT);
+        wd.b1 = e.alloc<float>(WARM_HID);
+        wd.b2 = e.alloc<float>(WARM_HID);
+        wd.b3 = e.alloc<float>(WARM_OUT);
+        b.warm_stat = e.alloc<float>(size_t(e.n_sys) * 4);
+        wd.stat = b.warm_stat;
+        wd.n_sys = e.n_sys;
+        wd.need = e.alloc<int>(1);
+        warm_alloc = true;
+    }
+    // weights: W1 (WARM_IN x WARM_HID), b1, W2 (WARM_HID x WARM_HID), b2,
+    // W3 (WARM_HID x WARM_OUT), b3, FP32 row-major; kept as bf16 on the device
+    bool set_warm(Engine& e, const float* const* p, int mode) override {
+        warm_buffers(e);
+        auto bf = [](const float* x, size_t n) {
+            std::vector<uint16_t> r(n);
+            for (size_t i = 0; i < n; ++i) {
+                uint32_t u;
+                std::memcpy(&u, &x[i], 4);
+                u += 0x7fffu + ((u >> 16) & 1u);  // round to nearest even
+                r[i] = uint16_t(u >> 16);
+            }
+            return r;
+        };
+        auto up16 = [&](const uint16_t* dst, const float* src, size_t n) {
+            auto v = bf(src, n);
+            UG_CK(cudaMemcpy(const_cast<uint16_t*>(dst), v.data(), 2 * n, cudaMemcpyHostToDevice));
+        };
+        auto up32 = [&](const float* dst, const float* src, size_t n) {
+            UG_CK(cudaMemcpy(const_cast<float*>(dst), src, 4 * n, cudaMemcpyHostToDevice));
+        };
+        if (p) {
+            up16(wd.W1, p[0], size_t(WARM_IN) * WARM_HID);
+            up32(wd.b1, p[1], WARM_HID);
+            up16(wd.W2, p[2], size_t(WARM_HID) * WARM_HID);
+            up32(wd.b2, p[3], WARM_HID);
+            up16(wd.W3, p[4], size_t(WARM_HID) * WARM_OUT);
+            up32(wd.b3, p[5], WARM_OUT);
+        }
+        UG_CK(cudaMemset(b.warm_stat, 0, sizeof(float) * 4 * size_t(e.n_sys)));
+        // mode 1: the network's prediction; mode 2: the marginals of the
+        // previous solve of each system; mode 3: the previous solve's final
+        // messages and marginals (starts that remember the last evaluation
+        // instead of predicting it)
+        warm_on = mode == 1;
+        b.warm = mode == 1 ? wd.belief : mode == 2 ? b.marg : nullptr;
+        b.reuse = mode == 3;
+        UG_CK(cudaMemset(b.prev_valid, 0, sizeof(int) * 2 * size_t(e.n_sys)));
+        return true;
+    }
     bool set_kernel_timer(cudaEvent_t* ev, int* used, int cap) override {
         b.kt_ev = ev;
         b.kt_used = used;
@@ -1853,6 +1972,40 @@ struct RotamerNode : GNode {
     std::vector<float> value_by_name(Engine& e, const std::string& w) override {
         if (w == "count_edges_by_type") return hg.count_edges_by_type();
         if (w == "n_node") return {float(n_res_sys.at(0))};
+        // warm-start training data and state, in BP node order (systems concatenated)
+        if (w == "bp_n_node") return {float(b.n_res)};
+        if (w == "warm_features") {
+            warm_buffers(e);
+            WarmDev all = wd;
+            all.need = nullptr;  // every node, whatever the solves would use
+            launch_warm_features(all, e.d_pos, e.atom_off_d, b.res_off, b.prob, b.nrot, e.n_sys, e.st);
+            std::vector<uint16_t> x(size_t(b.n_res) * WARM_IN);
+            UG_CK(cudaMemcpyAsync(x.data(), wd.X, 2 * x.size(), cudaMemcpyDeviceToHost, e.st));
+            UG_CK(cudaStreamSynchronize(e.st));
+            std::vector<float> r(x.size());
+            for (size_t i = 0; i < x.size(); ++i) {
+                uint32_t u = uint32_t(x[i]) << 16;
+                std::memcpy(&r[i], &u, 4);
+            }
+            return r;
+        }
+        if (w == "bp_marginal" || w == "warm_belief") {
+            if (w == "warm_belief" && !warm_alloc) throw Error("warm start not set");
+            std::vector<float> m(size_t(b.n_res) * 8);
+            UG_CK(cudaMemcpy(m.data(), w == "bp_marginal" ? b.marg : wd.belief, 4 * m.size(), cudaMemcpyDeviceToHost));
+            return m;
+        }
+        if (w == "bp_nrot") {
+            std::vector<int> nr(size_t(b.n_res));
+            UG_CK(cudaMemcpy(nr.data(), b.nrot, 4 * nr.size(), cudaMemcpyDeviceToHost));
+            return std::vector<float>(nr.begin(), nr.end());
+        }
+        if (w == "warm_stat") {
+            if (!warm_alloc) throw Error("warm start not set");
+            std::vector<float> st(size_t(e.n_sys) * 4);
+            UG_CK(cudaMemcpy(st.data(), b.warm_stat, 4 * st.size(), cudaMemcpyDeviceToHost));
+            return st;
+        }
         if (w == "n_iter") {
             std::vector<int> it(size_t(e.n_sys));
             UG_CK(cudaMemcpy(it.data(), b.n_iter, 4 * it.size(), cudaMemcpyDeviceToHost));
@@ -2021,7 +2174,7 @@ Engine::Engine(const std::vector<std::string>& paths, const std::vector<int>& n_
             else if (is_prefix("placement_fixed_point_vector_only", nm)) n.reset(new PlacementNode(*this, g, 2, false, false, O(0), nullptr));
             else if (is_prefix("placement_fixed_point_only", nm)) n.reset(new PlacementNode(*this, g, 1, false, false, O(0), nullptr));
             else if (is_prefix("placement_scalar", nm)) n.reset(new PlacementNode(*this, g, 0, true, true, O(0), &O(1)));
-            else if (is_prefix("rotamer", nm)) n.reset(new RotamerNode(*this, g, O(0)));
+            else if (is_prefix("rotamer", nm)) n.reset(new RotamerNode(*this, g, O(0), deps[nm].at(0)));
             else if (is_prefix("weighted_pos", nm)) n.reset(new WeightedPosNode(*this, g, O(0), O(1)));
             else if (is_prefix("environment_coverage", nm)) n.reset(new CoverageNode(*this, g, IK_ENVCOV, O(0), O(1)));
             else if (is_prefix("hb_environment_coverage", nm)) n.reset(new CoverageNode(*this, g, IK_HBENV, O(0), O(1)));
@@ -2157,6 +2310,15 @@ void Engine::capture(float dt, float timescale, int rounds) {
     graph_timed = false;
 }
 void Engine::launch_graph() { UG_CK(cudaGraphLaunch(graph_exec, st)); }
+
+void Engine::drop_graph() {
+    UG_CK(cudaStreamSynchronize(st));
+    if (graph_exec) cudaGraphExecDestroy(graph_exec);
+    if (graph) cudaGraphDestroy(graph);
+    graph_exec = nullptr;
+    graph = nullptr;
+    graph_timed = false;
+}
 
 // One-round graph whose measured-kernel launches are bracketed by event-record
 // nodes (kt_ev[0..kt_used)); each replay re-records them.

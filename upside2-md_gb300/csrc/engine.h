@@ -58,6 +58,11 @@ struct GNode {
     // ev[*used..cap) (ev null: stop), and the running total of its
     // algorithmic bytes; nodes without one return false / 0
     virtual bool set_kernel_timer(cudaEvent_t*, int*, int) { return false; }
+    // BP warm start (rotamer node): six FP32 weight arrays or null to keep the
+    // current ones; mode 0 off, 1 learned, 2 previous marginals, 3 previous
+    // messages and marginals; returns false
+    // for nodes without one
+    virtual bool set_warm(Engine&, const float* const*, int) { return false; }
     virtual double kernel_bytes(Engine&) { return 0.0; }
 };
 
@@ -113,6 +118,8 @@ public:
 
     // CUDA graph of `rounds_per_graph` integration rounds
     void capture(float dt, float timescale, int rounds_per_graph);
+    // forget the captured graph (its kernels hold parameters that changed)
+    void drop_graph();
     void launch_graph();
     cudaGraphExec_t graph_exec = nullptr;
     cudaGraph_t graph = nullptr;

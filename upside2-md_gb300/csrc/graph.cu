@@ -15,6 +15,7 @@
 
 #include "dev_math.cuh"
 #include "graph.h"
+#include "warm.h"
 
 namespace ug {
 
@@ -604,6 +605,7 @@ __global__ void bp_reset_kernel(DBP b) {
         b.E1x[r] = 0.f;
     }
     for (int s = grid_stride_start(); s < b.n_sys; s += grid_stride()) b.e11[s] = 0.0;
+    if (b.reuse && blockIdx.x == 0 && threadIdx.x == 0) *b.parity ^= 1;  // new evaluation
 }
 
 // 1-body energy per (residue, rotamer) from up to 4 input nodes (src/rotamer.cpp:862-884)
@@ -935,11 +937,78 @@ __global__ void __launch_bounds__(1024) bp_solve_kernel(DBP b, int want_energy, 
         return r;
     };
 
-    // N.old = N.cur = prob; E.old = 1 (own entries)
+    // Learned warm start: the first sweep starts from the predicted marginals
+    // instead of prob.  Per system, the mean sweep counts of warm and uniform
+    // starts are tracked (warm_stat: mean warm, mean uniform, solves); every
+    // WARM_PROBE-th solve starts uniform to refresh the comparison, and the
+    // warm start is used only while it needs no more sweeps than uniform.
+    const int par = b.reuse ? *b.parity : 0;
+    const bool use_prev = b.reuse && b.prev_valid[(par ^ 1) * b.n_sys + s];
+    const bool use_warm = use_prev || (b.warm && warm_start_used(b.warm_stat + 4 * s));
+    const float* init = use_prev ? b.marg : use_warm ? b.warm : b.prob;
+    // N.old = N.cur = prob (N.old = prediction when warm); E.old = 1 (own entries)
     if (tid == 0) s_multi = 0;
-    for (int i = tid; i < N * 8; i += nt) NB[0][i] = NB[1][i] = b.prob[r0 * 8 + i];
-    for (int i = tid; i < N; i += nt) s_nrot[i] = b.nrot[r0 + i];
-    for (int i = eo0 * 8 + tid; i < eo1 * 8; i += nt) EM[1][i] = 1.f;
+    for (int ul = tid; ul < N; ul += nt) {
+        // a start row that is not a distribution (no previous solve yet) falls
+        // back to prob for that node
+        const float* w = init + (r0 + ul) * 8;
+        float ws = 0.f;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) ws += w[k];
+        if (!(ws > 0.5f)) w = b.prob + (r0 + ul) * 8;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            NB[0][ul * 8 + k] = b.prob[(r0 + ul) * 8 + k];
+            NB[1][ul * 8 + k] = w[k];
+        }
+        s_nrot[ul] = b.nrot[r0 + ul];
+    }
+    __syncthreads();
+    if (use_prev) {
+        // the previous solve's final message of the same residue pair (u <- v),
+        // found in u's previous CSR row (columns ascending); uniform if the
+        // pair is new
+        const int q = par ^ 1;
+        const int* pr = b.prev_row_ptr + size_t(q) * (b.n_res + 1);
+        const int* pc = b.prev_col + size_t(q) * b.ent_cap;
+        const float* pm = b.prev_msg + size_t(q) * b.ent_cap * 8;
+        for (int f = eo0 + tid; f < eo1; f += nt) {
+            int u = b.erow[f], v = b.col[f];
+            int a = pr[u], z = pr[u + 1];
+            while (a < z) {  // first previous column >= v
+                int m = (a + z) >> 1;
+                if (pc[m] < v) a = m + 1; else z = m;
+            }
+            float4* dst = reinterpret_cast<float4*>(EM[1] + size_t(f) * 8);
+            if (a < pr[u + 1] && pc[a] == v) {
+                const float4* src = reinterpret_cast<const float4*>(pm + size_t(a) * 8);
+                dst[0] = src[0];
+                dst[1] = src[1];
+            } else {
+                dst[0] = dst[1] = make_float4(1.f, 1.f, 1.f, 1.f);
+            }
+        }
+    } else if (!use_warm) {
+        for (int i = eo0 * 8 + tid; i < eo1 * 8; i += nt) EM[1][i] = 1.f;
+    } else {
+        // messages consistent with the start: the d incoming messages of node
+        // u are all (start_u / prob_u)^(1/d), so that prob_u times their
+        // product is the start belief
+        for (int f = eo0 + tid; f < eo1; f += nt) {
+            int u = b.erow[f], ul = u - r0;
+            int n = s_nrot[ul];
+            float inv_d = 1.f / float(max(1, b.row_ptr[u + 1] - b.row_ptr[u]));
+            float m[8], sum = 0.f;
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                m[k] = k < n ? powf((1e-10f + NB[1][ul * 8 + k]) / (1e-10f + NB[0][ul * 8 + k]), inv_d) : 0.f;
+                sum += m[k];
+            }
+            float inv = 1.f / sum;
+#pragma unroll
+            for (int k = 0; k < 8; ++k) EM[1][size_t(f) * 8 + k] = k < n ? m[k] * inv : 1.f;
+        }
+    }
     __syncthreads();
     {  // multi-rotamer node count of the system, for the algorithmic-byte tally
         int m = 0;
@@ -978,6 +1047,14 @@ __global__ void __launch_bounds__(1024) bp_solve_kernel(DBP b, int want_energy, 
     if (tid == 0 && crank == 0) {
         b.n_iter[s] = iter;
         if (iter >= b.max_iter - b.chunk - 1) atomicOr(b.status, ST_BP_NOT_CONVERGED);
+        if (b.warm) {  // running means of the sweep counts of both starts
+            float* ws = b.warm_stat + 4 * s;
+            float sweeps = float(1 + iter);
+            int k = use_warm ? 0 : 1, known = int(ws[3]);
+            ws[k] = (known >> k & 1) ? 0.75f * ws[k] + 0.25f * sweeps : sweeps;
+            ws[2] += 1.f;
+            ws[3] = float(known | (1 << k));
+        }
         // algorithmic bytes of this launch for system s.  Per sweep, each
         // directed entry is read by the message phase (einfo 16 B, P 144 B,
         // old message 32 B), written once (new message 32 B) and read by the
@@ -1004,6 +1081,19 @@ __global__ void __launch_bounds__(1024) bp_solve_kernel(DBP b, int want_energy, 
         for (int k = 0; k < n; ++k) sum += Nf[ul * 8 + k];
         float inv = 1.f / sum;
         for (int k = 0; k < 8; ++k) b.marg[u * 8 + k] = k < n ? Nf[ul * 8 + k] * inv : 0.f;
+    }
+    if (b.reuse) {  // leave the final state for the next evaluation's solve
+        int* pr = b.prev_row_ptr + size_t(par) * (b.n_res + 1);
+        int* pc = b.prev_col + size_t(par) * b.ent_cap;
+        float* pm = b.prev_msg + size_t(par) * b.ent_cap * 8;
+        const float4* fin = reinterpret_cast<const float4*>(EM[ec]);
+        for (int e = eo0 + tid; e < eo1; e += nt) {
+            pc[e] = b.col[e];
+            reinterpret_cast<float4*>(pm)[2 * e] = fin[2 * e];
+            reinterpret_cast<float4*>(pm)[2 * e + 1] = fin[2 * e + 1];
+        }
+        for (int u = r0 + lo + tid; u <= r0 + hi; u += nt) pr[u] = min(b.row_ptr[u], e1);
+        if (tid == 0 && crank == 0) b.prev_valid[par * b.n_sys + s] = 1;
     }
     cluster.sync();  // every node marginal of the system is written
     // edge marginals of own entries
@@ -1103,7 +1193,8 @@ __global__ void bp_sens_kernel(DBP b, DGraph g, float* s0, float* s1, float* s2,
 }
 
 void launch_bp(DBP& b, const DGraph& g, const float* const* in, float* const* in_sens, const int* w, int n_in,
-               int prev_n_ent, int* scan_total, int want_energy, double* energy_out, cudaStream_t st) {
+               int prev_n_ent, int* scan_total, int want_energy, double* energy_out, const WarmDev* warm,
+               const float* pos, const int* atom_off, cudaStream_t st) {
     int blocks = 2 * 152;
     // n_ent is rewritten only by the scan below, after this kernel completes
     bp_reset_kernel<<<blocks, 256, 0, st>>>(b);
@@ -1118,6 +1209,7 @@ void launch_bp(DBP& b, const DGraph& g, const float* const* in, float* const* in
     bp_entry_init_kernel<<<blocks, 256, 0, st>>>(b);
     bp_edge_energy_kernel<<<blocks, 256, 0, st>>>(b, g);
     bp_prob_kernel<<<blocks, 256, 0, st>>>(b);
+    if (warm) launch_warm_start(*warm, pos, atom_off, b.res_off, b.prob, b.nrot, b.n_sys, b.n_res, st);
     size_t smem = bp_solve_smem_bytes(b.max_res_sys);
     static size_t configured = 0;
     if (smem > 48 * 1024 && smem > configured) {

@@ -126,6 +126,20 @@ struct DBP {
     // bytes (the formula is in bp_solve_kernel), and optional host-side CUDA
     // events bracketing each solve launch (kt_ev null: no events recorded)
     unsigned long long* alg_bytes;
+    // learned warm start: predicted marginals (res * 8; null = uniform start)
+    // and per-system sweep statistics (4 floats per system)
+    const float* warm;
+    float* warm_stat;
+    // previous-solve start (reuse != 0): each solve leaves its final messages,
+    // their columns and row offsets in the half `parity` of the prev_ arrays;
+    // the next solve (other half) starts from them, matched by residue pair,
+    // and from the previous marginals.  parity flips once per evaluation.
+    int reuse;
+    int* parity;                // device scalar
+    int* prev_valid;            // 2 x n_sys
+    int* prev_row_ptr;          // 2 x (n_res + 1)
+    int* prev_col;              // 2 x ent_cap
+    float* prev_msg;            // 2 x ent_cap x 8
     cudaEvent_t* kt_ev;
     int* kt_used;
     int kt_cap;
@@ -143,8 +157,11 @@ void launch_edge_eval(const DGraph& g, int* sys_start, int* sys_end, cudaStream_
 void launch_edge_scatter(const DGraph& g, cudaStream_t st);
 void launch_param_deriv(const DGraph& g, float* out, cudaStream_t st);
 // in: up to 4 one-body energy inputs (bead rows), in_sens their sensitivities
+// warm: learned warm start (null: off); pos / atom_off feed its features
+struct WarmDev;
 void launch_bp(DBP& b, const DGraph& g, const float* const* in, float* const* in_sens, const int* w, int n_in,
-               int prev_n_ent, int* scan_total, int want_energy, double* energy_out, cudaStream_t st);
+               int prev_n_ent, int* scan_total, int want_energy, double* energy_out, const WarmDev* warm,
+               const float* pos, const int* atom_off, cudaStream_t st);
 // standalone pair list of one point set (pairlist.cu); row_count and row_off
 // each hold ceil(n/4) ints, row_off one more
 cudaError_t launch_point_pairs(const float* pos, int n, float cutoff, int* pairs, int cap, int* n_pairs,

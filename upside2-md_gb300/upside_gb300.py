@@ -61,6 +61,16 @@ def lib():
         L.ug_bench.argtypes = [vp, ip, ctypes.c_float, ctypes.c_float, ip, ip, vp]
         L.ug_set_device.argtypes = [ip]
         L.ug_bench_kernel.argtypes = [vp, vp]
+        for nm in ["ug_set_param", "ug_get_param", "ug_param_deriv"]:
+            getattr(L, nm).argtypes = [vp, cp, vp, ip]
+        i64, f = ctypes.c_int64, ctypes.c_float
+        L.ug_set_warm_start.argtypes = [vp, vp, vp, vp, vp, vp, vp, ip]
+        L.ug_mlp_gemm.argtypes = [vp, i64, i64, vp, i64, i64, vp, ip, ip, ip, ip, ip, vp]
+        L.ug_mlp_bias_act.argtypes = [vp, vp, vp, vp, ip, ip, ip, vp]
+        L.ug_mlp_to_bf16.argtypes = [vp, vp, vp, i64, vp]
+        L.ug_mlp_softmax_xent.argtypes = [vp, vp, vp, vp, vp, ip, f, vp]
+        L.ug_mlp_colsum.argtypes = [vp, vp, ip, ip, vp]
+        L.ug_mlp_adam.argtypes = [vp, vp, vp, vp, vp, ip, f, f, f, f, ip, vp]
         L.ug_pair_list.argtypes = [vp, ip, ctypes.c_float, vp, ip, vp, vp]
         L.ug_pair_list_noalloc.argtypes = [vp, ip, ctypes.c_float, vp, ip, vp, vp]
         _lib = L
@@ -252,6 +262,21 @@ class Batch:
         self._chk(lib().ug_node_potential(self.h, name.encode(), o.ctypes.data))
         return o
 
+    def set_param(self, name, param):
+        p = _f32(param).ravel()
+        self._chk(lib().ug_set_param(self.h, name.encode(), p.ctypes.data, p.size))
+
+    def get_param(self, name, shape):
+        p = np.zeros(shape, np.float32)
+        self._chk(lib().ug_get_param(self.h, name.encode(), p.ctypes.data, p.size))
+        return p
+
+    def param_deriv(self, name, shape):
+        """dE/d(param) of the last evaluate(), summed over the batch's systems."""
+        p = np.zeros(shape, np.float32)
+        self._chk(lib().ug_param_deriv(self.h, name.encode(), p.ctypes.data, p.size))
+        return p
+
     def node_edges(self, name, cap=1 << 22):
         buf = np.zeros((cap, 2), np.int32)
         n = lib().ug_node_edges(self.h, name.encode(), buf.ctypes.data, cap)
@@ -263,6 +288,18 @@ class Batch:
         o = np.zeros(n, np.float32)
         self._chk(lib().ug_value_by_name(self.h, name.encode(), what.encode(), o.ctypes.data, n))
         return o
+
+    def set_warm_start(self, weights=None, enable=1):
+        """Load learned BP warm-start weights (dict W1, b1, W2, b2, W3, b3) and/or
+        select the BP start: 0 uniform, 1 learned, 2 previous marginals,
+        3 previous messages and marginals."""
+        if weights is None:
+            ptrs = [None] * 6
+            keep = []
+        else:
+            keep = [_f32(weights[k]) for k in ("W1", "b1", "W2", "b2", "W3", "b3")]
+            ptrs = [a.ctypes.data for a in keep]
+        self._chk(lib().ug_set_warm_start(self.h, *ptrs, int(enable)))
 
     def replica_exchange(self, pairs, seed, round_):
         pairs = np.ascontiguousarray(pairs, dtype=np.int32).reshape(-1, 2)
