@@ -39,6 +39,9 @@ def parse():
     ap.add_argument("--no-plain", action="store_true", help="skip the plain single-system GPU comparison")
     ap.add_argument("--bp-start", default="learned", choices=["uniform", "learned", "previous", "reuse"],
                     help="BP initial state of the batched run")
+    ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--equilibrate", type=int, default=300,
+                    help="untimed integration rounds from the initial coils before the warm-up")
     ap.add_argument("--profile", action="store_true", help="print per-node device times to stderr")
     return ap.parse_args()
 
@@ -139,16 +142,17 @@ def measured_peaks():
 
 # ------------------------------------------------------------ CPU oracle ---
 def _cpu_worker(args):
-    path, n_atom, seconds, seed = args
+    path, n_atom, seconds, seed, pos, mom = args
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     sys.path.insert(0, os.path.join(ROOT, "upside2-md_gb300"))
     import numpy as np
     import oracle_py
     from h5lite import H5File
-    with H5File(path) as f:
-        pos = f.read("/input/pos")[:, :, 0].astype(np.float32)
+    if pos is None:
+        with H5File(path) as f:
+            pos = f.read("/input/pos")[:, :, 0].astype(np.float32)
+        mom = np.zeros_like(pos)
     o = oracle_py.Oracle(path, n_atom)
-    mom = np.zeros_like(pos)
     t0 = time.perf_counter()
     rounds = 0
     while time.perf_counter() - t0 < seconds:
@@ -157,14 +161,17 @@ def _cpu_worker(args):
     return rounds, time.perf_counter() - t0, n_atom // 3
 
 
-def cpu_port_rate(configs, seconds, max_procs=None):
+def cpu_port_rate(configs, seconds, max_procs=None, states=None):
     """Oracle port (the CPU restatement) timed on the host cores: one process
     per system (the reference parallelises across systems only), each running
-    whole integration rounds for `seconds`.  Returns (residue-steps/s, cores, sample)."""
+    whole integration rounds for `seconds` from the given (positions, momenta)
+    of each system, or from the config's coordinates at rest.  Returns
+    (residue-steps/s, cores, sample)."""
     import multiprocessing as mp
     from workloads import n_res_of
     procs = min(len(configs), max_procs or os.cpu_count() or 1)
-    jobs = [(configs[i], 3 * n_res_of(configs[i]), seconds, 1 + i) for i in range(procs)]
+    jobs = [(configs[i], 3 * n_res_of(configs[i]), seconds, 1 + i) + (states[i] if states else (None, None))
+            for i in range(procs)]
     ctx = mp.get_context("spawn")
     with ctx.Pool(procs) as pool:
         res = pool.map(_cpu_worker, jobs)
@@ -208,6 +215,17 @@ def main():
     b.set_pos(workloads.initial_positions(W["configs"]))
     b.set_thermostat(W["temps"], np.array(W["seeds"], np.uint32))
     bp_start = set_bp_start(b, a.bp_start)
+    # equilibrate: the random initial coils relax for a few hundred rounds
+    # before the dynamics reach their steady state (untimed)
+    if a.equilibrate:
+        b.run(a.equilibrate, use_graph=True, graph_rounds=10)
+    tuned = None
+    if not a.no_autotune:  # untimed; the state is restored after the trials
+        trials, chosen = b.autotune(5)
+        tuned = {"chosen": chosen, "trial_ms_per_round": trials}
+    pos_eq, mom_eq = b.get_pos(), b.get_mom()
+    states = [(pos_eq[b.atom_off[i]:b.atom_off[i + 1]].copy(), mom_eq[b.atom_off[i]:b.atom_off[i + 1]].copy())
+              for i in range(b.n_sys)]
     b.run(a.warmup, use_graph=True, graph_rounds=1)
     launches, dev_bytes = b.info()
     if a.profile:
@@ -227,10 +245,11 @@ def main():
     t_e2e = d.max(float(ms_e2e.sum()) / 1e3)
     e2e_value = units / t_e2e
     st = b.status()
-    plain = plain_single_rate(W, a) if not a.no_plain else None
+    plain = plain_single_rate(W, a, states) if not a.no_plain else None
     cpu = None
     if d.rank == 0 and d.world == 1 and not a.no_cpu_baseline:
-        rate, cores, sample = cpu_port_rate(W["configs"], a.cpu_seconds)
+        rate, cores, sample = cpu_port_rate(W["configs"], a.cpu_seconds, states=states)
+        sample += ", from the same equilibrated state as the GPU run"
         cpu = {"value": rate, "unit": "residue-steps/s", "cores": cores, "kind": "port", "sample": sample}
     if d.rank != 0:
         return
@@ -241,6 +260,7 @@ def main():
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded ff_2.1 proteins, random initial chains)",
         "config": {"workload": a.workload, "systems": len(W["configs"]), "residues": n_res_total,
                    "step": "one integration round = 3 force evaluations + integrator stages per system",
+                   "equilibration_rounds": a.equilibrate, "autotune": tuned,
                    "l2": "256 MiB buffer rewritten before every timed round", "bp_init": bp_start,
                    "bp_sweeps_per_solve": bp_sweeps(b)},
         "e2e": {"value": e2e_value, "unit": "residue-steps/s", "h2d_bytes_per_step": state_bytes,
@@ -284,20 +304,21 @@ def bp_sweeps(b):
         return None
 
 
-def plain_single_rate(W, a, n_sample=6, rounds=8):
+def plain_single_rate(W, a, states, n_sample=6, rounds=8):
     """The plain single-replica GPU path on a sample of the same workload:
     each sampled system in an engine of its own (one system per launch, the
-    same kernels and one-round CUDA graph), timed like the batch.  Returns
-    residue-steps/s of running the sample one system after another."""
+    same kernels and one-round CUDA graph, the reference's uniform BP start),
+    from the same equilibrated state as the batch, timed like the batch.
+    Returns residue-steps/s of running the sample one system after another."""
     import numpy as np
     import upside_gb300 as U
-    import workloads
     idx = list(range(min(n_sample, len(W["configs"]))))
     units = t = 0.0
     for i in idx:
         c = W["configs"][i]
         s = U.Batch([c])
-        s.set_pos(workloads.initial_positions([c]))
+        s.set_pos(states[i][0])
+        s.set_mom(states[i][1])
         s.set_thermostat([W["temps"][i]], np.array([W["seeds"][i]], np.uint32))
         s.run(3, use_graph=True, graph_rounds=1)
         ms = s.bench(rounds, flush_l2=True)

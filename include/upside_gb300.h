@@ -92,6 +92,20 @@ int ug_bench(UgBatch* b, int n_round, float dt, float timescale, int flush_l2, i
  * each sweep touches; the count is kept by the kernel itself). */
 int ug_bench_kernel(UgBatch* b, double* stats);
 
+/* Autotuner (no counterpart in the reference): from the batch's current
+ * state, times n_round integration rounds for each candidate setting and
+ * keeps the fastest; the state is restored after every trial and at the end.
+ * Tuned: the candidate-cache buffer of the pair lists (1, 1.5, 2, 3 times the
+ * reference's 1 + 0.2 cutoff; results do not depend on it), then the BP
+ * solve's blocks per system, lanes per node and threads per block.  report
+ * receives '\n'-separated "setting\tms_per_round" lines and a final
+ * "chosen\tsetting" line.  Returns the number of candidates tried (or -1). */
+int ug_autotune(UgBatch* b, int n_round, float dt, float timescale, char* report, int cap);
+/* Set the tuned quantities directly: cache buffer scale (>= 1) and BP launch
+ * variant (0..5: blocks per system x lanes per node x threads = 2x8x1024,
+ * 2x4x1024, 2x16x1024, 1x8x1024, 4x8x512, 4x4x512). */
+int ug_set_tuning(UgBatch* b, float cache_buffer_scale, int bp_variant);
+
 /* Per-node device time of n_eval eager force evaluations (CUDA events on the
  * engine stream): names '\n'-separated "<node>:fwd" / "<node>:bwd", ms[k] the
  * mean time of entry k.  Returns the number of entries (or -1). */

@@ -561,6 +561,29 @@ int ug_bench(UgBatch* b, int n_round, float dt, float timescale, int flush_l2, i
     GUARD_END(1)
 }
 
+int ug_autotune(UgBatch* b, int n_round, float dt, float timescale, char* report, int cap) {
+    GUARD_BEGIN
+    auto r = b->e->autotune(n_round, dt, timescale);
+    std::string s;
+    for (auto& x : r) s += x.first + "\t" + std::to_string(x.second) + "\n";
+    int c, l, t;
+    ug::bp_variant_desc(b->e->tuned_bp_variant, &c, &l, &t);
+    s += "chosen\tcache_buffer_scale=" + std::to_string(b->e->tuned_buffer_scale).substr(0, 4) +
+         ",bp_blocks_per_system=" + std::to_string(c) + ",lanes_per_node=" + std::to_string(l) +
+         ",threads=" + std::to_string(t) + "\n";
+    if (int(s.size()) + 1 > cap) throw ug::Error("report buffer too small");
+    memcpy(report, s.c_str(), s.size() + 1);
+    return int(r.size());
+    GUARD_END(-1)
+}
+
+int ug_set_tuning(UgBatch* b, float cache_buffer_scale, int bp_variant) {
+    GUARD_BEGIN
+    b->e->set_tuning(cache_buffer_scale, bp_variant);
+    return 0;
+    GUARD_END(1)
+}
+
 int ug_bench_kernel(UgBatch* b, double* stats) {
     GUARD_BEGIN
     stats[0] = b->kt_ms;

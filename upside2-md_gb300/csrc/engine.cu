@@ -1041,6 +1041,7 @@ struct HGraph {
         g.cache_n = e.alloc<int>(size_t(e.n_sys));
         g.active_off = e.alloc<int>(size_t(e.n_sys) + 1);
         g.cache_force = e.alloc<int>(1);
+        g.rebuilds = e.alloc<unsigned long long>(1);
         for (size_t s = 0; s < grp.size(); ++s) {
             long long fs = sym ? (long long)c1[s] * (c1[s] - 1) / 2 : (long long)c1[s] * c2[s];
             long long want = std::min<long long>(std::max<long long>(fs, 1), 2LL * cap_per_elem * c1[s]);
@@ -1068,7 +1069,16 @@ struct HGraph {
         }
         if (c != g.cutoff) force_rebuild();
         g.cutoff = c;
-        g.buffer = 1.f + 0.2f * c;
+        g.buffer = buffer_scale * (1.f + 0.2f * c);
+    }
+    // candidate-cache buffer as a multiple of the reference's 1 + 0.2 cutoff
+    // (any buffer gives the same edges; a wider one rebuilds less often and
+    // refines more candidates)
+    float buffer_scale = 1.f;
+    void set_buffer_scale(float s) {
+        buffer_scale = s;
+        g.buffer = s * (1.f + 0.2f * g.cutoff);
+        force_rebuild();
     }
     void set_param(const std::vector<float>& p) {
         if (p.size() != param_host.size()) throw Error("Bad param size, got " + std::to_string(p.size()) +
@@ -1103,6 +1113,12 @@ struct HGraph {
         alloc_edges(int(std::min<long long>(2LL * g.cap, 1LL << 30)));
         force_rebuild();
         return true;
+    }
+    // system cache rebuilds so far (one number)
+    std::vector<float> rebuild_count() {
+        unsigned long long n = 0;
+        if (g.cached) UG_CK(cudaMemcpy(&n, g.rebuilds, sizeof(n), cudaMemcpyDeviceToHost));
+        return {float(n)};
     }
     std::vector<float> count_edges_by_type() {
         int ne = 0;
@@ -1193,8 +1209,10 @@ struct ProteinHBondNode : GNode {
     }
     DGraph* graph() override { return &hg.g; }
     bool grow(Engine&) override { return hg.grow_if_full(); }
+    void set_buffer_scale(float s) override { hg.set_buffer_scale(s); }
     std::vector<float> value_by_name(Engine& e, const std::string& w) override {
         if (w == "count_edges_by_type") return hg.count_edges_by_type();
+        if (w == "cache_rebuilds") return hg.rebuild_count();
         return GNode::value_by_name(e, w);
     }
 };
@@ -1368,8 +1386,10 @@ struct CoverageNode : GNode {
     }
     DGraph* graph() override { return &hg.g; }
     bool grow(Engine&) override { return hg.grow_if_full(); }
+    void set_buffer_scale(float s) override { hg.set_buffer_scale(s); }
     std::vector<float> value_by_name(Engine& e, const std::string& w) override {
         if (w == "count_edges_by_type") return hg.count_edges_by_type();
+        if (w == "cache_rebuilds") return hg.rebuild_count();
         return GNode::value_by_name(e, w);
     }
 };
@@ -1689,6 +1709,7 @@ struct BackbonePairsNode : GNode {
     }
     DGraph* graph() override { return &hg.g; }
     bool grow(Engine&) override { return hg.grow_if_full(); }
+    void set_buffer_scale(float s) override { hg.set_buffer_scale(s); }
 };
 
 // ============================================================ rotamer ===
@@ -1940,6 +1961,12 @@ struct RotamerNode : GNode {
         UG_CK(cudaMemset(b.prev_valid, 0, sizeof(int) * 2 * size_t(e.n_sys)));
         return true;
     }
+    void set_buffer_scale(float s) override { hg.set_buffer_scale(s); }
+    bool set_bp_variant(int v) override {
+        if (v < 0 || v >= bp_variant_count()) throw Error("no BP launch variant " + std::to_string(v));
+        b.variant = v;
+        return true;
+    }
     bool set_kernel_timer(cudaEvent_t* ev, int* used, int cap) override {
         b.kt_ev = ev;
         b.kt_used = used;
@@ -1971,6 +1998,7 @@ struct RotamerNode : GNode {
     }
     std::vector<float> value_by_name(Engine& e, const std::string& w) override {
         if (w == "count_edges_by_type") return hg.count_edges_by_type();
+        if (w == "cache_rebuilds") return hg.rebuild_count();
         if (w == "n_node") return {float(n_res_sys.at(0))};
         // warm-start training data and state, in BP node order (systems concatenated)
         if (w == "bp_n_node") return {float(b.n_res)};
@@ -2310,6 +2338,92 @@ void Engine::capture(float dt, float timescale, int rounds) {
     graph_timed = false;
 }
 void Engine::launch_graph() { UG_CK(cudaGraphLaunch(graph_exec, st)); }
+
+void Engine::set_tuning(float buffer_scale, int bp_variant) {
+    if (!(buffer_scale >= 1.f)) throw Error("the cache buffer scale must be at least 1");
+    if (bp_variant < 0 || bp_variant >= bp_variant_count()) throw Error("no BP launch variant " + std::to_string(bp_variant));
+    sync();
+    for (auto& n : nodes) {
+        n->set_buffer_scale(buffer_scale);
+        n->set_bp_variant(bp_variant);
+    }
+    tuned_buffer_scale = buffer_scale;
+    tuned_bp_variant = bp_variant;
+    drop_graph();
+}
+
+std::vector<std::pair<std::string, float>> Engine::autotune(int n_round, float dt, float timescale) {
+    std::vector<std::pair<std::string, float>> report;
+    if (n_round < 1) throw Error("autotune needs at least one timed round");
+    // the state every candidate starts from
+    size_t n3 = 3 * size_t(atom_total);
+    std::vector<float> pos0(n3), mom0(n3);
+    std::vector<unsigned long long> round0(static_cast<size_t>(n_sys));
+    sync();
+    UG_CK(cudaMemcpy(pos0.data(), d_pos, 4 * n3, cudaMemcpyDeviceToHost));
+    UG_CK(cudaMemcpy(mom0.data(), d_mom, 4 * n3, cudaMemcpyDeviceToHost));
+    UG_CK(cudaMemcpy(round0.data(), d_round, 8 * round0.size(), cudaMemcpyDeviceToHost));
+    auto restore = [&]() {
+        UG_CK(cudaMemcpy(d_pos, pos0.data(), 4 * n3, cudaMemcpyHostToDevice));
+        UG_CK(cudaMemcpy(d_mom, mom0.data(), 4 * n3, cudaMemcpyHostToDevice));
+        UG_CK(cudaMemcpy(d_round, round0.data(), 8 * round0.size(), cudaMemcpyHostToDevice));
+    };
+    auto apply = [&](float scale, int variant) {
+        for (auto& n : nodes) {
+            n->set_buffer_scale(scale);
+            n->set_bp_variant(variant);
+        }
+    };
+    cudaEvent_t ev[2];
+    UG_CK(cudaEventCreate(&ev[0]));
+    UG_CK(cudaEventCreate(&ev[1]));
+    auto trial = [&](float scale, int variant) -> float {
+        restore();
+        apply(scale, variant);
+        drop_graph();
+        capture(dt, timescale, 1);
+        for (int r = 0; r < 2; ++r) launch_graph();  // caches rebuilt, clocks up
+        UG_CK(cudaEventRecord(ev[0], st));
+        for (int r = 0; r < n_round; ++r) launch_graph();
+        UG_CK(cudaEventRecord(ev[1], st));
+        UG_CK(cudaStreamSynchronize(st));
+        float ms = 0.f;
+        UG_CK(cudaEventElapsedTime(&ms, ev[0], ev[1]));
+        if (status(true) & (ST_EDGE_OVERFLOW | ST_RES_EDGE_OVERFLOW)) {
+            for (auto& n : nodes) n->grow(*this);  // storage grew: this trial does not count
+            return 1e30f;
+        }
+        return ms / float(n_round);
+    };
+    bool has_bp = false;
+    for (auto& n : nodes) has_bp |= n->set_bp_variant(tuned_bp_variant);
+    float best_scale = 1.f, best_ms = 1e30f;
+    for (float scale : {1.f, 1.5f, 2.f, 3.f}) {
+        float ms = trial(scale, tuned_bp_variant);
+        report.emplace_back("cache_buffer_scale=" + std::to_string(scale).substr(0, 4), ms);
+        if (ms < best_ms) { best_ms = ms; best_scale = scale; }
+    }
+    int best_variant = tuned_bp_variant;
+    if (has_bp) {
+        for (int v = 0; v < bp_variant_count(); ++v) {
+            int c, l, t;
+            bp_variant_desc(v, &c, &l, &t);
+            float ms = v == tuned_bp_variant ? best_ms : trial(best_scale, v);
+            report.emplace_back("bp_blocks_per_system=" + std::to_string(c) + ",lanes_per_node=" + std::to_string(l) +
+                                    ",threads=" + std::to_string(t),
+                                ms);
+            if (ms < best_ms) { best_ms = ms; best_variant = v; }
+        }
+    }
+    cudaEventDestroy(ev[0]);
+    cudaEventDestroy(ev[1]);
+    restore();
+    apply(best_scale, best_variant);
+    drop_graph();
+    tuned_buffer_scale = best_scale;
+    tuned_bp_variant = best_variant;
+    return report;
+}
 
 void Engine::drop_graph() {
     UG_CK(cudaStreamSynchronize(st));

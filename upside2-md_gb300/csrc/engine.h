@@ -63,6 +63,10 @@ struct GNode {
     // messages and marginals; returns false
     // for nodes without one
     virtual bool set_warm(Engine&, const float* const*, int) { return false; }
+    // tuning knobs: candidate-cache buffer scale (pair-list nodes) and the BP
+    // solve's launch variant (rotamer node; false elsewhere)
+    virtual void set_buffer_scale(float) {}
+    virtual bool set_bp_variant(int) { return false; }
     virtual double kernel_bytes(Engine&) { return 0.0; }
 };
 
@@ -120,6 +124,16 @@ public:
     void capture(float dt, float timescale, int rounds_per_graph);
     // forget the captured graph (its kernels hold parameters that changed)
     void drop_graph();
+
+    // Autotuner: times n_round integration rounds (one-round graph, CUDA
+    // events) from the same saved state for each candidate setting and keeps
+    // the fastest: first the candidate-cache buffer scale, then the BP launch
+    // variant.  Returns (setting, ms per round) for every candidate tried.
+    std::vector<std::pair<std::string, float>> autotune(int n_round, float dt, float timescale);
+    // set the tuned quantities by hand
+    void set_tuning(float buffer_scale, int bp_variant);
+    float tuned_buffer_scale = 1.f;
+    int tuned_bp_variant = 0;
     void launch_graph();
     cudaGraphExec_t graph_exec = nullptr;
     cudaGraph_t graph = nullptr;

@@ -21,9 +21,6 @@ namespace ug {
 
 namespace cg = cooperative_groups;
 
-// blocks (SMs) per system in the BP solve
-constexpr int BP_CLUSTER = 2;
-
 // ---------------------------------------------------------------- scan ---
 // Exclusive scan of n ints into out[0..n] (out[n] = total) by one 1024-thread
 // block: each thread owns a contiguous chunk, then a block-level scan of the
@@ -216,6 +213,7 @@ __global__ void cache_check_kernel(DGraph g) {
 __global__ void cache_commit_kernel(DGraph g) {
     for (int s = grid_stride_start(); s < g.n_sys; s += grid_stride()) {
         if (!g.sys_flag[s]) continue;
+        atomicAdd(g.rebuilds, 1ull);
         int cnt = g.row_off[g.sys_first_row[s + 1]] - g.row_off[g.sys_first_row[s]];
         int cap = g.cache_off[s + 1] - g.cache_off[s];
         g.sys_over[s] = cnt > cap;
@@ -805,7 +803,7 @@ __device__ __forceinline__ void bp_messages(const DBP& b, int e0, int e1, const 
 // every BP_LANES-th incoming message, then the partial products are combined
 // across the group with shuffles, so a node's latency chain is its degree /
 // BP_LANES loads.
-constexpr int BP_LANES = 8;
+template <int BP_LANES>
 __device__ __forceinline__ float bp_beliefs(const DBP& b, int r0, int lo, int hi, int e1, const float* __restrict__ Nold,
                                             float* __restrict__ Ncur, const int* __restrict__ s_nrot,
                                             const float* __restrict__ Ecur, int mode, float damp, int tid,
@@ -878,7 +876,11 @@ __device__ __forceinline__ float bp_beliefs(const DBP& b, int r0, int lo, int hi
 // through global memory: a block writes the reverse entries of its rows, and
 // the cluster barrier between the phases (release/acquire at cluster scope)
 // makes them visible to their owners.  Beliefs never leave their block.
-__global__ void __launch_bounds__(1024) bp_solve_kernel(DBP b, int want_energy, double* energy_out) {
+// Template: BP_CLUSTER blocks (SMs) per system, BP_LANES lanes per node in
+// the belief phase, THREADS threads per block; the variants are listed in
+// bp_variants (the engine's autotuner picks one).
+template <int BP_CLUSTER, int BP_LANES, int THREADS>
+__global__ void __launch_bounds__(THREADS) bp_solve_kernel(DBP b, int want_energy, double* energy_out) {
     extern __shared__ float smem[];
     __shared__ float red[32];
     __shared__ double dred[32];
@@ -913,7 +915,7 @@ __global__ void __launch_bounds__(1024) bp_solve_kernel(DBP b, int want_energy, 
     auto sweep = [&](const float* Nold, float* Ncur, const float* Eold, float* Ecur, int mode, float damp) {
         bp_messages(b, eo0, eo1, Nold, s_nrot, Eold, Ecur, tid, nt);
         cluster.sync();
-        return bp_beliefs(b, r0, lo, hi, e1, Nold, Ncur, s_nrot, Ecur, mode, damp, tid, nt);
+        return bp_beliefs<BP_LANES>(b, r0, lo, hi, e1, Nold, Ncur, s_nrot, Ecur, mode, damp, tid, nt);
     };
     auto block_max = [&](float v) -> float {
 #pragma unroll
@@ -1162,6 +1164,31 @@ __global__ void __launch_bounds__(1024) bp_solve_kernel(DBP b, int want_energy, 
     }
 }
 
+// the solve's launch variants: blocks per system, lanes per node, threads
+// per block (a cluster of 4 uses 512-thread blocks so two fit on one SM)
+struct BpVariant {
+    const void* fn;
+    int cluster, lanes, threads;
+};
+static const BpVariant* bp_variants() {
+    static const BpVariant v[] = {
+        {reinterpret_cast<const void*>(bp_solve_kernel<2, 8, 1024>), 2, 8, 1024},
+        {reinterpret_cast<const void*>(bp_solve_kernel<2, 4, 1024>), 2, 4, 1024},
+        {reinterpret_cast<const void*>(bp_solve_kernel<2, 16, 1024>), 2, 16, 1024},
+        {reinterpret_cast<const void*>(bp_solve_kernel<1, 8, 1024>), 1, 8, 1024},
+        {reinterpret_cast<const void*>(bp_solve_kernel<4, 8, 512>), 4, 8, 512},
+        {reinterpret_cast<const void*>(bp_solve_kernel<4, 4, 512>), 4, 4, 512},
+    };
+    return v;
+}
+int bp_variant_count() { return 6; }
+void bp_variant_desc(int i, int* cluster, int* lanes, int* threads) {
+    const BpVariant& v = bp_variants()[i];
+    *cluster = v.cluster;
+    *lanes = v.lanes;
+    *threads = v.threads;
+}
+
 // bead-edge sensitivities from the marginals and 1-body sensitivities
 // (src/rotamer.cpp:1057-1086)
 __global__ void bp_sens_kernel(DBP b, DGraph g, float* s0, float* s1, float* s2, float* s3, int n_in, int w0,
@@ -1211,11 +1238,8 @@ void launch_bp(DBP& b, const DGraph& g, const float* const* in, float* const* in
     bp_prob_kernel<<<blocks, 256, 0, st>>>(b);
     if (warm) launch_warm_start(*warm, pos, atom_off, b.res_off, b.prob, b.nrot, b.n_sys, b.n_res, st);
     size_t smem = bp_solve_smem_bytes(b.max_res_sys);
-    static size_t configured = 0;
-    if (smem > 48 * 1024 && smem > configured) {
-        cudaFuncSetAttribute(bp_solve_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-        configured = smem;
-    }
+    const BpVariant& v = bp_variants()[b.variant];
+    if (smem > 48 * 1024) cudaFuncSetAttribute(v.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
     // external records: under stream capture they become event-record nodes
     // that every replay of the graph re-records (a plain record would only
     // order the capture)
@@ -1223,18 +1247,19 @@ void launch_bp(DBP& b, const DGraph& g, const float* const* in, float* const* in
     if (timed) cudaEventRecordWithFlags(b.kt_ev[(*b.kt_used)++], st, cudaEventRecordExternal);
     {
         cudaLaunchConfig_t cfg = {};
-        cfg.gridDim = dim3(unsigned(b.n_sys) * BP_CLUSTER);
-        cfg.blockDim = dim3(1024);
+        cfg.gridDim = dim3(unsigned(b.n_sys) * unsigned(v.cluster));
+        cfg.blockDim = dim3(unsigned(v.threads));
         cfg.dynamicSmemBytes = smem;
         cfg.stream = st;
         cudaLaunchAttribute at[1];
         at[0].id = cudaLaunchAttributeClusterDimension;
-        at[0].val.clusterDim.x = BP_CLUSTER;
+        at[0].val.clusterDim.x = unsigned(v.cluster);
         at[0].val.clusterDim.y = 1;
         at[0].val.clusterDim.z = 1;
         cfg.attrs = at;
         cfg.numAttrs = 1;
-        cudaLaunchKernelEx(&cfg, bp_solve_kernel, b, want_energy, energy_out);
+        void* args[] = {&b, &want_energy, &energy_out};
+        cudaLaunchKernelExC(&cfg, v.fn, args);
     }
     if (timed) cudaEventRecordWithFlags(b.kt_ev[(*b.kt_used)++], st, cudaEventRecordExternal);
     bp_sens_kernel<<<blocks, 256, 0, st>>>(b, g, in_sens[0], in_sens[1], in_sens[2], in_sens[3], n_in, w[0], w[1],

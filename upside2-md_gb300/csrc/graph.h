@@ -77,6 +77,7 @@ struct DGraph {
     int max_tiles;              // refine tiles if every segment were full
     int* tile_count;            // max_tiles + 1
     int* tile_off;              // max_tiles + 1
+    unsigned long long* rebuilds;  // running count of system cache rebuilds
 };
 
 // candidates per refine tile (one 256-thread block, 4 per thread)
@@ -115,6 +116,7 @@ struct DBP {
     float damping, tol;
     int max_iter, chunk;
     int max_res_sys;            // largest residue count of one system (shared-memory sizing)
+    int variant;                // launch variant of the solve (bp_variant_desc)
     // bead level
     int n_bead;
     const int* bead_res;        // bead -> residue (global)
@@ -148,6 +150,10 @@ struct DBP {
 // dynamic shared memory of the BP solve for a system of n residues: both
 // belief buffers (8 floats per node each) and the rotamer counts
 inline size_t bp_solve_smem_bytes(int n) { return size_t(n) * (2 * 8 * sizeof(float) + sizeof(int)); }
+
+// launch variants of the BP solve: blocks per system, lanes per node, threads per block
+int bp_variant_count();
+void bp_variant_desc(int i, int* cluster, int* lanes, int* threads);
 
 // --------------------------------------------------------------- launchers --
 void launch_scan(const int* in, int* out, int n, int* total_out, cudaStream_t st);

@@ -61,6 +61,8 @@ def lib():
         L.ug_bench.argtypes = [vp, ip, ctypes.c_float, ctypes.c_float, ip, ip, vp]
         L.ug_set_device.argtypes = [ip]
         L.ug_bench_kernel.argtypes = [vp, vp]
+        L.ug_autotune.argtypes = [vp, ip, ctypes.c_float, ctypes.c_float, ctypes.c_char_p, ip]
+        L.ug_set_tuning.argtypes = [vp, ctypes.c_float, ip]
         for nm in ["ug_set_param", "ug_get_param", "ug_param_deriv"]:
             getattr(L, nm).argtypes = [vp, cp, vp, ip]
         i64, f = ctypes.c_int64, ctypes.c_float
@@ -322,6 +324,25 @@ class Batch:
         self._chk(lib().ug_bench(self.h, int(n_round), float(dt), float(timescale), int(flush_l2), int(e2e),
                                  ms.ctypes.data))
         return ms
+
+    def autotune(self, n_round=5, dt=0.009, timescale=5.0):
+        """Tune cache buffer and BP launch variant from the current state;
+        returns ({setting: ms per round}, chosen setting)."""
+        buf = ctypes.create_string_buffer(1 << 14)
+        n = lib().ug_autotune(self.h, int(n_round), float(dt), float(timescale), buf, 1 << 14)
+        if n < 0:
+            raise RuntimeError(lib().ug_last_error().decode())
+        trials, chosen = {}, None
+        for line in buf.value.decode().splitlines():
+            k, v = line.split("\t")
+            if k == "chosen":
+                chosen = v
+            else:
+                trials[k] = float(v)
+        return trials, chosen
+
+    def set_tuning(self, cache_buffer_scale=1.0, bp_variant=0):
+        self._chk(lib().ug_set_tuning(self.h, float(cache_buffer_scale), int(bp_variant)))
 
     def bench_kernel(self):
         """The BP solve kernel over the last bench(): summed device ms, launches,
