@@ -40,6 +40,7 @@ def parse():
     ap.add_argument("--bp-start", default="learned", choices=["uniform", "learned", "previous", "reuse"],
                     help="BP initial state of the batched run")
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--tuning", default="", help="SCALE,VARIANT: set the tuned quantities instead of tuning")
     ap.add_argument("--equilibrate", type=int, default=300,
                     help="untimed integration rounds from the initial coils before the warm-up")
     ap.add_argument("--profile", action="store_true", help="print per-node device times to stderr")
@@ -220,7 +221,11 @@ def main():
     if a.equilibrate:
         b.run(a.equilibrate, use_graph=True, graph_rounds=10)
     tuned = None
-    if not a.no_autotune:  # untimed; the state is restored after the trials
+    if a.tuning:  # fixed setting (profiling runs)
+        scale, variant = a.tuning.split(",")
+        b.set_tuning(float(scale), int(variant))
+        tuned = {"chosen": "cache_buffer_scale=%s,bp_variant=%s (given)" % (scale, variant)}
+    elif not a.no_autotune:  # untimed; the state is restored after the trials
         trials, chosen = b.autotune(5)
         tuned = {"chosen": chosen, "trial_ms_per_round": trials}
     pos_eq, mom_eq = b.get_pos(), b.get_mom()

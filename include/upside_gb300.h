@@ -95,7 +95,7 @@ int ug_bench_kernel(UgBatch* b, double* stats);
 /* Autotuner (no counterpart in the reference): from the batch's current
  * state, times n_round integration rounds for each candidate setting and
  * keeps the fastest; the state is restored after every trial and at the end.
- * Tuned: the candidate-cache buffer of the pair lists (1, 1.5, 2, 3 times the
+ * Tuned: the candidate-cache buffer of the pair lists (1, 2, 3, 4, 6 times the
  * reference's 1 + 0.2 cutoff; results do not depend on it), then the BP
  * solve's blocks per system, lanes per node and threads per block.  report
  * receives '\n'-separated "setting\tms_per_round" lines and a final

@@ -40,7 +40,7 @@ def test_autotune_restores_state_and_reports(syn_configs):
     b.run(10, use_graph=True, graph_rounds=5)
     x, m = b.get_pos(), b.get_mom()
     trials, chosen = b.autotune(2)
-    assert len(trials) == 4 + 6 and chosen
+    assert len(trials) == 5 + 6 and chosen
     assert all(v > 0 for v in trials.values())
     assert np.array_equal(b.get_pos(), x) and np.array_equal(b.get_mom(), m)
     b.run(2, use_graph=True, graph_rounds=1)

@@ -296,18 +296,7 @@ int ug_set_round(UgBatch* b, const uint64_t* round) {
 
 int ug_run(UgBatch* b, int n_round, float dt, float timescale, int use_graph, int graph_rounds) {
     GUARD_BEGIN
-    Engine& e = *b->e;
-    if (!use_graph) {
-        for (int r = 0; r < n_round; ++r) e.round(dt, timescale, true);
-        e.sync();
-        return 0;
-    }
-    if (graph_rounds < 1) graph_rounds = 1;
-    if (!e.graph_exec || e.graph_rounds != graph_rounds) e.capture(dt, timescale, graph_rounds);
-    int full = n_round / graph_rounds;
-    for (int k = 0; k < full; ++k) e.launch_graph();
-    for (int r = full * graph_rounds; r < n_round; ++r) e.round(dt, timescale, true);
-    e.sync();
+    b->e->run_rounds(n_round, dt, timescale, use_graph != 0, graph_rounds);
     return 0;
     GUARD_END(1)
 }

@@ -1042,6 +1042,7 @@ struct HGraph {
         g.active_off = e.alloc<int>(size_t(e.n_sys) + 1);
         g.cache_force = e.alloc<int>(1);
         g.rebuilds = e.alloc<unsigned long long>(1);
+        g.any_flag = e.alloc<int>(1);
         for (size_t s = 0; s < grp.size(); ++s) {
             long long fs = sym ? (long long)c1[s] * (c1[s] - 1) / 2 : (long long)c1[s] * c2[s];
             long long want = std::min<long long>(std::max<long long>(fs, 1), 2LL * cap_per_elem * c1[s]);
@@ -2251,8 +2252,12 @@ Engine::~Engine() {
     if (graph_exec) cudaGraphExecDestroy(graph_exec);
     if (graph) cudaGraphDestroy(graph);
     for (auto& x : kt_ev) cudaEventDestroy(x);
+    for (auto* v : {&ev_fwd, &ev_bwd, &ev_lane})
+        for (auto& x : *v) cudaEventDestroy(x);
+    for (size_t l = 1; l < lanes.size(); ++l) cudaStreamDestroy(lanes[l]);
     nodes.clear();
     free_all();
+    if (!lanes.empty()) st = lanes[0];
     if (st) cudaStreamDestroy(st);
 }
 
@@ -2262,11 +2267,85 @@ GNode& Engine::node(const std::string& name) {
     return *nodes[size_t(it->second)];
 }
 
+// Lanes for the node DAG: every node is launched on one of kLanes streams.
+// A node continues the lane of an argument that was the last node placed on
+// it (a chain stays on one stream); otherwise it opens the least-used lane.
+// Forward of a node waits for its arguments' forwards; backward of a node
+// waits for its consumers' backwards (which follow their forwards).  All
+// sensitivity writes across nodes are atomic additions, so nodes on
+// different lanes may overlap.  Under stream capture the waits become graph
+// edges, so independent chains run as concurrent graph branches.
+void Engine::setup_lanes() {
+    const int kLanes = 4;
+    lanes.assign(kLanes, nullptr);
+    lanes[0] = st;
+    for (int l = 1; l < kLanes; ++l) UG_CK(cudaStreamCreateWithFlags(&lanes[size_t(l)], cudaStreamNonBlocking));
+    size_t n = nodes.size();
+    node_lane.assign(n, 0);
+    consumers.assign(n, {});
+    ev_fwd.resize(n);
+    ev_bwd.resize(n);
+    for (size_t i = 0; i < n; ++i) {
+        UG_CK(cudaEventCreateWithFlags(&ev_fwd[i], cudaEventDisableTiming));
+        UG_CK(cudaEventCreateWithFlags(&ev_bwd[i], cudaEventDisableTiming));
+        for (int a : nodes[i]->args) consumers[size_t(a)].push_back(int(i));
+    }
+    ev_lane.resize(size_t(kLanes));
+    for (auto& x : ev_lane) UG_CK(cudaEventCreateWithFlags(&x, cudaEventDisableTiming));
+    std::vector<int> tail(size_t(kLanes), -1), load(size_t(kLanes), 0);
+    for (size_t i = 0; i < n; ++i) {
+        int lane = -1;
+        for (int a : nodes[i]->args)
+            for (int l = 0; l < kLanes && lane < 0; ++l)
+                if (tail[size_t(l)] == a) lane = l;
+        if (lane < 0) lane = int(std::min_element(load.begin(), load.end()) - load.begin());
+        node_lane[i] = lane;
+        tail[size_t(lane)] = int(i);
+        load[size_t(lane)] += 1;
+    }
+}
+
 void Engine::compute(bool energy) {
-    UG_CK(cudaMemsetAsync(d_sens_arena, 0, sens_arena_floats * sizeof(float), st));
-    if (energy) UG_CK(cudaMemsetAsync(d_pot, 0, sizeof(double) * size_t(std::max(1, n_pot_slots)) * n_sys, st));
-    for (auto& n : nodes) n->forward(*this, energy);
-    for (size_t i = nodes.size(); i-- > 0;) nodes[i]->backward(*this);
+    if (!parallel_nodes) {
+        UG_CK(cudaMemsetAsync(d_sens_arena, 0, sens_arena_floats * sizeof(float), st));
+        if (energy) UG_CK(cudaMemsetAsync(d_pot, 0, sizeof(double) * size_t(std::max(1, n_pot_slots)) * n_sys, st));
+        for (auto& n : nodes) n->forward(*this, energy);
+        for (size_t i = nodes.size(); i-- > 0;) nodes[i]->backward(*this);
+        if (energy) sum_energy_kernel<<<1, 256, 0, st>>>(n_sys, n_pot_slots, d_pot, d_energy);
+        UG_CK(cudaGetLastError());
+        return;
+    }
+    if (lanes.empty()) setup_lanes();
+    cudaStream_t main = lanes[0];
+    UG_CK(cudaMemsetAsync(d_sens_arena, 0, sens_arena_floats * sizeof(float), main));
+    if (energy) UG_CK(cudaMemsetAsync(d_pot, 0, sizeof(double) * size_t(std::max(1, n_pot_slots)) * n_sys, main));
+    UG_CK(cudaEventRecord(ev_lane[0], main));
+    for (size_t l = 1; l < lanes.size(); ++l) UG_CK(cudaStreamWaitEvent(lanes[l], ev_lane[0], 0));
+    size_t n = nodes.size();
+    try {
+        for (size_t i = 0; i < n; ++i) {
+            st = lanes[size_t(node_lane[i])];
+            for (int a : nodes[i]->args)
+                if (node_lane[size_t(a)] != node_lane[i]) UG_CK(cudaStreamWaitEvent(st, ev_fwd[size_t(a)], 0));
+            nodes[i]->forward(*this, energy);
+            UG_CK(cudaEventRecord(ev_fwd[i], st));
+        }
+        for (size_t i = n; i-- > 0;) {
+            st = lanes[size_t(node_lane[i])];
+            for (int c : consumers[i])
+                if (node_lane[size_t(c)] != node_lane[i]) UG_CK(cudaStreamWaitEvent(st, ev_bwd[size_t(c)], 0));
+            nodes[i]->backward(*this);
+            UG_CK(cudaEventRecord(ev_bwd[i], st));
+        }
+    } catch (...) {
+        st = main;
+        throw;
+    }
+    st = main;
+    for (size_t l = 1; l < lanes.size(); ++l) {
+        UG_CK(cudaEventRecord(ev_lane[l], lanes[l]));
+        UG_CK(cudaStreamWaitEvent(main, ev_lane[l], 0));
+    }
     if (energy) sum_energy_kernel<<<1, 256, 0, st>>>(n_sys, n_pot_slots, d_pot, d_energy);
     UG_CK(cudaGetLastError());
 }
@@ -2322,7 +2401,56 @@ int Engine::status(bool clear) {
     UG_CK(cudaMemcpyAsync(&s, d_status, sizeof(int), cudaMemcpyDeviceToHost, st));
     UG_CK(cudaStreamSynchronize(st));
     if (clear && s) UG_CK(cudaMemsetAsync(d_status, 0, sizeof(int), st));
+    s |= kept_status;
+    if (clear) kept_status = 0;
     return s;
+}
+
+// Integration rounds in chunks (one graph replay of graph_rounds rounds, or up
+// to 8 eager rounds).  Before a chunk the state (positions, momenta, round
+// counters) is copied aside; if a pair list or the BP entry storage
+// overflowed during it, the state is put back, the storage grown and the
+// chunk run again, so overflow never leaves truncated interactions behind.
+void Engine::run_rounds(int n_round, float dt, float timescale, bool use_graph, int graph_rounds) {
+    if (graph_rounds < 1) graph_rounds = 1;
+    size_t n3 = 3 * size_t(atom_total);
+    if (!snap_pos) {
+        snap_pos = alloc<float>(n3);
+        snap_mom = alloc<float>(n3);
+        snap_round = alloc<unsigned long long>(size_t(n_sys));
+    }
+    const int overflow = ST_EDGE_OVERFLOW | ST_RES_EDGE_OVERFLOW;
+    int done = 0, retries = 0;
+    while (done < n_round) {
+        int k = use_graph ? std::min(graph_rounds, n_round - done) : std::min(8, n_round - done);
+        UG_CK(cudaMemcpyAsync(snap_pos, d_pos, 4 * n3, cudaMemcpyDeviceToDevice, st));
+        UG_CK(cudaMemcpyAsync(snap_mom, d_mom, 4 * n3, cudaMemcpyDeviceToDevice, st));
+        UG_CK(cudaMemcpyAsync(snap_round, d_round, 8 * size_t(n_sys), cudaMemcpyDeviceToDevice, st));
+        if (use_graph && k == graph_rounds) {
+            if (!graph_exec || this->graph_rounds != graph_rounds || graph_dt != dt || graph_timescale != timescale ||
+                graph_timed)
+                capture(dt, timescale, graph_rounds);
+            launch_graph();
+        } else {
+            for (int r = 0; r < k; ++r) round(dt, timescale, true);
+        }
+        int s = 0;
+        UG_CK(cudaMemcpyAsync(&s, d_status, sizeof(int), cudaMemcpyDeviceToHost, st));
+        UG_CK(cudaStreamSynchronize(st));
+        if (s & overflow) {
+            if (++retries > 8) throw Error("pair-list storage kept overflowing");
+            UG_CK(cudaMemcpyAsync(d_pos, snap_pos, 4 * n3, cudaMemcpyDeviceToDevice, st));
+            UG_CK(cudaMemcpyAsync(d_mom, snap_mom, 4 * n3, cudaMemcpyDeviceToDevice, st));
+            UG_CK(cudaMemcpyAsync(d_round, snap_round, 8 * size_t(n_sys), cudaMemcpyDeviceToDevice, st));
+            UG_CK(cudaMemsetAsync(d_status, 0, sizeof(int), st));
+            sync();
+            for (auto& n : nodes) n->grow(*this);
+            drop_graph();
+            kept_status |= s & ~overflow;
+            continue;
+        }
+        done += k;
+    }
 }
 void Engine::sync() { UG_CK(cudaStreamSynchronize(st)); }
 
@@ -2336,6 +2464,8 @@ void Engine::capture(float dt, float timescale, int rounds) {
     UG_CK(cudaGraphInstantiate(&graph_exec, graph, 0));
     graph_rounds = rounds;
     graph_timed = false;
+    graph_dt = dt;
+    graph_timescale = timescale;
 }
 void Engine::launch_graph() { UG_CK(cudaGraphLaunch(graph_exec, st)); }
 
@@ -2398,7 +2528,7 @@ std::vector<std::pair<std::string, float>> Engine::autotune(int n_round, float d
     bool has_bp = false;
     for (auto& n : nodes) has_bp |= n->set_bp_variant(tuned_bp_variant);
     float best_scale = 1.f, best_ms = 1e30f;
-    for (float scale : {1.f, 1.5f, 2.f, 3.f}) {
+    for (float scale : {1.f, 2.f, 3.f, 4.f, 6.f}) {
         float ms = trial(scale, tuned_bp_variant);
         report.emplace_back("cache_buffer_scale=" + std::to_string(scale).substr(0, 4), ms);
         if (ms < best_ms) { best_ms = ms; best_scale = scale; }

@@ -125,6 +125,21 @@ public:
     // forget the captured graph (its kernels hold parameters that changed)
     void drop_graph();
 
+    // node DAG on several streams (see engine.cu); off: one stream
+    bool parallel_nodes = true;
+    std::vector<cudaStream_t> lanes;  // lanes[0] is st
+    std::vector<int> node_lane;
+    std::vector<std::vector<int>> consumers;
+    std::vector<cudaEvent_t> ev_fwd, ev_bwd, ev_lane;
+    void setup_lanes();
+    float graph_dt = 0.f, graph_timescale = 0.f;  // of the captured graph
+    // integration rounds with overflow recovery (see engine.cu)
+    void run_rounds(int n_round, float dt, float timescale, bool use_graph, int graph_rounds);
+    float* snap_pos = nullptr;
+    float* snap_mom = nullptr;
+    unsigned long long* snap_round = nullptr;
+    int kept_status = 0;  // status bits read (and cleared) by internal checks
+
     // Autotuner: times n_round integration rounds (one-round graph, CUDA
     // events) from the same saved state for each candidate setting and keeps
     // the fastest: first the candidate-cache buffer scale, then the BP launch

@@ -26,7 +26,8 @@ namespace cg = cooperative_groups;
 // block: each thread owns a contiguous chunk, then a block-level scan of the
 // chunk sums.
 __global__ void __launch_bounds__(1024) scan_kernel(const int* __restrict__ in, int* __restrict__ out, int n,
-                                                    int* total_out) {
+                                                    int* total_out, const int* __restrict__ skip_unless) {
+    if (skip_unless && !*skip_unless) return;
     __shared__ int warp_sums[32];
     int t = threadIdx.x;
     int per = (n + blockDim.x - 1) / blockDim.x;
@@ -68,8 +69,8 @@ __global__ void __launch_bounds__(1024) scan_kernel(const int* __restrict__ in, 
     }
 }
 
-void launch_scan(const int* in, int* out, int n, int* total_out, cudaStream_t st) {
-    scan_kernel<<<1, 1024, 0, st>>>(in, out, n, total_out);
+void launch_scan(const int* in, int* out, int n, int* total_out, cudaStream_t st, const int* skip_unless) {
+    scan_kernel<<<1, 1024, 0, st>>>(in, out, n, total_out, skip_unless);
 }
 
 // --------------------------------------------------------- pair search ---
@@ -101,6 +102,7 @@ __device__ __forceinline__ float pair_d2(float4 a, float4 b) {
 
 template <int PASS, bool CACHED>
 __global__ void pair_kernel(DGraph g) {
+    if (CACHED && !*g.any_flag) return;  // no system rebuilt in this evaluation
     int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     int lane = threadIdx.x & 31;
     int n_warps = (gridDim.x * blockDim.x) >> 5;
@@ -188,9 +190,19 @@ __global__ void cap_check_kernel(int* n_edge, int cap, int* status) {
 // A system's cache is rebuilt when any of its elements moved more than half
 // the buffer since its last rebuild, or when a rebuild of every system was
 // requested (src/interaction_graph.h:51-91: same bound, same comparison).
+// (one block)
 __global__ void cache_flag_init_kernel(DGraph g) {
+    __shared__ int any;
+    if (threadIdx.x == 0) any = 0;
+    __syncthreads();
     int f = *g.cache_force;
-    for (int s = grid_stride_start(); s < g.n_sys; s += grid_stride()) g.sys_flag[s] = f | g.sys_over[s];
+    for (int s = threadIdx.x; s < g.n_sys; s += blockDim.x) {
+        int x = f | g.sys_over[s];
+        g.sys_flag[s] = x;
+        if (x) any = 1;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) *g.any_flag = any;
 }
 
 __global__ void cache_check_kernel(DGraph g) {
@@ -204,13 +216,17 @@ __global__ void cache_check_kernel(DGraph g) {
         float4 x = first ? g.x1[k] : g.x2[k];
         float4 c = first ? g.xc1[k] : g.xc2[k];
         float dx = x.x - c.x, dy = x.y - c.y, dz = x.z - c.z;
-        if (lim < dx * dx + dy * dy + dz * dz) g.sys_flag[sys] = 1;
+        if (lim < dx * dx + dy * dy + dz * dz) {
+            g.sys_flag[sys] = 1;
+            *g.any_flag = 1;
+        }
     }
 }
 
 // after the rebuild search: per system candidate counts (capped by the
 // segment, overflow flagged), and the refine pass's tile prefix over systems
 __global__ void cache_commit_kernel(DGraph g) {
+    if (!*g.any_flag) return;
     for (int s = grid_stride_start(); s < g.n_sys; s += grid_stride()) {
         if (!g.sys_flag[s]) continue;
         atomicAdd(g.rebuilds, 1ull);
@@ -229,6 +245,7 @@ __global__ void cache_commit_kernel(DGraph g) {
 // first thread also clears the rebuild-everything request and recomputes the
 // per-system prefix of active refine tiles
 __global__ void cache_positions_kernel(DGraph g) {
+    if (!*g.any_flag) return;  // nothing rebuilt: positions, tiles and request unchanged
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         *g.cache_force = 0;
         int t = 0;
@@ -334,7 +351,7 @@ void launch_pairs(const DGraph& g, cudaStream_t st) {
     cache_flag_init_kernel<<<1, 256, 0, st>>>(g);
     cache_check_kernel<<<eb, 256, 0, st>>>(g);
     pair_kernel<0, true><<<blocks, 256, 0, st>>>(g);
-    launch_scan(g.row_count, g.row_off, g.n_rows, nullptr, st);
+    launch_scan(g.row_count, g.row_off, g.n_rows, nullptr, st, g.any_flag);
     pair_kernel<1, true><<<blocks, 256, 0, st>>>(g);
     cache_commit_kernel<<<1, 256, 0, st>>>(g);
     cache_positions_kernel<<<eb, 256, 0, st>>>(g);
@@ -725,11 +742,24 @@ __global__ void bp_prob_kernel(DBP b) {
             b.prob[r * 8 + k] = k < n ? expf(m - b.E1[r * 8 + k]) * expf(-b.E1x[r * 8 + k]) : 0.f;
         b.eoff[r] = m;
     }
-    int n_ent = *b.n_ent;
-    for (int i = grid_stride_start(); i < n_ent * 36; i += grid_stride()) {
-        int e = i / 36, k = i - e * 36;
-        int a = k / 6, c = k - a * 6;
-        b.P[i] = (a < b.nrot[b.erow[e]] && c < b.nrot[b.col[e]]) ? expf(-b.esum[i]) : 0.f;
+    // one thread per entry: its 6x6 block as nine float4, zero outside the
+    // (row rotamers) x (column rotamers) corner
+    int n_ent = min(*b.n_ent, b.ent_cap);
+    for (int e = grid_stride_start(); e < n_ent; e += grid_stride()) {
+        int nu = b.nrot[b.erow[e]], nv = b.nrot[b.col[e]];
+        const float4* src = reinterpret_cast<const float4*>(b.esum + size_t(e) * 36);
+        float4* dst = reinterpret_cast<float4*>(b.P + size_t(e) * 36);
+#pragma unroll
+        for (int q = 0; q < 9; ++q) {
+            float4 x = src[q];
+            float v[4] = {x.x, x.y, x.z, x.w};
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                int k = 4 * q + j, a = k / 6, c = k - a * 6;
+                v[j] = (a < nu && c < nv) ? expf(-v[j]) : 0.f;
+            }
+            dst[q] = make_float4(v[0], v[1], v[2], v[3]);
+        }
     }
 }
 

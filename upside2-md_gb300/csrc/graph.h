@@ -78,6 +78,7 @@ struct DGraph {
     int* tile_count;            // max_tiles + 1
     int* tile_off;              // max_tiles + 1
     unsigned long long* rebuilds;  // running count of system cache rebuilds
+    int* any_flag;              // device scalar: some system is rebuilt in this evaluation
 };
 
 // candidates per refine tile (one 256-thread block, 4 per thread)
@@ -156,7 +157,8 @@ int bp_variant_count();
 void bp_variant_desc(int i, int* cluster, int* lanes, int* threads);
 
 // --------------------------------------------------------------- launchers --
-void launch_scan(const int* in, int* out, int n, int* total_out, cudaStream_t st);
+// skip_unless: optional device flag; the scan does nothing when it reads 0
+void launch_scan(const int* in, int* out, int n, int* total_out, cudaStream_t st, const int* skip_unless = nullptr);
 void launch_pack_positions(const DGraph& g, cudaStream_t st);
 void launch_pairs(const DGraph& g, cudaStream_t st);
 void launch_edge_eval(const DGraph& g, int* sys_start, int* sys_end, cudaStream_t st);

@@ -293,7 +293,13 @@ __global__ void warm_features_kernel(WarmDev w, const float* __restrict__ pos, c
     }
     __syncthreads();
     const int u0 = res_off[s], u1 = res_off[s + 1];
-    for (int u = u0 + threadIdx.x; u < u1; u += blockDim.x) {
+    // the system's nodes are spread over gridDim.y blocks
+    for (int u = u0 + blockIdx.y * blockDim.x + threadIdx.x; u < u1; u += blockDim.x * gridDim.y) {
+        if (nrot[u] == 1) {  // a single rotamer needs no prediction
+            uint16_t* x = w.X + size_t(u) * WARM_IN;
+            for (int k = 0; k < WARM_IN; ++k) x[k] = 0;
+            continue;
+        }
         float f[WARM_IN];
 #pragma unroll
         for (int k = 0; k < WARM_IN; ++k) f[k] = 0.f;
@@ -388,7 +394,7 @@ void launch_warm_features(const WarmDev& w, const float* pos, const int* atom_of
         cudaFuncSetAttribute(warm_features_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
         configured = smem;
     }
-    warm_features_kernel<<<n_sys, 256, smem, st>>>(w, pos, atom_off, res_off, prob, nrot);
+    warm_features_kernel<<<dim3(unsigned(n_sys), 4), 128, smem, st>>>(w, pos, atom_off, res_off, prob, nrot);
 }
 
 // need = 1 when some system's coming solve starts from the prediction (the
