@@ -222,9 +222,10 @@ def main():
         b.run(a.equilibrate, use_graph=True, graph_rounds=10)
     tuned = None
     if a.tuning:  # fixed setting (profiling runs)
-        scale, variant = a.tuning.split(",")
-        b.set_tuning(float(scale), int(variant))
-        tuned = {"chosen": "cache_buffer_scale=%s,bp_variant=%s (given)" % (scale, variant)}
+        parts = a.tuning.split(",")
+        streams = int(parts[2]) if len(parts) > 2 else 4
+        b.set_tuning(float(parts[0]), int(parts[1]), streams)
+        tuned = {"chosen": "cache_buffer_scale=%s,bp_variant=%s,node_streams=%d (given)" % (parts[0], parts[1], streams)}
     elif not a.no_autotune:  # untimed; the state is restored after the trials
         trials, chosen = b.autotune(5)
         tuned = {"chosen": chosen, "trial_ms_per_round": trials}

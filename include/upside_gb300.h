@@ -97,14 +97,16 @@ int ug_bench_kernel(UgBatch* b, double* stats);
  * keeps the fastest; the state is restored after every trial and at the end.
  * Tuned: the candidate-cache buffer of the pair lists (1, 2, 3, 4, 6 times the
  * reference's 1 + 0.2 cutoff; results do not depend on it), then the BP
- * solve's blocks per system, lanes per node and threads per block.  report
+ * solve's blocks per system, lanes per node and threads per block, then the
+ * number of streams the node graph is spread over (1, 2, 4, 8).  report
  * receives '\n'-separated "setting\tms_per_round" lines and a final
  * "chosen\tsetting" line.  Returns the number of candidates tried (or -1). */
 int ug_autotune(UgBatch* b, int n_round, float dt, float timescale, char* report, int cap);
-/* Set the tuned quantities directly: cache buffer scale (>= 1) and BP launch
+/* Set the tuned quantities directly: cache buffer scale (>= 1), BP launch
  * variant (0..5: blocks per system x lanes per node x threads = 2x8x1024,
- * 2x4x1024, 2x16x1024, 1x8x1024, 4x8x512, 4x4x512). */
-int ug_set_tuning(UgBatch* b, float cache_buffer_scale, int bp_variant);
+ * 2x4x1024, 2x16x1024, 1x8x1024, 4x8x512, 4x4x512) and the number of streams
+ * the node graph is spread over (1..16). */
+int ug_set_tuning(UgBatch* b, float cache_buffer_scale, int bp_variant, int node_streams);
 
 /* Per-node device time of n_eval eager force evaluations (CUDA events on the
  * engine stream): names '\n'-separated "<node>:fwd" / "<node>:bwd", ms[k] the

@@ -559,16 +559,21 @@ int ug_autotune(UgBatch* b, int n_round, float dt, float timescale, char* report
     ug::bp_variant_desc(b->e->tuned_bp_variant, &c, &l, &t);
     s += "chosen\tcache_buffer_scale=" + std::to_string(b->e->tuned_buffer_scale).substr(0, 4) +
          ",bp_blocks_per_system=" + std::to_string(c) + ",lanes_per_node=" + std::to_string(l) +
-         ",threads=" + std::to_string(t) + "\n";
+         ",threads=" + std::to_string(t) + ",node_streams=" + std::to_string(b->e->n_lanes) + "\n";
     if (int(s.size()) + 1 > cap) throw ug::Error("report buffer too small");
     memcpy(report, s.c_str(), s.size() + 1);
     return int(r.size());
     GUARD_END(-1)
 }
 
-int ug_set_tuning(UgBatch* b, float cache_buffer_scale, int bp_variant) {
+int ug_set_tuning(UgBatch* b, float cache_buffer_scale, int bp_variant, int node_streams) {
     GUARD_BEGIN
+    if (node_streams < 1 || node_streams > 16) throw ug::Error("node_streams must be 1..16");
     b->e->set_tuning(cache_buffer_scale, bp_variant);
+    if (node_streams != b->e->n_lanes) {
+        b->e->n_lanes = node_streams;
+        b->e->setup_lanes();
+    }
     return 0;
     GUARD_END(1)
 }

@@ -125,8 +125,9 @@ public:
     // forget the captured graph (its kernels hold parameters that changed)
     void drop_graph();
 
-    // node DAG on several streams (see engine.cu); off: one stream
+    // node DAG on n_lanes streams (see engine.cu); off: one stream
     bool parallel_nodes = true;
+    int n_lanes = 4;
     std::vector<cudaStream_t> lanes;  // lanes[0] is st
     std::vector<int> node_lane;
     std::vector<std::vector<int>> consumers;

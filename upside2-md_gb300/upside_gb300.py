@@ -62,7 +62,7 @@ def lib():
         L.ug_set_device.argtypes = [ip]
         L.ug_bench_kernel.argtypes = [vp, vp]
         L.ug_autotune.argtypes = [vp, ip, ctypes.c_float, ctypes.c_float, ctypes.c_char_p, ip]
-        L.ug_set_tuning.argtypes = [vp, ctypes.c_float, ip]
+        L.ug_set_tuning.argtypes = [vp, ctypes.c_float, ip, ip]
         for nm in ["ug_set_param", "ug_get_param", "ug_param_deriv"]:
             getattr(L, nm).argtypes = [vp, cp, vp, ip]
         i64, f = ctypes.c_int64, ctypes.c_float
@@ -341,8 +341,8 @@ class Batch:
                 trials[k] = float(v)
         return trials, chosen
 
-    def set_tuning(self, cache_buffer_scale=1.0, bp_variant=0):
-        self._chk(lib().ug_set_tuning(self.h, float(cache_buffer_scale), int(bp_variant)))
+    def set_tuning(self, cache_buffer_scale=1.0, bp_variant=0, node_streams=4):
+        self._chk(lib().ug_set_tuning(self.h, float(cache_buffer_scale), int(bp_variant), int(node_streams)))
 
     def bench_kernel(self):
         """The BP solve kernel over the last bench(): summed device ms, launches,
