@@ -165,12 +165,13 @@ class _Cfg:
 
 
 def write_config(path, seq, seed, chain_first_residue=(), pos=None, environment_potential_type=1,
-                 damping=0.4, chain_offsets=None, params=None):
+                 damping=0.4, chain_offsets=None, params=None, bp_tol=1e-3):
     """Write an ff_2.1 `.up` file for `seq` (list of 3-letter codes).
 
     chain_first_residue: residue indices (excluding 0) where new chains start.
     pos: optional (n_atom,3) initial coordinates; otherwise random_initial_config
       per chain, chains translated by `chain_offsets` (n_chains,3) if given.
+    bp_tol: the rotamer BP convergence tolerance (the recipe's 1e-3).
     """
     P = load_params(params)
     rng = np.random.RandomState(seed)
@@ -366,7 +367,7 @@ def write_config(path, seq, seed, chain_first_residue=(), pos=None, environment_
 
     # ---- rotamer BP node
     g = c.grp("rotamer", [sc_name, pl_name, "hbond_coverage", "hbond_coverage_hydrophobe"],
-              integrator_level=1, max_iter=1000, tol=1e-3, damping=damping, iteration_chunk_size=2)
+              integrator_level=1, max_iter=1000, tol=bp_tol, damping=damping, iteration_chunk_size=2)
     pg = g + "/pair_interaction"
     w.group(pg)
     if big:
