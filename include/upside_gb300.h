@@ -103,9 +103,9 @@ int ug_bench_kernel(UgBatch* b, double* stats);
  * "chosen\tsetting" line.  Returns the number of candidates tried (or -1). */
 int ug_autotune(UgBatch* b, int n_round, float dt, float timescale, char* report, int cap);
 /* Set the tuned quantities directly: cache buffer scale (>= 1), BP launch
- * variant (0..5: blocks per system x lanes per node x threads = 2x8x1024,
- * 2x4x1024, 2x16x1024, 1x8x1024, 4x8x512, 4x4x512) and the number of streams
- * the node graph is spread over (1..16). */
+ * variant (0..8: blocks per system x lanes per node x threads = 2x8x1024,
+ * 2x4x1024, 2x16x1024, 1x8x1024, 4x8x512, 4x4x512, 8x4x256, 8x8x256,
+ * 16x4x128) and the number of streams the node graph is spread over (1..16). */
 int ug_set_tuning(UgBatch* b, float cache_buffer_scale, int bp_variant, int node_streams);
 
 /* Per-node device time of n_eval eager force evaluations (CUDA events on the

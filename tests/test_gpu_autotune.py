@@ -25,7 +25,7 @@ def test_tuning_knobs_do_not_change_results(syn_configs):
     e0, f0 = b.evaluate()
     edges0 = {g: b.node_edges(g) for g in GRAPHS}
     for scale in (1.0, 2.0, 3.0):
-        for variant in range(6):
+        for variant in range(9):
             b.set_tuning(scale, variant, (1, 2, 4, 8)[variant % 4])
             b.set_pos(x)
             e, f = b.evaluate()
@@ -40,7 +40,7 @@ def test_autotune_restores_state_and_reports(syn_configs):
     b.run(10, use_graph=True, graph_rounds=5)
     x, m = b.get_pos(), b.get_mom()
     trials, chosen = b.autotune(2)
-    assert len(trials) == 5 + 6 + 4 and chosen
+    assert len(trials) == 5 + 9 + 4 and chosen
     assert all(v > 0 for v in trials.values())
     assert np.array_equal(b.get_pos(), x) and np.array_equal(b.get_mom(), m)
     b.run(2, use_graph=True, graph_rounds=1)

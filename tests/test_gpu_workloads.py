@@ -24,11 +24,13 @@ def _scale(path, eng):
 
 
 def _check_vs_oracle(path, x, bp_slack=False):
-    """GPU against both oracles.  Against FP64 the force bound is 1e-4 of
-    max |F|, or twice the FP32 oracle's own distance from FP64 when that is
-    larger: in a 2000-residue system an FP32 force component sums thousands
-    of terms, and no FP32 evaluation order gets closer than the FP32 oracle.
-    bp_slack: force bound 5e-4 (BP stopped at the recipe's tolerance)."""
+    """GPU against both oracles.  The force bound is 1e-4 of max |F|, or twice
+    the FP32 oracle's own distance from FP64 when that is larger: in a
+    2000-residue system an FP32 force component sums thousands of terms, no
+    FP32 evaluation order gets much closer to FP64 than the FP32 oracle, and
+    two FP32 orders (GPU and FP32 oracle) differ by up to the sum of their
+    distances from FP64.  bp_slack: 5e-4 in place of 1e-4 (BP stopped at the
+    recipe's tolerance)."""
     f_tol = 5e-4 if bp_slack else F_ORC
     import oracle_py
     import upside_gb300 as U
@@ -38,12 +40,13 @@ def _check_vs_oracle(path, x, bp_slack=False):
     e32, d32 = oracle_py.Oracle(path, x.shape[0]).evaluate(x)
     e64, d64 = oracle_py.Oracle(path, x.shape[0], fp64=True).evaluate(x)
     fmax = np.abs(d64).max()
-    assert abs(e - e32) < E_ORC * sc, (e, e32)
-    assert np.abs(d - d32).max() < f_tol * np.abs(d32).max(), np.abs(d - d32).max() / np.abs(d32).max()
-    assert abs(e - e64) < E_ORC * sc, (e, e64)
     fp32_gap = np.abs(d32 - d64).max() / fmax
+    bound = max(f_tol, 2 * fp32_gap)
+    assert abs(e - e32) < E_ORC * sc, (e, e32)
+    assert abs(e - e64) < E_ORC * sc, (e, e64)
+    assert np.abs(d - d32).max() / fmax < bound, (np.abs(d - d32).max() / fmax, fp32_gap)
     gpu_gap = np.abs(d - d64).max() / fmax
-    assert gpu_gap < max(f_tol, 2 * fp32_gap), (gpu_gap, fp32_gap)
+    assert gpu_gap < bound, (gpu_gap, fp32_gap)
 
 
 @pytest.mark.parametrize("name", ["C2", "C5"])
@@ -54,8 +57,13 @@ def test_workload_energy_forces_vs_oracle(built, name, tmp_path):
     tolerance tightened to 1e-7: at the recipe's 1e-3 two solves that iterate
     in different float orders may stop at marginals up to ~1e-3 apart on
     near-degenerate residues, and in the 2000-residue system that alone moves
-    some forces by ~2e-4 of max |F| (observed).  With the tight tolerance the
-    1e-4 bound holds; with the recipe's the bound is 5e-4."""
+    some forces by ~2e-4 of max |F| (observed).  The bound is 5e-4 at the
+    recipe's tolerance and 1e-4 (or the FP32 rule of _check_vs_oracle) at the
+    tight one.  FP32 cannot resolve 1e-7, so the GPU and FP32-oracle solves of
+    the tight copy run to the 1000-iteration cap while FP64 converges in
+    ~60 sweeps; on the 2000-residue frame the FP32 oracle then sits
+    1.2e-4..2.0e-4 of max |F| from FP64 and the GPU 0.5e-4..1.4e-4 from the
+    FP32 oracle (observed over independent trajectories)."""
     import config_gen
     import upside_gb300 as U
     import workloads

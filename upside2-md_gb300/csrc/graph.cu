@@ -1195,7 +1195,8 @@ __global__ void __launch_bounds__(THREADS) bp_solve_kernel(DBP b, int want_energ
 }
 
 // the solve's launch variants: blocks per system, lanes per node, threads
-// per block (a cluster of 4 uses 512-thread blocks so two fit on one SM)
+// per block (clusters of 4, 8 and 16 use smaller blocks so that several
+// systems' blocks share an SM)
 struct BpVariant {
     const void* fn;
     int cluster, lanes, threads;
@@ -1208,10 +1209,13 @@ static const BpVariant* bp_variants() {
         {reinterpret_cast<const void*>(bp_solve_kernel<1, 8, 1024>), 1, 8, 1024},
         {reinterpret_cast<const void*>(bp_solve_kernel<4, 8, 512>), 4, 8, 512},
         {reinterpret_cast<const void*>(bp_solve_kernel<4, 4, 512>), 4, 4, 512},
+        {reinterpret_cast<const void*>(bp_solve_kernel<8, 4, 256>), 8, 4, 256},
+        {reinterpret_cast<const void*>(bp_solve_kernel<8, 8, 256>), 8, 8, 256},
+        {reinterpret_cast<const void*>(bp_solve_kernel<16, 4, 128>), 16, 4, 128},
     };
     return v;
 }
-int bp_variant_count() { return 6; }
+int bp_variant_count() { return 9; }
 void bp_variant_desc(int i, int* cluster, int* lanes, int* threads) {
     const BpVariant& v = bp_variants()[i];
     *cluster = v.cluster;
@@ -1270,6 +1274,8 @@ void launch_bp(DBP& b, const DGraph& g, const float* const* in, float* const* in
     size_t smem = bp_solve_smem_bytes(b.max_res_sys);
     const BpVariant& v = bp_variants()[b.variant];
     if (smem > 48 * 1024) cudaFuncSetAttribute(v.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    // clusters above the portable 8 blocks have to be allowed per kernel
+    if (v.cluster > 8) cudaFuncSetAttribute(v.fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
     // external records: under stream capture they become event-record nodes
     // that every replay of the graph re-records (a plain record would only
     // order the capture)
