@@ -66,3 +66,58 @@ def test_missing_and_corrupt(built, tmp_path):
         return
     with pytest.raises(KeyError):
         f.read("/input/potential/rotamer/pair_interaction/interaction_param")
+
+
+def _walk(f, path="/"):
+    out = []
+    for k in f.list(path):
+        q = path.rstrip("/") + "/" + k
+        out.append(q)
+        if f.kind(q) == 1:
+            out += _walk(f, q)
+    return out
+
+
+def test_cpp_writer_copies_reference_config_exactly(built, tmp_path):
+    """The C++ writer the upside driver logs with rewrites the reference's own
+    PyTables-written config: every dataset and attribute byte for byte
+    (datasets come back contiguous and uncompressed), PyTables' empty TITLE
+    attributes (null dataspaces) included, and skipped paths left out."""
+    import h5lite
+    from h5lite import H5File
+    src = os.path.join(GOLDEN, "chig.up")
+    dst = str(tmp_path / "copy.up")
+    h5lite.copy_file(src, dst, ["/input/potential/rama_map_pot"])
+    a, b = H5File(src), H5File(dst)
+    pa, pb = _walk(a), _walk(b)
+    assert set(pa) - set(pb) == {"/input/potential/rama_map_pot"} | {
+        p for p in pa if p.startswith("/input/potential/rama_map_pot/")}
+    assert set(pb) <= set(pa)
+    n = 0
+    for q in pb + ["/"]:
+        if q != "/" and a.kind(q) == 0:
+            x, y = a.read(q), b.read(q)
+            assert x.dtype == y.dtype and x.shape == y.shape and x.tobytes() == y.tobytes(), q
+            n += 1
+        ax, bx = a.attrs(q), b.attrs(q)
+        assert set(ax) == set(bx), q
+        for k in ax:
+            if ax[k] is None:
+                assert bx[k] is None, (q, k)
+            else:
+                assert np.asarray(ax[k]).tobytes() == np.asarray(bx[k]).tobytes(), (q, k)
+    assert n > 100
+    # and a file the Python writer made, scalars and strings included
+    w = h5lite.H5Writer()
+    w.dataset("/s/f", np.float32(2.5))
+    w.dataset("/s/u", np.arange(5, dtype=np.uint16))
+    w.dataset("/s/names", np.array([b"ab", b"cde"]))
+    w.set_attr("/s", "k", np.array([1, 2, 3], np.int64))
+    p1, p2 = str(tmp_path / "p1.h5"), str(tmp_path / "p2.h5")
+    w.save(p1)
+    h5lite.copy_file(p1, p2)
+    c = H5File(p2)
+    assert float(c.read("/s/f")) == 2.5 and c.read("/s/f").shape == ()
+    assert c.read("/s/u").dtype == np.uint16 and list(c.read("/s/u")) == [0, 1, 2, 3, 4]
+    assert [x.decode() for x in c.read("/s/names")] == ["ab", "cde"]
+    assert list(c.attr("/s", "k")) == [1, 2, 3]

@@ -1,7 +1,7 @@
 """Build the in-tree shared libraries of the GB300 Upside engine.
 
   libupside.so          the engine: sm_103a kernels + drop-in C ABI + batch API
-  libupside_h5lite.so   HDF5-subset reader for Python (config/fixture tools)
+  libupside_h5lite.so   HDF5-subset reader and writer for Python (config/fixture tools)
 
 Compilation runs in parallel, one process per translation unit, and only
 rebuilds what is older than its sources.
@@ -53,6 +53,9 @@ def build(verbose=False):
     h5o = os.path.join(BUILD, "h5lite.o")
     if _stale(h5o, [os.path.join(CSRC, "h5lite.cpp"), os.path.join(CSRC, "h5lite.h")]):
         jobs.append([CXX, "-O2", "-std=c++17", "-fPIC", "-c", os.path.join(CSRC, "h5lite.cpp"), "-o", h5o])
+    h5w = os.path.join(BUILD, "h5lite_write.o")
+    if _stale(h5w, [os.path.join(CSRC, "h5lite_write.cpp"), os.path.join(CSRC, "h5lite.h")]):
+        jobs.append([CXX, "-O2", "-std=c++17", "-fPIC", "-c", os.path.join(CSRC, "h5lite_write.cpp"), "-o", h5w])
     capo = os.path.join(BUILD, "h5lite_capi.o")
     if _stale(capo, [os.path.join(CSRC, "h5lite_capi.cpp"), os.path.join(CSRC, "h5lite.h")]):
         jobs.append([CXX, "-O2", "-std=c++17", "-fPIC", "-c", os.path.join(CSRC, "h5lite_capi.cpp"), "-o", capo])
@@ -61,11 +64,11 @@ def build(verbose=False):
             if verbose and out.strip():
                 print(out)
     lib = os.path.join(HERE, "libupside.so")
-    if _stale(lib, objs + [h5o]):
-        _run([NVCC] + ARCH + ["-shared", "-o", lib] + objs + [h5o])
+    if _stale(lib, objs + [h5o, h5w]):
+        _run([NVCC] + ARCH + ["-shared", "-o", lib] + objs + [h5o, h5w])
     h5lib = os.path.join(HERE, "libupside_h5lite.so")
-    if _stale(h5lib, [h5o, capo]):
-        _run([CXX, "-shared", "-o", h5lib, h5o, capo])
+    if _stale(h5lib, [h5o, h5w, capo]):
+        _run([CXX, "-shared", "-o", h5lib, h5o, h5w, capo])
     return lib
 
 

@@ -301,7 +301,10 @@ std::vector<uint64_t> parse_dataspace(const uint8_t* p, bool* scalar, bool* null
 void File::parse_message(Object& obj, int type, const uint8_t* p, size_t n) {
     switch (type) {
         case 0x0001: obj.dims = parse_dataspace(p, &obj.is_scalar); break;
-        case 0x0003: obj.dt = parse_dtype(p); break;
+        case 0x0003:
+            obj.dt = parse_dtype(p);
+            obj.dt.raw.assign(p, p + n);
+            break;
         case 0x0008: {
             int version = p[0];
             if (version == 3) {
@@ -369,6 +372,7 @@ void File::parse_message(Object& obj, int type, const uint8_t* p, size_t n) {
             a.name.assign(reinterpret_cast<const char*>(q), strnlen(reinterpret_cast<const char*>(q), name_sz));
             q += pad(name_sz);
             a.dt = parse_dtype(q);
+            a.dt.raw.assign(q, q + dt_sz);
             q += pad(dt_sz);
             bool scalar, null_space = false;
             a.dims = parse_dataspace(q, &scalar, &null_space);

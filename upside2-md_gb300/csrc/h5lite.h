@@ -34,6 +34,7 @@ struct Dtype {
     int size = 0;           // bytes per element
     bool is_signed = false;
     bool big_endian = false;
+    std::vector<uint8_t> raw;  // the datatype message as stored (Writer copies it verbatim)
 };
 
 struct Attribute {
@@ -101,6 +102,46 @@ private:
     void read_chunk_btree(const Object& obj, uint64_t addr, std::vector<uint8_t>& out);
     const uint8_t* at(uint64_t addr, size_t n) const;
 };
+
+// Writer for the same subset: symbol-table groups, version-1 object headers,
+// contiguous datasets, attribute messages.  Build a tree in memory, then
+// save() writes the whole file (to `<path>.tmp`, renamed over `path`, so a
+// reader never sees a half-written file).  Groups hold at most 1024 links and
+// an attribute at most 64 KiB (one object-header message).
+class Writer {
+public:
+    struct Node {
+        bool is_group = true;
+        std::map<std::string, std::unique_ptr<Node>> children;
+        std::vector<Attribute> attrs;
+        Dtype dt;
+        std::vector<uint64_t> dims;  // empty: scalar
+        std::vector<uint8_t> data;
+    };
+    Writer();
+    Node& group(const std::string& path);
+    // dims empty => scalar; data holds product(dims) * dt.size bytes
+    void dataset(const std::string& path, const Dtype& dt, const std::vector<uint64_t>& dims,
+                 std::vector<uint8_t> data);
+    // dims and data both empty => a null dataspace (no value)
+    void attr(const std::string& path, const std::string& name, const Dtype& dt, const std::vector<uint64_t>& dims,
+              std::vector<uint8_t> data);
+    void remove(const std::string& path);
+    void save(const std::string& filename) const;
+    Node root;
+};
+
+// Datatype of a native little-endian number or fixed-length string.
+Dtype dtype_int(int size, bool is_signed);
+Dtype dtype_float(int size);
+Dtype dtype_string(int size);
+
+// Copy the object at src_path of `src` (group: recursively, with attributes)
+// to dst_path of `dst`.  Datasets are written back contiguous and
+// uncompressed; variable-length and reference data cannot be copied (Error).
+// Links whose full path is in `skip` are left out.
+void copy_tree(File& src, const std::string& src_path, Writer& dst, const std::string& dst_path,
+               const std::vector<std::string>& skip = {});
 
 // Element conversion helper shared with the Python binding.
 void convert_elements(const Dtype& dt, const uint8_t* src, size_t n, int dst_kind, void* dst);

@@ -82,6 +82,15 @@ int h5l_attr_shape(void* f, const char* path, const char* name, int64_t* dims, i
           info[4] = int(a.data.size()); return int(a.dims.size());)
 }
 
+// Rewrite `src` as `dst` with the h5lite writer, leaving out the
+// '\n'-separated paths in `skip` (may be empty or NULL).
+int h5l_copy_file(const char* src, const char* dst, const char* skip) {
+    GUARD(File f(src); h5lite::Writer w; std::vector<std::string> sk; std::string s = skip ? skip : "";
+          size_t i = 0; while (i < s.size()) { size_t j = s.find('\n', i); if (j == std::string::npos) j = s.size();
+                                               if (j > i) sk.push_back(s.substr(i, j - i)); i = j + 1; }
+          h5lite::copy_tree(f, "/", w, "/", sk); w.save(dst); return 0;)
+}
+
 int h5l_attr_read_raw(void* f, const char* path, const char* name, void* out, int64_t nbytes) {
     GUARD(auto& a = static_cast<File*>(f)->attr(path, name);
           if (int64_t(a.data.size()) != nbytes) { g_err = "size mismatch"; return -1; }

@@ -1,7 +1,9 @@
 """Python access to HDF5 `.up` files without h5py/PyTables.
 
 Reading goes through the package's C++ reader (``csrc/h5lite.cpp``, loaded
-from ``libupside_h5lite.so``).  Writing is done here in pure Python: the
+from ``libupside_h5lite.so``); ``copy_file`` rewrites a file through the C++
+writer (``csrc/h5lite_write.cpp``) that the upside driver logs with.
+``H5Writer`` below is a pure-Python writer for configurations: the
 writer emits the same conservative subset the reader understands (superblock
 v0, symbol-table groups, version-1 object headers, contiguous datasets,
 version-1 attribute messages), which is also what HDF5 1.8+ libraries read.
@@ -38,8 +40,16 @@ def _load():
         lib.h5l_read_raw.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_void_p, ctypes.c_int64]
         lib.h5l_attr_read_raw.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_char_p,
                                           ctypes.c_void_p, ctypes.c_int64]
+        lib.h5l_copy_file.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p]
         _lib = lib
     return _lib
+
+
+def copy_file(src, dst, skip=()):
+    """Rewrite `src` as `dst` with the C++ writer, leaving out the paths in
+    `skip` (datasets come out contiguous and uncompressed)."""
+    if _load().h5l_copy_file(src.encode(), dst.encode(), "\n".join(skip).encode()):
+        raise RuntimeError(_load().h5l_last_error().decode())
 
 
 def _np_dtype(info):
