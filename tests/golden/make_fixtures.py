@@ -5,6 +5,8 @@ this script, which are committed (the GPU host has no reference checkout):
 
   chig.up            the reference's own ff_2.1 example config
                      (example/15.SpatialTransformation/inputs/chig.up)
+  chig_run_output.npz  every /output array of that run and its invocation
+                     (python make_fixtures.py chig_run writes only this file)
   chig_frames.npz    the 20 logged frames of the reference's example run
                      (outputs/simple_test/chig.run.up /output/pos, /output/potential)
                      plus the locally built reference engine's energy and
@@ -100,6 +102,16 @@ def chig(L):
                         ref_energy=np.array(E), ref_deriv=np.array(D))
 
 
+def chig_run_output():
+    """Every /output array of the reference's logged example run and its
+    command line, for the driver tests: frame 0 is logged before any
+    integration, so the driver must reproduce it from the same invocation."""
+    run = H5File(os.path.join(EX, "outputs", "simple_test", "chig.run.up"))
+    out = {k: run.read("/output/" + k) for k in run.list("/output")}
+    out["invocation"] = np.array(run.attr("/output", "invocation"))
+    np.savez_compressed(os.path.join(HERE, "chig_run_output.npz"), **out)
+
+
 def synthetic(L, n_res, seed, n_frames=3, tmpdir="/tmp"):
     rng = np.random.RandomState(seed)
     seq = config_gen.random_sequence(n_res, rng)
@@ -166,9 +178,13 @@ def threefry_kat():
 
 
 def main():
+    if sys.argv[1:] == ["chig_run"]:
+        chig_run_output()
+        return
     threefry_kat()
     L = load_ref()
     chig(L)
+    chig_run_output()
     synthetic(L, 60, 1)
     synthetic(L, 150, 2, n_frames=2)
 

@@ -1,6 +1,8 @@
 """Build the in-tree shared libraries of the GB300 Upside engine.
 
   libupside.so          the engine: sm_103a kernels + drop-in C ABI + batch API
+                        + the upside driver (upside_main)
+  upside                the upside command line over libupside.so
   libupside_h5lite.so   HDF5-subset reader and writer for Python (config/fixture tools)
 
 Compilation runs in parallel, one process per translation unit, and only
@@ -18,7 +20,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC = os.environ.get("NVCC", "nvcc")
 CXX = os.environ.get("CXX", "g++")
 
-CU_SOURCES = ["engine.cu", "graph.cu", "pairlist.cu", "warm.cu", "capi.cu"]
+CU_SOURCES = ["engine.cu", "graph.cu", "pairlist.cu", "warm.cu", "capi.cu", "driver.cu"]
 HEADERS = ["engine.h", "graph.h", "warm.h", "dev_math.cuh", "h5lite.h"]
 
 
@@ -40,7 +42,8 @@ def build(verbose=False):
     os.makedirs(BUILD, exist_ok=True)
     hdrs = [os.path.join(CSRC, h) for h in HEADERS] + [
         os.path.join(HERE, "..", "include", "engine_c_library.h"),
-        os.path.join(HERE, "..", "include", "upside_gb300.h")]
+        os.path.join(HERE, "..", "include", "upside_gb300.h"),
+        os.path.join(HERE, "..", "include", "upside_main.h")]
     jobs = []
     objs = []
     for src in CU_SOURCES:
@@ -66,6 +69,10 @@ def build(verbose=False):
     lib = os.path.join(HERE, "libupside.so")
     if _stale(lib, objs + [h5o, h5w]):
         _run([NVCC] + ARCH + ["-shared", "-o", lib] + objs + [h5o, h5w])
+    exe = os.path.join(HERE, "upside")
+    cli = os.path.join(CSRC, "upside_cli.cpp")
+    if _stale(exe, [lib, cli]):
+        _run([CXX, "-O2", "-std=c++17", "-o", exe, cli, "-L" + HERE, "-lupside", "-Wl,-rpath,$ORIGIN"])
     h5lib = os.path.join(HERE, "libupside_h5lite.so")
     if _stale(h5lib, [h5o, h5w, capo]):
         _run([CXX, "-shared", "-o", h5lib, h5o, h5w, capo])

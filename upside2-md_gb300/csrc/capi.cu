@@ -394,7 +394,8 @@ int ug_node_potential(UgBatch* b, const char* node, double* out) {
 // on the change of the log Boltzmann factors.  Energies are FP64 sums and the
 // acceptance arithmetic is FP64; the uniform draws come from the replica
 // exchange Threefry stream keyed by (seed, stream 1) at counter (round, 0, 0, k).
-namespace {
+}  // extern "C"
+namespace ug {
 void threefry_host(const uint32_t c[4], const uint32_t k[4], uint32_t out[4]) {
     static const int R[8][2] = {{10, 26}, {11, 21}, {13, 27}, {23, 5}, {6, 20}, {17, 11}, {25, 10}, {18, 20}};
     uint32_t ks[5] = {k[0], k[1], k[2], k[3], 0x1BD11BDAu ^ k[0] ^ k[1] ^ k[2] ^ k[3]};
@@ -426,7 +427,10 @@ void swap_coords(Engine& e, int s1, int s2, float* tmp) {
     UG_CK(cudaMemcpyAsync(a, b, n, cudaMemcpyDeviceToDevice, e.st));
     UG_CK(cudaMemcpyAsync(b, tmp, n, cudaMemcpyDeviceToDevice, e.st));
 }
-}  // namespace
+}  // namespace ug
+using ug::swap_coords;
+using ug::threefry_host;
+extern "C" {
 
 int ug_replica_exchange(UgBatch* b, int n_pairs, const int* pairs, uint32_t seed, uint64_t round, int* accepted) {
     GUARD_BEGIN

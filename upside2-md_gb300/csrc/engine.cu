@@ -2136,6 +2136,36 @@ __global__ void round_advance_kernel(int n_sys, unsigned long long* round) {
     for (int s = grid_stride_start(); s < n_sys; s += grid_stride()) round[s] += 1;
 }
 
+// Move each system's centroid to the origin (xy_only: leave z alone); one
+// block of 256 threads per system (recenter, src/deriv_engine.cpp:39-50)
+__global__ void recenter_kernel(const int* __restrict__ atom_off, float* pos, int xy_only) {
+    int s = blockIdx.x;
+    int a0 = atom_off[s], a1 = atom_off[s + 1];
+    __shared__ float red[3][256 / 32];
+    __shared__ float center[3];
+    float c[3] = {0.f, 0.f, 0.f};
+    for (int a = a0 + int(threadIdx.x); a < a1; a += blockDim.x)
+        for (int d = 0; d < 3; ++d) c[d] += pos[3 * size_t(a) + d];
+    for (int d = 0; d < 3; ++d) {
+        float v = c[d];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if ((threadIdx.x & 31) == 0) red[d][threadIdx.x >> 5] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < 3) {
+        float t = 0.f;
+        for (int w = 0; w < int(blockDim.x >> 5); ++w) t += red[threadIdx.x][w];
+        center[threadIdx.x] = (a1 > a0) ? t / float(a1 - a0) : 0.f;
+    }
+    __syncthreads();
+    float cx = center[0], cy = center[1], cz = xy_only ? 0.f : center[2];
+    for (int a = a0 + int(threadIdx.x); a < a1; a += blockDim.x) {
+        pos[3 * size_t(a) + 0] -= cx;
+        pos[3 * size_t(a) + 1] -= cy;
+        pos[3 * size_t(a) + 2] -= cz;
+    }
+}
+
 }  // namespace
 
 // ================================================================ Engine ===
@@ -2359,12 +2389,22 @@ void Engine::compute(bool energy) {
     UG_CK(cudaGetLastError());
 }
 
+void Engine::thermalize(float dt, float timescale) {
+    // (3 x interval) x dt in FP32, the reference's thermostat time step
+    // (src/main.cpp:780)
+    thermostat_kernel<<<nblk(atom_total), 256, 0, st>>>(n_sys, atom_off_d, atom_sys_d, atom_total,
+                                                        (3.f * thermo_span) * dt, timescale, d_temp, d_seed, d_round,
+                                                        d_mom);
+    round_advance_kernel<<<1, 256, 0, st>>>(n_sys, d_round);
+}
+
+void Engine::recenter(bool xy_only) {
+    recenter_kernel<<<n_sys, 256, 0, st>>>(atom_off_d, d_pos, xy_only ? 1 : 0);
+    UG_CK(cudaGetLastError());
+}
+
 void Engine::round(float dt, float timescale, bool thermostat) {
-    if (thermostat) {
-        thermostat_kernel<<<nblk(atom_total), 256, 0, st>>>(n_sys, atom_off_d, atom_sys_d, atom_total, 3.f * dt, timescale,
-                                                            d_temp, d_seed, d_round, d_mom);
-        round_advance_kernel<<<1, 256, 0, st>>>(n_sys, d_round);
-    }
+    if (thermostat) thermalize(dt, timescale);
     for (int stage = 0; stage < 3; ++stage) {
         compute(false);
         integrate_kernel<<<nblk(3LL * atom_total), 256, 0, st>>>(3 * atom_total, dt, nodes[0]->sens, d_mom, d_pos);
@@ -2420,8 +2460,12 @@ int Engine::status(bool clear) {
 // counters) is copied aside; if a pair list or the BP entry storage
 // overflowed during it, the state is put back, the storage grown and the
 // chunk run again, so overflow never leaves truncated interactions behind.
-void Engine::run_rounds(int n_round, float dt, float timescale, bool use_graph, int graph_rounds) {
+void Engine::run_rounds(int n_round, float dt, float timescale, bool use_graph, int graph_rounds,
+                        int thermo_interval, unsigned long long first_round) {
     if (graph_rounds < 1) graph_rounds = 1;
+    if (thermo_interval < 1) thermo_interval = 1;
+    // the captured graph applies the thermostat every round
+    if (thermo_interval > 1) use_graph = false;
     size_t n3 = 3 * size_t(atom_total);
     if (!snap_pos) {
         snap_pos = alloc<float>(n3);
@@ -2437,11 +2481,15 @@ void Engine::run_rounds(int n_round, float dt, float timescale, bool use_graph, 
         UG_CK(cudaMemcpyAsync(snap_round, d_round, 8 * size_t(n_sys), cudaMemcpyDeviceToDevice, st));
         if (use_graph && k == graph_rounds) {
             if (!graph_exec || this->graph_rounds != graph_rounds || graph_dt != dt || graph_timescale != timescale ||
-                graph_timed)
+                graph_span != thermo_span || graph_timed)
                 capture(dt, timescale, graph_rounds);
             launch_graph();
         } else {
-            for (int r = 0; r < k; ++r) round(dt, timescale, true);
+            for (int r = 0; r < k; ++r)
+                round(dt, timescale,
+                      (first_round + static_cast<unsigned long long>(done + r)) %
+                              static_cast<unsigned long long>(thermo_interval) ==
+                          0);
         }
         int s = 0;
         UG_CK(cudaMemcpyAsync(&s, d_status, sizeof(int), cudaMemcpyDeviceToHost, st));
@@ -2475,6 +2523,7 @@ void Engine::capture(float dt, float timescale, int rounds) {
     graph_timed = false;
     graph_dt = dt;
     graph_timescale = timescale;
+    graph_span = thermo_span;
 }
 void Engine::launch_graph() { UG_CK(cudaGraphLaunch(graph_exec, st)); }
 

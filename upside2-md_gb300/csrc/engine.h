@@ -110,6 +110,12 @@ public:
     void compute(bool energy);
     // one integration round: thermostat, then 3 x {compute; p -= dt F; x += dt p}
     void round(float dt, float timescale, bool thermostat);
+    // the thermostat alone (one invocation: counters advance); its time step
+    // is 3 dt thermo_span (the reference's thermostat interval in rounds)
+    void thermalize(float dt, float timescale);
+    float thermo_span = 1.f;
+    // move each system's centroid to the origin (xy_only: x and y only)
+    void recenter(bool xy_only);
     // host helpers
     void set_pos(const float* pos_all);     // atom_total*3
     void get_pos(float* pos_all);
@@ -133,9 +139,12 @@ public:
     std::vector<std::vector<int>> consumers;
     std::vector<cudaEvent_t> ev_fwd, ev_bwd, ev_lane;
     void setup_lanes();
-    float graph_dt = 0.f, graph_timescale = 0.f;  // of the captured graph
-    // integration rounds with overflow recovery (see engine.cu)
-    void run_rounds(int n_round, float dt, float timescale, bool use_graph, int graph_rounds);
+    float graph_dt = 0.f, graph_timescale = 0.f, graph_span = 1.f;  // of the captured graph
+    // integration rounds with overflow recovery (see engine.cu); with
+    // thermo_interval > 1 the thermostat runs only in rounds whose number
+    // (first_round + index) is a multiple of it, and no graph is used
+    void run_rounds(int n_round, float dt, float timescale, bool use_graph, int graph_rounds,
+                    int thermo_interval = 1, unsigned long long first_round = 0);
     float* snap_pos = nullptr;
     float* snap_mom = nullptr;
     unsigned long long* snap_round = nullptr;
@@ -173,5 +182,11 @@ private:
     std::vector<void*> allocations_;
     std::vector<std::unique_ptr<h5lite::File>> files_;
 };
+
+// Threefry-4x32-20 on the host (the replica-exchange random stream)
+void threefry_host(const uint32_t c[4], const uint32_t k[4], uint32_t out[4]);
+// exchange the coordinates of systems s1 and s2 (equal atom counts) through
+// tmp (device, 3 n_atom floats), on the engine stream
+void swap_coords(Engine& e, int s1, int s2, float* tmp);
 
 }  // namespace ug

@@ -4,6 +4,7 @@
 energy / deriv / set_param / get_param / get_param_deriv / get_output /
 get_sens / get_value_by_name) over the drop-in C ABI of libupside.so.
 `Batch` drives many systems at once through the batch API (upside_gb300.h).
+`upside_main` runs the upside command line (trajectories logged to /output).
 
 The CUDA library is required: importing this module on a host without the
 built libupside.so raises immediately; there is no CPU fallback.
@@ -75,6 +76,8 @@ def lib():
         L.ug_mlp_adam.argtypes = [vp, vp, vp, vp, vp, ip, f, f, f, f, ip, vp]
         L.ug_pair_list.argtypes = [vp, ip, ctypes.c_float, vp, ip, vp, vp]
         L.ug_pair_list_noalloc.argtypes = [vp, ip, ctypes.c_float, vp, ip, vp, vp]
+        L.upside_main.restype = ip
+        L.upside_main.argtypes = [ip, ctypes.POINTER(ctypes.c_char_p), ip]
         _lib = L
     return _lib
 
@@ -90,6 +93,18 @@ def pair_list_noalloc(pos_ptr, n, cutoff, pairs_ptr, cap, n_pairs_ptr, stream=0)
     (n <= 262144), asynchronous on `stream`."""
     if lib().ug_pair_list_noalloc(pos_ptr, n, cutoff, pairs_ptr, cap, n_pairs_ptr, stream):
         raise RuntimeError(lib().ug_last_error().decode())
+
+
+def upside_main(args, verbose=True):
+    """Run the upside command line in this process on the GPU (the
+    reference's in_process_upside, py/upside_engine.py:94-118): `args` are
+    the arguments after the program name.  Raises RuntimeError on a non-zero
+    return code."""
+    argv = ["python_library", "--re-raise-signal"] + [str(a) for a in args]
+    arr = (ctypes.c_char_p * len(argv))(*[a.encode() for a in argv])
+    rc = lib().upside_main(len(argv), arr, int(bool(verbose)))
+    if rc:
+        raise RuntimeError("In process Upside returned %i" % rc)
 
 
 def _f32(a):
