@@ -145,8 +145,10 @@ int ug_pair_list_noalloc(const float* pos, int n, float cutoff, int32_t* pairs, 
  * predicts each residue's converged rotamer marginal; the solve starts from
  * the prediction and still iterates to the configured tolerance.  Per system
  * the engine tracks the sweeps needed from the learned and from the uniform
- * start (every 16th solve tries the other one) and uses the learned start
- * only while it needs no more sweeps.  Weights are FP32 row-major (W1 64x128,
+ * start (every 64th solve tries the other one) and uses the learned start
+ * only while it saves at least 8 sweeps, about what the network's kernels
+ * cost in device time; systems on the uniform start skip the network's
+ * feature kernel.  Weights are FP32 row-major (W1 64x128,
  * b1 128, W2 128x128, b2 128, W3 128x8, b3 8), stored as bf16; pass all six
  * or none (none: keep the loaded weights, only switch).  enable selects the
  * start: 0 uniform (the reference's), 1 learned, 2 the previous solve's

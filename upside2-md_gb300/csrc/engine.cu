@@ -1958,6 +1958,7 @@ struct RotamerNode : GNode {
         // instead of predicting it)
         warm_on = mode == 1;
         b.warm = mode == 1 ? wd.belief : mode == 2 ? b.marg : nullptr;
+        b.warm_gain = mode == 1 ? WARM_MIN_GAIN : WARM_MIN_GAIN_FREE;
         b.reuse = mode == 3;
         UG_CK(cudaMemset(b.prev_valid, 0, sizeof(int) * 2 * size_t(e.n_sys)));
         return true;
@@ -2007,6 +2008,7 @@ struct RotamerNode : GNode {
             warm_buffers(e);
             WarmDev all = wd;
             all.need = nullptr;  // every node, whatever the solves would use
+            all.stat = nullptr;
             launch_warm_features(all, e.d_pos, e.atom_off_d, b.res_off, b.prob, b.nrot, e.n_sys, e.st);
             std::vector<uint16_t> x(size_t(b.n_res) * WARM_IN);
             UG_CK(cudaMemcpyAsync(x.data(), wd.X, 2 * x.size(), cudaMemcpyDeviceToHost, e.st));

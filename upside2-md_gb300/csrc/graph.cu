@@ -972,11 +972,12 @@ __global__ void __launch_bounds__(THREADS) bp_solve_kernel(DBP b, int want_energ
     // Learned warm start: the first sweep starts from the predicted marginals
     // instead of prob.  Per system, the mean sweep counts of warm and uniform
     // starts are tracked (warm_stat: mean warm, mean uniform, solves); every
-    // WARM_PROBE-th solve starts uniform to refresh the comparison, and the
-    // warm start is used only while it needs no more sweeps than uniform.
+    // WARM_PROBE-th solve tries the other start to refresh the comparison,
+    // and the warm start is used only while it saves WARM_MIN_GAIN sweeps
+    // (warm_start_used).
     const int par = b.reuse ? *b.parity : 0;
     const bool use_prev = b.reuse && b.prev_valid[(par ^ 1) * b.n_sys + s];
-    const bool use_warm = use_prev || (b.warm && warm_start_used(b.warm_stat + 4 * s));
+    const bool use_warm = use_prev || (b.warm && warm_start_used(b.warm_stat + 4 * s, b.warm_gain));
     const float* init = use_prev ? b.marg : use_warm ? b.warm : b.prob;
     // N.old = N.cur = prob (N.old = prediction when warm); E.old = 1 (own entries)
     if (tid == 0) s_multi = 0;

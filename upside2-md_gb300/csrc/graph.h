@@ -133,6 +133,9 @@ struct DBP {
     // and per-system sweep statistics (4 floats per system)
     const float* warm;
     float* warm_stat;
+    // sweeps a warm start must save to be used: the network's cost for the
+    // learned start, less for a start that costs no kernels
+    float warm_gain;
     // previous-solve start (reuse != 0): each solve leaves its final messages,
     // their columns and row offsets in the half `parity` of the prev_ arrays;
     // the next solve (other half) starts from them, matched by residue pair,

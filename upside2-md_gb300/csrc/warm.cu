@@ -280,8 +280,10 @@ __global__ void warm_features_kernel(WarmDev w, const float* __restrict__ pos, c
                                      const int* __restrict__ res_off, const float* __restrict__ prob,
                                      const int* __restrict__ nrot) {
     if (w.need && !*w.need) return;  // block-uniform
-    extern __shared__ float wsm[];
     const int s = blockIdx.x;
+    // only systems whose solve starts from the prediction need features
+    if (w.stat && !warm_start_used(w.stat + 4 * s)) return;
+    extern __shared__ float wsm[];
     const int a0 = atom_off[s], nres = (atom_off[s + 1] - a0) / 3;
     f3* CA = reinterpret_cast<f3*>(wsm);
     f3* CB = CA + nres;

@@ -8,20 +8,27 @@ namespace ug {
 constexpr int WARM_IN = 64;    // features per residue (51 used, zero-padded)
 constexpr int WARM_HID = 128;  // hidden width of both layers
 constexpr int WARM_OUT = 8;    // rotamer logits (6 used)
-// every WARM_PROBE-th solve of a system starts from the uniform state, to
-// keep measuring whether the learned start still helps
-constexpr int WARM_PROBE = 16;
+// every WARM_PROBE-th solve of a system tries the start it does not use, to
+// keep measuring whether the learned start pays
+constexpr int WARM_PROBE = 64;
 
 // Whether a system's next BP solve starts from the warm start, from its sweep
 // statistics ws = (mean sweeps warm, mean sweeps uniform, solves, known bits:
-// 1 warm mean set, 2 uniform mean set): the warm start while it saves at
-// least WARM_MIN_GAIN sweeps (its own cost is about that much), except that
-// every WARM_PROBE-th solve tries the other start.
-constexpr float WARM_MIN_GAIN = 0.5f;
-__host__ __device__ inline bool warm_start_used(const float* ws) {
+// 1 warm mean set, 2 uniform mean set).  The first solve measures the uniform
+// start, the second the warm one; after that the warm start is used only
+// while it saves at least WARM_MIN_GAIN sweeps, the price of the network: its
+// feature and MLP kernels sit on the rotamer node's critical path and cost
+// about as much device time as ten BP sweeps (measured on 64 systems of
+// 40-400 residues: 0.13 ms per force evaluation against 13 us per sweep).
+// Every WARM_PROBE-th solve tries the other start.  A start that runs no
+// kernels of its own (the previous solve's marginals) needs to save only
+// WARM_MIN_GAIN_FREE sweeps.
+constexpr float WARM_MIN_GAIN = 8.f;
+constexpr float WARM_MIN_GAIN_FREE = 0.5f;
+__host__ __device__ inline bool warm_start_used(const float* ws, float min_gain = WARM_MIN_GAIN) {
     int solves = int(ws[2]), known = int(ws[3]);
-    bool prefer_warm = (known & 3) != 3 || ws[0] + WARM_MIN_GAIN <= ws[1];
-    bool probe = solves % WARM_PROBE == WARM_PROBE - 1;
+    bool prefer_warm = (known & 2) != 0 && ((known & 1) == 0 || ws[0] + min_gain <= ws[1]);
+    bool probe = (known & 3) == 3 && solves % WARM_PROBE == WARM_PROBE - 1;
     return prefer_warm != probe;
 }
 
