@@ -912,9 +912,9 @@ __device__ __forceinline__ float bp_beliefs(const DBP& b, int r0, int lo, int hi
 template <int BP_CLUSTER, int BP_LANES, int THREADS>
 __global__ void __launch_bounds__(THREADS) bp_solve_kernel(DBP b, int want_energy, double* energy_out) {
     extern __shared__ float smem[];
-    __shared__ float red[32];
     __shared__ double dred[32];
-    __shared__ float s_dev[BP_CLUSTER];
+    __shared__ float s_dev[2][BP_CLUSTER];  // per chunk parity: every block's deviation maximum
+    __shared__ int s_bmax[2];               // this block's maximum (non-negative float bits)
     __shared__ double s_en[BP_CLUSTER];
     __shared__ int s_multi;
     cg::cluster_group cluster = cg::this_cluster();
@@ -947,27 +947,7 @@ __global__ void __launch_bounds__(THREADS) bp_solve_kernel(DBP b, int want_energ
         cluster.sync();
         return bp_beliefs<BP_LANES>(b, r0, lo, hi, e1, Nold, Ncur, s_nrot, Ecur, mode, damp, tid, nt);
     };
-    auto block_max = [&](float v) -> float {
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
-        if (lane == 0) red[warp] = v;
-        __syncthreads();
-        float r = 0.f;
-        for (int w = 0; w < nw; ++w) r = fmaxf(r, red[w]);
-        __syncthreads();
-        return r;
-    };
-    // largest deviation over the cluster: every block posts its own maximum
-    // into slot crank of every block, then one cluster barrier
-    auto cluster_max = [&](float v) -> float {
-        v = block_max(v);
-        if (tid < BP_CLUSTER) *cluster.map_shared_rank(&s_dev[crank], tid) = v;
-        cluster.sync();
-        float r = 0.f;
-#pragma unroll
-        for (int c = 0; c < BP_CLUSTER; ++c) r = fmaxf(r, s_dev[c]);
-        return r;
-    };
+    if (tid < 2) s_bmax[tid] = 0;
 
     // Learned warm start: the first sweep starts from the predicted marginals
     // instead of prob.  Per system, the mean sweep counts of warm and uniform
@@ -1064,18 +1044,55 @@ __global__ void __launch_bounds__(THREADS) bp_solve_kernel(DBP b, int want_energ
         for (int k = 0; k < 6; ++k) c[k] *= inv;
     }
     __syncthreads();
-    int nc = 1, ec = 0;
+    // Chunks of damped sweeps until the largest one-sided deviation of a
+    // chunk's last sweep is within tol (src/rotamer.cpp:1137-1156).  The
+    // cluster-wide maximum needs no barrier of its own: each block posts its
+    // maximum into slot crank of every block (parity cpar), and the slots are
+    // read after the next sweep's message-phase barrier.  When they say
+    // "converged", that message phase (written into the older message buffer,
+    // which nothing reads afterwards) is discarded and the state is the one
+    // after the converged chunk: the same sweeps and results as a separate
+    // barrier before every test.
+    const int chunk = max(1, b.chunk);
+    int nc = 1, ec = 0, cpar = 0;
+    bool pending = false;
     float dev = 1e10f;
     int iter = 0;
-    for (; dev > b.tol && iter < b.max_iter; iter += b.chunk) {
+    while (iter < b.max_iter) {
         float d = 0.f;
-        for (int j = 0; j < b.chunk; ++j) {
+        bool converged = false;
+        for (int j = 0; j < chunk; ++j) {
             nc ^= 1;
             ec ^= 1;
-            d = sweep(NB[nc ^ 1], NB[nc], EM[ec ^ 1], EM[ec], 1, b.damping);
+            bp_messages(b, eo0, eo1, NB[nc ^ 1], s_nrot, EM[ec ^ 1], EM[ec], tid, nt);
+            cluster.sync();
+            if (pending) {  // the previous chunk's maximum, posted before this barrier
+                pending = false;
+                float r = 0.f;
+#pragma unroll
+                for (int c = 0; c < BP_CLUSTER; ++c) r = fmaxf(r, s_dev[cpar ^ 1][c]);
+                dev = r;
+                if (!(dev > b.tol)) {
+                    nc ^= 1;
+                    ec ^= 1;
+                    converged = true;
+                    break;
+                }
+            }
+            d = bp_beliefs<BP_LANES>(b, r0, lo, hi, e1, NB[nc ^ 1], NB[nc], s_nrot, EM[ec], 1, b.damping, tid, nt);
+            if (j == chunk - 1) {
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) d = fmaxf(d, __shfl_xor_sync(0xffffffffu, d, o));
+                if (lane == 0) atomicMax(&s_bmax[cpar], __float_as_int(d));  // d >= 0
+            }
             __syncthreads();
         }
-        dev = cluster_max(d);
+        if (converged) break;
+        iter += chunk;
+        if (tid < BP_CLUSTER) *cluster.map_shared_rank(&s_dev[cpar][crank], tid) = __int_as_float(s_bmax[cpar]);
+        if (tid == 0) s_bmax[cpar ^ 1] = 0;
+        cpar ^= 1;
+        pending = true;
     }
     if (tid == 0 && crank == 0) {
         b.n_iter[s] = iter;
