@@ -5,8 +5,10 @@ Pins, in order of strength:
     chig.run.up, committed as tests/golden/chig_run_output.npz): frame 0 is
     logged before any integration step, so the same command line must give
     the same positions, potential, kinetic energy (the thermostat's first
-    draw from zero momenta), time, temperature and hbond array, and the arrays
-    must have the reference's names, shapes and types;
+    draw from zero momenta), time, temperature, hbond and node-level arrays
+    (rotamer free energy, average energy, entropy and one-body energies per
+    residue, Rama and sigmoid-coupling energies per residue, bad BP solves),
+    and the arrays must have the reference's names, shapes and types;
   * the oracle integrating the same schedule (recentre + log every round,
     thermalise once at the start, thermostat each round) for the first frames;
   * replica exchange bookkeeping, restarts from logged momenta, annealing.
@@ -57,6 +59,15 @@ def test_chig_frame0_matches_reference_run(built, tmp_path):
     assert np.array_equal(out["time"], ref["time"][:2])  # (3 dt) * round in FP32, as logged
     assert np.array_equal(out["temperature"][:, 0], ref["temperature"][:2, 0])
     assert np.abs(out["hbond"][0] - ref["hbond"][0]).max() < 1e-4
+    # the node-level arrays of the default (detailed) log level: the same set,
+    # shapes and types, and frame 0's values.  The rotamer decomposition
+    # follows the marginals, which two builds stop at the BP tolerance (1e-3)
+    # in different float orders: 1e-3 of the array's scale (observed <= 2.3e-4)
+    assert set(out) == set(ref.files) - {"invocation"}
+    for k in set(out) - {"pos", "kinetic", "potential", "time", "temperature", "hbond"}:
+        assert out[k].dtype == ref[k].dtype and out[k].shape[1:] == ref[k].shape[1:], k
+        diff = np.abs(out[k][0].astype(np.float64) - ref[k][0]).max()
+        assert diff < 1e-3 * max(1., np.abs(ref[k][0]).max()), (k, out[k][0], ref[k][0])
     # frame 1 lies 1852 rounds later on a chaotic trajectory: only its scale
     assert 0.2 < out["kinetic"][1, 0] / (1.5 * 0.8) < 3.0
 

@@ -659,9 +659,15 @@ int run(const Args& A, const std::string& invocation, int verbose) {
         if (do_recenter)
             for (auto& e : engines) e->recenter(xy_only);
         std::vector<double> pot;
+        // at the detailed level the nodes also fill their per-element logs
+        for (auto& e : engines) e->log_detail = log_level >= 1;
         evaluate_all(pot);
+        for (auto& e : engines) e->log_detail = false;
         for (size_t k = 0; k < engines.size(); ++k) {
             Engine& e = *engines[k];
+            std::vector<ug::GNode::Log> node_logs;
+            if (log_level >= 1)
+                for (auto& n : e.nodes) n->detailed_logs(e, node_logs);
             std::vector<float> pos(3 * size_t(e.atom_total)), mom(3 * size_t(e.atom_total));
             UG_CK(cudaMemcpyAsync(pos.data(), e.d_pos, 4 * pos.size(), cudaMemcpyDeviceToHost, e.st));
             UG_CK(cudaMemcpyAsync(mom.data(), e.d_mom, 4 * mom.size(), cudaMemcpyDeviceToHost, e.st));
@@ -711,6 +717,27 @@ int run(const Args& A, const std::string& invocation, int verbose) {
                     if (count_hbonds) {
                         n_hbond = 0.;
                         for (float c : col) n_hbond += c;
+                    }
+                }
+                // node-level arrays (rotamer_*, rama_map_potential,
+                // sigmoid_coupling), registered at the first frame
+                for (auto& lg : node_logs) {
+                    int a = lg.off[j], z = lg.off[j + 1];
+                    bool known = false;
+                    for (auto& se : L.series) known = known || se.name == lg.name;
+                    if (!known) {
+                        if (L.buffered != 0) throw Error("node log '" + lg.name + "' appeared after the first frame");
+                        L.add(lg.name, lg.integer ? h5lite::dtype_int(8, true) : h5lite::dtype_float(4),
+                              {uint64_t(z - a)});
+                    }
+                    if (lg.integer) {
+                        std::vector<int64_t> row;
+                        for (int i = a; i < z; ++i) row.push_back(int64_t(lg.values[size_t(i)]));
+                        L.push_vec(lg.name, row);
+                    } else {
+                        std::vector<float> row;
+                        for (int i = a; i < z; ++i) row.push_back(float(lg.values[size_t(i)]));
+                        L.push_vec(lg.name, row);
                     }
                 }
                 if (verbose) {

@@ -458,13 +458,14 @@ struct PasteNode : GNode {
 // (RamaMapPot, src/rama_map_pot.cpp:15-94; LayeredPeriodicSpline2D src/spline.h:444-499)
 __global__ void rama_map_kernel(int n, const int* __restrict__ res, const int* __restrict__ layer,
                                 const int* __restrict__ sys, const float* __restrict__ coeff, int nxp, int nyp,
-                                float scale, const float* __restrict__ rama, float* rs, double* pot) {
+                                float scale, const float* __restrict__ rama, float* rs, double* pot, float* res_log) {
     for (int i = grid_stride_start(); i < n; i += grid_stride()) {
         int r = res[i];
         float x = (rama[2 * r] + 3.14159265358979f) * scale, y = (rama[2 * r + 1] + 3.14159265358979f) * scale;
         float v, dx, dy;
         periodic2d(coeff + size_t(layer[i]) * nxp * nyp, nyp, x, y, v, dx, dy);
         add_energy(pot, sys[i], v);
+        if (res_log) res_log[i] = v;
         atomicAdd(rs + 2 * r, dx * scale);
         atomicAdd(rs + 2 * r + 1, dy * scale);
     }
@@ -474,8 +475,14 @@ struct RamaMapNode : GNode {
     float* coeff = nullptr;
     int n = 0, nxp = 0, nyp = 0;
     float scale = 0;
+    // per-residue potential for the driver's log, when the node logs it
+    // (attribute log_pot, default 1: src/rama_map_pot.cpp:34, 50-54)
+    bool log_pot = true;
+    float* res_log = nullptr;
+    std::vector<int> log_off;
     RamaMapNode(Engine& e, const Groups& g, const std::vector<int>& o) {
         potential = true;
+        log_pot = shared_attr(g, "log_pot", 1.0) != 0.0;
         LayerPool pool;
         std::vector<int> lay;
         auto c = counts(g, "residue_id");
@@ -497,11 +504,23 @@ struct RamaMapNode : GNode {
         layer = e.upload(lay);
         sysv = e.upload(sys_of(offsets(c)));
         coeff = e.upload(pool.coeff);
+        log_off = offsets(c);
     }
     void forward(Engine& e, bool energy) override {
         auto& a = e.arg(*this, 0);
+        float* lg = nullptr;
+        if (e.log_detail && log_pot && n) {
+            if (!res_log) res_log = e.alloc<float>(size_t(n));
+            lg = res_log;
+        }
         rama_map_kernel<<<nblk(n), 256, 0, e.st>>>(n, res, layer, sysv, coeff, nxp, nyp, scale, a.out, a.sens,
-                                                   energy ? e.d_pot + size_t(pot_slot) * e.n_sys : nullptr);
+                                                   energy ? e.d_pot + size_t(pot_slot) * e.n_sys : nullptr, lg);
+    }
+    void detailed_logs(Engine& e, std::vector<Log>& out) override {
+        if (!res_log) return;
+        std::vector<float> v(static_cast<size_t>(n));
+        UG_CK(cudaMemcpy(v.data(), res_log, 4 * v.size(), cudaMemcpyDeviceToHost));
+        out.push_back({"rama_map_potential", std::vector<double>(v.begin(), v.end()), log_off, false});
     }
 };
 
@@ -1401,7 +1420,7 @@ struct CoverageNode : GNode {
 __global__ void sig_coupling_kernel(int n, int n_rt, const int* __restrict__ ctype, const int* __restrict__ sys,
                                     const float* __restrict__ w, const float* __restrict__ scale,
                                     const float* __restrict__ center, const float* __restrict__ sharp,
-                                    const float* __restrict__ in, float* is, double* pot) {
+                                    const float* __restrict__ in, float* is, double* pot, float* res_log) {
     for (int r = grid_stride_start(); r < n; r += grid_stride()) {
         int c = ctype[r];
         const float* wr = w + size_t(c) * n_rt;
@@ -1411,6 +1430,7 @@ __global__ void sig_coupling_kernel(int n, int n_rt, const int* __restrict__ cty
         float v, d;
         csig(wn - center[c], sharp[c], v, d);
         add_energy(pot, sys[r], scale[c] * v);
+        if (res_log) res_log[r] = scale[c] * v;  // src/environment.cpp:893-901
         for (int a = 0; a < n_rt; ++a) atomicAdd(is + size_t(r) * n_rt + a, wr[a] * scale[c] * d);
     }
 }
@@ -1479,6 +1499,8 @@ struct CouplingNode : GNode {
     float *w = nullptr, *scale = nullptr, *center = nullptr, *sharp = nullptr, *coeff = nullptr;
     std::vector<float> h_w, h_a, h_b, h_c, h_coeff;
     float offset = 0, inv_dx = 0, s_scale = 0, s_center = 0, s_sharp = 0, s_hbw = 0;
+    float* res_log = nullptr;  // sigmoid: per-residue energy for the driver's log
+    std::vector<int> log_off;
     CouplingNode(Engine& e, const Groups& g, Kind k, const GNode& in) : kind(k) {
         potential = true;
         h_w = shared_f(g, "weights");
@@ -1497,7 +1519,8 @@ struct CouplingNode : GNode {
             auto ct = cat_idx(g, "coupling_types", nullptr);
             n = int(ct.size());
             ctype = e.upload(ct);
-            sysv = e.upload(sys_of(offsets(counts(g, "coupling_types"))));
+            log_off = offsets(counts(g, "coupling_types"));
+            sysv = e.upload(sys_of(log_off));
             n_indep = int(shared_attr(g, "number_independent_weights"));
             if (k == SIGMOID) {
                 h_a = shared_f(g, "scale");
@@ -1520,11 +1543,24 @@ struct CouplingNode : GNode {
         }
         w = e.upload(h_w);
     }
+    void detailed_logs(Engine&, std::vector<Log>& out) override {
+        if (!res_log) return;
+        std::vector<float> v(static_cast<size_t>(n));
+        UG_CK(cudaMemcpy(v.data(), res_log, 4 * v.size(), cudaMemcpyDeviceToHost));
+        out.push_back({"sigmoid_coupling", std::vector<double>(v.begin(), v.end()), log_off, false});
+    }
     void forward(Engine& e, bool energy) override {
         double* pot = energy ? e.d_pot + size_t(pot_slot) * e.n_sys : nullptr;
         auto& a = e.arg(*this, 0);
-        if (kind == SIGMOID)
-            sig_coupling_kernel<<<nblk(n), 256, 0, e.st>>>(n, n_rt, ctype, sysv, w, scale, center, sharp, a.out, a.sens, pot);
+        if (kind == SIGMOID) {
+            float* lg = nullptr;
+            if (e.log_detail && n) {
+                if (!res_log) res_log = e.alloc<float>(size_t(n));
+                lg = res_log;
+            }
+            sig_coupling_kernel<<<nblk(n), 256, 0, e.st>>>(n, n_rt, ctype, sysv, w, scale, center, sharp, a.out, a.sens,
+                                                           pot, lg);
+        }
         else if (kind == NONLINEAR)
             nl_coupling_kernel<<<nblk(n), 256, 0, e.st>>>(n, n_rt, n_coeff, offset, inv_dx, ctype, sysv, w, coeff, a.out,
                                                           a.sens, pot);
@@ -1828,6 +1864,8 @@ struct RotamerNode : GNode {
         b.marg = e.alloc<float>(size_t(b.n_res) * 8);
         b.n_iter = e.alloc<int>(size_t(e.n_sys));
         b.e11 = e.alloc<double>(size_t(e.n_sys));
+        b.bad_solves = e.alloc<unsigned long long>(size_t(e.n_sys));
+        UG_CK(cudaMemset(b.bad_solves, 0, sizeof(unsigned long long) * size_t(e.n_sys)));
         b.alg_bytes = e.alloc<unsigned long long>(size_t(e.n_sys));
         b.parity = e.alloc<int>(1);
         b.prev_valid = e.alloc<int>(size_t(e.n_sys) * 2);
@@ -1865,9 +1903,50 @@ struct RotamerNode : GNode {
             w[k] = pn.width;
         }
         for (int k = n_prob; k < 4; ++k) { in[k] = in[0]; ins[k] = ins[0]; w[k] = w[0]; }
-        launch_bp(b, hg.g, in, ins, w, n_prob, prev_n_ent, nullptr, energy ? 1 : 0, d_energy, warm_on ? &wd : nullptr,
+        if (e.log_detail && !log_buf) {
+            log_buf = e.alloc<float>(size_t(b.n_res) * (4 + 4));
+            UG_CK(cudaMemset(log_buf, 0, sizeof(float) * size_t(b.n_res) * 8));
+        }
+        DBP bl = b;  // the logging pointers only for this launch
+        if (e.log_detail) {
+            size_t R = size_t(b.n_res);
+            bl.log_fe = log_buf;
+            bl.log_pot = log_buf + R;
+            bl.log_ent = log_buf + 2 * R;
+            bl.log_e11 = log_buf + 3 * R;
+            bl.log_1b = log_buf + 4 * R;
+            logged = true;
+        } else {
+            bl.log_fe = bl.log_pot = bl.log_ent = bl.log_e11 = bl.log_1b = nullptr;
+        }
+        launch_bp(bl, hg.g, in, ins, w, n_prob, prev_n_ent, nullptr, energy ? 1 : 0, d_energy, warm_on ? &wd : nullptr,
                   e.d_pos, e.atom_off_d, e.st);
         if (energy) add_pot(e);
+    }
+    // per-residue decomposition of the last logged evaluation
+    // (src/rotamer.cpp:708-733): free energy, average energy, entropy, the
+    // one-body energy of each input, and the cumulative count of solves that
+    // reached max_iter
+    float* log_buf = nullptr;
+    bool logged = false;
+    void detailed_logs(Engine& e, std::vector<Log>& out) override {
+        std::vector<unsigned long long> bad(static_cast<size_t>(e.n_sys));
+        UG_CK(cudaMemcpy(bad.data(), b.bad_solves, 8 * bad.size(), cudaMemcpyDeviceToHost));
+        std::vector<int> sys_off(static_cast<size_t>(e.n_sys) + 1);
+        for (int s = 0; s <= e.n_sys; ++s) sys_off[size_t(s)] = s;
+        out.push_back({"rotamer_bad_solves_cumulative", std::vector<double>(bad.begin(), bad.end()), sys_off, true});
+        if (!logged) return;
+        size_t R = size_t(b.n_res);
+        std::vector<float> v(R * size_t(4 + n_prob));
+        UG_CK(cudaMemcpy(v.data(), log_buf, 4 * v.size(), cudaMemcpyDeviceToHost));
+        std::vector<int> off(static_cast<size_t>(e.n_sys) + 1, 0);
+        for (int s = 0; s < e.n_sys; ++s) off[size_t(s) + 1] = off[size_t(s)] + n_res_sys[size_t(s)];
+        auto part = [&](size_t k) { return std::vector<double>(v.begin() + long(k * R), v.begin() + long((k + 1) * R)); };
+        out.push_back({"rotamer_free_energy", part(0), off, false});
+        out.push_back({"rotamer_potential", part(1), off, false});
+        out.push_back({"rotamer_entropy", part(2), off, false});
+        for (int k = 0; k < n_prob; ++k)
+            out.push_back({"rotamer_1body_energy" + std::to_string(k), part(size_t(4 + k)), off, false});
     }
     void add_pot(Engine& e);
     void backward(Engine& e) override { launch_edge_scatter(hg.g, e.st); }

@@ -68,6 +68,17 @@ struct GNode {
     virtual void set_buffer_scale(float) {}
     virtual bool set_bp_variant(int) { return false; }
     virtual double kernel_bytes(Engine&) { return 0.0; }
+    // The per-element arrays the reference's node logs at its default log
+    // level, from the last evaluation made with Engine::log_detail set: name,
+    // values of all systems concatenated, per-system offsets (n_sys + 1); an
+    // int64 array when integer is set.
+    struct Log {
+        std::string name;
+        std::vector<double> values;
+        std::vector<int> off;
+        bool integer = false;
+    };
+    virtual void detailed_logs(Engine&, std::vector<Log>&) {}
 };
 
 class Engine {
@@ -173,6 +184,9 @@ public:
 
     size_t device_bytes = 0;
     int launches_per_compute = 0;
+    // evaluations made while set also fill the nodes' log arrays
+    // (GNode::detailed_logs); graphs captured while it is clear never do
+    bool log_detail = false;
     // number of kernel nodes in one captured force evaluation
     int count_launches();
     // per-node device time (ms) of n eager evaluations, CUDA events on the stream

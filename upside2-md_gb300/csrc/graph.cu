@@ -650,6 +650,10 @@ __global__ void bp_mark_kernel(DBP b, DGraph g) {
             b.slot[slot_index(b, r2, r1)] = -2;
         } else if (n1 == 1 && n2 == 1) {
             atomicAdd(&b.e11[b.res_sys[r1]], double(v));
+            if (b.log_e11) {
+                atomicAdd(&b.log_e11[r1], 0.5f * v);
+                atomicAdd(&b.log_e11[r2], 0.5f * v);
+            }
         } else if (n1 == 1) {
             atomicAdd(&b.E1x[r2 * 8 + b.bead_rot[ij.y]], v);
         } else {
@@ -1096,7 +1100,10 @@ __global__ void __launch_bounds__(THREADS) bp_solve_kernel(DBP b, int want_energ
     }
     if (tid == 0 && crank == 0) {
         b.n_iter[s] = iter;
-        if (iter >= b.max_iter - b.chunk - 1) atomicOr(b.status, ST_BP_NOT_CONVERGED);
+        if (iter >= b.max_iter - b.chunk - 1) {
+            atomicOr(b.status, ST_BP_NOT_CONVERGED);
+            if (b.bad_solves) b.bad_solves[s] += 1ull;
+        }
         if (b.warm) {  // running means of the sweep counts of both starts
             float* ws = b.warm_stat + 4 * s;
             float sweeps = float(1 + iter);
@@ -1241,6 +1248,56 @@ void bp_variant_desc(int i, int* cluster, int* lanes, int* threads) {
     *threads = v.threads;
 }
 
+// Per-node decomposition of the solved free energy for the driver's logs
+// (residue_free_energies, residue_entropy<0/1>, rotamer_1body_energy,
+// src/rotamer.cpp:292-320, 451-500, 929-1023): every node's own term plus
+// half of each of its edges' terms, the 1-1 edges included in the free and
+// average energies; and per input, the belief-weighted one-body energies.
+__global__ void bp_node_log_kernel(DBP b, const float* p0, const float* p1, const float* p2, const float* p3, int n_in,
+                                   int w0, int w1, int w2, int w3) {
+    for (int u = grid_stride_start(); u < b.n_res; u += grid_stride()) {
+        int n = b.nrot[u];
+        const float* m = b.marg + u * 8;
+        const float* pr = b.prob + u * 8;
+        float fe = b.eoff[u], pot = b.eoff[u], ent = 0.f;
+        for (int k = 0; k < n; ++k) {
+            fe += m[k] * logf((1e-10f + m[k]) / (1e-10f + pr[k]));
+            pot -= m[k] * logf(1e-10f + pr[k]);
+            ent += m[k] * logf(1e-10f + m[k]);
+        }
+        if (n > 1) {
+            int eb = b.row_ptr[u], ee = min(b.row_ptr[u + 1], b.ent_cap);
+            for (int e = eb; e < ee; ++e) {
+                int v = b.col[e], nv = b.nrot[v];
+                const float* p = b.emarg + size_t(e) * 36;
+                const float* P = b.P + size_t(e) * 36;
+                const float* mv = b.marg + v * 8;
+                float f = 0.f, a = 0.f, h = 0.f;
+                for (int i = 0; i < n; ++i)
+                    for (int j = 0; j < nv; ++j) {
+                        float x = p[i * 6 + j], q = P[i * 6 + j], bb = m[i] * mv[j];
+                        f += x * logf((1e-10f + x) / (1e-10f + q * bb));
+                        a -= x * logf(1e-10f + q);
+                        h += x * logf((1e-10f + x) / (1e-10f + bb));
+                    }
+                fe += 0.5f * f;
+                pot += 0.5f * a;
+                ent += 0.5f * h;
+            }
+        }
+        b.log_fe[u] = fe + b.log_e11[u];
+        b.log_pot[u] = pot + b.log_e11[u];
+        b.log_ent[u] = ent;
+    }
+    const float* pin[4] = {p0, p1, p2, p3};
+    const int w[4] = {w0, w1, w2, w3};
+    for (int i = grid_stride_start(); i < b.n_bead; i += grid_stride()) {
+        int r = b.bead_res[i], l = b.bead_loc[i];
+        float m = b.marg[r * 8 + b.bead_rot[i]];
+        for (int k = 0; k < n_in; ++k) atomicAdd(&b.log_1b[size_t(k) * b.n_res + r], m * pin[k][size_t(l) * w[k]]);
+    }
+}
+
 // bead-edge sensitivities from the marginals and 1-body sensitivities
 // (src/rotamer.cpp:1057-1086)
 __global__ void bp_sens_kernel(DBP b, DGraph g, float* s0, float* s1, float* s2, float* s3, int n_in, int w0,
@@ -1277,6 +1334,10 @@ void launch_bp(DBP& b, const DGraph& g, const float* const* in, float* const* in
     int blocks = 2 * 152;
     // n_ent is rewritten only by the scan below, after this kernel completes
     bp_reset_kernel<<<blocks, 256, 0, st>>>(b);
+    if (b.log_fe) {
+        cudaMemsetAsync(b.log_e11, 0, sizeof(float) * size_t(b.n_res), st);
+        cudaMemsetAsync(b.log_1b, 0, sizeof(float) * size_t(b.n_res) * size_t(n_in), st);
+    }
     (void)prev_n_ent;
     bp_bead_energy_kernel<<<blocks, 256, 0, st>>>(b, in[0], in[1], in[2], in[3], n_in, w[0], w[1], w[2], w[3]);
     bp_mark_kernel<<<blocks, 256, 0, st>>>(b, g);
@@ -1316,6 +1377,8 @@ void launch_bp(DBP& b, const DGraph& g, const float* const* in, float* const* in
         cudaLaunchKernelExC(&cfg, v.fn, args);
     }
     if (timed) cudaEventRecordWithFlags(b.kt_ev[(*b.kt_used)++], st, cudaEventRecordExternal);
+    if (b.log_fe)
+        bp_node_log_kernel<<<blocks, 256, 0, st>>>(b, in[0], in[1], in[2], in[3], n_in, w[0], w[1], w[2], w[3]);
     bp_sens_kernel<<<blocks, 256, 0, st>>>(b, g, in_sens[0], in_sens[1], in_sens[2], in_sens[3], n_in, w[0], w[1],
                                            w[2], w[3]);
     (void)scan_total;

@@ -124,6 +124,11 @@ struct DBP {
     const int* bead_rot;        // bead -> rotamer
     const int* bead_loc;        // bead -> row in the bead node output
     double* e11;                // per system sum of energies of 1-1 bead edges
+    unsigned long long* bad_solves;  // per system: solves that ran into max_iter (cumulative)
+    // per-node decomposition for the driver's logs (null: not computed):
+    // free energy, average energy, entropy (res each), one-body energy of each
+    // input (log_n1b x res), half of the 1-1 edge energies of each node (res)
+    float *log_fe, *log_pot, *log_ent, *log_1b, *log_e11;
     int* status;
     // measurement: running per-system total of the solve kernel's algorithmic
     // bytes (the formula is in bp_solve_kernel), and optional host-side CUDA
