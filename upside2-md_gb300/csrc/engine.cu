@@ -1772,6 +1772,7 @@ struct RotamerNode : GNode {
     bool warm_on = false, warm_alloc = false;
     RotamerNode(Engine& e, const Groups& g, const std::vector<int>& obead, const std::string& bead_node) {
         potential = true;
+        early_args = {0};
         hg.setup(e, IK_ROTAMER, EX_ROTAMER, true, 6, 6, 54, g, "pair_interaction", obead, obead, 96);
         b.damping = float(shared_attr(g, "damping"));
         b.max_iter = int(shared_attr(g, "max_iter"));
@@ -1893,10 +1894,35 @@ struct RotamerNode : GNode {
         b.prev_msg = e.alloc<float>(size_t(cap) * 16);
         if (b.prev_valid) UG_CK(cudaMemset(b.prev_valid, 0, sizeof(int) * 2 * size_t(e.n_sys)));
     }
-    void forward(Engine& e, bool energy) override {
+    // the bead pair list, its energies and the solve's structure need only
+    // the bead positions (argument 0)
+    void forward_early(Engine& e) override {
         auto& beads = e.arg(*this, 0);
         hg.bind(beads, beads);
         hg.search_and_eval(e.st);
+        DBP bl = launch_state(e);
+        launch_bp_structure(bl, hg.g, e.st);
+    }
+    // the bound DBP with the logging pointers of this evaluation
+    DBP launch_state(Engine& e) {
+        if (e.log_detail && !log_buf) {
+            log_buf = e.alloc<float>(size_t(b.n_res) * (4 + 4));
+            UG_CK(cudaMemset(log_buf, 0, sizeof(float) * size_t(b.n_res) * 8));
+        }
+        DBP bl = b;
+        if (e.log_detail) {
+            size_t R = size_t(b.n_res);
+            bl.log_fe = log_buf;
+            bl.log_pot = log_buf + R;
+            bl.log_ent = log_buf + 2 * R;
+            bl.log_e11 = log_buf + 3 * R;
+            bl.log_1b = log_buf + 4 * R;
+        } else {
+            bl.log_fe = bl.log_pot = bl.log_ent = bl.log_e11 = bl.log_1b = nullptr;
+        }
+        return bl;
+    }
+    void forward(Engine& e, bool energy) override {
         n_prob = int(args.size()) - 1;
         if (n_prob < 1 || n_prob > 4) throw Error("rotamer node needs 1 to 4 one-body energy inputs");
         const float* in[4] = {nullptr, nullptr, nullptr, nullptr};
@@ -1909,22 +1935,8 @@ struct RotamerNode : GNode {
             w[k] = pn.width;
         }
         for (int k = n_prob; k < 4; ++k) { in[k] = in[0]; ins[k] = ins[0]; w[k] = w[0]; }
-        if (e.log_detail && !log_buf) {
-            log_buf = e.alloc<float>(size_t(b.n_res) * (4 + 4));
-            UG_CK(cudaMemset(log_buf, 0, sizeof(float) * size_t(b.n_res) * 8));
-        }
-        DBP bl = b;  // the logging pointers only for this launch
-        if (e.log_detail) {
-            size_t R = size_t(b.n_res);
-            bl.log_fe = log_buf;
-            bl.log_pot = log_buf + R;
-            bl.log_ent = log_buf + 2 * R;
-            bl.log_e11 = log_buf + 3 * R;
-            bl.log_1b = log_buf + 4 * R;
-            logged = true;
-        } else {
-            bl.log_fe = bl.log_pot = bl.log_ent = bl.log_e11 = bl.log_1b = nullptr;
-        }
+        DBP bl = launch_state(e);
+        if (e.log_detail) logged = true;
         launch_bp(bl, hg.g, in, ins, w, n_prob, prev_n_ent, nullptr, energy ? 1 : 0, d_energy, warm_on ? &wd : nullptr,
                   e.d_pos, e.atom_off_d, e.st);
         if (energy) add_pot(e);
@@ -2418,13 +2430,25 @@ void Engine::setup_lanes() {
     }
     ev_lane.resize(size_t(kLanes));
     for (auto& x : ev_lane) UG_CK(cudaEventCreateWithFlags(&x, cudaEventDisableTiming));
+    // A node with an early stage (the rotamer node) gets the last lane to
+    // itself, so that stage never queues behind another node's work; the
+    // others continue an argument's lane or take the least-loaded one.
+    int own = -1;
+    for (size_t i = 0; i < n && own < 0; ++i)
+        if (!nodes[i]->early_args.empty() && kLanes > 1) own = int(i);
+    const int shared = own >= 0 ? kLanes - 1 : kLanes;
     std::vector<int> tail(size_t(kLanes), -1), load(size_t(kLanes), 0);
     for (size_t i = 0; i < n; ++i) {
+        if (int(i) == own) {
+            node_lane[i] = kLanes - 1;
+            tail[size_t(kLanes - 1)] = int(i);
+            continue;
+        }
         int lane = -1;
         for (int a : nodes[i]->args)
-            for (int l = 0; l < kLanes && lane < 0; ++l)
+            for (int l = 0; l < shared && lane < 0; ++l)
                 if (tail[size_t(l)] == a) lane = l;
-        if (lane < 0) lane = int(std::min_element(load.begin(), load.end()) - load.begin());
+        if (lane < 0) lane = int(std::min_element(load.begin(), load.begin() + shared) - load.begin());
         node_lane[i] = lane;
         tail[size_t(lane)] = int(i);
         load[size_t(lane)] += 1;
@@ -2435,7 +2459,10 @@ void Engine::compute(bool energy) {
     if (!parallel_nodes) {
         UG_CK(cudaMemsetAsync(d_sens_arena, 0, sens_arena_floats * sizeof(float), st));
         if (energy) UG_CK(cudaMemsetAsync(d_pot, 0, sizeof(double) * size_t(std::max(1, n_pot_slots)) * n_sys, st));
-        for (auto& n : nodes) n->forward(*this, energy);
+        for (auto& n : nodes) {
+            n->forward_early(*this);
+            n->forward(*this, energy);
+        }
         for (size_t i = nodes.size(); i-- > 0;) nodes[i]->backward(*this);
         if (energy) sum_energy_kernel<<<1, 256, 0, st>>>(n_sys, n_pot_slots, d_pot, d_energy);
         UG_CK(cudaGetLastError());
@@ -2451,6 +2478,14 @@ void Engine::compute(bool energy) {
     try {
         for (size_t i = 0; i < n; ++i) {
             st = lanes[size_t(node_lane[i])];
+            auto& ea = nodes[i]->early_args;
+            if (!ea.empty()) {  // the early stage waits for its own arguments only
+                for (int k : ea) {
+                    int a = nodes[i]->args.at(size_t(k));
+                    if (node_lane[size_t(a)] != node_lane[i]) UG_CK(cudaStreamWaitEvent(st, ev_fwd[size_t(a)], 0));
+                }
+                nodes[i]->forward_early(*this);
+            }
             for (int a : nodes[i]->args)
                 if (node_lane[size_t(a)] != node_lane[i]) UG_CK(cudaStreamWaitEvent(st, ev_fwd[size_t(a)], 0));
             nodes[i]->forward(*this, energy);
@@ -2779,6 +2814,7 @@ std::vector<std::pair<std::string, float>> Engine::profile_nodes(int n) {
         size_t k = 0;
         UG_CK(cudaEventRecord(ev[k++], st));
         for (auto& nd : nodes) {
+            nd->forward_early(*this);
             nd->forward(*this, false);
             UG_CK(cudaEventRecord(ev[k++], st));
         }

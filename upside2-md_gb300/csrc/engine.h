@@ -44,6 +44,11 @@ struct GNode {
     int pot_slot = -1;
     virtual ~GNode() {}
     virtual void forward(Engine& e, bool energy) = 0;
+    // Part of the forward work that needs only the arguments listed in
+    // early_args (indices into args): the engine enqueues it once those are
+    // ready, before forward(), which waits for all arguments.
+    std::vector<int> early_args;
+    virtual void forward_early(Engine&) {}
     virtual void backward(Engine&) {}
     virtual std::vector<float> get_param(Engine&) { return {}; }
     virtual void set_param(Engine&, const std::vector<float>&) { throw Error("set_param not supported for this node"); }

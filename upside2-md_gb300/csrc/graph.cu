@@ -1328,18 +1328,16 @@ __global__ void bp_sens_kernel(DBP b, DGraph g, float* s0, float* s1, float* s2,
     }
 }
 
-void launch_bp(DBP& b, const DGraph& g, const float* const* in, float* const* in_sens, const int* w, int n_in,
-               int prev_n_ent, int* scan_total, int want_energy, double* energy_out, const WarmDev* warm,
-               const float* pos, const int* atom_off, cudaStream_t st) {
+// The structure of the solve from the bead pair list alone: residue-pair
+// entries (CSR rows, reverse entries, descriptors), folded 1-rotamer partner
+// energies and the summed pair energies.  It needs no one-body energy, so the
+// engine runs it as soon as the bead positions are known, while the one-body
+// inputs are still being computed.
+void launch_bp_structure(DBP& b, const DGraph& g, cudaStream_t st) {
     int blocks = 2 * 152;
     // n_ent is rewritten only by the scan below, after this kernel completes
     bp_reset_kernel<<<blocks, 256, 0, st>>>(b);
-    if (b.log_fe) {
-        cudaMemsetAsync(b.log_e11, 0, sizeof(float) * size_t(b.n_res), st);
-        cudaMemsetAsync(b.log_1b, 0, sizeof(float) * size_t(b.n_res) * size_t(n_in), st);
-    }
-    (void)prev_n_ent;
-    bp_bead_energy_kernel<<<blocks, 256, 0, st>>>(b, in[0], in[1], in[2], in[3], n_in, w[0], w[1], w[2], w[3]);
+    if (b.log_fe) cudaMemsetAsync(b.log_e11, 0, sizeof(float) * size_t(b.n_res), st);
     bp_mark_kernel<<<blocks, 256, 0, st>>>(b, g);
     int rb = min(4 * 152, (b.n_res * 32 + 255) / 256);
     bp_rows_kernel<0><<<rb, 256, 0, st>>>(b);
@@ -1348,6 +1346,17 @@ void launch_bp(DBP& b, const DGraph& g, const float* const* in, float* const* in
     bp_cap_check_kernel<<<1, 1, 0, st>>>(b);
     bp_entry_init_kernel<<<blocks, 256, 0, st>>>(b);
     bp_edge_energy_kernel<<<blocks, 256, 0, st>>>(b, g);
+}
+
+// The rest, after launch_bp_structure: one-body energies, probabilities,
+// warm start, the solve, the logging decomposition and the sensitivities.
+void launch_bp(DBP& b, const DGraph& g, const float* const* in, float* const* in_sens, const int* w, int n_in,
+               int prev_n_ent, int* scan_total, int want_energy, double* energy_out, const WarmDev* warm,
+               const float* pos, const int* atom_off, cudaStream_t st) {
+    int blocks = 2 * 152;
+    (void)prev_n_ent;
+    if (b.log_fe) cudaMemsetAsync(b.log_1b, 0, sizeof(float) * size_t(b.n_res) * size_t(n_in), st);
+    bp_bead_energy_kernel<<<blocks, 256, 0, st>>>(b, in[0], in[1], in[2], in[3], n_in, w[0], w[1], w[2], w[3]);
     bp_prob_kernel<<<blocks, 256, 0, st>>>(b);
     if (warm) launch_warm_start(*warm, pos, atom_off, b.res_off, b.prob, b.nrot, b.n_sys, b.n_res, st);
     size_t smem = bp_solve_smem_bytes(b.max_res_sys);
