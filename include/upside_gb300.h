@@ -43,7 +43,20 @@ int ug_evaluate(UgBatch* b, double* energy, float* deriv);
 int ug_set_thermostat(UgBatch* b, const float* temperature, const uint32_t* seed);
 int ug_set_round(UgBatch* b, const uint64_t* round);
 
-/* Advance n_round rounds of {thermostat; 3 x (force, p -= dt F, x += dt p)}.
+/* Integrator of the rounds: multistep = 0 the three-stage cycle (inner_step
+ * must be 3); multistep = 1 the reference's multistep integrator
+ * (src/deriv_engine.cpp:333-351): per round the forces of the slow nodes
+ * (config attribute integrator_level 1) kick the momenta once by inner_step
+ * dt, then inner_step stages of the fast nodes' forces (level 0) move them.
+ * The thermostat's time step is inner_step dt per round. */
+int ug_set_integrator(UgBatch* b, int multistep, int inner_step);
+/* dE/dx of the nodes of one integrator level (0 fast, 1 slow) at the current
+ * positions: the forces each part of a multistep round uses; deriv is
+ * (atom_total, 3).  The two levels sum to ug_evaluate's derivative. */
+int ug_level_forces(UgBatch* b, int level, float* deriv);
+
+/* Advance n_round rounds of {thermostat; 3 x (force, p -= dt F, x += dt p)}
+ * (or the multistep round, ug_set_integrator).
  * use_graph != 0 replays a captured CUDA graph of graph_rounds rounds. */
 int ug_run(UgBatch* b, int n_round, float dt, float timescale, int use_graph, int graph_rounds);
 

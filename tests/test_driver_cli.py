@@ -38,7 +38,7 @@ def test_arguments(built, capfd):
     assert _main(["--duration", "1", "--frame-interval"]) == 1
     assert "Missing a value" in capfd.readouterr().err
     for extra, word in ((["--monte-carlo-interval", "1"], "Monte Carlo"),
-                        (["--integrator", "mv"], "integrator"),
+                        (["--integrator", "leapfrog"], "integrator"),
                         (["--curvature-changer-interval", "2"], "curvature"),
                         (["--potential-deriv-agreement"], "deriv-agreement"),
                         (["--log-level", "loud"], "log-level")):

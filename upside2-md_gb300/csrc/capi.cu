@@ -286,6 +286,25 @@ int ug_set_thermostat(UgBatch* b, const float* temperature, const uint32_t* seed
     GUARD_END(1)
 }
 
+int ug_level_forces(UgBatch* b, int level, float* deriv) {
+    GUARD_BEGIN
+    if (level != 0 && level != 1) throw ug::Error("integrator level must be 0 or 1");
+    b->e->compute_checked(false, level);
+    b->e->get_deriv(deriv);
+    return 0;
+    GUARD_END(1)
+}
+
+int ug_set_integrator(UgBatch* b, int multistep, int inner_step) {
+    GUARD_BEGIN
+    if (inner_step < 1) throw ug::Error("inner_step must be at least 1");
+    if (!multistep && inner_step != 3) throw ug::Error("the three-stage integrator has inner_step 3");
+    b->e->multistep = multistep != 0;
+    b->e->inner_step = inner_step;
+    return 0;
+    GUARD_END(1)
+}
+
 int ug_set_round(UgBatch* b, const uint64_t* round) {
     GUARD_BEGIN
     UG_CK(cudaMemcpyAsync(b->e->d_round, round, sizeof(uint64_t) * size_t(b->e->n_sys), cudaMemcpyHostToDevice, b->e->st));

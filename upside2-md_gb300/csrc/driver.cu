@@ -359,9 +359,13 @@ bool has_hbond_energy(Engine& e) {
 }
 
 int run(const Args& A, const std::string& invocation, int verbose) {
-    const int inner_step = 3;
-    if (!A.integrator.empty() && A.integrator != "v")
-        throw Error("integrator '" + A.integrator + "' is not available in the GPU driver (only verlet, 'v')");
+    // "mv": the multistep integrator with --inner-step fast stages per round
+    // (src/main.cpp:552-555); otherwise the three-stage cycle
+    if (!A.integrator.empty() && A.integrator != "v" && A.integrator != "mv")
+        throw Error("Illegal value for --integrator: '" + A.integrator + "' (v or mv)");
+    const bool multistep = A.integrator == "mv";
+    const int inner_step = multistep ? A.inner_step : 3;
+    if (inner_step < 1) throw Error("--inner-step must be at least 1");
     if (A.mc_interval > 0.) throw Error("Monte Carlo moves (--monte-carlo-interval) are not available in the GPU driver");
     if (A.curvature_interval != 0.) throw Error("--curvature-changer-interval is not available in the GPU driver");
     if (A.deriv_agreement) throw Error("--potential-deriv-agreement is not available in the GPU driver");
@@ -551,6 +555,8 @@ int run(const Args& A, const std::string& invocation, int verbose) {
         UG_CK(cudaMemcpyAsync(e.d_round, rounds.data(), sizeof(unsigned long long) * rounds.size(),
                               cudaMemcpyHostToDevice, e.st));
         e.thermo_span = float(thermo_interval);
+        e.multistep = multistep;
+        e.inner_step = inner_step;
         // a fresh start thermalises the zero momenta once (src/main.cpp:787-791)
         if (!A.restart_momentum) e.thermalize(dt, float(A.thermostat_timescale));
         e.sync();
@@ -642,6 +648,16 @@ int run(const Args& A, const std::string& invocation, int verbose) {
         }
     };
 
+    if (verbose && multistep) {  // src/deriv_engine.cpp:214-236
+        Engine& e = *engines[0];
+        printf("\nUsing the multi-step integrator\nslow motion\n  time step: %g\n  potential terms:\n",
+               double(dt) * inner_step);
+        for (auto& n : e.nodes)
+            if (n->potential && n->level == 1) printf("    %s\n", n->name.c_str());
+        printf("\nfast motion\n  time step: %g\n  potential terms:\n", double(dt));
+        for (auto& n : e.nodes)
+            if (n->potential && n->level == 0) printf("    %s\n", n->name.c_str());
+    }
     if (verbose) {
         printf("\n");
         for (int s = 0; s < n_sys; ++s) printf("%s\nn_atom %i\n\n", sys[s].config.c_str(), sys[s].n_atom);

@@ -2175,6 +2175,10 @@ __global__ void sum_energy_kernel(int n_sys, int n_slots, const double* __restri
 }
 
 // p -= dt F ; x += dt p   (integration_cycle, src/deriv_engine.cpp:317-331)
+// p -= h F  (the multistep integrator's slow-force kick)
+__global__ void kick_kernel(int n, float h, const float* __restrict__ f, float* __restrict__ mom) {
+    for (int i = grid_stride_start(); i < n; i += grid_stride()) mom[i] -= h * f[i];
+}
 __global__ void integrate_kernel(int n, float dt, const float* __restrict__ f, float* __restrict__ mom, float* __restrict__ pos) {
     for (int i = grid_stride_start(); i < n; i += grid_stride()) {
         float p = mom[i] - dt * f[i];
@@ -2347,9 +2351,32 @@ Engine::Engine(const std::vector<std::string>& paths, const std::vector<int>& n_
         }
         n->name = nm;
         n->args = a;
+        n->level = int(shared_attr(g, "integrator_level", 2.0));
         if (n->potential) n->pot_slot = n_pot_slots++;
         index[nm] = int(nodes.size());
         nodes.push_back(std::move(n));
+    }
+    // integrator levels (build_integrator_levels, src/deriv_engine.cpp:180-212):
+    // a potential keeps its attribute (0 when missing or out of range); a
+    // coordinate node folds its consumers' levels, consumers first: all slow
+    // 1, all fast 0, mixed -1 (computed at both)
+    {
+        std::vector<std::vector<int>> cons(nodes.size());
+        for (size_t i = 0; i < nodes.size(); ++i)
+            for (int a : nodes[i]->args) cons[size_t(a)].push_back(int(i));
+        for (auto& n : nodes)
+            if (n->potential && (n->level >= 2 || n->level < 0)) n->level = 0;
+        nodes[0]->level = 2;  // pos: no attribute
+        for (size_t i = nodes.size(); i-- > 0;) {
+            auto& n = *nodes[i];
+            if (n.potential) continue;
+            for (int c : cons[i]) {
+                int l = nodes[size_t(c)]->level;
+                if (l == 1) n.level = n.level <= 0 ? -1 : 1;
+                else if (l == 0) n.level = (n.level == 1 || n.level == -1) ? -1 : 0;
+                else n.level = -1;
+            }
+        }
     }
     // node output / sensitivity arenas
     size_t tot = 0;
@@ -2455,15 +2482,18 @@ void Engine::setup_lanes() {
     }
 }
 
-void Engine::compute(bool energy) {
+void Engine::compute(bool energy, int level) {
+    auto runs = [&](size_t i) { return level < 0 || nodes[i]->level == level || nodes[i]->level == -1; };
     if (!parallel_nodes) {
         UG_CK(cudaMemsetAsync(d_sens_arena, 0, sens_arena_floats * sizeof(float), st));
         if (energy) UG_CK(cudaMemsetAsync(d_pot, 0, sizeof(double) * size_t(std::max(1, n_pot_slots)) * n_sys, st));
-        for (auto& n : nodes) {
-            n->forward_early(*this);
-            n->forward(*this, energy);
+        for (size_t i = 0; i < nodes.size(); ++i) {
+            if (!runs(i)) continue;
+            nodes[i]->forward_early(*this);
+            nodes[i]->forward(*this, energy);
         }
-        for (size_t i = nodes.size(); i-- > 0;) nodes[i]->backward(*this);
+        for (size_t i = nodes.size(); i-- > 0;)
+            if (runs(i)) nodes[i]->backward(*this);
         if (energy) sum_energy_kernel<<<1, 256, 0, st>>>(n_sys, n_pot_slots, d_pot, d_energy);
         UG_CK(cudaGetLastError());
         return;
@@ -2476,7 +2506,10 @@ void Engine::compute(bool energy) {
     for (size_t l = 1; l < lanes.size(); ++l) UG_CK(cudaStreamWaitEvent(lanes[l], ev_lane[0], 0));
     size_t n = nodes.size();
     try {
+        // a node that runs at this level only takes arguments that run too,
+        // and waits only for consumers that run
         for (size_t i = 0; i < n; ++i) {
+            if (!runs(i)) continue;
             st = lanes[size_t(node_lane[i])];
             auto& ea = nodes[i]->early_args;
             if (!ea.empty()) {  // the early stage waits for its own arguments only
@@ -2492,9 +2525,11 @@ void Engine::compute(bool energy) {
             UG_CK(cudaEventRecord(ev_fwd[i], st));
         }
         for (size_t i = n; i-- > 0;) {
+            if (!runs(i)) continue;
             st = lanes[size_t(node_lane[i])];
             for (int c : consumers[i])
-                if (node_lane[size_t(c)] != node_lane[i]) UG_CK(cudaStreamWaitEvent(st, ev_bwd[size_t(c)], 0));
+                if (runs(size_t(c)) && node_lane[size_t(c)] != node_lane[i])
+                    UG_CK(cudaStreamWaitEvent(st, ev_bwd[size_t(c)], 0));
             nodes[i]->backward(*this);
             UG_CK(cudaEventRecord(ev_bwd[i], st));
         }
@@ -2515,7 +2550,7 @@ void Engine::thermalize(float dt, float timescale) {
     // (3 x interval) x dt in FP32, the reference's thermostat time step
     // (src/main.cpp:780)
     thermostat_kernel<<<nblk(atom_total), 256, 0, st>>>(n_sys, atom_off_d, atom_sys_d, atom_total,
-                                                        (3.f * thermo_span) * dt, timescale, d_temp, d_seed, d_round,
+                                                        (float(inner_step) * thermo_span) * dt, timescale, d_temp, d_seed, d_round,
                                                         d_mom);
     round_advance_kernel<<<1, 256, 0, st>>>(n_sys, d_round);
 }
@@ -2527,6 +2562,17 @@ void Engine::recenter(bool xy_only) {
 
 void Engine::round(float dt, float timescale, bool thermostat) {
     if (thermostat) thermalize(dt, timescale);
+    if (multistep) {
+        compute(false, 1);  // slow forces: one kick of inner_step dt
+        kick_kernel<<<nblk(3LL * atom_total), 256, 0, st>>>(3 * atom_total, float(inner_step) * dt, nodes[0]->sens,
+                                                            d_mom);
+        for (int stage = 0; stage < inner_step; ++stage) {
+            compute(false, 0);
+            integrate_kernel<<<nblk(3LL * atom_total), 256, 0, st>>>(3 * atom_total, dt, nodes[0]->sens, d_mom, d_pos);
+        }
+        UG_CK(cudaGetLastError());
+        return;
+    }
     for (int stage = 0; stage < 3; ++stage) {
         compute(false);
         integrate_kernel<<<nblk(3LL * atom_total), 256, 0, st>>>(3 * atom_total, dt, nodes[0]->sens, d_mom, d_pos);
@@ -2534,9 +2580,9 @@ void Engine::round(float dt, float timescale, bool thermostat) {
     UG_CK(cudaGetLastError());
 }
 
-void Engine::compute_checked(bool energy) {
+void Engine::compute_checked(bool energy, int level) {
     for (int attempt = 0; attempt < 8; ++attempt) {
-        compute(energy);
+        compute(energy, level);
         int s = status(true);
         if (!(s & (ST_EDGE_OVERFLOW | ST_RES_EDGE_OVERFLOW))) return;
         bool grew = false;
@@ -2603,7 +2649,7 @@ void Engine::run_rounds(int n_round, float dt, float timescale, bool use_graph, 
         UG_CK(cudaMemcpyAsync(snap_round, d_round, 8 * size_t(n_sys), cudaMemcpyDeviceToDevice, st));
         if (use_graph && k == graph_rounds) {
             if (!graph_exec || this->graph_rounds != graph_rounds || graph_dt != dt || graph_timescale != timescale ||
-                graph_span != thermo_span || graph_timed)
+                graph_span != thermo_span || graph_multistep != multistep || graph_inner != inner_step || graph_timed)
                 capture(dt, timescale, graph_rounds);
             launch_graph();
         } else {
@@ -2646,6 +2692,8 @@ void Engine::capture(float dt, float timescale, int rounds) {
     graph_dt = dt;
     graph_timescale = timescale;
     graph_span = thermo_span;
+    graph_multistep = multistep;
+    graph_inner = inner_step;
 }
 void Engine::launch_graph() { UG_CK(cudaGraphLaunch(graph_exec, st)); }
 

@@ -42,6 +42,9 @@ struct GNode {
     float* out = nullptr;  // total*width
     float* sens = nullptr;
     int pot_slot = -1;
+    // multistep integrator level: 1 slow, 0 fast, -1 both (coordinate nodes
+    // feeding both); from the config attribute integrator_level
+    int level = 0;
     virtual ~GNode() {}
     virtual void forward(Engine& e, bool energy) = 0;
     // Part of the forward work that needs only the arguments listed in
@@ -122,8 +125,16 @@ public:
     GNode& node(const std::string& name);
     GNode& arg(const GNode& n, int i) { return *nodes[size_t(n.args.at(size_t(i)))]; }
 
-    // enqueue one force evaluation (forward + adjoint) on the stream
-    void compute(bool energy);
+    // enqueue one force evaluation (forward + adjoint) on the stream; with
+    // level 0 or 1 only the nodes of that integrator level (and those of both)
+    // run, so the position sensitivity holds that level's forces
+    void compute(bool energy, int level = -2);
+    // Multistep integrator (the reference's integration_cycle with
+    // inner_step, src/deriv_engine.cpp:333-351): per round one slow-force
+    // kick of inner_step dt, then inner_step fast stages.  Off: the plain
+    // three-stage cycle.  inner_step also sets the thermostat time step.
+    bool multistep = false;
+    int inner_step = 3;
     // one integration round: thermostat, then 3 x {compute; p -= dt F; x += dt p}
     void round(float dt, float timescale, bool thermostat);
     // the thermostat alone (one invocation: counters advance); its time step
@@ -139,7 +150,7 @@ public:
     void energies(double* e);               // n_sys, valid after compute(true)
     int status(bool clear);
     // evaluate with automatic growth of pair-list storage on overflow
-    void compute_checked(bool energy);
+    void compute_checked(bool energy, int level = -2);
     void sync();
 
     // CUDA graph of `rounds_per_graph` integration rounds
@@ -156,6 +167,8 @@ public:
     std::vector<cudaEvent_t> ev_fwd, ev_bwd, ev_lane;
     void setup_lanes();
     float graph_dt = 0.f, graph_timescale = 0.f, graph_span = 1.f;  // of the captured graph
+    bool graph_multistep = false;
+    int graph_inner = 3;
     // integration rounds with overflow recovery (see engine.cu); with
     // thermo_interval > 1 the thermostat runs only in rounds whose number
     // (first_round + index) is a multiple of it, and no graph is used

@@ -48,6 +48,8 @@ def lib():
         L.ug_evaluate.argtypes = [vp, vp, vp]
         L.ug_set_thermostat.argtypes = [vp, vp, vp]
         L.ug_set_round.argtypes = [vp, vp]
+        L.ug_set_integrator.argtypes = [vp, ip, ip]
+        L.ug_level_forces.argtypes = [vp, ip, vp]
         L.ug_run.argtypes = [vp, ip, ctypes.c_float, ctypes.c_float, ip, ip]
         L.ug_node_dims.argtypes = [vp, cp, vp, vp]
         L.ug_node_output.argtypes = [vp, cp, vp, ip]
@@ -258,6 +260,17 @@ class Batch:
     def set_round(self, rounds):
         r = np.ascontiguousarray(rounds, dtype=np.uint64)
         self._chk(lib().ug_set_round(self.h, r.ctypes.data))
+
+    def set_integrator(self, multistep=False, inner_step=3):
+        """The three-stage cycle, or the multistep integrator: per round a
+        slow-force kick of inner_step dt, then inner_step fast stages."""
+        self._chk(lib().ug_set_integrator(self.h, int(bool(multistep)), int(inner_step)))
+
+    def level_forces(self, level):
+        """dE/dx of the integrator level's nodes (0 fast, 1 slow)."""
+        d = np.zeros((self.atom_total, 3), np.float32)
+        self._chk(lib().ug_level_forces(self.h, int(level), d.ctypes.data))
+        return d
 
     def run(self, n_round, dt=0.009, timescale=5.0, use_graph=True, graph_rounds=1):
         self._chk(lib().ug_run(self.h, int(n_round), float(dt), float(timescale), int(use_graph), int(graph_rounds)))
