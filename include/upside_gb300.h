@@ -84,6 +84,16 @@ int ug_param_deriv(UgBatch* b, const char* node, float* deriv, int n);
  * (src/main.cpp:243-316).  accepted[k] receives 0/1. */
 int ug_replica_exchange(UgBatch* b, int n_pairs, const int* pairs, uint32_t seed, uint64_t round, int* accepted);
 
+/* Monte Carlo moves over the batch (the reference's MultipleMonteCarloSampler,
+ * src/monte_carlo_sampler.cpp:248-308): for every system with
+ * /input/pivot_moves, then every system with /input/jump_moves, one move
+ * drawn from the sampler's random stream keyed by the system's thermostat
+ * seed and `round`, accepted by the Metropolis test on the energy change at
+ * the system's temperature (rejected moves are undone).  accepted[2*s + k]
+ * (may be NULL): 1 accepted, 0 rejected, -1 system s has no sampler k
+ * (k = 0 pivot, 1 jump). */
+int ug_monte_carlo(UgBatch* b, uint64_t round, int* accepted);
+
 /* status bits: 1 pair list overflow (grown automatically), 2 BP hit max_iter,
  * 4 residue-pair storage overflow */
 int ug_status(UgBatch* b, int clear);

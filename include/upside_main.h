@@ -6,8 +6,8 @@
  * to --output / --output-base files), return value 0 on success, 1 on a bad
  * argument or a failed run (message on stderr).  The GPU driver runs on the
  * current CUDA device; options of the reference that it does not support
- * (--monte-carlo-interval, --curvature-changer-interval,
- * --potential-deriv-agreement) are refused with an error. */
+ * (--curvature-changer-interval, --potential-deriv-agreement) are refused
+ * with an error. */
 #ifndef UPSIDE_GB300_MAIN_H
 #define UPSIDE_GB300_MAIN_H
 #ifdef __cplusplus

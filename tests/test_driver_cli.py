@@ -37,8 +37,7 @@ def test_arguments(built, capfd):
     assert "invalid float" in capfd.readouterr().err
     assert _main(["--duration", "1", "--frame-interval"]) == 1
     assert "Missing a value" in capfd.readouterr().err
-    for extra, word in ((["--monte-carlo-interval", "1"], "Monte Carlo"),
-                        (["--integrator", "leapfrog"], "integrator"),
+    for extra, word in ((["--integrator", "leapfrog"], "integrator"),
                         (["--curvature-changer-interval", "2"], "curvature"),
                         (["--potential-deriv-agreement"], "deriv-agreement"),
                         (["--log-level", "loud"], "log-level")):

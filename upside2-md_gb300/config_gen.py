@@ -165,13 +165,18 @@ class _Cfg:
 
 
 def write_config(path, seq, seed, chain_first_residue=(), pos=None, environment_potential_type=1,
-                 damping=0.4, chain_offsets=None, params=None, bp_tol=1e-3):
+                 damping=0.4, chain_offsets=None, params=None, bp_tol=1e-3, moves=False,
+                 jump_length_scale=5., jump_rotation_scale=30.):
     """Write an ff_2.1 `.up` file for `seq` (list of 3-letter codes).
 
     chain_first_residue: residue indices (excluding 0) where new chains start.
     pos: optional (n_atom,3) initial coordinates; otherwise random_initial_config
       per chain, chains translated by `chain_offsets` (n_chains,3) if given.
     bp_tol: the rotamer BP convergence tolerance (the recipe's 1e-3).
+    moves: write the Monte Carlo move tables as the reference's config script
+      does (py/upside_config.py:2520-2552): jump moves of whole chains for
+      several chains (widths jump_length_scale in angstrom and
+      jump_rotation_scale in degrees), pivot moves otherwise.
     """
     P = load_params(params)
     rng = np.random.RandomState(seed)
@@ -494,6 +499,23 @@ def write_config(path, seq, seed, chain_first_residue=(), pos=None, environment_
     g = c.grp("affine_alignment", ["pos"])
     c.ds(g + "/atoms", np.column_stack((N_id, N_id + 1, N_id + 2)))
     c.ds(g + "/ref_geom", ref_geom)
+
+    if moves:
+        if c.n_chains > 1:
+            starts = np.append(c.chain_starts, n_atom)
+            ranges = np.array([[starts[i], starts[i + 1]] for i in range(c.n_chains)], dtype=np.int32)
+            w.dataset("/input/jump_moves/atom_range", ranges)
+            w.dataset("/input/jump_moves/sigma_trans", np.full(len(ranges), jump_length_scale, dtype=np.float32))
+            w.dataset("/input/jump_moves/sigma_rot",
+                      np.full(len(ranges), jump_rotation_scale * np.pi / 180., dtype=np.float32))
+        else:
+            inner = np.array([-1 not in tuple(x) for x in id3])
+            piv = id3[inner]
+            w.dataset("/input/pivot_moves/proposal_pot", maps)
+            w.dataset("/input/pivot_moves/pivot_atom", piv.astype(np.int32))
+            w.dataset("/input/pivot_moves/pivot_restype", np.arange(maps.shape[0])[inner].astype(np.int32))
+            w.dataset("/input/pivot_moves/pivot_range",
+                      np.column_stack((piv[:, 4] + 1, np.full(len(piv), n_atom))).astype(np.int32))
 
     w.save(path)
     return np.asarray(pos, dtype=np.float32)

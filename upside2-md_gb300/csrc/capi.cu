@@ -8,6 +8,7 @@
 #include <vector>
 
 #include "engine.h"
+#include "mc.h"
 #include "warm.h"
 #include "../../include/engine_c_library.h"
 #include "../../include/upside_gb300.h"
@@ -45,6 +46,8 @@ struct DerivEngine {
 };
 struct UgBatch {
     std::unique_ptr<Engine> e;
+    std::vector<std::string> paths;       // the systems' configurations
+    std::unique_ptr<ug::McSampler> mc;    // their Monte Carlo moves, read at first use
     // measured kernel over the last ug_bench: device ms, launches, algorithmic bytes
     double kt_ms = 0.0, kt_bytes = 0.0;
     long long kt_launches = 0;
@@ -234,6 +237,7 @@ UgBatch* ug_create(int n_sys, const char* const* paths, const int* n_atom) {
     std::vector<int> na(n_atom, n_atom + n_sys);
     auto* b = new UgBatch;
     b->e.reset(new Engine(p, na));
+    b->paths = p;
     return b;
     GUARD_END(nullptr)
 }
@@ -291,6 +295,14 @@ int ug_level_forces(UgBatch* b, int level, float* deriv) {
     if (level != 0 && level != 1) throw ug::Error("integrator level must be 0 or 1");
     b->e->compute_checked(false, level);
     b->e->get_deriv(deriv);
+    return 0;
+    GUARD_END(1)
+}
+
+int ug_monte_carlo(UgBatch* b, uint64_t round, int* accepted) {
+    GUARD_BEGIN
+    if (!b->mc) b->mc.reset(new ug::McSampler(*b->e, b->paths));
+    b->mc->step(round, accepted);
     return 0;
     GUARD_END(1)
 }

@@ -1,6 +1,7 @@
 // Device math shared by the sm_103a kernels: small vector algebra, the
 // clamped / periodic cubic B-splines, compact sigmoid.  FP32 throughout.
 #pragma once
+#include <cstdint>
 #include <cuda_runtime.h>
 
 namespace ug {
@@ -133,6 +134,42 @@ __device__ __forceinline__ bool acceptable_ids(int rule, int a, int b) {
     if (rule == 0) return (unsigned(a) >> 4) != (unsigned(b) >> 4);
     if (rule == 1) return (a - b > 1) || (b - a > 1);
     return (a - b > 2) || (b - a > 2);
+}
+
+// Threefry-4x32-20 (Salmon et al. 2011): the counter-based generator of the
+// reference's random streams (src/random.h:19-67), key (seed, stream, 0, 0)
+__device__ __forceinline__ uint32_t rotl32(uint32_t x, int r) { return (x << r) | (x >> (32 - r)); }
+__device__ inline void threefry4x32(const uint32_t c[4], const uint32_t k[4], uint32_t out[4]) {
+    const int R[8][2] = {{10, 26}, {11, 21}, {13, 27}, {23, 5}, {6, 20}, {17, 11}, {25, 10}, {18, 20}};
+    uint32_t ks[5] = {k[0], k[1], k[2], k[3], 0x1BD11BDAu ^ k[0] ^ k[1] ^ k[2] ^ k[3]};
+    uint32_t x[4];
+    for (int i = 0; i < 4; ++i) x[i] = c[i] + ks[i];
+#pragma unroll
+    for (int r = 0; r < 20; ++r) {
+        if (r % 2 == 0) {
+            x[0] += x[1]; x[1] = rotl32(x[1], R[r % 8][0]); x[1] ^= x[0];
+            x[2] += x[3]; x[3] = rotl32(x[3], R[r % 8][1]); x[3] ^= x[2];
+        } else {
+            x[0] += x[3]; x[3] = rotl32(x[3], R[r % 8][0]); x[3] ^= x[0];
+            x[2] += x[1]; x[1] = rotl32(x[1], R[r % 8][1]); x[1] ^= x[2];
+        }
+        if (r % 4 == 3) {
+            uint32_t s = uint32_t(r / 4 + 1);
+            for (int i = 0; i < 4; ++i) x[i] += ks[(s + uint32_t(i)) % 5];
+            x[3] += s;
+        }
+    }
+    for (int i = 0; i < 4; ++i) out[i] = x[i];
+}
+// uniform in (0, 1] (r123::u01<float>) and a Box-Muller pair from two words
+// (r123::boxmuller: angle from the signed word, radius from the unsigned one)
+__device__ __forceinline__ float u01f(uint32_t b) { return float(b) * (1.f / 4294967296.f) + (0.5f / 4294967296.f); }
+__device__ __forceinline__ void box_muller(uint32_t b0, uint32_t b1, float& x, float& y) {
+    const float PIf = 3.1415926535897932f;
+    float a = PIf * (float(int32_t(b0)) * (1.f / 2147483648.f) + (0.5f / 2147483648.f));
+    float r = sqrtf(-2.f * logf(u01f(b1)));
+    x = sinf(a) * r;
+    y = cosf(a) * r;
 }
 
 __device__ __forceinline__ int grid_stride_start() { return blockIdx.x * blockDim.x + threadIdx.x; }

@@ -32,6 +32,7 @@
 
 #include "engine.h"
 #include "h5lite.h"
+#include "mc.h"
 
 using ug::Engine;
 using ug::Error;
@@ -366,7 +367,6 @@ int run(const Args& A, const std::string& invocation, int verbose) {
     const bool multistep = A.integrator == "mv";
     const int inner_step = multistep ? A.inner_step : 3;
     if (inner_step < 1) throw Error("--inner-step must be at least 1");
-    if (A.mc_interval > 0.) throw Error("Monte Carlo moves (--monte-carlo-interval) are not available in the GPU driver");
     if (A.curvature_interval != 0.) throw Error("--curvature-changer-interval is not available in the GPU driver");
     if (A.deriv_agreement) throw Error("--potential-deriv-agreement is not available in the GPU driver");
     int log_level = 1;
@@ -439,6 +439,8 @@ int run(const Args& A, const std::string& invocation, int verbose) {
     }
     int replica_interval = 0;
     if (A.replica_interval != 0.) replica_interval = int(std::max(1., A.replica_interval / (inner_step * dt)));
+    // src/main.cpp:567-569
+    const int mc_interval = A.mc_interval > 0. ? std::max(1, int(A.mc_interval / (inner_step * dt))) : 0;
 
     // ---- configurations, positions, momenta; systems grouped into batches
     std::vector<std::vector<float>> pos0(static_cast<size_t>(n_sys)), mom0(static_cast<size_t>(n_sys));
@@ -571,6 +573,16 @@ int run(const Args& A, const std::string& invocation, int verbose) {
         }
     };
 
+    // ---- Monte Carlo moves (src/main.cpp:838-841): per engine, from each
+    // system's /input/pivot_moves and /input/jump_moves
+    std::vector<std::unique_ptr<ug::McSampler>> samplers;
+    if (mc_interval)
+        for (size_t k = 0; k < engines.size(); ++k) {
+            std::vector<std::string> paths;
+            for (int s : members[k]) paths.push_back(sys[size_t(s)].config);
+            samplers.emplace_back(new ug::McSampler(*engines[k], paths));
+        }
+
     // ---- replica exchange (src/main.cpp:147-317)
     std::vector<std::vector<SwapPair>> swap_sets;
     std::vector<std::vector<std::pair<int, int>>> participating(static_cast<size_t>(n_sys));  // (set, pair)
@@ -631,6 +643,11 @@ int run(const Args& A, const std::string& invocation, int verbose) {
             L.add("replica_cumulative_swaps", h5lite::dtype_int(4, true), {uint64_t(participating[s].size()), 2});
         }
         L.add("temperature", h5lite::dtype_float(8), {1});
+        if (mc_interval) {  // [successes, attempts] since the previous frame
+            auto& smp = *samplers[size_t(sys[s].eng)];
+            if (smp.has_pivot[size_t(sys[s].local)]) L.add("pivot_stats", h5lite::dtype_int(4, true), {2});
+            if (smp.has_jump[size_t(sys[s].local)]) L.add("jump_stats", h5lite::dtype_int(4, true), {2});
+        }
         ug::GNode* hbn = find_node(*engines[size_t(sys[s].eng)], "protein_hbond");
         if (log_level >= 1 && hbn) {
             int ne = hbn->off[size_t(sys[s].local) + 1] - hbn->off[size_t(sys[s].local)];
@@ -724,6 +741,15 @@ int run(const Args& A, const std::string& invocation, int verbose) {
                     L.push("replica_cumulative_swaps", cum.data());
                 }
                 L.push_vec("temperature", std::vector<double>{double(S.T)});
+                if (mc_interval) {
+                    auto& smp = *samplers[k];
+                    for (int q = 0; q < 2; ++q) {
+                        if (!(q == 0 ? smp.has_pivot : smp.has_jump)[j]) continue;
+                        L.push_vec(q == 0 ? "pivot_stats" : "jump_stats",
+                                   std::vector<int32_t>{int32_t(smp.success[q][j]), int32_t(smp.attempt[q][j])});
+                        smp.success[q][j] = smp.attempt[q][j] = 0;
+                    }
+                }
                 double n_hbond = -1.;
                 if (hbn) {
                     int r0 = hbn->off[j], r1 = hbn->off[j + 1];
@@ -862,6 +888,9 @@ int run(const Args& A, const std::string& invocation, int verbose) {
                 break;
             }
             unsigned long long nr = round_num;
+            // Monte Carlo moves, not at round 0 (src/main.cpp:941-944)
+            if (nr && mc_interval && nr % (unsigned long long)mc_interval == 0)
+                for (auto& smp : samplers) smp->step(nr, nullptr);
             if (nr % (unsigned long long)frame_interval == 0) log_frame();
             // the rounds up to the next host event
             unsigned long long end = std::min<unsigned long long>(n_round, (nr / frame_interval + 1) * frame_interval);
@@ -872,6 +901,7 @@ int run(const Args& A, const std::string& invocation, int verbose) {
                 brk = r;
                 end = std::min(end, brk + 1);
             }
+            if (mc_interval) end = std::min(end, (nr / mc_interval + 1) * (unsigned long long)mc_interval);
             if (annealing) {
                 if (nr % (unsigned long long)thermo_interval == 0) {
                     for (auto& S : sys) S.T = float(anneal_temp(S.T0, double(inner_step) * double(dt) * double(nr + 1)));

@@ -2187,31 +2187,8 @@ __global__ void integrate_kernel(int n, float dt, const float* __restrict__ f, f
     }
 }
 
-// Threefry-4x32-20 (Salmon et al. 2011) keyed by (seed, stream 0), counter
-// (invocation, atom): the reference thermostat's random stream (src/random.h:19-67)
-__device__ __forceinline__ uint32_t rotl32(uint32_t x, int r) { return (x << r) | (x >> (32 - r)); }
-__device__ void threefry4x32(const uint32_t c[4], const uint32_t k[4], uint32_t out[4]) {
-    const int R[8][2] = {{10, 26}, {11, 21}, {13, 27}, {23, 5}, {6, 20}, {17, 11}, {25, 10}, {18, 20}};
-    uint32_t ks[5] = {k[0], k[1], k[2], k[3], 0x1BD11BDAu ^ k[0] ^ k[1] ^ k[2] ^ k[3]};
-    uint32_t x[4];
-    for (int i = 0; i < 4; ++i) x[i] = c[i] + ks[i];
-#pragma unroll
-    for (int r = 0; r < 20; ++r) {
-        if (r % 2 == 0) {
-            x[0] += x[1]; x[1] = rotl32(x[1], R[r % 8][0]); x[1] ^= x[0];
-            x[2] += x[3]; x[3] = rotl32(x[3], R[r % 8][1]); x[3] ^= x[2];
-        } else {
-            x[0] += x[3]; x[3] = rotl32(x[3], R[r % 8][0]); x[3] ^= x[0];
-            x[2] += x[1]; x[1] = rotl32(x[1], R[r % 8][1]); x[1] ^= x[2];
-        }
-        if (r % 4 == 3) {
-            uint32_t s = uint32_t(r / 4 + 1);
-            for (int i = 0; i < 4; ++i) x[i] += ks[(s + uint32_t(i)) % 5];
-            x[3] += s;
-        }
-    }
-    for (int i = 0; i < 4; ++i) out[i] = x[i];
-}
+// The thermostat's random stream: Threefry-4x32-20 keyed by (seed, stream 0),
+// counter (invocation, atom) (src/random.h:19-67); threefry4x32 is in dev_math.cuh.
 // OU thermostat p <- e^{-dt/tau} p + sqrt(T (1 - e^{-2dt/tau})) N(0,1)
 // (OrnsteinUhlenbeckThermostat::apply, src/thermostat.cpp:9-18)
 __global__ void thermostat_kernel(int n_sys, const int* __restrict__ atom_off, const int* __restrict__ atom_sys,

@@ -50,6 +50,7 @@ def lib():
         L.ug_set_round.argtypes = [vp, vp]
         L.ug_set_integrator.argtypes = [vp, ip, ip]
         L.ug_level_forces.argtypes = [vp, ip, vp]
+        L.ug_monte_carlo.argtypes = [vp, ctypes.c_uint64, vp]
         L.ug_run.argtypes = [vp, ip, ctypes.c_float, ctypes.c_float, ip, ip]
         L.ug_node_dims.argtypes = [vp, cp, vp, vp]
         L.ug_node_output.argtypes = [vp, cp, vp, ip]
@@ -265,6 +266,13 @@ class Batch:
         """The three-stage cycle, or the multistep integrator: per round a
         slow-force kick of inner_step dt, then inner_step fast stages."""
         self._chk(lib().ug_set_integrator(self.h, int(bool(multistep)), int(inner_step)))
+
+    def monte_carlo(self, round):
+        """One pivot and one jump move per system (where the config has them);
+        returns (n_sys, 2) accepted flags: 1, 0, or -1 without that sampler."""
+        acc = np.zeros((self.n_sys, 2), np.int32)
+        self._chk(lib().ug_monte_carlo(self.h, int(round), acc.ctypes.data))
+        return acc
 
     def level_forces(self, level):
         """dE/dx of the integrator level's nodes (0 fast, 1 slow)."""
