@@ -1967,7 +1967,7 @@ struct RotamerNode : GNode {
             out.push_back({"rotamer_1body_energy" + std::to_string(k), part(size_t(4 + k)), off, false});
     }
     void add_pot(Engine& e);
-    void backward(Engine& e) override { launch_edge_scatter(hg.g, e.st); }
+    void backward(Engine&) override {}  // the solve's sensitivity kernel scatters the edges
     std::vector<float> get_param(Engine&) override { return hg.param_host; }
     void set_param(Engine&, const std::vector<float>& p) override { hg.set_param(p); }
     std::vector<float> param_deriv(Engine& e) override {

@@ -737,7 +737,7 @@ __global__ void bp_edge_energy_kernel(DBP b, DGraph g) {
 }
 
 // node probabilities (src/rotamer.cpp:239-256, :398-405) and edge matrices
-__global__ void bp_prob_kernel(DBP b) {
+__global__ void bp_node_prob_kernel(DBP b) {
     for (int r = grid_stride_start(); r < b.n_res; r += grid_stride()) {
         int n = b.nrot[r];
         float m = b.E1[r * 8];
@@ -746,8 +746,11 @@ __global__ void bp_prob_kernel(DBP b) {
             b.prob[r * 8 + k] = k < n ? expf(m - b.E1[r * 8 + k]) * expf(-b.E1x[r * 8 + k]) : 0.f;
         b.eoff[r] = m;
     }
-    // one thread per entry: its 6x6 block as nine float4, zero outside the
-    // (row rotamers) x (column rotamers) corner
+}
+// pair probability matrices from the summed pair energies alone (they need no
+// one-body energy): one thread per entry, its 6x6 block as nine float4, zero
+// outside the (row rotamers) x (column rotamers) corner
+__global__ void bp_pair_prob_kernel(DBP b) {
     int n_ent = min(*b.n_ent, b.ent_cap);
     for (int e = grid_stride_start(); e < n_ent; e += grid_stride()) {
         int nu = b.nrot[b.erow[e]], nv = b.nrot[b.col[e]];
@@ -1298,8 +1301,8 @@ __global__ void bp_node_log_kernel(DBP b, const float* p0, const float* p1, cons
     }
 }
 
-// bead-edge sensitivities from the marginals and 1-body sensitivities
-// (src/rotamer.cpp:1057-1086)
+// bead-edge sensitivities from the marginals, their scatter into the bead
+// sensitivities, and 1-body sensitivities (src/rotamer.cpp:1057-1086)
 __global__ void bp_sens_kernel(DBP b, DGraph g, float* s0, float* s1, float* s2, float* s3, int n_in, int w0,
                                int w1, int w2, int w3) {
     int ne = *g.n_edge;
@@ -1317,6 +1320,15 @@ __global__ void bp_sens_kernel(DBP b, DGraph g, float* s0, float* s1, float* s2,
             s = en >= 0 ? b.emarg[size_t(en) * 36 + k1 * 6 + k2] : 0.f;
         }
         g.esens[e] = s;
+        // the graph's adjoint (edge_scatter_kernel) for this edge, here rather
+        // than in a kernel of its own
+        if (s == 0.f) continue;
+        const int dw = g.d1 + g.d2;
+        const float* da = g.deriv + size_t(e) * dw;
+        float* p1 = g.sens1 + size_t(g.loc1[ij.x]) * g.w1;
+        float* p2 = g.sens2 + size_t(g.loc2[ij.y]) * g.w2;
+        for (int d = 0; d < g.d1; ++d) atomicAdd(p1 + d, s * da[d]);
+        for (int d = 0; d < g.d2; ++d) atomicAdd(p2 + d, s * da[g.d1 + d]);
     }
     for (int i = grid_stride_start(); i < b.n_bead; i += grid_stride()) {
         float m = b.marg[b.bead_res[i] * 8 + b.bead_rot[i]];
@@ -1330,7 +1342,7 @@ __global__ void bp_sens_kernel(DBP b, DGraph g, float* s0, float* s1, float* s2,
 
 // The structure of the solve from the bead pair list alone: residue-pair
 // entries (CSR rows, reverse entries, descriptors), folded 1-rotamer partner
-// energies and the summed pair energies.  It needs no one-body energy, so the
+// energies, the summed pair energies and their probability matrices.  It needs no one-body energy, so the
 // engine runs it as soon as the bead positions are known, while the one-body
 // inputs are still being computed.
 void launch_bp_structure(DBP& b, const DGraph& g, cudaStream_t st) {
@@ -1346,10 +1358,13 @@ void launch_bp_structure(DBP& b, const DGraph& g, cudaStream_t st) {
     bp_cap_check_kernel<<<1, 1, 0, st>>>(b);
     bp_entry_init_kernel<<<blocks, 256, 0, st>>>(b);
     bp_edge_energy_kernel<<<blocks, 256, 0, st>>>(b, g);
+    bp_pair_prob_kernel<<<blocks, 256, 0, st>>>(b);
 }
 
-// The rest, after launch_bp_structure: one-body energies, probabilities,
-// warm start, the solve, the logging decomposition and the sensitivities.
+// The rest, after launch_bp_structure: one-body energies, node
+// probabilities, warm start, the solve, the logging decomposition and the
+// sensitivities, whose bead-edge part is scattered into the bead
+// sensitivities here (the rotamer node needs no backward of its own).
 void launch_bp(DBP& b, const DGraph& g, const float* const* in, float* const* in_sens, const int* w, int n_in,
                int prev_n_ent, int* scan_total, int want_energy, double* energy_out, const WarmDev* warm,
                const float* pos, const int* atom_off, cudaStream_t st) {
@@ -1357,7 +1372,7 @@ void launch_bp(DBP& b, const DGraph& g, const float* const* in, float* const* in
     (void)prev_n_ent;
     if (b.log_fe) cudaMemsetAsync(b.log_1b, 0, sizeof(float) * size_t(b.n_res) * size_t(n_in), st);
     bp_bead_energy_kernel<<<blocks, 256, 0, st>>>(b, in[0], in[1], in[2], in[3], n_in, w[0], w[1], w[2], w[3]);
-    bp_prob_kernel<<<blocks, 256, 0, st>>>(b);
+    bp_node_prob_kernel<<<blocks, 256, 0, st>>>(b);
     if (warm) launch_warm_start(*warm, pos, atom_off, b.res_off, b.prob, b.nrot, b.n_sys, b.n_res, st);
     size_t smem = bp_solve_smem_bytes(b.max_res_sys);
     const BpVariant& v = bp_variants()[b.variant];
