@@ -561,6 +561,175 @@ template <class T> struct RamaMapNode : Node<T> {
     }
 };
 
+// RamaMap2: Rama map potential scaled per residue by a switch coordinate
+// lambda (row = position in the residue list) (src/rama_map_pot.cpp:96-175)
+template <class T> struct RamaMap2Node : Node<T> {
+    vector<int> res, map_id;
+    Periodic2D<T> sp;
+    RamaMap2Node(const H5& h) {
+        this->potential_node = true;
+        res = h.ri("residue_id");
+        map_id = h.ri("rama_map_id");
+        auto d = h.dims("rama_pot");
+        if (d.size() != 3 || d[1] != d[2]) throw Err("rama_pot must be (n_layer, n, n)");
+        sp.fit(int(d[0]), int(d[1]), int(d[2]), h.rd("rama_pot"));
+    }
+    void forward(Engine<T>& e, bool energy) override {
+        auto& r = e.arg(*this, 0);
+        auto& lam = e.arg(*this, 1);
+        const T scale = T(sp.nx) * (T(0.5f / float(M_PI)) - T(1e-7f));
+        const T shift = T(float(M_PI));
+        this->pot = 0;
+        for (size_t i = 0; i < res.size(); ++i) {
+            T* ro = &r.out[size_t(res[i]) * 2];
+            T v, dx, dy;
+            sp.eval(map_id[i], (ro[0] + shift) * scale, (ro[1] + shift) * scale, v, dx, dy);
+            T l = lam.out[i * size_t(lam.width)];
+            if (energy) this->pot += v * l;
+            r.sens[size_t(res[i]) * 2] += dx * scale * l;
+            r.sens[size_t(res[i]) * 2 + 1] += dy * scale * l;
+            lam.sens[i * size_t(lam.width)] += v;
+        }
+    }
+};
+
+// SigmoidCoord: compact sigmoid of one column of a coordinate, or its
+// complement for a negative sign (src/coord_map.cpp:609-675)
+template <class T> struct SigmoidCoordNode : Node<T> {
+    vector<int> id;
+    vector<T> c, s, sign, der;
+    int dim1;
+    SigmoidCoordNode(const H5& h) {
+        id = h.ri("id");
+        c = h.rf<T>("c");
+        s = h.rf<T>("s");
+        sign = h.rf<T>("sign");
+        dim1 = int(h.attr("dim1"));
+        this->alloc(int(id.size()), 1);
+        der.assign(id.size(), T(0));
+    }
+    void forward(Engine<T>& e, bool) override {
+        auto& p = e.arg(*this, 0);
+        for (size_t i = 0; i < id.size(); ++i) {
+            T v, d;
+            compact_sigmoid(p.out[size_t(id[i]) * p.width + dim1] - c[i], s[i], v, d);
+            this->out[i] = sign[i] > T(0) ? v : T(1) - v;
+            der[i] = sign[i] > T(0) ? d : -d;
+        }
+    }
+    void backward(Engine<T>& e) override {
+        auto& p = e.arg(*this, 0);
+        for (size_t i = 0; i < id.size(); ++i) p.sens[size_t(id[i]) * p.width + dim1] += this->sens[i] * der[i];
+    }
+};
+
+// Add, Mean and Multiply of two coordinates into n_size rows of n_dim
+// (src/coord_operator.cpp:15-112, 114-226, 228-351).  As in the reference,
+// Multiply scales the sensitivity passed to each factor by that factor's own
+// last value written to the row, not by the other factor.
+template <class T> struct CombineNode : Node<T> {
+    enum Op { ADD, MEAN, MUL } op;
+    vector<int> ip1, ip2, o1, o2, d1, d2, count;
+    vector<T> s1, s2, scl;
+    CombineNode(const H5& h, Op o) : op(o) {
+        int n_size = int(h.attr("n_size")), n_dim = int(h.attr("n_dim"));
+        this->alloc(n_size, n_dim);
+        ip1 = h.ri("id_pos1"); ip2 = h.ri("id_pos2");
+        o1 = h.ri("id1_out"); o2 = h.ri("id2_out");
+        d1 = h.ri("dim1"); d2 = h.ri("dim2");
+        if (int(d1.size()) != n_dim || int(d2.size()) != n_dim || o1.size() != ip1.size() || o2.size() != ip2.size())
+            throw Err("inconsistent sizes");
+        count.assign(size_t(n_size), 0);
+        for (int i : o1) { if (i < 0 || i >= n_size) throw Err("output id out of range"); ++count[size_t(i)]; }
+        for (int i : o2) { if (i < 0 || i >= n_size) throw Err("output id out of range"); ++count[size_t(i)]; }
+        s1.assign(size_t(n_size), T(1));
+        s2.assign(size_t(n_size), T(1));
+        scl.assign(size_t(n_size), T(1));
+        if (op == MEAN)
+            for (int i = 0; i < n_size; ++i) scl[size_t(i)] = count[size_t(i)] ? T(1) / T(count[size_t(i)]) : T(1);
+    }
+    void forward(Engine<T>& e, bool) override {
+        auto& a = e.arg(*this, 0); auto& b = e.arg(*this, 1);
+        int nd = this->width;
+        std::fill(this->out.begin(), this->out.end(), op == MUL ? T(1) : T(0));
+        auto pass = [&](const vector<int>& ip, const vector<int>& oo, const vector<int>& dd, Node<T>& src,
+                        vector<T>& keep) {
+            for (size_t i = 0; i < ip.size(); ++i)
+                for (int d = 0; d < nd; ++d) {
+                    T v = src.out[size_t(ip[i]) * src.width + dd[size_t(d)]];
+                    T& o = this->out[size_t(oo[i]) * nd + d];
+                    if (op == MUL) { o *= v; keep[size_t(oo[i])] = v; }
+                    else o += v * scl[size_t(oo[i])];
+                }
+        };
+        pass(ip1, o1, d1, a, s2);
+        pass(ip2, o2, d2, b, s1);
+        if (op == MUL)
+            for (int i = 0; i < this->n_elem; ++i)
+                if (!count[size_t(i)])
+                    for (int d = 0; d < nd; ++d) this->out[size_t(i) * nd + d] = T(0);
+    }
+    void backward(Engine<T>& e) override {
+        auto& a = e.arg(*this, 0); auto& b = e.arg(*this, 1);
+        int nd = this->width;
+        auto pass = [&](const vector<int>& ip, const vector<int>& oo, const vector<int>& dd, Node<T>& dst,
+                        const vector<T>& f) {
+            for (size_t i = 0; i < ip.size(); ++i)
+                for (int d = 0; d < nd; ++d)
+                    dst.sens[size_t(ip[i]) * dst.width + dd[size_t(d)]] +=
+                        this->sens[size_t(oo[i]) * nd + d] * f[size_t(oo[i])];
+        };
+        pass(ip1, o1, d1, a, op == MUL ? s2 : scl);
+        pass(ip2, o2, d2, b, op == MUL ? s1 : scl);
+    }
+};
+
+// SigmoidEnergy / SigmoidLEnergy: a + b * compact_sigmoid(x - c, s) on one
+// column, optionally times a switch coordinate lambda; with use_cutoff only
+// x in [min, max] counts, otherwise x beyond c -+ 1/s takes the plateau
+// value (src/sigmoid_energy.cpp:9-91, 93-185)
+template <class T> struct SigmoidEnergyNode : Node<T> {
+    bool with_lambda;
+    vector<int> id, id2;
+    vector<T> a, b, c, s, lo, hi;
+    int dim1;
+    bool use_cutoff;
+    SigmoidEnergyNode(const H5& h, bool lam) : with_lambda(lam) {
+        this->potential_node = true;
+        id = h.ri(lam ? "id1" : "id");
+        if (lam) id2 = h.ri("id2");
+        a = h.rf<T>("a"); b = h.rf<T>("b"); c = h.rf<T>("c"); s = h.rf<T>("s");
+        lo = h.rf<T>("min"); hi = h.rf<T>("max");
+        dim1 = int(h.attr("dim1"));
+        use_cutoff = h.attr("use_cutoff") != 0;
+        if (!use_cutoff)
+            for (size_t i = 0; i < id.size(); ++i) {
+                lo[i] = c[i] - T(1) / s[i];
+                hi[i] = c[i] + T(1) / s[i];
+            }
+    }
+    void forward(Engine<T>& e, bool energy) override {
+        auto& p = e.arg(*this, 0);
+        this->pot = 0;
+        for (size_t i = 0; i < id.size(); ++i) {
+            T x = p.out[size_t(id[i]) * p.width + dim1];
+            T l = with_lambda ? e.arg(*this, 1).out[size_t(id2[i]) * e.arg(*this, 1).width] : T(1);
+            if (use_cutoff && (x > hi[i] || x < lo[i])) continue;
+            if (x > hi[i]) {
+                if (energy) this->pot += l * a[i];
+            } else if (x < lo[i]) {
+                if (energy) this->pot += l * (a[i] + b[i]);
+            } else {
+                T v, d;
+                compact_sigmoid(x - c[i], s[i], v, d);
+                if (energy) this->pot += l * (a[i] + b[i] * v);
+                p.sens[size_t(id[i]) * p.width + dim1] += l * b[i] * d;
+                if (with_lambda) e.arg(*this, 1).sens[size_t(id2[i]) * e.arg(*this, 1).width] += a[i] + b[i] * v;
+            }
+        }
+    }
+};
+
 // Rigid frame per residue from N, CA, C (AffineAlignment, src/eig.cpp:277-470).
 // Output (center, quaternion); sensitivity slots 3..5 carry the torque.
 template <class T> struct AffineNode : Node<T> {
@@ -1896,6 +2065,13 @@ template <class T> std::unique_ptr<Node<T>> make_node(const string& name, const 
     if (is_prefix("Spring", name)) return P(new SpringNode<T>(h));
     if (is_prefix("rama_coord", name)) return P(new PasteRamaNode<T>(h));
     if (is_prefix("rama_map_pot", name)) return P(new RamaMapNode<T>(h));
+    if (is_prefix("RamaMap2", name)) return P(new RamaMap2Node<T>(h));
+    if (is_prefix("SigmoidCoord", name)) return P(new SigmoidCoordNode<T>(h));
+    if (is_prefix("SigmoidEnergy", name)) return P(new SigmoidEnergyNode<T>(h, false));
+    if (is_prefix("SigmoidLEnergy", name)) return P(new SigmoidEnergyNode<T>(h, true));
+    if (is_prefix("Add", name)) return P(new CombineNode<T>(h, CombineNode<T>::ADD));
+    if (is_prefix("Mean", name)) return P(new CombineNode<T>(h, CombineNode<T>::MEAN));
+    if (is_prefix("Multiply", name)) return P(new CombineNode<T>(h, CombineNode<T>::MUL));
     if (is_prefix("affine_alignment", name)) return P(new AffineNode<T>(h));
     if (is_prefix("backbone_pairs", name)) return P(new BackbonePairsNode<T>(h));
     if (is_prefix("infer_H_O", name)) return P(new InferHONode<T>(h));

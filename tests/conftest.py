@@ -38,6 +38,18 @@ def syn_configs(tmp_path_factory, built):
     return out
 
 
+@pytest.fixture(scope="session")
+def transcis_config(tmp_path_factory, built):
+    """The trans-cis proline fixture config (golden/transcis_spec.py) and its
+    reference data."""
+    if GOLDEN not in sys.path:
+        sys.path.insert(0, GOLDEN)
+    import transcis_spec
+    path = str(tmp_path_factory.mktemp("tc") / "syn_transcis.up")
+    transcis_spec.write(path)
+    return path, np.load(os.path.join(GOLDEN, "syn_transcis_ref.npz"))
+
+
 def quat_align(a, ref):
     """Flip the quaternion columns (3:7) of affine outputs to the sign of ref
     (q and -q are the same rotation)."""

@@ -15,6 +15,10 @@ this script, which are committed (the GPU host has no reference checkout):
                      seed, coordinates (initial + perturbed frames), and the
                      reference engine's energy, derivative, per-node outputs,
                      sensitivities, potentials and pair-list counts by type
+  syn_transcis_ref.npz the trans-cis proline fixture (transcis_spec.py):
+                     frames, reference energy and derivative, and the
+                     trans-cis nodes' outputs and sensitivities per frame
+                     (python make_fixtures.py trans_cis writes only this file)
 
 The reference engine is oracle/_ref/libupside_ref.so (oracle/build.py).
 """
@@ -148,6 +152,37 @@ def synthetic(L, n_res, seed, n_frames=3, tmpdir="/tmp"):
     np.savez_compressed(os.path.join(HERE, "syn%d_ref.npz" % n_res), **out)
 
 
+TRANS_CIS_NODES = ["Dihedral_OmegaTransCis", "SigmoidCoord_trans1", "SigmoidCoord_trans2", "SigmoidCoord_cis1",
+                   "SigmoidCoord_cis2", "Add_lambda_trans", "Multiply_lambda_cis", "Mean_lambda_mix", "Multiply_dup",
+                   "SigmoidEnergy_trans1", "SigmoidEnergy_cis0", "SigmoidEnergy_cis1", "SigmoidEnergy_trans0",
+                   "RamaMap2_trans", "RamaMap2_cis", "SigmoidLEnergy_mix", "SigmoidLEnergy_dup", "rama_coord",
+                   "rama_map_pot", "Spring_omega"]
+
+
+def trans_cis(L, tmpdir="/tmp"):
+    """syn_transcis_ref.npz: the trans-cis fixture of transcis_spec.py, the
+    reference engine's energy and derivative at each frame, and the outputs
+    and sensitivities of the trans-cis nodes at each frame."""
+    import transcis_spec as T
+    path = os.path.join(tmpdir, "syn_transcis.up")
+    T.write(path)
+    frames = T.frames()
+    eng = RefEngine(L, path, frames.shape[1])
+    out = {"pos": frames}
+    E, D = [], []
+    for k, x in enumerate(frames):
+        e, d = eng.eval(x)
+        E.append(e)
+        D.append(d)
+        for nm in TRANS_CIS_NODES:
+            out.setdefault("out/" + nm, []).append(eng.node(nm))
+            out.setdefault("sens/" + nm, []).append(eng.node(nm, sens=True))
+    out = {k: np.array(v) for k, v in out.items()}
+    out["ref_energy"] = np.array(E)
+    out["ref_deriv"] = np.array(D)
+    np.savez_compressed(os.path.join(HERE, "syn_transcis_ref.npz"), **out)
+
+
 KAT_SRC = r"""
 #include <cstdio>
 #include <cstdint>
@@ -181,12 +216,16 @@ def main():
     if sys.argv[1:] == ["chig_run"]:
         chig_run_output()
         return
+    if sys.argv[1:] == ["trans_cis"]:
+        trans_cis(load_ref())
+        return
     threefry_kat()
     L = load_ref()
     chig(L)
     chig_run_output()
     synthetic(L, 60, 1)
     synthetic(L, 150, 2, n_frames=2)
+    trans_cis(L)
 
 
 if __name__ == "__main__":

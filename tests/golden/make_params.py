@@ -25,7 +25,7 @@ def main():
     with H5File(os.path.join(P, "ff_2.1", "sidechain.h5")) as f:
         for k in ["restype_order", "rotamer_center_fixed", "rotamer_prob", "rotamer_start_stop_bead",
                   "bead_order", "coverage_interaction", "hydrophobe_placement", "hydrophobe_interaction",
-                  "pair_interaction"]:
+                  "pair_interaction", "restype_and_chi_and_state"]:
             out["sc_" + k] = f.read("/" + k)
     with H5File(os.path.join(P, "ff_2.1", "environment.h5")) as f:
         for k in ["restype_order", "weights", "coverage_param", "energies", "scale", "center", "sharpness"]:

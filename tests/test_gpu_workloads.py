@@ -57,8 +57,9 @@ def test_workload_energy_forces_vs_oracle(built, name, tmp_path):
     tolerance tightened to 1e-7: at the recipe's 1e-3 two solves that iterate
     in different float orders may stop at marginals up to ~1e-3 apart on
     near-degenerate residues, and in the 2000-residue system that alone moves
-    some forces by ~2e-4 of max |F| (observed).  The bound is 5e-4 at the
-    recipe's tolerance and 1e-4 (or the FP32 rule of _check_vs_oracle) at the
+    some forces by ~2e-4 of max |F| (observed; 1.25e-4 on a relaxed
+    300-residue frame).  The bound is 5e-4 at the recipe's tolerance (the
+    2000-residue coil and both relaxed frames) and 1e-4 (or the FP32 rule of _check_vs_oracle) at the
     tight one.  FP32 cannot resolve 1e-7, so the GPU and FP32-oracle solves of
     the tight copy run to the 1000-iteration cap while FP64 converges in
     ~60 sweeps; on the 2000-residue frame the FP32 oracle then sits
@@ -77,7 +78,10 @@ def test_workload_energy_forces_vs_oracle(built, name, tmp_path):
     b.set_thermostat(W["temps"], np.array(W["seeds"], np.uint32))
     b.run(20, use_graph=True, graph_rounds=5)
     x1 = b.get_pos()
-    _check_vs_oracle(path, x1, bp_slack=name == "C5")
+    # a relaxed frame at the recipe's tolerance: both chains' solves may stop
+    # at marginals ~1e-3 apart (C2 observed at 1.25e-4 of max |F|); the
+    # tight copy below holds the 1e-4 bound
+    _check_vs_oracle(path, x1, bp_slack=True)
     with H5File(path) as f:
         seq = [s.decode() for s in f.read("/input/sequence")]
         starts = list(f.read("/input/chain_break/chain_first_residue")) if f.exists("/input/chain_break") else []

@@ -152,3 +152,94 @@ def test_reference_engine_if_built(syn_configs):
     e, d = r.eval(z["pos"][2])
     assert rel_e(e, z["ref_energy"][2]) < 1e-6
     assert rel_f(d, z["ref_deriv"][2]) < 1e-5
+
+
+# The trans-cis frames are chains built from random torsions, with close
+# contacts where the reference's approximate reciprocal square roots move the
+# largest force by up to 1.1e-3 of max |F| from the FP64 instantiation (the
+# trans-cis nodes themselves agree to 1e-6; see the node checks below).
+F_REF_TOL_TC = 2e-3
+
+
+@pytest.mark.parametrize("fp64", [False, True])
+def test_trans_cis_golden_frames(transcis_config, fp64):
+    """RamaMap2, SigmoidCoord, Add/Mean/Multiply and SigmoidEnergy/LEnergy
+    (src/rama_map_pot.cpp:96-175, src/coord_map.cpp:609-675,
+    src/coord_operator.cpp:15-351, src/sigmoid_energy.cpp) against the
+    reference engine: energy, forces, and every trans-cis node's output and
+    sensitivity at frames whose proline omegas sweep the barrier and switch
+    segments."""
+    import oracle_py
+    path, z = transcis_config
+    o = oracle_py.Oracle(path, z["pos"].shape[1], fp64=fp64)
+    for k in range(len(z["pos"])):
+        e, d = o.evaluate(z["pos"][k])
+        assert rel_e(e, z["ref_energy"][k], energy_scale(o, path)) < E_REF_TOL, k
+        assert rel_f(d, z["ref_deriv"][k]) < F_REF_TOL_TC, k
+        for key in z.files:
+            if not key.startswith("out/"):
+                continue
+            nm = key[4:]
+            for got, ref, tol in ((o.node(nm), z[key][k], 1e-5),
+                                  # rama_coord's sensitivity also collects the
+                                  # hbond energy's Rama derivative, where the
+                                  # reference's approximations enter (7e-5)
+                                  (o.node(nm, sens=True), z["sens/" + nm][k], 2e-4 if nm == "rama_coord" else 1e-5)):
+                assert got.shape == ref.shape, nm
+                assert np.abs(got - ref).max() <= tol * max(np.abs(ref).max(), 1.0), (k, nm)
+
+
+def test_trans_cis_frames_cover_switches(transcis_config):
+    """The fixture frames visit every barrier segment and both ramps of every
+    switch, so each branch of the nodes is compared somewhere."""
+    _, z = transcis_config
+    om = z["out/Dihedral_OmegaTransCis"][..., 0]
+    seg = np.floor((om + np.pi) / (np.pi / 2)).astype(int).clip(0, 3)
+    assert set(seg.ravel().tolist()) == {0, 1, 2, 3}
+    for nm in ("SigmoidCoord_trans1", "SigmoidCoord_trans2", "SigmoidCoord_cis1", "SigmoidCoord_cis2"):
+        v = z["out/" + nm].ravel()
+        assert ((v > 0) & (v < 1)).any(), nm
+        assert (v == 0).any() and (v == 1).any(), nm
+    # the empty row of the repeated-output Multiply is zero, and its repeated
+    # row carries the reference's own-factor sensitivity
+    assert np.all(z["out/Multiply_dup"][:, 2] == 0)
+
+
+def test_config_trans_cis_and_fixed_rotamers(transcis_config):
+    """Structure of the trans-cis writer (py/upside_config.py:571-673,
+    848-993) and of fixed rotamers (:1077-1190)."""
+    import config_gen
+    import transcis_spec
+    from h5lite import H5File
+    path, _ = transcis_config
+    f = H5File(path)
+    seq = [s.decode() for s in f.read("/input/sequence")]
+    assert seq[transcis_spec.CPR] == "CPR"
+    pot = "/input/potential/"
+    names = f.list("/input/potential")
+    for nm in ("Dihedral_OmegaTransCis", "Add_lambda_trans", "Multiply_lambda_cis", "RamaMap2_trans",
+               "RamaMap2_cis") + tuple("SigmoidEnergy_" + x for x in ("trans1", "cis0", "cis1", "trans0")):
+        assert nm in names, nm
+    om = f.read(pot + "Dihedral_OmegaTransCis/id")
+    assert sorted(((om[:, 3] - 1) // 3).tolist()) == sorted(transcis_spec.PRO_TC)
+    sp = f.read(pot + "Dihedral_omega/id")
+    rid = (sp[:, 3] - 1) // 3
+    assert not set(rid.tolist()) & set(transcis_spec.PRO_TC)
+    eq = f.read(pot + "Spring_omega/equil_dist")
+    assert np.all(eq[rid == transcis_spec.CPR] == 0.0) and np.all(eq[rid != transcis_spec.CPR] == np.pi)
+    assert list(f.read(pot + "RamaMap2_cis/residue_id")) == list(transcis_spec.PRO_TC)
+    assert not set(f.read(pot + "rama_map_pot/residue_id").tolist()) & set(transcis_spec.PRO_TC)
+    # GLU 3 at chi1 -60 (class 2), chi2 170: the state with the most negative
+    # wrapped chi2 offset; CYS 7 has one state at chi1 65; residue 12 (chi1
+    # NaN) stays free
+    fix = dict(f.read(pot + "placement_fixed_point_vector_only/fix_rotamer").tolist())
+    assert fix == {3: 3, 7: 0}
+    assert config_gen.fix_rotamer_states([(3, seq[3], 'A', 3, -60.0, 170.0)], seq) == {3: 3}
+    ids = f.read(pot + "placement_fixed_point_vector_only/id_seq")
+    res = f.read(pot + "placement_fixed_point_vector_only/affine_residue")
+    n_rot = (ids >> config_gen.N_BIT_ROTAMER) & ((1 << config_gen.N_BIT_ROTAMER) - 1)
+    for r in (3, 7):
+        assert np.all(n_rot[res == r] == 1) and (res == r).sum() == 1
+    assert (res == 12).sum() > 1
+    with pytest.raises(ValueError):
+        config_gen.read_trans_cis([(4, 0, 1.0, 0.5, 45.0)], seq)  # not a proline

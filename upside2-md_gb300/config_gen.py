@@ -24,7 +24,9 @@ write_infer_H_O :332-368, write_count_hbond :1018-1047, write_short_hbond
 :1049-1075, write_rotamer_placement :1077-1201, write_rotamer_backbone
 :1204-1300, write_rotamer :1302-1334, write_environment :1341-1426,
 write_bb_environment :1428-1538, write_weighted_pos :370-377,
-write_rama_coord2 :407-446, write_affine_alignment :314-330.
+write_rama_coord2 :407-446, write_affine_alignment :314-330,
+write_omega_spring2 :571-673 and write_rama_map_pot2 :848-993 (--trans-cis),
+read_fasta :240-253 (CPR, cis proline).
 """
 import os
 
@@ -127,6 +129,16 @@ def synthetic_rama_maps(seq, rng, n=72):
             a, b = rng.uniform(0, 2 * np.pi, size=2)
             m = m + 0.25 * rng.randn() * np.cos(kx * phi + a) * np.cos(ky * psi + b)
         type_maps[aa] = m
+    if 'CPR' in seq:
+        # cis proline: drawn after the standard types, so configurations
+        # without CPR keep their maps
+        m = 2.0 - basin(-75 * DEG, 150 * DEG, 2.5) - basin(-80 * DEG, -20 * DEG, 1.5)
+        m = m + 3.0 * (1 + np.cos(phi + 70 * DEG)) * 0.5
+        for _ in range(6):
+            kx, ky = rng.randint(0, 4, size=2)
+            a, b = rng.uniform(0, 2 * np.pi, size=2)
+            m = m + 0.25 * rng.randn() * np.cos(kx * phi + a) * np.cos(ky * psi + b)
+        type_maps['CPR'] = m
     maps = np.array([type_maps[s] for s in seq])
     # maps are -log of normalized probabilities over the grid, as library maps are
     maps += np.log(np.exp(-maps).sum(axis=(-2, -1), keepdims=True))
@@ -164,9 +176,95 @@ class _Cfg:
         return np.all(chain == chain[..., :1], axis=-1)
 
 
+TRANS_CIS_HEADER = 'residue init_state energy k width'
+FIX_ROTAMER_HEADER = 'residue restype chain resnum chi1 chi2'
+
+
+def read_trans_cis(table, seq):
+    """Rows (residue, init_state, energy, k, width) of a --trans-cis table:
+    a path whose first line is TRANS_CIS_HEADER, or the rows themselves
+    (write_omega_spring2, py/upside_config.py:571-604).  Every residue must
+    be a proline (PRO or CPR)."""
+    if isinstance(table, str):
+        fields = [ln.split() for ln in open(table)]
+        if [x.lower() for x in fields[0]] != TRANS_CIS_HEADER.split():
+            raise ValueError('First line of restraint table must be "%s"' % TRANS_CIS_HEADER)
+        if not all(len(f) == 5 for f in fields):
+            raise ValueError('Invalid format for restraint file')
+        fields = fields[1:]
+    else:
+        fields = list(table)
+    res = np.array([int(f[0]) for f in fields], dtype=int)
+    state = np.array([int(f[1]) for f in fields], dtype=int)
+    energy, k, width = (np.array([float(f[i]) for f in fields]) for i in (2, 3, 4))
+    for r in res:
+        if not (0 <= r < len(seq)):
+            raise ValueError('Double wall energy specified for residue %i (zero is first residue) but there '
+                             'are only %i residues in the FASTA' % (r, len(seq)))
+        if seq[r] not in ('PRO', 'CPR'):
+            raise ValueError('trans-cis residue %i is %s, not a proline' % (r, seq[r]))
+    if np.any(width <= 0.):
+        raise ValueError('Cannot have negative width value')
+    return res, state, energy, k, width
+
+
+def _chi1_state(angles):
+    s = np.ones(angles.shape, dtype='i')
+    s[(0. * DEG <= angles) & (angles < 120. * DEG)] = 0
+    s[(-120. * DEG <= angles) & (angles < 0. * DEG)] = 2
+    return s
+
+
+def fix_rotamer_states(table, seq, params=None):
+    """{residue: rotamer state} for a --fix-rotamer table (a path whose first
+    line is FIX_ROTAMER_HEADER, or its rows): GLY and ALA take state 0;
+    otherwise the states of the residue type with the same chi1 class, and
+    among those the first whose chi2 offset, wrapped to (-pi, pi], is
+    smallest (write_rotamer_placement, py/upside_config.py:1078-1140).
+    Residues with a NaN chi1 (or a NaN chi2 where chi2 decides) stay free."""
+    P = load_params(params)
+    if isinstance(table, str):
+        fields = [x.split() for x in open(table)]
+        if [x.lower() for x in fields[0]] != FIX_ROTAMER_HEADER.split():
+            raise ValueError('First line of fix-rotamer table must be "%s" but is "%s" for file %s'
+                             % (FIX_ROTAMER_HEADER, " ".join(fields[0]), table))
+        fields = fields[1:]
+    else:
+        fields = list(table)
+    restype_num = {a.decode(): i for i, a in enumerate(P["sc_restype_order"])}
+    tab = P["sc_restype_and_chi_and_state"]
+    find_restype, find_chi2, find_state = tab[:, 0].astype('i'), tab[:, 2], tab[:, 3].astype('i')
+    find_chi1_state = _chi1_state(tab[:, 1])
+    fix = {}
+    for residue, restype, _chain, _resnum, chi1, chi2 in fields:
+        r = int(residue)
+        if seq[r] != (restype if restype != 'CPR' else 'PRO'):
+            raise ValueError("fix-rotamer file does not match FASTA, residue %i should be %s but fix-rotamer "
+                             "file has %s" % (r, seq[r], restype))
+        chi1, chi2 = float(chi1) * DEG, float(chi2) * DEG
+        if restype in ('GLY', 'ALA'):
+            state = 0
+        else:
+            if np.isnan(chi1):
+                continue
+            ok = (find_restype == restype_num[seq[r]]) & (find_chi1_state == _chi1_state(np.array([chi1]))[0])
+            cand_chi2, cand_state = find_chi2[ok], find_state[ok]
+            if len(cand_state) == 1:
+                state = cand_state[0]
+            else:
+                if np.isnan(chi2):
+                    continue
+                d = (cand_chi2 - chi2) % (2 * np.pi)
+                d[d > np.pi] -= 2 * np.pi
+                state = cand_state[np.argmin(d)]
+        fix[r] = int(state)
+    return fix
+
+
 def write_config(path, seq, seed, chain_first_residue=(), pos=None, environment_potential_type=1,
                  damping=0.4, chain_offsets=None, params=None, bp_tol=1e-3, moves=False,
-                 jump_length_scale=5., jump_rotation_scale=30.):
+                 jump_length_scale=5., jump_rotation_scale=30., trans_cis=None, fix_rotamer=None,
+                 extra_nodes=()):
     """Write an ff_2.1 `.up` file for `seq` (list of 3-letter codes).
 
     chain_first_residue: residue indices (excluding 0) where new chains start.
@@ -177,15 +275,35 @@ def write_config(path, seq, seed, chain_first_residue=(), pos=None, environment_
       does (py/upside_config.py:2520-2552): jump moves of whole chains for
       several chains (widths jump_length_scale in angstrom and
       jump_rotation_scale in degrees), pivot moves otherwise.
+    trans_cis: a --trans-cis table (path or rows, see read_trans_cis): the
+      omega of each listed proline gets the four-segment sigmoid barrier
+      (SigmoidEnergy) instead of a spring, and its Rama potential becomes the
+      omega-weighted mixture of trans and cis maps (RamaMap2 over
+      SigmoidCoord/Add/Multiply switches).
+    fix_rotamer: a --fix-rotamer table (path or rows, see fix_rotamer_states)
+      or a {residue: state} dict; fixed residues keep one rotamer.
+    seq may hold CPR (cis proline): its omega spring targets 0 and it has
+    its own Rama map; every other term treats it as PRO.
+    extra_nodes: further nodes, each (name, arguments, attributes dict,
+      datasets dict), written after the standard ones.
     """
     P = load_params(params)
     rng = np.random.RandomState(seed)
+    seq_cpr = np.array(seq)
+    seq = [s if s != 'CPR' else 'PRO' for s in seq]
+    tc = read_trans_cis(trans_cis, seq_cpr) if trans_cis is not None else None
+    if fix_rotamer is None:
+        fix = {}
+    elif isinstance(fix_rotamer, dict):
+        fix = {int(r): int(v) for r, v in fix_rotamer.items()}
+    else:
+        fix = fix_rotamer_states(fix_rotamer, seq, params)
     c = _Cfg(seq, chain_first_residue)
     n_res, n_atom = c.n_res, c.n_atom
     w = c.w
 
     # ---- sequence and coordinates
-    w.dataset("/input/sequence", np.array([s.encode() for s in seq]))
+    w.dataset("/input/sequence", np.array([s.encode() for s in seq_cpr]))
     if pos is None:
         starts = list(np.asarray(chain_first_residue, dtype=int))
         bounds = [0] + starts + [n_res]
@@ -233,22 +351,80 @@ def write_config(path, seq, seed, chain_first_residue=(), pos=None, environment_
 
     ids = np.arange(1, n_atom - 3, 3)
     ids = np.column_stack((ids, ids + 1, ids + 2, ids + 3))
-    keep = c.between_chain_ok(ids)
+    ids = ids[c.between_chain_ok(ids)]
+    rid = (ids[:, 3] - 1) // 3  # the residue the omega leads into
+    target = np.where(seq_cpr[rid] == 'CPR', 0. * DEG, 180. * DEG)
+    free = np.ones(len(ids), bool) if tc is None else ~np.isin(rid, tc[0])
     g = c.grp("Dihedral_omega", ["pos"])
-    c.ds(g + "/id", ids[keep])
+    c.ds(g + "/id", ids[free])
     g = c.grp("Spring_omega", ["Dihedral_omega"], integrator_level=0, dim1=0, pbc=1, box_len=np.pi * 2)
-    c.ds(g + "/id", np.arange(keep.sum()))
-    c.ds(g + "/equil_dist", np.pi * np.ones(keep.sum()))
-    c.ds(g + "/spring_const", 30. * np.ones(keep.sum()))
+    c.ds(g + "/id", np.arange(free.sum()))
+    c.ds(g + "/equil_dist", target[free])
+    c.ds(g + "/spring_const", 30. * np.ones(free.sum()))
+    if tc is not None:
+        # double-well barrier on the trans-cis omegas: four compact-sigmoid
+        # segments over [-pi, pi] (write_omega_spring2)
+        res_tc, _, energy, kk, width = tc
+        n_pro = len(res_tc)
+        g = c.grp("Dihedral_OmegaTransCis", ["pos"])
+        c.ds(g + "/id", ids[~free])
+        one, sharp = np.ones(n_pro), 1. / (width * DEG)
+        border = np.linspace(-np.pi, np.pi, 9)
+        seg_a = [energy, energy * (1. - kk), energy, energy * 0.]
+        seg_b = [-energy, energy * kk, -energy * kk, energy]
+        for si, nm in enumerate(['trans1', 'cis0', 'cis1', 'trans0']):
+            g = c.grp("SigmoidEnergy_" + nm, ["Dihedral_OmegaTransCis"], integrator_level=0, use_cutoff=1, dim1=0)
+            c.ds(g + "/id", np.arange(n_pro))
+            c.ds(g + "/a", seg_a[si])
+            c.ds(g + "/b", seg_b[si])
+            c.ds(g + "/c", one * border[2 * si + 1])
+            c.ds(g + "/s", sharp)
+            c.ds(g + "/min", one * border[2 * si])
+            c.ds(g + "/max", one * border[2 * si + 2])
 
     # ---- Rama map potential (synthetic maps; see module docstring)
-    g = c.grp("rama_map_pot", ["rama_coord"], integrator_level=0)
     # maps get their own stream so a config is the same whether or not the
     # caller supplies coordinates
-    maps = synthetic_rama_maps(seq, np.random.RandomState(seed + 104729))
-    c.ds(g + "/residue_id", np.arange(n_res))
-    c.ds(g + "/rama_map_id", np.arange(n_res))
-    c.ds(g + "/rama_pot", maps)
+    def rama_maps(sq):
+        return synthetic_rama_maps(list(sq), np.random.RandomState(seed + 104729))
+    g = c.grp("rama_map_pot", ["rama_coord"], integrator_level=0)
+    if tc is None:
+        maps = rama_maps(seq_cpr)
+        c.ds(g + "/residue_id", np.arange(n_res))
+        c.ds(g + "/rama_map_id", np.arange(n_res))
+        c.ds(g + "/rama_pot", maps)
+    else:
+        # trans-cis prolines leave the plain map for the trans and cis maps,
+        # mixed by omega switches (write_rama_map_pot2)
+        res_tc = tc[0]
+        n_pro = len(res_tc)
+        seq_trans, seq_cis = seq_cpr.copy(), seq_cpr.copy()
+        seq_trans[res_tc], seq_cis[res_tc] = 'PRO', 'CPR'
+        maps, maps_cis = rama_maps(seq_trans), rama_maps(seq_cis)
+        rest = np.array([r for r in range(n_res) if r not in set(res_tc.tolist())], dtype=int)
+        c.ds(g + "/residue_id", rest)
+        c.ds(g + "/rama_map_id", rest)
+        c.ds(g + "/rama_map_id_all", np.arange(n_res))
+        c.ds(g + "/rama_pot", maps)
+        ar = np.arange(n_pro)
+        for nm, cen, sign in (("trans1", -0.5, 1.), ("trans2", 0.5, -1.), ("cis1", -0.5, -1.), ("cis2", 0.5, 1.)):
+            g = c.grp("SigmoidCoord_" + nm, ["Dihedral_OmegaTransCis"], dim1=0)
+            c.ds(g + "/id", ar)
+            c.ds(g + "/c", np.ones(n_pro) * cen * np.pi)
+            c.ds(g + "/s", np.ones(n_pro) * 3.0 / np.pi)
+            c.ds(g + "/sign", np.ones(n_pro) * sign)
+        for op, nm in (("Add", "trans"), ("Multiply", "cis")):
+            g = c.grp("%s_lambda_%s" % (op, nm), ["SigmoidCoord_%s1" % nm, "SigmoidCoord_%s2" % nm],
+                      n_dim=1, n_size=n_pro)
+            for dsn in ("dim1", "dim2"):
+                c.ds(g + "/" + dsn, np.array([0]))
+            for dsn in ("id_pos1", "id_pos2", "id1_out", "id2_out"):
+                c.ds(g + "/" + dsn, ar)
+        for nm, op, mp in (("trans", "Add", maps), ("cis", "Multiply", maps_cis)):
+            g = c.grp("RamaMap2_" + nm, ["rama_coord", "%s_lambda_%s" % (op, nm)], integrator_level=0)
+            c.ds(g + "/residue_id", res_tc)
+            c.ds(g + "/rama_map_id", res_tc)
+            c.ds(g + "/rama_pot", mp)
 
     ref = np.log(P["rama_reference"])
     ref -= ref.mean()
@@ -310,6 +486,12 @@ def write_config(path, seq, seed, chain_first_residue=(), pos=None, environment_
     for rnum, aa in enumerate(seq):
         start, stop, n_bead = start_stop[restype_num[aa]]
         n_rot = (stop - start) // n_bead
+        if rnum in fix:
+            # a fixed residue keeps the beads of its one state
+            if not (0 <= fix[rnum] < n_rot):
+                raise ValueError('invalid fix rotamer state')
+            start, stop = start + n_bead * fix[rnum], start + n_bead * (fix[rnum] + 1)
+            n_rot = 1
         count_by_n_rot.setdefault(n_rot, 0)
         base_id = (count_by_n_rot[n_rot] << N_BIT_ROTAMER) + n_rot
         count_by_n_rot[n_rot] += 1
@@ -327,6 +509,8 @@ def write_config(path, seq, seed, chain_first_residue=(), pos=None, environment_
     c.ds(g + "/placement_data", placement_pos[..., :6])
     c.ds(g + "/beadtype_seq", np.array([b.encode() for b in beadtype_seq]))
     c.ds(g + "/id_seq", np.array(id_seq))
+    if fix:
+        c.ds(g + "/fix_rotamer", np.array(sorted(fix.items())))
     g = c.grp(pl_name, ["affine_alignment", "rama_coord"])
     c.ds(g + "/rama_residue", np.array(rama_residue))
     c.ds(g + "/affine_residue", np.array(affine_residue))
@@ -499,6 +683,11 @@ def write_config(path, seq, seed, chain_first_residue=(), pos=None, environment_
     g = c.grp("affine_alignment", ["pos"])
     c.ds(g + "/atoms", np.column_stack((N_id, N_id + 1, N_id + 2)))
     c.ds(g + "/ref_geom", ref_geom)
+
+    for name, args, attrs, dsets in extra_nodes:
+        g = c.grp(name, args, **attrs)
+        for k, v in dsets.items():
+            c.ds(g + "/" + k, np.asarray(v))
 
     if moves:
         if c.n_chains > 1:

@@ -80,6 +80,13 @@ std::vector<int> cat_idx(const Groups& g, const std::string& ds, const std::vect
     }
     return out;
 }
+// as cat_idx, for datasets where every index must name a row
+std::vector<int> cat_rows(const Groups& g, const std::string& ds, const std::vector<int>& target_off) {
+    auto v = cat_idx(g, ds, &target_off);
+    for (int x : v)
+        if (x < 0) throw Error("negative index in '" + g.p(ds) + "'");
+    return v;
+}
 std::vector<float> cat_f(const Groups& g, const std::string& ds) {
     std::vector<float> out;
     for (size_t s = 0; s < g.size(); ++s) {
@@ -456,18 +463,28 @@ struct PasteNode : GNode {
 // ========================================================= rama maps ===
 // per-residue periodic bicubic potential over (phi, psi)
 // (RamaMapPot, src/rama_map_pot.cpp:15-94; LayeredPeriodicSpline2D src/spline.h:444-499)
+// With lam_row set (RamaMap2, src/rama_map_pot.cpp:96-175), entry i is
+// scaled by the switch coordinate row lam_row[i] (the entry's position in
+// its system's residue list), which receives the unscaled map value.
 __global__ void rama_map_kernel(int n, const int* __restrict__ res, const int* __restrict__ layer,
                                 const int* __restrict__ sys, const float* __restrict__ coeff, int nxp, int nyp,
-                                float scale, const float* __restrict__ rama, float* rs, double* pot, float* res_log) {
+                                float scale, const float* __restrict__ rama, float* rs, double* pot, float* res_log,
+                                const int* __restrict__ lam_row, int lam_w, const float* __restrict__ lam, float* lam_s) {
     for (int i = grid_stride_start(); i < n; i += grid_stride()) {
         int r = res[i];
         float x = (rama[2 * r] + 3.14159265358979f) * scale, y = (rama[2 * r + 1] + 3.14159265358979f) * scale;
         float v, dx, dy;
         periodic2d(coeff + size_t(layer[i]) * nxp * nyp, nyp, x, y, v, dx, dy);
-        add_energy(pot, sys[i], v);
+        float l = 1.f;
+        if (lam_row) {
+            size_t lr = size_t(lam_row[i]) * lam_w;
+            l = lam[lr];
+            atomicAdd(lam_s + lr, v);
+        }
+        add_energy(pot, sys[i], v * l);
         if (res_log) res_log[i] = v;
-        atomicAdd(rs + 2 * r, dx * scale);
-        atomicAdd(rs + 2 * r + 1, dy * scale);
+        atomicAdd(rs + 2 * r, dx * scale * l);
+        atomicAdd(rs + 2 * r + 1, dy * scale * l);
     }
 }
 struct RamaMapNode : GNode {
@@ -480,9 +497,12 @@ struct RamaMapNode : GNode {
     bool log_pot = true;
     float* res_log = nullptr;
     std::vector<int> log_off;
-    RamaMapNode(Engine& e, const Groups& g, const std::vector<int>& o) {
+    int* lam_row = nullptr;  // RamaMap2: switch coordinate row of each entry
+    // lam_off: per-system rows of the switch coordinate (RamaMap2), else null
+    RamaMapNode(Engine& e, const Groups& g, const std::vector<int>& o, const std::vector<int>* lam_off = nullptr) {
         potential = true;
-        log_pot = shared_attr(g, "log_pot", 1.0) != 0.0;
+        // RamaMap2 keeps no per-residue log
+        log_pot = !lam_off && shared_attr(g, "log_pot", 1.0) != 0.0;
         LayerPool pool;
         std::vector<int> lay;
         auto c = counts(g, "residue_id");
@@ -500,11 +520,22 @@ struct RamaMapNode : GNode {
         nyp = pool.ny + 3;
         scale = float(pool.nx) * (0.5f / 3.14159265358979f - 1e-7f);
         n = int(lay.size());
-        res = e.upload(cat_idx(g, "residue_id", &o));
+        res = e.upload(cat_rows(g, "residue_id", o));
         layer = e.upload(lay);
         sysv = e.upload(sys_of(offsets(c)));
         coeff = e.upload(pool.coeff);
         log_off = offsets(c);
+        if (lam_off) {
+            std::vector<int> lr;
+            for (size_t s = 0; s < g.size(); ++s) {
+                int lim = (*lam_off)[s + 1] - (*lam_off)[s];
+                if (c[s] > lim)
+                    throw Error("switch coordinate has " + std::to_string(lim) + " rows for " + std::to_string(c[s]) +
+                                " residues");
+                for (int i = 0; i < c[s]; ++i) lr.push_back((*lam_off)[s] + i);
+            }
+            lam_row = e.upload(lr);
+        }
     }
     void forward(Engine& e, bool energy) override {
         auto& a = e.arg(*this, 0);
@@ -513,14 +544,247 @@ struct RamaMapNode : GNode {
             if (!res_log) res_log = e.alloc<float>(size_t(n));
             lg = res_log;
         }
+        const GNode* lam = lam_row ? &e.arg(*this, 1) : nullptr;
         rama_map_kernel<<<nblk(n), 256, 0, e.st>>>(n, res, layer, sysv, coeff, nxp, nyp, scale, a.out, a.sens,
-                                                   energy ? e.d_pot + size_t(pot_slot) * e.n_sys : nullptr, lg);
+                                                   energy ? e.d_pot + size_t(pot_slot) * e.n_sys : nullptr, lg,
+                                                   lam_row, lam ? lam->width : 0, lam ? lam->out : nullptr,
+                                                   lam ? lam->sens : nullptr);
     }
     void detailed_logs(Engine& e, std::vector<Log>& out) override {
         if (!res_log) return;
         std::vector<float> v(static_cast<size_t>(n));
         UG_CK(cudaMemcpy(v.data(), res_log, 4 * v.size(), cudaMemcpyDeviceToHost));
         out.push_back({"rama_map_potential", std::vector<double>(v.begin(), v.end()), log_off, false});
+    }
+};
+
+// ====================================================== switch nodes ===
+// SigmoidCoord: compact sigmoid of one column, or its complement for a
+// negative sign (SigmoidCoord, src/coord_map.cpp:609-675)
+__global__ void sigcoord_fwd(int n, const int* __restrict__ id, const float4* __restrict__ prm, int w, int dim1,
+                             const float* __restrict__ x, float* __restrict__ out, float* __restrict__ der) {
+    for (int i = grid_stride_start(); i < n; i += grid_stride()) {
+        float4 p = prm[i];  // c, s, sign
+        float v, d;
+        csig(x[size_t(id[i]) * w + dim1] - p.x, p.y, v, d);
+        out[i] = p.z > 0.f ? v : 1.f - v;
+        der[i] = p.z > 0.f ? d : -d;
+    }
+}
+__global__ void sigcoord_bwd(int n, const int* __restrict__ id, const float* __restrict__ der,
+                             const float* __restrict__ sens, int w, int dim1, float* xs) {
+    for (int i = grid_stride_start(); i < n; i += grid_stride())
+        atomicAdd(xs + size_t(id[i]) * w + dim1, sens[i] * der[i]);
+}
+struct SigmoidCoordNode : GNode {
+    int* id = nullptr;
+    float4* prm = nullptr;
+    float* der = nullptr;
+    int dim1 = 0;
+    SigmoidCoordNode(Engine& e, const Groups& g, const GNode& src) {
+        off = offsets(counts(g, "id"));
+        total = off.back();
+        width = 1;
+        dim1 = int(shared_attr(g, "dim1"));
+        if (dim1 < 0 || dim1 >= src.width) throw Error("dim1 out of range");
+        id = e.upload(cat_rows(g, "id", src.off));
+        auto c = cat_f(g, "c"), sh = cat_f(g, "s"), sg = cat_f(g, "sign");
+        if (int(c.size()) != total || int(sh.size()) != total || int(sg.size()) != total)
+            throw Error("c, s and sign must have one entry per id");
+        std::vector<float4> p;
+        for (int i = 0; i < total; ++i) p.push_back(make_float4(c[size_t(i)], sh[size_t(i)], sg[size_t(i)], 0.f));
+        prm = e.upload(p);
+        der = e.alloc<float>(size_t(std::max(1, total)));
+    }
+    void forward(Engine& e, bool) override {
+        auto& a = e.arg(*this, 0);
+        sigcoord_fwd<<<nblk(total), 256, 0, e.st>>>(total, id, prm, a.width, dim1, a.out, out, der);
+    }
+    void backward(Engine& e) override {
+        auto& a = e.arg(*this, 0);
+        sigcoord_bwd<<<nblk(total), 256, 0, e.st>>>(total, id, der, sens, a.width, dim1, a.sens);
+    }
+};
+
+// Add, Mean and Multiply of two coordinates into n_size rows of n_dim
+// (src/coord_operator.cpp:15-112, 114-226, 228-351).  Each output row
+// combines its entries in the reference's order (first argument's, then the
+// second's) from a per-row list.  As in the reference, Multiply passes each
+// factor the row's sensitivity times that factor's own last value written to
+// the row (not the other factor's), and rows without entries are 0.
+enum CombineOp { COMB_ADD = 0, COMB_MEAN = 1, COMB_MUL = 2 };
+__global__ void combine_fwd(int n_row, int op, int nd, const int* __restrict__ ptr, const int2* __restrict__ ent,
+                            const int* __restrict__ dims, const float* __restrict__ a, int aw,
+                            const float* __restrict__ b, int bw, float* __restrict__ out, float* __restrict__ fac) {
+    for (int r = grid_stride_start(); r < n_row; r += grid_stride()) {
+        int e0 = ptr[r], e1 = ptr[r + 1];
+        float last[2] = {1.f, 1.f};  // last value of each argument written to the row
+        for (int d = 0; d < nd; ++d) {
+            float acc = op == COMB_MUL ? 1.f : 0.f;
+            for (int k = e0; k < e1; ++k) {
+                int2 en = ent[k];  // (source row, argument)
+                float v = en.y ? b[size_t(en.x) * bw + dims[nd + d]] : a[size_t(en.x) * aw + dims[d]];
+                if (op == COMB_MUL) { acc *= v; last[en.y] = v; }
+                else acc += v;
+            }
+            if (op == COMB_MEAN && e1 > e0) acc *= 1.f / float(e1 - e0);
+            if (op == COMB_MUL && e1 == e0) acc = 0.f;
+            out[size_t(r) * nd + d] = acc;
+        }
+        // factor applied to the sensitivity an entry of argument 0 / 1 receives
+        fac[2 * r] = op == COMB_MUL ? last[0] : (op == COMB_MEAN && e1 > e0 ? 1.f / float(e1 - e0) : 1.f);
+        fac[2 * r + 1] = op == COMB_MUL ? last[1] : fac[2 * r];
+    }
+}
+__global__ void combine_bwd(int n_ent, int nd, const int* __restrict__ ent_row, const int2* __restrict__ ent,
+                            const int* __restrict__ dims, const float* __restrict__ sens, const float* __restrict__ fac,
+                            float* as, int aw, float* bs, int bw) {
+    for (int k = grid_stride_start(); k < n_ent; k += grid_stride()) {
+        int r = ent_row[k];
+        int2 en = ent[k];
+        float f = fac[2 * r + en.y];
+        for (int d = 0; d < nd; ++d) {
+            float g = sens[size_t(r) * nd + d] * f;
+            if (en.y) atomicAdd(bs + size_t(en.x) * bw + dims[nd + d], g);
+            else atomicAdd(as + size_t(en.x) * aw + dims[d], g);
+        }
+    }
+}
+struct CombineNode : GNode {
+    int op = COMB_ADD, n_ent = 0;
+    int *ptr = nullptr, *ent_row = nullptr, *dims = nullptr;
+    int2* ent = nullptr;
+    float* fac = nullptr;
+    std::vector<int> dim_h;
+    CombineNode(Engine& e, const Groups& g, int op_, const GNode& A, const GNode& B) : op(op_) {
+        const std::vector<int>&oa = A.off, &ob = B.off;
+        width = int(shared_attr(g, "n_dim"));
+        if (width < 1) throw Error("n_dim must be positive");
+        auto d1 = read_i(g.f(0), g.p("dim1")), d2 = read_i(g.f(0), g.p("dim2"));
+        for (size_t s = 1; s < g.size(); ++s)
+            if (read_i(g.f(s), g.p("dim1")) != d1 || read_i(g.f(s), g.p("dim2")) != d2)
+                throw Error("dim1/dim2 differ between systems of one batch");
+        if (int(d1.size()) != width || int(d2.size()) != width) throw Error("dim1 and dim2 need n_dim entries");
+        for (int i = 0; i < width; ++i)
+            if (d1[size_t(i)] < 0 || d1[size_t(i)] >= A.width || d2[size_t(i)] < 0 || d2[size_t(i)] >= B.width)
+                throw Error("The dim you gave is out of range!");
+        dim_h = d1;
+        dim_h.insert(dim_h.end(), d2.begin(), d2.end());
+        std::vector<int> p{0}, er;
+        std::vector<int2> en;
+        off.push_back(0);
+        for (size_t s = 0; s < g.size(); ++s) {
+            int n_size = int(attr_d(g.f(s), g.path, "n_size"));
+            auto ip1 = read_i(g.f(s), g.p("id_pos1")), ip2 = read_i(g.f(s), g.p("id_pos2"));
+            auto o1 = read_i(g.f(s), g.p("id1_out")), o2 = read_i(g.f(s), g.p("id2_out"));
+            if (o1.size() != ip1.size() || o2.size() != ip2.size()) throw Error("id*_out must match id_pos* in size");
+            int la = oa[s + 1] - oa[s], lb = ob[s + 1] - ob[s];
+            std::vector<std::vector<int2>> rows(size_t(std::max(0, n_size)));
+            auto put = [&](const std::vector<int>& ip, const std::vector<int>& oo, int lim, int base, int which) {
+                for (size_t i = 0; i < ip.size(); ++i) {
+                    if (ip[i] < 0 || ip[i] >= lim || oo[i] < 0 || oo[i] >= n_size)
+                        throw Error("The ID you gave is out of range!");
+                    rows[size_t(oo[i])].push_back(make_int2(base + ip[i], which));
+                }
+            };
+            put(ip1, o1, la, oa[s], 0);
+            put(ip2, o2, lb, ob[s], 1);
+            for (int r = 0; r < n_size; ++r) {
+                for (auto& x : rows[size_t(r)]) {
+                    en.push_back(x);
+                    er.push_back(off.back() + r);
+                }
+                p.push_back(int(en.size()));
+            }
+            off.push_back(off.back() + n_size);
+        }
+        total = off.back();
+        n_ent = int(en.size());
+        ptr = e.upload(p);
+        ent = e.upload(en);
+        ent_row = e.upload(er);
+        dims = e.upload(dim_h);
+        fac = e.alloc<float>(size_t(std::max(1, 2 * total)));
+    }
+    void forward(Engine& e, bool) override {
+        auto &a = e.arg(*this, 0), &b = e.arg(*this, 1);
+        combine_fwd<<<nblk(total), 256, 0, e.st>>>(total, op, width, ptr, ent, dims, a.out, a.width, b.out, b.width,
+                                                   out, fac);
+    }
+    void backward(Engine& e) override {
+        auto &a = e.arg(*this, 0), &b = e.arg(*this, 1);
+        combine_bwd<<<nblk(n_ent), 256, 0, e.st>>>(n_ent, width, ent_row, ent, dims, sens, fac, a.sens, a.width,
+                                                   b.sens, b.width);
+    }
+};
+
+// SigmoidEnergy / SigmoidLEnergy: a + b * compact_sigmoid(x - c, s) on one
+// column, times a switch coordinate row for the L form; with use_cutoff only
+// x within [min, max] counts, otherwise x beyond c -+ 1/s takes the plateau
+// value with no force (src/sigmoid_energy.cpp:9-91, 93-185)
+struct SigE {
+    float a, b, c, s, lo, hi;
+};
+__global__ void sigmoid_energy_kernel(int n, const int* __restrict__ id, const int* __restrict__ id2,
+                                      const SigE* __restrict__ prm, const int* __restrict__ sys, int w, int dim1,
+                                      int use_cutoff, const float* __restrict__ x, float* xs, int lw,
+                                      const float* __restrict__ lam, float* lam_s, double* pot) {
+    for (int i = grid_stride_start(); i < n; i += grid_stride()) {
+        SigE p = prm[i];
+        size_t r = size_t(id[i]) * w + dim1;
+        float v = x[r];
+        float l = id2 ? lam[size_t(id2[i]) * lw] : 1.f;
+        if (use_cutoff && (v > p.hi || v < p.lo)) continue;
+        if (v > p.hi) {
+            add_energy(pot, sys[i], l * p.a);
+        } else if (v < p.lo) {
+            add_energy(pot, sys[i], l * (p.a + p.b));
+        } else {
+            float sv, sd;
+            csig(v - p.c, p.s, sv, sd);
+            add_energy(pot, sys[i], l * (p.a + p.b * sv));
+            atomicAdd(xs + r, l * p.b * sd);
+            if (id2) atomicAdd(lam_s + size_t(id2[i]) * lw, p.a + p.b * sv);
+        }
+    }
+}
+struct SigmoidEnergyNode : GNode {
+    int *id = nullptr, *id2 = nullptr, *sysv = nullptr;
+    SigE* prm = nullptr;
+    int n = 0, dim1 = 0, use_cutoff = 0;
+    SigmoidEnergyNode(Engine& e, const Groups& g, const GNode& src, const GNode* lam) {
+        potential = true;
+        const char* idn = lam ? "id1" : "id";
+        auto so = offsets(counts(g, idn));
+        n = so.back();
+        id = e.upload(cat_rows(g, idn, src.off));
+        if (lam) id2 = e.upload(cat_rows(g, "id2", lam->off));
+        dim1 = int(shared_attr(g, "dim1"));
+        if (dim1 < 0 || dim1 >= src.width) throw Error("dim1 out of range");
+        use_cutoff = int(shared_attr(g, "use_cutoff"));
+        auto a = cat_f(g, "a"), b = cat_f(g, "b"), c = cat_f(g, "c"), sh = cat_f(g, "s"), lo = cat_f(g, "min"),
+             hi = cat_f(g, "max");
+        for (auto* v : {&a, &b, &c, &sh, &lo, &hi})
+            if (int(v->size()) != n) throw Error("parameter arrays must have one entry per id");
+        std::vector<SigE> p;
+        for (int i = 0; i < n; ++i) {
+            SigE q{a[size_t(i)], b[size_t(i)], c[size_t(i)], sh[size_t(i)], lo[size_t(i)], hi[size_t(i)]};
+            if (!use_cutoff) {
+                q.lo = q.c - 1.f / q.s;
+                q.hi = q.c + 1.f / q.s;
+            }
+            p.push_back(q);
+        }
+        prm = e.upload(p);
+        sysv = e.upload(sys_of(so));
+    }
+    void forward(Engine& e, bool energy) override {
+        auto& a = e.arg(*this, 0);
+        const GNode* lam = id2 ? &e.arg(*this, 1) : nullptr;
+        sigmoid_energy_kernel<<<nblk(n), 256, 0, e.st>>>(n, id, id2, prm, sysv, a.width, dim1, use_cutoff, a.out,
+                                                         a.sens, lam ? lam->width : 0, lam ? lam->out : nullptr,
+                                                         lam ? lam->sens : nullptr,
+                                                         energy ? e.d_pot + size_t(pot_slot) * e.n_sys : nullptr);
     }
 };
 
@@ -2294,6 +2558,7 @@ Engine::Engine(const std::vector<std::string>& paths, const std::vector<int>& n_
         std::vector<int> a;
         for (auto& x : deps[nm]) a.push_back(index.at(x));
         auto O = [&](int i) -> const std::vector<int>& { return nodes[size_t(a.at(size_t(i)))]->off; };
+        auto N = [&](int i) -> const GNode& { return *nodes[size_t(a.at(size_t(i)))]; };
         std::unique_ptr<GNode> n;
         try {
             if (is_prefix("Distance3D", nm)) n.reset(new DistNode(*this, g, O(0), O(1)));
@@ -2303,6 +2568,13 @@ Engine::Engine(const std::vector<std::string>& paths, const std::vector<int>& n_
             else if (is_prefix("rama_coord", nm)) n.reset(new PasteNode(*this, g, false, O(0), O(1)));
             else if (is_prefix("cat_pos", nm)) n.reset(new PasteNode(*this, g, true, O(0), O(1)));
             else if (is_prefix("rama_map_pot", nm)) n.reset(new RamaMapNode(*this, g, O(0)));
+            else if (is_prefix("RamaMap2", nm)) n.reset(new RamaMapNode(*this, g, O(0), &O(1)));
+            else if (is_prefix("SigmoidCoord", nm)) n.reset(new SigmoidCoordNode(*this, g, N(0)));
+            else if (is_prefix("SigmoidEnergy", nm)) n.reset(new SigmoidEnergyNode(*this, g, N(0), nullptr));
+            else if (is_prefix("SigmoidLEnergy", nm)) n.reset(new SigmoidEnergyNode(*this, g, N(0), &N(1)));
+            else if (is_prefix("Add", nm)) n.reset(new CombineNode(*this, g, COMB_ADD, N(0), N(1)));
+            else if (is_prefix("Mean", nm)) n.reset(new CombineNode(*this, g, COMB_MEAN, N(0), N(1)));
+            else if (is_prefix("Multiply", nm)) n.reset(new CombineNode(*this, g, COMB_MUL, N(0), N(1)));
             else if (is_prefix("affine_alignment", nm)) n.reset(new AffineNode(*this, g, O(0)));
             else if (is_prefix("backbone_pairs", nm)) n.reset(new BackbonePairsNode(*this, g, O(0)));
             else if (is_prefix("infer_H_O", nm)) n.reset(new InferHONode(*this, g, O(0)));
