@@ -730,6 +730,190 @@ template <class T> struct SigmoidEnergyNode : Node<T> {
     }
 };
 
+// Const3D: fixed 3-vectors, or positions of chosen rows of the argument
+// taken at the first evaluation and kept (ConstantCoord3D,
+// src/coord_const.cpp:107-179)
+template <class T> struct Const3DNode : Node<T> {
+    bool by_coord, done = false;
+    vector<int> id;
+    int dim[3];
+    Const3DNode(const H5& h) {
+        by_coord = h.attr("initialized_by_coord") != 0;
+        for (int k = 0; k < 3; ++k) dim[k] = int(h.attr(k == 0 ? "dim1" : (k == 1 ? "dim2" : "dim3")));
+        if (by_coord) {
+            id = h.ri("id");
+            this->alloc(int(id.size()), 3);
+        } else {
+            auto v = h.rd("value");
+            auto d = h.dims("value");
+            if (d.size() != 2 || d[1] != 3) throw Err("value must be (n, 3)");
+            this->alloc(int(d[0]), 3);
+            for (size_t i = 0; i < v.size(); ++i) this->out[i] = T(float(v[i]));
+        }
+    }
+    void forward(Engine<T>& e, bool) override {
+        if (!by_coord || done) return;
+        auto& p = e.arg(*this, 0);
+        for (size_t i = 0; i < id.size(); ++i)
+            for (int k = 0; k < 3; ++k) this->out[3 * i + size_t(k)] = p.out[size_t(id[i]) * p.width + dim[k]];
+        done = true;
+    }
+};
+
+// depth coordinate of a point for the membrane terms: z, or on a curved
+// bilayer sign * (|x - centre| - radius), with its gradient
+template <class T> T membrane_depth(const T* x, const T* cc, bool curved, T sign, T radius, T grad[3]) {
+    if (!curved) {
+        grad[0] = grad[1] = 0;
+        grad[2] = 1;
+        return x[2];
+    }
+    V3<T> d = V3<T>(x[0], x[1], x[2]) - V3<T>(cc[0], cc[1], cc[2]);
+    T dist = std::sqrt(mag2(d)), r = T(1) / dist;
+    // the reference's gradient uses (x, y, z - sign*radius*-1), which is
+    // x - centre for the centre (0, 0, -sign*radius) the config writes
+    grad[0] = sign * x[0] * r;
+    grad[1] = sign * x[1] * r;
+    grad[2] = sign * (x[2] - sign * radius * T(-1)) * r;
+    return sign * (dist - radius);
+}
+
+// left/right mirrored clamped spline of depth: ll * f(z) + lr * f(-z), with
+// ll the compact sigmoid switch at left_right_node; returns value, d/dz
+template <class T> void mirrored_spline(const T* c, int n, T z, T z0, T zs, T lr_node, T lr_sharp, T& v, T& dv) {
+    T sl, dsl;
+    compact_sigmoid(z - lr_node, lr_sharp, sl, dsl);
+    T ll = sl, lr = T(1) - sl, dll = dsl, dlr = -dsl;
+    T fl, dfl, fr, dfr;
+    clamped(c, (z - z0) * zs, n, fl, dfl);
+    clamped(c, (-z - z0) * zs, n, fr, dfr);
+    v = ll * fl + lr * fr;
+    dv = ll * dfl * zs + dll * fl - lr * dfr * zs + dlr * fr;
+}
+
+// CB membrane energy: burial level (weighted environment coverage) blended
+// over burial bins by compact sigmoids, times the mirrored depth spline of
+// the residue type and bin (MembraneCBPotential, src/membrane_potential.cpp:221-486)
+template <class T> struct MembraneCBNode : Node<T> {
+    vector<int> cb_index, res_type;
+    vector<T> weights, bl_nodes, coeff;
+    int n_restype, n_bl, n_node;
+    T bl_sharp, lr_node, lr_sharp, radius, sign, z0, zs;
+    bool curved;
+    MembraneCBNode(const H5& h) {
+        this->potential_node = true;
+        cb_index = h.ri("cb_index");
+        res_type = h.ri("res_type");
+        weights = h.rf<T>("weights");
+        bl_nodes = h.rf<T>("bl_nodes");
+        auto d = h.dims("coeff");
+        if (d.size() != 3) throw Err("coeff must be (n_restype, n_bl, n_node)");
+        n_restype = int(d[0]); n_bl = int(d[1]); n_node = int(d[2]);
+        if (int(bl_nodes.size()) != n_bl - 1) throw Err("bl_nodes must have n_bl - 1 entries");
+        coeff = h.rf<T>("coeff");
+        bl_sharp = T(float(h.attr("bl_range_sharpness")));
+        lr_node = T(float(h.attr("left_right_node")));
+        lr_sharp = T(float(h.attr("left_right_sharpness")));
+        curved = h.attr("use_curvature") != 0;
+        radius = T(float(h.attr("curvature_radius")));
+        sign = T(float(h.attr("curvature_sign")));
+        z0 = T(float(h.attr("z_start")));
+        zs = T(float(h.attr("z_scale")));
+    }
+    void forward(Engine<T>& e, bool energy) override {
+        auto& cb = e.arg(*this, 0);
+        auto& env = e.arg(*this, 1);
+        auto& cc = e.arg(*this, 2);
+        radius = cc.out[2] * T(-1) * sign;
+        T pot = 0;
+        const size_t nb = static_cast<size_t>(n_bl);
+        vector<T> s1(nb), ds1(nb), s2(nb), ds2(nb), bs(nb), dbs(nb);
+        for (size_t nr = 0; nr < cb_index.size(); ++nr) {
+            int rt = res_type[nr], ri = cb_index[nr];
+            T bl = 0;
+            for (int a = 0; a < n_restype; ++a) bl += weights[size_t(a)] * env.out[size_t(ri) * n_restype + a];
+            for (int i = 0; i < n_bl - 1; ++i) {
+                T v, dd;
+                compact_sigmoid(bl - bl_nodes[size_t(i)], bl_sharp, v, dd);
+                s1[size_t(i)] = v; ds1[size_t(i)] = dd;
+                compact_sigmoid(bl_nodes[size_t(i)] - bl, bl_sharp, v, dd);
+                s2[size_t(i)] = v; ds2[size_t(i)] = -dd;
+            }
+            bs[0] = s1[0]; dbs[0] = ds1[0];
+            bs[size_t(n_bl - 1)] = s2[size_t(n_bl - 2)]; dbs[size_t(n_bl - 1)] = ds2[size_t(n_bl - 2)];
+            for (int i = 0; i < n_bl - 2; ++i) {
+                bs[size_t(i + 1)] = s2[size_t(i)] * s1[size_t(i + 1)];
+                dbs[size_t(i + 1)] = ds2[size_t(i)] * s1[size_t(i + 1)] + s2[size_t(i)] * ds1[size_t(i + 1)];
+            }
+            T* x = &cb.out[size_t(ri) * cb.width];
+            T gz[3];
+            T z = membrane_depth(x, &cc.out[0], curved, sign, radius, gz);
+            T dz = 0, dbl = 0;
+            for (int i = 0; i < n_bl; ++i) {
+                T f, df;
+                mirrored_spline(&coeff[(size_t(rt) * n_bl + size_t(i)) * n_node], n_node, z, z0, zs, lr_node, lr_sharp,
+                                f, df);
+                pot += bs[size_t(i)] * f;
+                dbl += dbs[size_t(i)] * f;
+                dz += bs[size_t(i)] * df;
+            }
+            T* xs = &cb.sens[size_t(ri) * cb.width];
+            for (int k = 0; k < 3; ++k) xs[k] += dz * gz[k];
+            for (int a = 0; a < n_restype; ++a) env.sens[size_t(ri) * n_restype + a] += weights[size_t(a)] * dbl;
+        }
+        this->pot = energy ? pot : T(0);
+    }
+};
+
+// backbone H/O membrane energy: (1 - p)^2 f0(depth) + (1 - (1 - p)^2) f1(depth)
+// with p the hbond probability of the donor/acceptor (column 6 of
+// protein_hbond) (MembraneHBPotential, src/membrane_potential.cpp:488-672)
+template <class T> struct MembraneHBNode : Node<T> {
+    vector<int> hb_index, hb_type;
+    vector<T> coeff;
+    int n_node;
+    T lr_node, lr_sharp, radius, sign, z0, zs;
+    bool curved;
+    MembraneHBNode(const H5& h) {
+        this->potential_node = true;
+        hb_index = h.ri("hb_index");
+        hb_type = h.ri("hb_type");
+        auto d = h.dims("coeff");
+        if (d.size() != 3 || d[0] != 2 || d[1] != 2) throw Err("coeff must be (2, 2, n_node)");
+        n_node = int(d[2]);
+        coeff = h.rf<T>("coeff");
+        lr_node = T(float(h.attr("left_right_node")));
+        lr_sharp = T(float(h.attr("left_right_sharpness")));
+        curved = h.attr("use_curvature") != 0;
+        radius = T(float(h.attr("curvature_radius")));
+        sign = T(float(h.attr("curvature_sign")));
+        z0 = T(float(h.attr("z_start")));
+        zs = T(float(h.attr("z_scale")));
+    }
+    void forward(Engine<T>& e, bool energy) override {
+        auto& hb = e.arg(*this, 0);
+        auto& cc = e.arg(*this, 1);
+        radius = cc.out[2] * T(-1) * sign;
+        T pot = 0;
+        for (size_t nv = 0; nv < hb_index.size(); ++nv) {
+            int rt = hb_type[nv], ri = hb_index[nv];
+            T* x = &hb.out[size_t(ri) * hb.width];
+            T* xs = &hb.sens[size_t(ri) * hb.width];
+            T gz[3];
+            T z = membrane_depth(x, &cc.out[0], curved, sign, radius, gz);
+            T p = x[6], u = T(1) - p;
+            T f1, df1, f2, df2;
+            mirrored_spline(&coeff[size_t(rt) * 2 * n_node], n_node, z, z0, zs, lr_node, lr_sharp, f1, df1);
+            mirrored_spline(&coeff[(size_t(rt) * 2 + 1) * n_node], n_node, z, z0, zs, lr_node, lr_sharp, f2, df2);
+            T w1 = u * u, w2 = T(1) - u * u;
+            pot += w1 * f1 + w2 * f2;
+            xs[6] += -T(2) * u * f1 + T(2) * u * f2;
+            for (int k = 0; k < 3; ++k) xs[k] += (w1 * df1 + w2 * df2) * gz[k];
+        }
+        this->pot = energy ? pot : T(0);
+    }
+};
+
 // Rigid frame per residue from N, CA, C (AffineAlignment, src/eig.cpp:277-470).
 // Output (center, quaternion); sensitivity slots 3..5 carry the torque.
 template <class T> struct AffineNode : Node<T> {
@@ -2066,6 +2250,9 @@ template <class T> std::unique_ptr<Node<T>> make_node(const string& name, const 
     if (is_prefix("rama_coord", name)) return P(new PasteRamaNode<T>(h));
     if (is_prefix("rama_map_pot", name)) return P(new RamaMapNode<T>(h));
     if (is_prefix("RamaMap2", name)) return P(new RamaMap2Node<T>(h));
+    if (is_prefix("Const3D", name)) return P(new Const3DNode<T>(h));
+    if (is_prefix("cb_membrane_potential", name)) return P(new MembraneCBNode<T>(h));
+    if (is_prefix("hb_membrane_potential", name)) return P(new MembraneHBNode<T>(h));
     if (is_prefix("SigmoidCoord", name)) return P(new SigmoidCoordNode<T>(h));
     if (is_prefix("SigmoidEnergy", name)) return P(new SigmoidEnergyNode<T>(h, false));
     if (is_prefix("SigmoidLEnergy", name)) return P(new SigmoidEnergyNode<T>(h, true));

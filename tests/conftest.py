@@ -50,6 +50,21 @@ def transcis_config(tmp_path_factory, built):
     return path, np.load(os.path.join(GOLDEN, "syn_transcis_ref.npz"))
 
 
+@pytest.fixture(scope="session")
+def membrane_configs(tmp_path_factory, built):
+    """The membrane fixture configs (golden/membrane_spec.py), by variant,
+    and their reference data."""
+    if GOLDEN not in sys.path:
+        sys.path.insert(0, GOLDEN)
+    import membrane_spec
+    d = tmp_path_factory.mktemp("memb")
+    paths = {}
+    for var in membrane_spec.VARIANTS:
+        paths[var] = str(d / ("syn_membrane_%s.up" % var))
+        membrane_spec.write(paths[var], var)
+    return paths, np.load(os.path.join(GOLDEN, "syn_membrane_ref.npz"))
+
+
 def quat_align(a, ref):
     """Flip the quaternion columns (3:7) of affine outputs to the sign of ref
     (q and -q are the same rotation)."""

@@ -19,6 +19,10 @@ this script, which are committed (the GPU host has no reference checkout):
                      frames, reference energy and derivative, and the
                      trans-cis nodes' outputs and sensitivities per frame
                      (python make_fixtures.py trans_cis writes only this file)
+  syn_membrane_ref.npz the membrane fixture (membrane_spec.py), flat and
+                     curved: frames, reference energy and derivative, and the
+                     membrane nodes' outputs and sensitivities per frame
+                     (python make_fixtures.py membrane writes only this file)
 
 The reference engine is oracle/_ref/libupside_ref.so (oracle/build.py).
 """
@@ -183,6 +187,36 @@ def trans_cis(L, tmpdir="/tmp"):
     np.savez_compressed(os.path.join(HERE, "syn_transcis_ref.npz"), **out)
 
 
+MEMBRANE_NODES = ["cb_membrane_potential", "hb_membrane_potential", "Const3D_curvature_center", "Const3D_probe",
+                  "placement_fixed_point_only_CB"]
+
+
+def membrane(L, tmpdir="/tmp"):
+    """syn_membrane_ref.npz: both variants of membrane_spec.py at the same
+    frames (evaluated in order, so the probe keeps frame 0's positions): the
+    reference engine's energy, derivative, and the membrane nodes' outputs
+    and sensitivities."""
+    import membrane_spec as M
+    frames = M.frames()
+    out = {"pos": frames}
+    for var in M.VARIANTS:
+        path = os.path.join(tmpdir, "syn_membrane_%s.up" % var)
+        M.write(path, var)
+        eng = RefEngine(L, path, frames.shape[1])
+        E, D = [], []
+        for x in frames:
+            e, d = eng.eval(x)
+            E.append(e)
+            D.append(d)
+            for nm in MEMBRANE_NODES:
+                out.setdefault("%s/out/%s" % (var, nm), []).append(eng.node(nm))
+                out.setdefault("%s/sens/%s" % (var, nm), []).append(eng.node(nm, sens=True))
+        out[var + "/ref_energy"] = E
+        out[var + "/ref_deriv"] = D
+    out = {k: np.array(v) for k, v in out.items()}
+    np.savez_compressed(os.path.join(HERE, "syn_membrane_ref.npz"), **out)
+
+
 KAT_SRC = r"""
 #include <cstdio>
 #include <cstdint>
@@ -219,6 +253,9 @@ def main():
     if sys.argv[1:] == ["trans_cis"]:
         trans_cis(load_ref())
         return
+    if sys.argv[1:] == ["membrane"]:
+        membrane(load_ref())
+        return
     threefry_kat()
     L = load_ref()
     chig(L)
@@ -226,6 +263,7 @@ def main():
     synthetic(L, 60, 1)
     synthetic(L, 150, 2, n_frames=2)
     trans_cis(L)
+    membrane(L)
 
 
 if __name__ == "__main__":

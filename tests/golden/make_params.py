@@ -3,7 +3,7 @@ from the reference checkout into tests/golden/ff21_params.npz.
 
 Run here (where the reference checkout exists); the .npz is committed so the
 generator works on hosts without the reference.  Sources:
-parameters/ff_2.1/{sidechain.h5,environment.h5,hbond.h5,bb_env.dat} and
+parameters/ff_2.1/{sidechain.h5,environment.h5,hbond.h5,bb_env.dat,membrane.h5} and
 parameters/common/rama_reference.pkl.
 """
 import os
@@ -35,6 +35,11 @@ def main():
     with H5File(os.path.join(P, "ff_2.1", "hbond.h5")) as f:
         out["hbond_parameter"] = f.read("/parameter")
     out["bb_env"] = np.loadtxt(os.path.join(P, "ff_2.1", "bb_env.dat"))
+    with H5File(os.path.join(P, "ff_2.1", "membrane.h5")) as f:
+        for k in ["names", "cb_energy", "hb_energy", "burial_nodes"]:
+            out["mem_" + k] = f.read("/" + k)
+        for k in ["cb_z_min", "cb_z_max", "hb_z_min", "hb_z_max"]:
+            out["mem_" + k] = np.float64(f.attr("/", k))
     with open(os.path.join(P, "common", "rama_reference.pkl"), "rb") as fh:
         out["rama_reference"] = np.asarray(pickle.load(fh, encoding="latin1"), dtype=np.float64)
     np.savez_compressed(os.path.join(HERE, "ff21_params.npz"), **out)

@@ -243,3 +243,57 @@ def test_config_trans_cis_and_fixed_rotamers(transcis_config):
     assert (res == 12).sum() > 1
     with pytest.raises(ValueError):
         config_gen.read_trans_cis([(4, 0, 1.0, 0.5, 45.0)], seq)  # not a proline
+
+
+@pytest.mark.parametrize("fp64", [False, True])
+@pytest.mark.parametrize("variant", ["flat", "curved"])
+def test_membrane_golden_frames(membrane_configs, variant, fp64):
+    """cb_membrane_potential, hb_membrane_potential and Const3D
+    (src/membrane_potential.cpp:221-672, src/coord_const.cpp:107-179) against
+    the reference engine, frames evaluated in order so the position-captured
+    Const3D keeps the first frame's atoms."""
+    import oracle_py
+    paths, z = membrane_configs
+    path = paths[variant]
+    o = oracle_py.Oracle(path, z["pos"].shape[1], fp64=fp64)
+    for k in range(len(z["pos"])):
+        e, d = o.evaluate(z["pos"][k])
+        assert rel_e(e, z[variant + "/ref_energy"][k], energy_scale(o, path)) < E_REF_TOL, k
+        assert rel_f(d, z[variant + "/ref_deriv"][k]) < F_REF_TOL, k
+        for key in z.files:
+            if not key.startswith(variant + "/out/"):
+                continue
+            nm = key.split("/", 2)[2]
+            ref, sref = z[key][k], z[variant + "/sens/" + nm][k]
+            assert np.abs(o.node(nm) - ref).max() <= 1e-5 * max(np.abs(ref).max(), 1.0), (k, nm)
+            # the CB placement's sensitivity sums the membrane force with the
+            # reference's other consumers of the point (approximate rsqrt)
+            tol = 1e-4 if nm == "placement_fixed_point_only_CB" else 1e-5
+            assert np.abs(o.node(nm, sens=True) - sref).max() <= tol * max(np.abs(sref).max(), 1.0), (k, nm)
+
+
+def test_membrane_frames_cover_slab(membrane_configs):
+    """The frames put CB atoms inside the slab, in both head-group regions
+    and outside, and the probe keeps frame 0's coordinates."""
+    _, z = membrane_configs
+    cbz = z["flat/out/placement_fixed_point_only_CB"][..., 2].ravel()
+    for lo, hi in ((-np.inf, -20), (-20, -10), (-5, 5), (10, 20), (20, np.inf)):
+        assert ((cbz > lo) & (cbz < hi)).any(), (lo, hi)
+    assert np.array_equal(z["flat/out/Const3D_probe"][3], z["pos"][0][[5, 17]])
+
+
+def test_config_membrane(membrane_configs):
+    """Structure of the membrane writer (py/upside_config.py:1727-1835)."""
+    import membrane_spec
+    from h5lite import H5File
+    paths, _ = membrane_configs
+    f = H5File(paths["curved"])
+    g = "/input/potential/cb_membrane_potential"
+    assert [a.decode() for a in f.attr(g, "arguments")] == [
+        "placement_fixed_point_only_CB", "environment_coverage_sc", "Const3D_curvature_center"]
+    assert f.attr(g, "z_start") == -17.0 - 15.0 and f.attr(g, "z_scale") == 0.5
+    cb = f.read(g + "/cb_index")
+    assert len(cb) == membrane_spec.N_RES - 3 and not set(cb) & set(membrane_spec.EXCLUDE)
+    h = "/input/potential/hb_membrane_potential"
+    assert f.attr(h, "z_start") == -33.0 - 15.0 and f.attr(h, "use_curvature") == 1
+    assert np.array_equal(f.read("/input/potential/Const3D_curvature_center/value"), [[0., 0., 60.]])

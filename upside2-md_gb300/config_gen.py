@@ -264,7 +264,8 @@ def fix_rotamer_states(table, seq, params=None):
 def write_config(path, seq, seed, chain_first_residue=(), pos=None, environment_potential_type=1,
                  damping=0.4, chain_offsets=None, params=None, bp_tol=1e-3, moves=False,
                  jump_length_scale=5., jump_rotation_scale=30., trans_cis=None, fix_rotamer=None,
-                 extra_nodes=()):
+                 extra_nodes=(), membrane_thickness=None, membrane_exclude_residues=(), use_curvature=False,
+                 curvature_radius=200., curvature_sign=1):
     """Write an ff_2.1 `.up` file for `seq` (list of 3-letter codes).
 
     chain_first_residue: residue indices (excluding 0) where new chains start.
@@ -286,6 +287,13 @@ def write_config(path, seq, seed, chain_first_residue=(), pos=None, environment_
     its own Rama map; every other term treats it as PRO.
     extra_nodes: further nodes, each (name, arguments, attributes dict,
       datasets dict), written after the standard ones.
+    membrane_thickness: write the ff_2.1 membrane potential for a bilayer of
+      this thickness (angstrom) normal to z, as --membrane-potential does:
+      burial- and depth-dependent CB energies, depth-dependent energies of
+      free and bonded backbone H/O, a CB placement and the curvature centre
+      (write_membrane_potential3, py/upside_config.py:1727-1835, and write_CB
+      :379-395).  membrane_exclude_residues skip the CB term; use_curvature,
+      curvature_radius and curvature_sign bend the bilayer into a sphere.
     """
     P = load_params(params)
     rng = np.random.RandomState(seed)
@@ -683,6 +691,45 @@ def write_config(path, seq, seed, chain_first_residue=(), pos=None, environment_
     g = c.grp("affine_alignment", ["pos"])
     c.ds(g + "/atoms", np.column_stack((N_id, N_id + 1, N_id + 2)))
     c.ds(g + "/ref_geom", ref_geom)
+
+    if membrane_thickness is not None:
+        half = 0.5 * membrane_thickness
+        names = [x.decode() for x in P["mem_names"]]
+        cb_e, hb_e, nodes = P["mem_cb_energy"], P["mem_hb_energy"], P["mem_burial_nodes"]
+        if nodes.size + 1 != cb_e.shape[1]:
+            raise ValueError("burial nodes do not match the membrane energy table")
+        cb_dz = (P["mem_cb_z_max"] - P["mem_cb_z_min"]) / (cb_e.shape[2] - 2)
+        hb_dz = (P["mem_hb_z_max"] - P["mem_hb_z_min"]) / (hb_e.shape[2] - 2)
+        g = c.grp("Const3D_curvature_center", ["pos"], dim1=0, dim2=1, dim3=2, initialized_by_coord=0)
+        c.ds(g + "/id", np.arange(1))
+        c.ds(g + "/value", np.array([[0., 0., curvature_radius * -1 * curvature_sign]]))
+        common = dict(integrator_level=0, left_right_node=0.0, half_thickness=half, use_curvature=int(use_curvature),
+                      curvature_radius=curvature_radius, curvature_sign=curvature_sign)
+        g = c.grp("cb_membrane_potential",
+                  ["placement_fixed_point_only_CB", "environment_coverage_sc", "Const3D_curvature_center"],
+                  z_start=P["mem_cb_z_min"] - half, z_scale=1. / cb_dz, bl_range_sharpness=1.0,
+                  left_right_sharpness=1. / cb_dz, **common)
+        used = np.array([r for r in range(n_res) if r not in set(membrane_exclude_residues)], dtype=int)
+        c.ds(g + "/cb_index", used)
+        c.ds(g + "/res_type", np.array([names.index(seq[r]) for r in used], dtype=int))
+        c.ds(g + "/weights", weights[:20])
+        c.ds(g + "/bl_nodes", nodes)
+        c.ds(g + "/coeff", cb_e)
+        g = c.grp("hb_membrane_potential", ["protein_hbond", "Const3D_curvature_center"],
+                  z_start=P["mem_hb_z_min"] - half, z_scale=1. / hb_dz, left_right_sharpness=1. / hb_dz, **common)
+        res_hb = np.concatenate([donors, acceptors])
+        c.ds(g + "/hb_index", np.array([i for i, r in enumerate(res_hb) if r not in excluded], dtype=int))
+        c.ds(g + "/hb_type", np.concatenate([np.zeros(n_don, dtype='i'), np.ones(n_acc, dtype='i')]))
+        c.ds(g + "/coeff", hb_e)
+        ref_cb = np.zeros((4, 3))
+        ref_cb[0] = (-1.19280531, -0.83127186, 0.)
+        ref_cb[2] = (1.25222632, -0.87268266, 0.)
+        ref_cb[3] = (0., 0.94375626, 1.2068012)
+        ref_cb -= ref_cb[:3].mean(axis=0, keepdims=True)
+        g = c.grp("placement_fixed_point_only_CB", ["affine_alignment"])
+        c.ds(g + "/affine_residue", np.arange(n_res))
+        c.ds(g + "/layer_index", np.zeros(n_res, dtype='i'))
+        c.ds(g + "/placement_data", ref_cb[3][None])
 
     for name, args, attrs, dsets in extra_nodes:
         g = c.grp(name, args, **attrs)

@@ -788,6 +788,257 @@ struct SigmoidEnergyNode : GNode {
     }
 };
 
+// ========================================================== Const3D ===
+// fixed 3-vectors, or chosen rows of the argument taken at the first
+// evaluation and kept (ConstantCoord3D, src/coord_const.cpp:107-179); a
+// per-row flag makes the capture happen once, also inside a replayed graph
+__global__ void const3d_kernel(int n, const float* __restrict__ val, const int* __restrict__ src, int w, int3 dim,
+                               const float* __restrict__ x, int* taken, float* __restrict__ out) {
+    for (int i = grid_stride_start(); i < n; i += grid_stride()) {
+        if (!src) {
+            for (int k = 0; k < 3; ++k) out[3 * size_t(i) + k] = val[3 * size_t(i) + k];
+        } else if (!taken[i]) {
+            const float* r = x + size_t(src[i]) * w;
+            out[3 * size_t(i)] = r[dim.x];
+            out[3 * size_t(i) + 1] = r[dim.y];
+            out[3 * size_t(i) + 2] = r[dim.z];
+            taken[i] = 1;
+        }
+    }
+}
+struct Const3DNode : GNode {
+    float* val = nullptr;
+    int *src = nullptr, *taken = nullptr;
+    int3 dim{0, 1, 2};
+    Const3DNode(Engine& e, const Groups& g, const GNode& a) {
+        width = 3;
+        bool by_coord = shared_attr(g, "initialized_by_coord") != 0.0;
+        dim = make_int3(int(shared_attr(g, "dim1")), int(shared_attr(g, "dim2")), int(shared_attr(g, "dim3")));
+        if (by_coord) {
+            for (int d : {dim.x, dim.y, dim.z})
+                if (d < 0 || d >= a.width) throw Error("dim out of range");
+            off = offsets(counts(g, "id"));
+            total = off.back();
+            src = e.upload(cat_rows(g, "id", a.off));
+            taken = e.alloc<int>(size_t(std::max(1, total)));
+            UG_CK(cudaMemsetAsync(taken, 0, 4 * size_t(std::max(1, total)), e.st));
+        } else {
+            std::vector<float> v;
+            off.push_back(0);
+            for (size_t s = 0; s < g.size(); ++s) {
+                auto d = g.f(s).dims(g.p("value"));
+                if (d.size() != 2 || d[1] != 3) throw Error("value must be (n, 3)");
+                auto x = read_f(g.f(s), g.p("value"));
+                v.insert(v.end(), x.begin(), x.end());
+                off.push_back(off.back() + int(d[0]));
+            }
+            total = off.back();
+            val = e.upload(v);
+        }
+    }
+    void forward(Engine& e, bool) override {
+        auto& a = e.arg(*this, 0);
+        const3d_kernel<<<nblk(total), 256, 0, e.st>>>(total, val, src, a.width, dim, a.out, taken, out);
+    }
+};
+
+// ========================================================= membrane ===
+// Depth of a point for the membrane terms: z, or on a curved bilayer
+// sign * (|x - centre| - radius), with d(depth)/dx; radius is the centre's
+// -z * sign as the reference recomputes it every evaluation
+__device__ __forceinline__ float membrane_depth(f3 x, f3 cc, int curved, float sign, f3& g) {
+    if (!curved) {
+        g = mk(0.f, 0.f, 1.f);
+        return x.z;
+    }
+    float radius = cc.z * -1.f * sign;
+    f3 d = x - cc;
+    float dist = sqrtf(mag2(d)), r = 1.f / dist;
+    // the reference's gradient is sign * (x, y, z - sign*radius*-1) / dist
+    g = mk(sign * x.x * r, sign * x.y * r, sign * (x.z - sign * radius * -1.f) * r);
+    return sign * (dist - radius);
+}
+// ll * f(z) + lr * f(-z) with ll the compact sigmoid switch at lr_node;
+// value and d/dz (src/membrane_potential.cpp:330-360)
+__device__ __forceinline__ void mirrored_spline(const float* c, int n, float z, float z0, float zs, float lr_node,
+                                                float lr_sharp, float& v, float& dv) {
+    float sl, dsl;
+    csig(z - lr_node, lr_sharp, sl, dsl);
+    float fl, dfl, fr, dfr;
+    clamped(c, (z - z0) * zs, n, fl, dfl);
+    clamped(c, (-z - z0) * zs, n, fr, dfr);
+    float ll = sl, lr = 1.f - sl;
+    v = ll * fl + lr * fr;
+    dv = ll * dfl * zs + dsl * fl - lr * dfr * zs - dsl * fr;
+}
+struct MembParams {
+    float z0, zs, lr_node, lr_sharp, sign, bl_sharp;
+    int curved, n_node;
+};
+// CB term (MembraneCBPotential, src/membrane_potential.cpp:221-486): burial
+// level = weights . environment coverage of the residue, blended over the
+// burial bins by compact sigmoids, times each bin's mirrored depth spline of
+// the residue type
+__global__ void memb_cb_kernel(int n, MembParams P, int n_rt, int n_bl, const int* __restrict__ cb_row,
+                               const int* __restrict__ env_row, const int* __restrict__ cc_row,
+                               const int* __restrict__ rtype, const int* __restrict__ sys,
+                               const float* __restrict__ wts, const float* __restrict__ bl_nodes,
+                               const float* __restrict__ coeff, int cbw, const float* __restrict__ cb, float* cbs,
+                               int ew, const float* __restrict__ env, float* envs, const float* __restrict__ cc,
+                               double* pot) {
+    for (int i = grid_stride_start(); i < n; i += grid_stride()) {
+        const size_t er = size_t(env_row[i]);
+        float bl = 0.f;
+        for (int a = 0; a < n_rt; ++a) bl += wts[a] * env[(er + a) * ew];
+        f3 x = ld3(cb + size_t(cb_row[i]) * cbw);
+        f3 g;
+        float z = membrane_depth(x, ld3(cc + 3 * size_t(cc_row[i])), P.curved, P.sign, g);
+        float e = 0.f, dz = 0.f, dbl = 0.f;
+        // bins: 0 = above node 0, k = between nodes k-1 and k, last = below
+        // the last node; s1/s2 the rising/falling sigmoids of each node
+        float s2p = 0.f, ds2p = 0.f;
+        for (int b = 0; b < n_bl; ++b) {
+            float s1 = 1.f, ds1 = 0.f, s2 = 0.f, ds2 = 0.f;
+            if (b < n_bl - 1) {
+                float v, d;
+                csig(bl - bl_nodes[b], P.bl_sharp, v, d);
+                s1 = v; ds1 = d;
+                csig(bl_nodes[b] - bl, P.bl_sharp, v, d);
+                s2 = v; ds2 = -d;
+            }
+            float w, dw;
+            if (b == 0) { w = s1; dw = ds1; }
+            else if (b == n_bl - 1) { w = s2p; dw = ds2p; }
+            else { w = s2p * s1; dw = ds2p * s1 + s2p * ds1; }
+            float f, df;
+            mirrored_spline(coeff + (size_t(rtype[i]) * n_bl + b) * P.n_node, P.n_node, z, P.z0, P.zs, P.lr_node,
+                            P.lr_sharp, f, df);
+            e += w * f;
+            dbl += dw * f;
+            dz += w * df;
+            s2p = s2;
+            ds2p = ds2;
+        }
+        add_energy(pot, sys[i], e);
+        atomic_add3(cbs + size_t(cb_row[i]) * cbw, g * dz);
+        for (int a = 0; a < n_rt; ++a) atomicAdd(envs + (er + a) * ew, wts[a] * dbl);
+    }
+}
+// backbone H/O term (MembraneHBPotential, src/membrane_potential.cpp:488-672):
+// (1-p)^2 f0(depth) + (1 - (1-p)^2) f1(depth), p the hbond probability
+// (column 6 of protein_hbond), f0/f1 the mirrored splines of the donor or
+// acceptor type
+__global__ void memb_hb_kernel(int n, MembParams P, const int* __restrict__ hb_row, const int* __restrict__ cc_row,
+                               const int* __restrict__ htype, const int* __restrict__ sys,
+                               const float* __restrict__ coeff, int hw, const float* __restrict__ hb, float* hbs,
+                               const float* __restrict__ cc, double* pot) {
+    for (int i = grid_stride_start(); i < n; i += grid_stride()) {
+        const float* r = hb + size_t(hb_row[i]) * hw;
+        f3 g;
+        float z = membrane_depth(ld3(r), ld3(cc + 3 * size_t(cc_row[i])), P.curved, P.sign, g);
+        float f1, df1, f2, df2;
+        const float* c = coeff + size_t(htype[i]) * 2 * P.n_node;
+        mirrored_spline(c, P.n_node, z, P.z0, P.zs, P.lr_node, P.lr_sharp, f1, df1);
+        mirrored_spline(c + P.n_node, P.n_node, z, P.z0, P.zs, P.lr_node, P.lr_sharp, f2, df2);
+        float u = 1.f - r[6], w1 = u * u, w2 = 1.f - u * u;
+        add_energy(pot, sys[i], w1 * f1 + w2 * f2);
+        float* rs = hbs + size_t(hb_row[i]) * hw;
+        atomicAdd(rs + 6, -2.f * u * f1 + 2.f * u * f2);
+        atomic_add3(rs, g * (w1 * df1 + w2 * df2));
+    }
+}
+struct MembraneNode : GNode {
+    bool cb_term;
+    int n = 0, n_rt = 0, n_bl = 1;
+    MembParams P{};
+    int *row = nullptr, *env_row = nullptr, *cc_row = nullptr, *type = nullptr, *sysv = nullptr;
+    float *wts = nullptr, *bl_nodes = nullptr, *coeff = nullptr;
+    std::vector<float> h_coeff;
+    // cb: arguments (CB points, environment coverage, curvature centre);
+    // hb: (protein_hbond, curvature centre)
+    MembraneNode(Engine& e, const Groups& g, bool cb, const GNode& pts, const GNode* env, const GNode& cc)
+        : cb_term(cb) {
+        potential = true;
+        const char* idx = cb ? "cb_index" : "hb_index";
+        auto so = offsets(counts(g, idx));
+        n = so.back();
+        if (pts.width < (cb ? 3 : 7)) throw Error(cb ? "CB coordinates need width 3" : "protein_hbond needs width 7");
+        auto d = g.f(0).dims(g.p("coeff"));
+        if (d.size() != 3) throw Error("coeff must be 3-dimensional");
+        h_coeff = shared_f(g, "coeff");
+        P.n_node = int(d[2]);
+        if (P.n_node < 4) throw Error("coeff needs at least 4 nodes");
+        P.z0 = float(shared_attr(g, "z_start"));
+        P.zs = float(shared_attr(g, "z_scale"));
+        P.lr_node = float(shared_attr(g, "left_right_node"));
+        P.lr_sharp = float(shared_attr(g, "left_right_sharpness"));
+        P.curved = int(shared_attr(g, "use_curvature"));
+        P.sign = float(shared_attr(g, "curvature_sign"));
+        auto rows = cat_rows(g, idx, pts.off);
+        auto types = cat_f(g, cb ? "res_type" : "hb_type");
+        if (int(types.size()) != n) throw Error(std::string(cb ? "res_type" : "hb_type") + " needs one entry per index");
+        std::vector<int> ty, ccr, envr;
+        for (size_t s = 0; s < g.size(); ++s) {
+            if (cc.off[s + 1] - cc.off[s] < 1) throw Error("curvature centre has no row");
+            for (int i = so[s]; i < so[s + 1]; ++i) ccr.push_back(cc.off[s]);
+        }
+        if (cb) {
+            n_rt = int(d[0]);
+            n_bl = int(d[1]);
+            P.bl_sharp = float(shared_attr(g, "bl_range_sharpness"));
+            auto w = shared_f(g, "weights");
+            auto bn = shared_f(g, "bl_nodes");
+            if (int(w.size()) < n_rt) throw Error("weights needs one entry per residue type");
+            if (int(bn.size()) != n_bl - 1 || n_bl < 2) throw Error("bl_nodes must have n_bl - 1 entries");
+            wts = e.upload(w);
+            bl_nodes = e.upload(bn);
+            for (size_t s = 0; s < g.size(); ++s) {
+                auto loc = read_i(g.f(s), g.p(idx));
+                int lim = env->off[s + 1] - env->off[s];
+                for (int r : loc) {
+                    if ((r + 1) * n_rt > lim) throw Error("environment coverage has no row for residue " + std::to_string(r));
+                    envr.push_back(env->off[s] + r * n_rt);
+                }
+            }
+            env_row = e.upload(envr);
+        } else if (d[0] != 2 || d[1] != 2) {
+            throw Error("coeff must be (2, 2, n_node)");
+        }
+        for (float t : types) {
+            int ti = int(t);
+            if (ti < 0 || ti >= (cb ? n_rt : 2)) throw Error("type out of range");
+            ty.push_back(ti);
+        }
+        row = e.upload(rows);
+        cc_row = e.upload(ccr);
+        type = e.upload(ty);
+        sysv = e.upload(sys_of(so));
+        coeff = e.upload(h_coeff);
+    }
+    void forward(Engine& e, bool energy) override {
+        double* pot = energy ? e.d_pot + size_t(pot_slot) * e.n_sys : nullptr;
+        auto& pts = e.arg(*this, 0);
+        if (cb_term) {
+            auto &env = e.arg(*this, 1), &cc = e.arg(*this, 2);
+            memb_cb_kernel<<<nblk(n), 256, 0, e.st>>>(n, P, n_rt, n_bl, row, env_row, cc_row, type, sysv, wts, bl_nodes,
+                                                      coeff, pts.width, pts.out, pts.sens, env.width, env.out, env.sens,
+                                                      cc.out, pot);
+        } else {
+            auto& cc = e.arg(*this, 1);
+            memb_hb_kernel<<<nblk(n), 256, 0, e.st>>>(n, P, row, cc_row, type, sysv, coeff, pts.width, pts.out,
+                                                      pts.sens, cc.out, pot);
+        }
+    }
+    // the spline coefficients (get_param / set_param of the reference node)
+    std::vector<float> get_param(Engine&) override { return h_coeff; }
+    void set_param(Engine& e, const std::vector<float>& p) override {
+        if (p.size() != h_coeff.size()) throw Error("the size of parameters should be " + std::to_string(h_coeff.size()));
+        h_coeff = p;
+        UG_CK(cudaMemcpyAsync(coeff, h_coeff.data(), 4 * h_coeff.size(), cudaMemcpyHostToDevice, e.st));
+        UG_CK(cudaStreamSynchronize(e.st));
+    }
+};
+
 // ===================================================== affine frames ===
 // Rigid frame (centroid, quaternion) per residue: the quaternion is the top
 // eigenvector of the 4x4 key matrix of the N/CA/C fit, found by cyclic
@@ -2575,6 +2826,9 @@ Engine::Engine(const std::vector<std::string>& paths, const std::vector<int>& n_
             else if (is_prefix("Add", nm)) n.reset(new CombineNode(*this, g, COMB_ADD, N(0), N(1)));
             else if (is_prefix("Mean", nm)) n.reset(new CombineNode(*this, g, COMB_MEAN, N(0), N(1)));
             else if (is_prefix("Multiply", nm)) n.reset(new CombineNode(*this, g, COMB_MUL, N(0), N(1)));
+            else if (is_prefix("Const3D", nm)) n.reset(new Const3DNode(*this, g, N(0)));
+            else if (is_prefix("cb_membrane_potential", nm)) n.reset(new MembraneNode(*this, g, true, N(0), &N(1), N(2)));
+            else if (is_prefix("hb_membrane_potential", nm)) n.reset(new MembraneNode(*this, g, false, N(0), nullptr, N(1)));
             else if (is_prefix("affine_alignment", nm)) n.reset(new AffineNode(*this, g, O(0)));
             else if (is_prefix("backbone_pairs", nm)) n.reset(new BackbonePairsNode(*this, g, O(0)));
             else if (is_prefix("infer_H_O", nm)) n.reset(new InferHONode(*this, g, O(0)));
