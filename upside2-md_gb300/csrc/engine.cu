@@ -8,6 +8,7 @@
 #include "engine.h"
 
 #include <algorithm>
+#include <cstdlib>
 #include <cmath>
 #include <cstring>
 #include <numeric>
@@ -15,6 +16,7 @@
 #include <unordered_map>
 
 #include "dev_math.cuh"
+#include "launch.cuh"
 #include "warm.h"
 
 namespace ug {
@@ -37,6 +39,14 @@ template <class T> T* Engine::upload(const std::vector<T>& v) {
     if (!v.empty()) UG_CK(cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, st));
     return p;
 }
+bool pdl_enabled() {
+    static const bool on = [] {
+        const char* v = std::getenv("UPSIDE_GB300_PDL");
+        return !(v && v[0] == '0');
+    }();
+    return on;
+}
+
 void Engine::free_all() {
     for (void* p : allocations_) cudaFree(p);
     allocations_.clear();
@@ -201,6 +211,7 @@ struct PosNode : GNode {
 // |x1 - x2| (DistCoord, src/coord_basic.cpp:13-66)
 __global__ void dist_fwd(int n, const int2* __restrict__ id, const float* __restrict__ p1, const float* __restrict__ p2,
                          float* __restrict__ out, float* __restrict__ der) {
+    grid_dep_entry();
     for (int i = grid_stride_start(); i < n; i += grid_stride()) {
         int2 a = id[i];
         f3 d = ld3(p1 + 3 * size_t(a.x)) - ld3(p2 + 3 * size_t(a.y));
@@ -211,6 +222,7 @@ __global__ void dist_fwd(int n, const int2* __restrict__ id, const float* __rest
 }
 __global__ void dist_bwd(int n, const int2* __restrict__ id, const float* __restrict__ sens, const float* __restrict__ der,
                          float* s1, float* s2) {
+    grid_dep_entry();
     for (int i = grid_stride_start(); i < n; i += grid_stride()) {
         float s = sens[i];
         f3 d = ld3(der + 3 * size_t(i)) * s;
@@ -235,10 +247,10 @@ struct DistNode : GNode {
         der = e.alloc<float>(size_t(total) * 3);
     }
     void forward(Engine& e, bool) override {
-        dist_fwd<<<nblk(total), 256, 0, e.st>>>(total, id, e.arg(*this, 0).out, e.arg(*this, 1).out, out, der);
+        ug::launch(dist_fwd, nblk(total), 256, 0, e.st, total, id, e.arg(*this, 0).out, e.arg(*this, 1).out, out, der);
     }
     void backward(Engine& e) override {
-        dist_bwd<<<nblk(total), 256, 0, e.st>>>(total, id, sens, der, e.arg(*this, 0).sens, e.arg(*this, 1).sens);
+        ug::launch(dist_bwd, nblk(total), 256, 0, e.st, total, id, sens, der, e.arg(*this, 0).sens, e.arg(*this, 1).sens);
     }
 };
 
@@ -246,6 +258,7 @@ struct DistNode : GNode {
 // cosine of the angle at the third atom (AngleCoord, src/coord_basic.cpp:183-243)
 __global__ void angle_fwd(int n, const int* __restrict__ id, const float* __restrict__ p, float* __restrict__ out,
                           float* __restrict__ der) {
+    grid_dep_entry();
     for (int i = grid_stride_start(); i < n; i += grid_stride()) {
         f3 a = ld3(p + 3 * size_t(id[3 * i])), b = ld3(p + 3 * size_t(id[3 * i + 1])), c = ld3(p + 3 * size_t(id[3 * i + 2]));
         f3 x1 = a - c, x2 = b - c;
@@ -259,6 +272,7 @@ __global__ void angle_fwd(int n, const int* __restrict__ id, const float* __rest
 }
 __global__ void angle_bwd(int n, const int* __restrict__ id, const float* __restrict__ sens, const float* __restrict__ der,
                           float* ps) {
+    grid_dep_entry();
     for (int i = grid_stride_start(); i < n; i += grid_stride()) {
         float s = sens[i];
         f3 d1 = ld3(der + 6 * size_t(i)) * s, d2 = ld3(der + 6 * size_t(i) + 3) * s;
@@ -284,10 +298,10 @@ struct AngleNode : GNode {
         der = e.alloc<float>(size_t(total) * 6);
     }
     void forward(Engine& e, bool) override {
-        angle_fwd<<<nblk(total), 256, 0, e.st>>>(total, id, e.arg(*this, 0).out, out, der);
+        ug::launch(angle_fwd, nblk(total), 256, 0, e.st, total, id, e.arg(*this, 0).out, out, der);
     }
     void backward(Engine& e) override {
-        angle_bwd<<<nblk(total), 256, 0, e.st>>>(total, id, sens, der, e.arg(*this, 0).sens);
+        ug::launch(angle_bwd, nblk(total), 256, 0, e.st, total, id, sens, der, e.arg(*this, 0).sens);
     }
 };
 
@@ -296,6 +310,7 @@ struct AngleNode : GNode {
 // (DihedralCoord, src/coord_basic.cpp:311-374; dihedral_germ src/vector_math.h:766-800)
 __global__ void dihedral_fwd(int n, const int4* __restrict__ id, const float* __restrict__ p, float* __restrict__ out,
                              float* __restrict__ jac) {
+    grid_dep_entry();
     for (int i = grid_stride_start(); i < n; i += grid_stride()) {
         int4 a = id[i];
         if (a.x < 0 || a.w < 0) {
@@ -320,6 +335,7 @@ __global__ void dihedral_fwd(int n, const int4* __restrict__ id, const float* __
 }
 __global__ void dihedral_bwd(int n, const int4* __restrict__ id, const float* __restrict__ sens,
                              const float* __restrict__ jac, float* ps) {
+    grid_dep_entry();
     for (int i = grid_stride_start(); i < n; i += grid_stride()) {
         int4 a = id[i];
         if (a.x < 0 || a.w < 0) continue;
@@ -349,10 +365,10 @@ struct DihedralNode : GNode {
         jac = e.alloc<float>(size_t(total) * 12);
     }
     void forward(Engine& e, bool) override {
-        dihedral_fwd<<<nblk(total), 256, 0, e.st>>>(total, id, e.arg(*this, 0).out, out, jac);
+        ug::launch(dihedral_fwd, nblk(total), 256, 0, e.st, total, id, e.arg(*this, 0).out, out, jac);
     }
     void backward(Engine& e) override {
-        dihedral_bwd<<<nblk(total), 256, 0, e.st>>>(total, id, sens, jac, e.arg(*this, 0).sens);
+        ug::launch(dihedral_bwd, nblk(total), 256, 0, e.st, total, id, sens, jac, e.arg(*this, 0).sens);
     }
 };
 
@@ -361,6 +377,7 @@ struct DihedralNode : GNode {
 __global__ void spring_kernel(int n, const int* __restrict__ id, const float* __restrict__ eq, const float* __restrict__ k,
                               const int* __restrict__ sys, int w, int dim1, int pbc, float box, const float* __restrict__ x,
                               float* xs, double* pot) {
+    grid_dep_entry();
     for (int i = grid_stride_start(); i < n; i += grid_stride()) {
         int r = id[i] * w + dim1;
         float v = x[r];
@@ -395,7 +412,7 @@ struct SpringNode : GNode {
     }
     void forward(Engine& e, bool energy) override {
         auto& a = e.arg(*this, 0);
-        spring_kernel<<<nblk(n), 256, 0, e.st>>>(n, id, eq, kk, sysv, a.width, dim1, pbc, box, a.out, a.sens,
+        ug::launch(spring_kernel, nblk(n), 256, 0, e.st, n, id, eq, kk, sysv, a.width, dim1, pbc, box, a.out, a.sens,
                                                  energy ? e.d_pot + size_t(pot_slot) * e.n_sys : nullptr);
     }
 };
@@ -405,6 +422,7 @@ struct SpringNode : GNode {
 __global__ void paste_fwd(int n1, int n2, const int* __restrict__ i1, const int* __restrict__ i2,
                           const int* __restrict__ dst1, const int* __restrict__ dst2, int w, int wa, int wb, int col_b,
                           const float* __restrict__ a, const float* __restrict__ b, float* __restrict__ out) {
+    grid_dep_entry();
     for (int i = grid_stride_start(); i < n1; i += grid_stride())
         for (int d = 0; d < wa; ++d) out[size_t(dst1[i]) * w + d] = a[size_t(i1[i]) * wa + d];
     for (int i = grid_stride_start(); i < n2; i += grid_stride())
@@ -413,6 +431,7 @@ __global__ void paste_fwd(int n1, int n2, const int* __restrict__ i1, const int*
 __global__ void paste_bwd(int n1, int n2, const int* __restrict__ i1, const int* __restrict__ i2,
                           const int* __restrict__ dst1, const int* __restrict__ dst2, int w, int wa, int wb, int col_b,
                           const float* __restrict__ sens, float* as, float* bs) {
+    grid_dep_entry();
     for (int i = grid_stride_start(); i < n1; i += grid_stride())
         for (int d = 0; d < wa; ++d) atomicAdd(as + size_t(i1[i]) * wa + d, sens[size_t(dst1[i]) * w + d]);
     for (int i = grid_stride_start(); i < n2; i += grid_stride())
@@ -450,12 +469,12 @@ struct PasteNode : GNode {
     }
     void forward(Engine& e, bool) override {
         auto &a = e.arg(*this, 0), &b = e.arg(*this, 1);
-        paste_fwd<<<nblk(std::max(n1, n2)), 256, 0, e.st>>>(n1, n2, i1, i2, d1, d2, width, a.width, b.width, col_b,
+        ug::launch(paste_fwd, nblk(std::max(n1, n2)), 256, 0, e.st, n1, n2, i1, i2, d1, d2, width, a.width, b.width, col_b,
                                                              a.out, b.out, out);
     }
     void backward(Engine& e) override {
         auto &a = e.arg(*this, 0), &b = e.arg(*this, 1);
-        paste_bwd<<<nblk(std::max(n1, n2)), 256, 0, e.st>>>(n1, n2, i1, i2, d1, d2, width, a.width, b.width, col_b,
+        ug::launch(paste_bwd, nblk(std::max(n1, n2)), 256, 0, e.st, n1, n2, i1, i2, d1, d2, width, a.width, b.width, col_b,
                                                              sens, a.sens, b.sens);
     }
 };
@@ -470,6 +489,7 @@ __global__ void rama_map_kernel(int n, const int* __restrict__ res, const int* _
                                 const int* __restrict__ sys, const float* __restrict__ coeff, int nxp, int nyp,
                                 float scale, const float* __restrict__ rama, float* rs, double* pot, float* res_log,
                                 const int* __restrict__ lam_row, int lam_w, const float* __restrict__ lam, float* lam_s) {
+    grid_dep_entry();
     for (int i = grid_stride_start(); i < n; i += grid_stride()) {
         int r = res[i];
         float x = (rama[2 * r] + 3.14159265358979f) * scale, y = (rama[2 * r + 1] + 3.14159265358979f) * scale;
@@ -545,7 +565,7 @@ struct RamaMapNode : GNode {
             lg = res_log;
         }
         const GNode* lam = lam_row ? &e.arg(*this, 1) : nullptr;
-        rama_map_kernel<<<nblk(n), 256, 0, e.st>>>(n, res, layer, sysv, coeff, nxp, nyp, scale, a.out, a.sens,
+        ug::launch(rama_map_kernel, nblk(n), 256, 0, e.st, n, res, layer, sysv, coeff, nxp, nyp, scale, a.out, a.sens,
                                                    energy ? e.d_pot + size_t(pot_slot) * e.n_sys : nullptr, lg,
                                                    lam_row, lam ? lam->width : 0, lam ? lam->out : nullptr,
                                                    lam ? lam->sens : nullptr);
@@ -563,6 +583,7 @@ struct RamaMapNode : GNode {
 // negative sign (SigmoidCoord, src/coord_map.cpp:609-675)
 __global__ void sigcoord_fwd(int n, const int* __restrict__ id, const float4* __restrict__ prm, int w, int dim1,
                              const float* __restrict__ x, float* __restrict__ out, float* __restrict__ der) {
+    grid_dep_entry();
     for (int i = grid_stride_start(); i < n; i += grid_stride()) {
         float4 p = prm[i];  // c, s, sign
         float v, d;
@@ -573,6 +594,7 @@ __global__ void sigcoord_fwd(int n, const int* __restrict__ id, const float4* __
 }
 __global__ void sigcoord_bwd(int n, const int* __restrict__ id, const float* __restrict__ der,
                              const float* __restrict__ sens, int w, int dim1, float* xs) {
+    grid_dep_entry();
     for (int i = grid_stride_start(); i < n; i += grid_stride())
         atomicAdd(xs + size_t(id[i]) * w + dim1, sens[i] * der[i]);
 }
@@ -598,11 +620,11 @@ struct SigmoidCoordNode : GNode {
     }
     void forward(Engine& e, bool) override {
         auto& a = e.arg(*this, 0);
-        sigcoord_fwd<<<nblk(total), 256, 0, e.st>>>(total, id, prm, a.width, dim1, a.out, out, der);
+        ug::launch(sigcoord_fwd, nblk(total), 256, 0, e.st, total, id, prm, a.width, dim1, a.out, out, der);
     }
     void backward(Engine& e) override {
         auto& a = e.arg(*this, 0);
-        sigcoord_bwd<<<nblk(total), 256, 0, e.st>>>(total, id, der, sens, a.width, dim1, a.sens);
+        ug::launch(sigcoord_bwd, nblk(total), 256, 0, e.st, total, id, der, sens, a.width, dim1, a.sens);
     }
 };
 
@@ -616,6 +638,7 @@ enum CombineOp { COMB_ADD = 0, COMB_MEAN = 1, COMB_MUL = 2 };
 __global__ void combine_fwd(int n_row, int op, int nd, const int* __restrict__ ptr, const int2* __restrict__ ent,
                             const int* __restrict__ dims, const float* __restrict__ a, int aw,
                             const float* __restrict__ b, int bw, float* __restrict__ out, float* __restrict__ fac) {
+    grid_dep_entry();
     for (int r = grid_stride_start(); r < n_row; r += grid_stride()) {
         int e0 = ptr[r], e1 = ptr[r + 1];
         float last[2] = {1.f, 1.f};  // last value of each argument written to the row
@@ -639,6 +662,7 @@ __global__ void combine_fwd(int n_row, int op, int nd, const int* __restrict__ p
 __global__ void combine_bwd(int n_ent, int nd, const int* __restrict__ ent_row, const int2* __restrict__ ent,
                             const int* __restrict__ dims, const float* __restrict__ sens, const float* __restrict__ fac,
                             float* as, int aw, float* bs, int bw) {
+    grid_dep_entry();
     for (int k = grid_stride_start(); k < n_ent; k += grid_stride()) {
         int r = ent_row[k];
         int2 en = ent[k];
@@ -708,12 +732,12 @@ struct CombineNode : GNode {
     }
     void forward(Engine& e, bool) override {
         auto &a = e.arg(*this, 0), &b = e.arg(*this, 1);
-        combine_fwd<<<nblk(total), 256, 0, e.st>>>(total, op, width, ptr, ent, dims, a.out, a.width, b.out, b.width,
+        ug::launch(combine_fwd, nblk(total), 256, 0, e.st, total, op, width, ptr, ent, dims, a.out, a.width, b.out, b.width,
                                                    out, fac);
     }
     void backward(Engine& e) override {
         auto &a = e.arg(*this, 0), &b = e.arg(*this, 1);
-        combine_bwd<<<nblk(n_ent), 256, 0, e.st>>>(n_ent, width, ent_row, ent, dims, sens, fac, a.sens, a.width,
+        ug::launch(combine_bwd, nblk(n_ent), 256, 0, e.st, n_ent, width, ent_row, ent, dims, sens, fac, a.sens, a.width,
                                                    b.sens, b.width);
     }
 };
@@ -729,6 +753,7 @@ __global__ void sigmoid_energy_kernel(int n, const int* __restrict__ id, const i
                                       const SigE* __restrict__ prm, const int* __restrict__ sys, int w, int dim1,
                                       int use_cutoff, const float* __restrict__ x, float* xs, int lw,
                                       const float* __restrict__ lam, float* lam_s, double* pot) {
+    grid_dep_entry();
     for (int i = grid_stride_start(); i < n; i += grid_stride()) {
         SigE p = prm[i];
         size_t r = size_t(id[i]) * w + dim1;
@@ -781,7 +806,7 @@ struct SigmoidEnergyNode : GNode {
     void forward(Engine& e, bool energy) override {
         auto& a = e.arg(*this, 0);
         const GNode* lam = id2 ? &e.arg(*this, 1) : nullptr;
-        sigmoid_energy_kernel<<<nblk(n), 256, 0, e.st>>>(n, id, id2, prm, sysv, a.width, dim1, use_cutoff, a.out,
+        ug::launch(sigmoid_energy_kernel, nblk(n), 256, 0, e.st, n, id, id2, prm, sysv, a.width, dim1, use_cutoff, a.out,
                                                          a.sens, lam ? lam->width : 0, lam ? lam->out : nullptr,
                                                          lam ? lam->sens : nullptr,
                                                          energy ? e.d_pot + size_t(pot_slot) * e.n_sys : nullptr);
@@ -794,6 +819,7 @@ struct SigmoidEnergyNode : GNode {
 // per-row flag makes the capture happen once, also inside a replayed graph
 __global__ void const3d_kernel(int n, const float* __restrict__ val, const int* __restrict__ src, int w, int3 dim,
                                const float* __restrict__ x, int* taken, float* __restrict__ out) {
+    grid_dep_entry();
     for (int i = grid_stride_start(); i < n; i += grid_stride()) {
         if (!src) {
             for (int k = 0; k < 3; ++k) out[3 * size_t(i) + k] = val[3 * size_t(i) + k];
@@ -838,7 +864,7 @@ struct Const3DNode : GNode {
     }
     void forward(Engine& e, bool) override {
         auto& a = e.arg(*this, 0);
-        const3d_kernel<<<nblk(total), 256, 0, e.st>>>(total, val, src, a.width, dim, a.out, taken, out);
+        ug::launch(const3d_kernel, nblk(total), 256, 0, e.st, total, val, src, a.width, dim, a.out, taken, out);
     }
 };
 
@@ -886,6 +912,7 @@ __global__ void memb_cb_kernel(int n, MembParams P, int n_rt, int n_bl, const in
                                const float* __restrict__ coeff, int cbw, const float* __restrict__ cb, float* cbs,
                                int ew, const float* __restrict__ env, float* envs, const float* __restrict__ cc,
                                double* pot) {
+    grid_dep_entry();
     for (int i = grid_stride_start(); i < n; i += grid_stride()) {
         const size_t er = size_t(env_row[i]);
         float bl = 0.f;
@@ -932,6 +959,7 @@ __global__ void memb_hb_kernel(int n, MembParams P, const int* __restrict__ hb_r
                                const int* __restrict__ htype, const int* __restrict__ sys,
                                const float* __restrict__ coeff, int hw, const float* __restrict__ hb, float* hbs,
                                const float* __restrict__ cc, double* pot) {
+    grid_dep_entry();
     for (int i = grid_stride_start(); i < n; i += grid_stride()) {
         const float* r = hb + size_t(hb_row[i]) * hw;
         f3 g;
@@ -1020,12 +1048,12 @@ struct MembraneNode : GNode {
         auto& pts = e.arg(*this, 0);
         if (cb_term) {
             auto &env = e.arg(*this, 1), &cc = e.arg(*this, 2);
-            memb_cb_kernel<<<nblk(n), 256, 0, e.st>>>(n, P, n_rt, n_bl, row, env_row, cc_row, type, sysv, wts, bl_nodes,
+            ug::launch(memb_cb_kernel, nblk(n), 256, 0, e.st, n, P, n_rt, n_bl, row, env_row, cc_row, type, sysv, wts, bl_nodes,
                                                       coeff, pts.width, pts.out, pts.sens, env.width, env.out, env.sens,
                                                       cc.out, pot);
         } else {
             auto& cc = e.arg(*this, 1);
-            memb_hb_kernel<<<nblk(n), 256, 0, e.st>>>(n, P, row, cc_row, type, sysv, coeff, pts.width, pts.out,
+            ug::launch(memb_hb_kernel, nblk(n), 256, 0, e.st, n, P, row, cc_row, type, sysv, coeff, pts.width, pts.out,
                                                       pts.sens, cc.out, pot);
         }
     }
@@ -1088,6 +1116,7 @@ __device__ void jacobi4(float A[4][4], float V[4][4]) {
 }
 __global__ void affine_fwd(int n, const int* __restrict__ atoms, const float* __restrict__ ref,
                            const float* __restrict__ pos, float* __restrict__ out, float* __restrict__ eig) {
+    grid_dep_entry();
     for (int r = grid_stride_start(); r < n; r += grid_stride()) {
         f3 x[3];
         for (int a = 0; a < 3; ++a) x[a] = ld3(pos + 3 * size_t(atoms[3 * r + a]));
@@ -1132,6 +1161,7 @@ __global__ void affine_fwd(int n, const int* __restrict__ atoms, const float* __
 }
 __global__ void affine_bwd(int n, const int* __restrict__ atoms, const float* __restrict__ ref,
                            const float* __restrict__ eig, const float* __restrict__ sens, float* ps) {
+    grid_dep_entry();
     for (int r = grid_stride_start(); r < n; r += grid_stride()) {
         const float* s = sens + 7 * size_t(r);
         const float* E = eig + 20 * size_t(r);
@@ -1190,10 +1220,10 @@ struct AffineNode : GNode {
         eig = e.alloc<float>(size_t(total) * 20);
     }
     void forward(Engine& e, bool) override {
-        affine_fwd<<<nblk(total, 128), 128, 0, e.st>>>(total, atoms, ref, e.arg(*this, 0).out, out, eig);
+        ug::launch(affine_fwd, nblk(total, 128), 128, 0, e.st, total, atoms, ref, e.arg(*this, 0).out, out, eig);
     }
     void backward(Engine& e) override {
-        affine_bwd<<<nblk(total, 128), 128, 0, e.st>>>(total, atoms, ref, eig, sens, e.arg(*this, 0).sens);
+        ug::launch(affine_bwd, nblk(total, 128), 128, 0, e.st, total, atoms, ref, eig, sens, e.arg(*this, 0).sens);
     }
 };
 
@@ -1204,6 +1234,7 @@ struct AffineNode : GNode {
 template <int NB, bool SCALAR>
 __global__ void place_fixed_fwd(int n, const int* __restrict__ aff, const int* __restrict__ layer, const float* __restrict__ data,
                                 const float* __restrict__ af, float* __restrict__ out) {
+    grid_dep_entry();
     constexpr int W = 3 * NB + (SCALAR ? 1 : 0);
     for (int i = grid_stride_start(); i < n; i += grid_stride()) {
         const float* a = af + 7 * size_t(aff[i]);
@@ -1220,6 +1251,7 @@ __global__ void place_fixed_fwd(int n, const int* __restrict__ aff, const int* _
 template <int NB, bool SCALAR>
 __global__ void place_fixed_bwd(int n, const int* __restrict__ aff, const float* __restrict__ af, const float* __restrict__ out,
                                 const float* __restrict__ sens, float* as) {
+    grid_dep_entry();
     constexpr int W = 3 * NB + (SCALAR ? 1 : 0);
     for (int i = grid_stride_start(); i < n; i += grid_stride()) {
         const float* a = af + 7 * size_t(aff[i]);
@@ -1237,6 +1269,7 @@ __global__ void place_fixed_bwd(int n, const int* __restrict__ aff, const float*
 __global__ void place_rama_fwd(int n, const int* __restrict__ rres, const int* __restrict__ layer, const float* __restrict__ coeff,
                                int nxp, int nyp, float sx, float sy, const float* __restrict__ rama, float* __restrict__ out,
                                float* __restrict__ der) {
+    grid_dep_entry();
     for (int i = grid_stride_start(); i < n; i += grid_stride()) {
         const float* r = rama + 2 * size_t(rres[i]);
         float v, dx, dy;
@@ -1249,6 +1282,7 @@ __global__ void place_rama_fwd(int n, const int* __restrict__ rres, const int* _
 }
 __global__ void place_rama_bwd(int n, const int* __restrict__ rres, float sx, float sy, const float* __restrict__ der,
                                const float* __restrict__ sens, float* rs) {
+    grid_dep_entry();
     for (int i = grid_stride_start(); i < n; i += grid_stride()) {
         float s = sens[i];
         atomicAdd(rs + 2 * size_t(rres[i]), sx * s * der[2 * size_t(i)]);
@@ -1300,24 +1334,24 @@ struct PlacementNode : GNode {
     }
     void forward(Engine& e, bool) override {
         if (rama) {
-            place_rama_fwd<<<nblk(total), 256, 0, e.st>>>(total, rres, layer, data, nxp, nyp, sx, sy, e.arg(*this, 1).out, out, der);
+            ug::launch(place_rama_fwd, nblk(total), 256, 0, e.st, total, rres, layer, data, nxp, nyp, sx, sy, e.arg(*this, 1).out, out, der);
             return;
         }
         const float* af = e.arg(*this, 0).out;
-        if (nb == 2 && !scalar) place_fixed_fwd<2, false><<<nblk(total), 256, 0, e.st>>>(total, aff, layer, data, af, out);
-        else if (nb == 2 && scalar) place_fixed_fwd<2, true><<<nblk(total), 256, 0, e.st>>>(total, aff, layer, data, af, out);
-        else if (nb == 1 && !scalar) place_fixed_fwd<1, false><<<nblk(total), 256, 0, e.st>>>(total, aff, layer, data, af, out);
+        if (nb == 2 && !scalar) ug::launch((place_fixed_fwd<2, false>), nblk(total), 256, 0, e.st, total, aff, layer, data, af, out);
+        else if (nb == 2 && scalar) ug::launch((place_fixed_fwd<2, true>), nblk(total), 256, 0, e.st, total, aff, layer, data, af, out);
+        else if (nb == 1 && !scalar) ug::launch((place_fixed_fwd<1, false>), nblk(total), 256, 0, e.st, total, aff, layer, data, af, out);
         else throw Error("unsupported placement signature");
     }
     void backward(Engine& e) override {
         if (rama) {
-            place_rama_bwd<<<nblk(total), 256, 0, e.st>>>(total, rres, sx, sy, der, sens, e.arg(*this, 1).sens);
+            ug::launch(place_rama_bwd, nblk(total), 256, 0, e.st, total, rres, sx, sy, der, sens, e.arg(*this, 1).sens);
             return;
         }
         auto& a = e.arg(*this, 0);
-        if (nb == 2 && !scalar) place_fixed_bwd<2, false><<<nblk(total), 256, 0, e.st>>>(total, aff, a.out, out, sens, a.sens);
-        else if (nb == 2 && scalar) place_fixed_bwd<2, true><<<nblk(total), 256, 0, e.st>>>(total, aff, a.out, out, sens, a.sens);
-        else place_fixed_bwd<1, false><<<nblk(total), 256, 0, e.st>>>(total, aff, a.out, out, sens, a.sens);
+        if (nb == 2 && !scalar) ug::launch((place_fixed_bwd<2, false>), nblk(total), 256, 0, e.st, total, aff, a.out, out, sens, a.sens);
+        else if (nb == 2 && scalar) ug::launch((place_fixed_bwd<2, true>), nblk(total), 256, 0, e.st, total, aff, a.out, out, sens, a.sens);
+        else ug::launch((place_fixed_bwd<1, false>), nblk(total), 256, 0, e.st, total, aff, a.out, out, sens, a.sens);
     }
 };
 
@@ -1325,6 +1359,7 @@ struct PlacementNode : GNode {
 // (bead xyz, exp(-E_1body)) (WeightedPos, src/environment.cpp:489-533)
 __global__ void wpos_fwd(int n, const int* __restrict__ ip, const int* __restrict__ iw, const float* __restrict__ p, int wp,
                          const float* __restrict__ en, int we, float* __restrict__ out) {
+    grid_dep_entry();
     for (int i = grid_stride_start(); i < n; i += grid_stride()) {
         const float* x = p + size_t(ip[i]) * wp;
         out[4 * i] = x[0];
@@ -1335,6 +1370,7 @@ __global__ void wpos_fwd(int n, const int* __restrict__ ip, const int* __restric
 }
 __global__ void wpos_bwd(int n, const int* __restrict__ ip, const int* __restrict__ iw, int wp, int we,
                          const float* __restrict__ out, const float* __restrict__ sens, float* ps, float* es) {
+    grid_dep_entry();
     for (int i = grid_stride_start(); i < n; i += grid_stride()) {
         atomic_add3(ps + size_t(ip[i]) * wp, ld3(sens + 4 * i));
         atomicAdd(es + size_t(iw[i]) * we, -out[4 * i + 3] * sens[4 * i + 3]);
@@ -1351,11 +1387,11 @@ struct WeightedPosNode : GNode {
     }
     void forward(Engine& e, bool) override {
         auto &p = e.arg(*this, 0), &w = e.arg(*this, 1);
-        wpos_fwd<<<nblk(total), 256, 0, e.st>>>(total, ip, iw, p.out, p.width, w.out, w.width, out);
+        ug::launch(wpos_fwd, nblk(total), 256, 0, e.st, total, ip, iw, p.out, p.width, w.out, w.width, out);
     }
     void backward(Engine& e) override {
         auto &p = e.arg(*this, 0), &w = e.arg(*this, 1);
-        wpos_bwd<<<nblk(total), 256, 0, e.st>>>(total, ip, iw, p.width, w.width, out, sens, p.sens, w.sens);
+        ug::launch(wpos_bwd, nblk(total), 256, 0, e.st, total, ip, iw, p.width, w.width, out, sens, p.sens, w.sens);
     }
 };
 
@@ -1363,6 +1399,7 @@ struct WeightedPosNode : GNode {
 // virtual H / O positions and bond directions (Infer_H_O, src/hbond.cpp:20-127)
 __global__ void infer_fwd(int n, const int* __restrict__ id, const float* __restrict__ bl, const float* __restrict__ p,
                           float* __restrict__ out, float* __restrict__ cache) {
+    grid_dep_entry();
     for (int i = grid_stride_start(); i < n; i += grid_stride()) {
         f3 pc = ld3(p + 3 * size_t(id[3 * i])), cc = ld3(p + 3 * size_t(id[3 * i + 1])), nc = ld3(p + 3 * size_t(id[3 * i + 2]));
         f3 pv = pc - cc; float pi = rsqrtf(mag2(pv)); pv = pv * pi;
@@ -1376,6 +1413,7 @@ __global__ void infer_fwd(int n, const int* __restrict__ id, const float* __rest
 }
 __global__ void infer_bwd(int n, const int* __restrict__ id, const float* __restrict__ bl, const float* __restrict__ cache,
                           const float* __restrict__ sens, float* ps) {
+    grid_dep_entry();
     for (int i = grid_stride_start(); i < n; i += grid_stride()) {
         const float* s = sens + 6 * size_t(i);
         const float* c = cache + 12 * size_t(i);
@@ -1415,10 +1453,10 @@ struct InferHONode : GNode {
         cache = e.alloc<float>(size_t(total) * 12);
     }
     void forward(Engine& e, bool) override {
-        infer_fwd<<<nblk(total), 256, 0, e.st>>>(total, id, bl, e.arg(*this, 0).out, out, cache);
+        ug::launch(infer_fwd, nblk(total), 256, 0, e.st, total, id, bl, e.arg(*this, 0).out, out, cache);
     }
     void backward(Engine& e) override {
-        infer_bwd<<<nblk(total), 256, 0, e.st>>>(total, id, bl, cache, sens, e.arg(*this, 0).sens);
+        ug::launch(infer_bwd, nblk(total), 256, 0, e.st, total, id, bl, cache, sens, e.arg(*this, 0).sens);
     }
 };
 
@@ -1678,6 +1716,7 @@ struct HGraph {
 // ====================================================== protein_hbond ===
 // hbond score per donor / acceptor in multiplicative space (ProteinHBond, src/hbond.cpp:357-435)
 __global__ void phb_init(int n, const int* __restrict__ src_row, const float* __restrict__ in, float* __restrict__ out) {
+    grid_dep_entry();
     for (int i = grid_stride_start(); i < n; i += grid_stride()) {
         const float* x = in + 6 * size_t(src_row[i]);
         float* o = out + 7 * size_t(i);
@@ -1686,6 +1725,7 @@ __global__ void phb_init(int n, const int* __restrict__ src_row, const float* __
     }
 }
 __global__ void phb_accum(DGraph g, const int* __restrict__ row1, const int* __restrict__ row2, float* out) {
+    grid_dep_entry();
     int ne = *g.n_edge;
     for (int e = grid_stride_start(); e < ne; e += grid_stride()) {
         int2 ij = g.edges[e];
@@ -1695,10 +1735,12 @@ __global__ void phb_accum(DGraph g, const int* __restrict__ row1, const int* __r
     }
 }
 __global__ void phb_final(int n, float* out) {
+    grid_dep_entry();
     for (int i = grid_stride_start(); i < n; i += grid_stride()) out[7 * size_t(i) + 6] = 1.f - expf(-out[7 * size_t(i) + 6]);
 }
 __global__ void phb_esens(DGraph g, const int* __restrict__ row1, const int* __restrict__ row2, const float* __restrict__ out,
                           const float* __restrict__ sens) {
+    grid_dep_entry();
     int ne = *g.n_edge;
     for (int e = grid_stride_start(); e < ne; e += grid_stride()) {
         int2 ij = g.edges[e];
@@ -1707,6 +1749,7 @@ __global__ void phb_esens(DGraph g, const int* __restrict__ row1, const int* __r
     }
 }
 __global__ void phb_pass(int n, const int* __restrict__ src_row, const float* __restrict__ sens, float* in_sens) {
+    grid_dep_entry();
     for (int i = grid_stride_start(); i < n; i += grid_stride()) {
         const float* s = sens + 7 * size_t(i);
         float* d = in_sens + 6 * size_t(src_row[i]);
@@ -1737,16 +1780,16 @@ struct ProteinHBondNode : GNode {
     void forward(Engine& e, bool) override {
         auto& in = e.arg(*this, 0);
         hg.bind(in, in);
-        phb_init<<<nblk(total), 256, 0, e.st>>>(total, src, in.out, out);
+        ug::launch(phb_init, nblk(total), 256, 0, e.st, total, src, in.out, out);
         hg.search_and_eval(e.st);
-        phb_accum<<<nblk(hg.g.cap), 256, 0, e.st>>>(hg.g, row1, row2, out);
-        phb_final<<<nblk(total), 256, 0, e.st>>>(total, out);
+        ug::launch(phb_accum, nblk(hg.g.cap), 256, 0, e.st, hg.g, row1, row2, out);
+        ug::launch(phb_final, nblk(total), 256, 0, e.st, total, out);
     }
     void backward(Engine& e) override {
         auto& in = e.arg(*this, 0);
-        phb_esens<<<nblk(hg.g.cap), 256, 0, e.st>>>(hg.g, row1, row2, out, sens);
+        ug::launch(phb_esens, nblk(hg.g.cap), 256, 0, e.st, hg.g, row1, row2, out, sens);
         launch_edge_scatter(hg.g, e.st);
-        phb_pass<<<nblk(total), 256, 0, e.st>>>(total, src, sens, in.sens);
+        ug::launch(phb_pass, nblk(total), 256, 0, e.st, total, src, sens, in.sens);
     }
     DGraph* graph() override { return &hg.g; }
     bool grow(Engine&) override { return hg.grow_if_full(); }
@@ -1764,6 +1807,7 @@ __global__ void hbe_kernel(int n, const float* __restrict__ prm, const int* __re
                            const int* __restrict__ don_row, const int* __restrict__ acc_row,
                            const int* __restrict__ next_don_row, const int* __restrict__ sys, const float* __restrict__ pp,
                            float* ps, const float* __restrict__ ra, float* rs, double* pot) {
+    grid_dep_entry();
     for (int i = grid_stride_start(); i < n; i += grid_stride()) {
         float phi = ra[2 * size_t(rama_row[i])], psi = ra[2 * size_t(rama_row[i]) + 1];
         float p1v, p1d, p2v, p2d, s1v, s1d, s2v, s2d;
@@ -1836,7 +1880,7 @@ struct HBondEnergyNode : GNode {
     }
     void forward(Engine& e, bool energy) override {
         auto &pp = e.arg(*this, 0), &ra = e.arg(*this, 1);
-        hbe_kernel<<<nblk(n), 256, 0, e.st>>>(n, prm, rama_row, don_row, acc_row, next_don, sysv, pp.out, pp.sens, ra.out,
+        ug::launch(hbe_kernel, nblk(n), 256, 0, e.st, n, prm, rama_row, don_row, acc_row, next_don, sysv, pp.out, pp.sens, ra.out,
                                               ra.sens, energy ? e.d_pot + size_t(pot_slot) * e.n_sys : nullptr);
     }
 };
@@ -1845,9 +1889,11 @@ struct HBondEnergyNode : GNode {
 // coverage of side-chain beads by backbone H/O or hydrophobe points
 // (HBondCoverage, src/hbond.cpp:438-484)
 __global__ void zero_kernel(float* p, int n) {
+    grid_dep_entry();
     for (int i = grid_stride_start(); i < n; i += grid_stride()) p[i] = 0.f;
 }
 __global__ void cov_accum(DGraph g, float* out, int by_first, int n_aa, const int* __restrict__ aa2) {
+    grid_dep_entry();
     int ne = *g.n_edge;
     for (int e = grid_stride_start(); e < ne; e += grid_stride()) {
         int2 ij = g.edges[e];
@@ -1856,6 +1902,7 @@ __global__ void cov_accum(DGraph g, float* out, int by_first, int n_aa, const in
     }
 }
 __global__ void cov_esens(DGraph g, const float* __restrict__ sens, int by_first, int n_aa, const int* __restrict__ aa2) {
+    grid_dep_entry();
     int ne = *g.n_edge;
     for (int e = grid_stride_start(); e < ne; e += grid_stride()) {
         int2 ij = g.edges[e];
@@ -1903,11 +1950,11 @@ struct CoverageNode : GNode {
     void forward(Engine& e, bool) override {
         hg.bind(e.arg(*this, 0), e.arg(*this, 1));
         hg.search_and_eval(e.st);
-        zero_kernel<<<nblk(total), 256, 0, e.st>>>(out, total);
-        cov_accum<<<nblk(hg.g.cap), 256, 0, e.st>>>(hg.g, out, by_first, n_aa, aa2);
+        ug::launch(zero_kernel, nblk(total), 256, 0, e.st, out, total);
+        ug::launch(cov_accum, nblk(hg.g.cap), 256, 0, e.st, hg.g, out, by_first, n_aa, aa2);
     }
     void backward(Engine& e) override {
-        cov_esens<<<nblk(hg.g.cap), 256, 0, e.st>>>(hg.g, sens, by_first, n_aa, aa2);
+        ug::launch(cov_esens, nblk(hg.g.cap), 256, 0, e.st, hg.g, sens, by_first, n_aa, aa2);
         launch_edge_scatter(hg.g, e.st);
     }
     std::vector<float> get_param(Engine&) override { return hg.param_host; }
@@ -1942,6 +1989,7 @@ __global__ void sig_coupling_kernel(int n, int n_rt, const int* __restrict__ cty
                                     const float* __restrict__ w, const float* __restrict__ scale,
                                     const float* __restrict__ center, const float* __restrict__ sharp,
                                     const float* __restrict__ in, float* is, double* pot, float* res_log) {
+    grid_dep_entry();
     for (int r = grid_stride_start(); r < n; r += grid_stride()) {
         int c = ctype[r];
         const float* wr = w + size_t(c) * n_rt;
@@ -1958,6 +2006,7 @@ __global__ void sig_coupling_kernel(int n, int n_rt, const int* __restrict__ cty
 __global__ void nl_coupling_kernel(int n, int n_rt, int n_coeff, float offset, float inv_dx, const int* __restrict__ ctype,
                                    const int* __restrict__ sys, const float* __restrict__ w, const float* __restrict__ coeff,
                                    const float* __restrict__ in, float* is, double* pot) {
+    grid_dep_entry();
     for (int r = grid_stride_start(); r < n; r += grid_stride()) {
         int c = ctype[r];
         const float* wr = w + size_t(c) * n_rt;
@@ -1974,6 +2023,7 @@ __global__ void nl_coupling_kernel(int n, int n_rt, int n_coeff, float offset, f
 __global__ void nl_param_deriv_kernel(int n, int n_rt, int n_coeff, int n_indep, float offset, float inv_dx,
                                       const int* __restrict__ ctype, const float* __restrict__ w,
                                       const float* __restrict__ coeff, const float* __restrict__ in, float* out) {
+    grid_dep_entry();
     for (int r = grid_stride_start(); r < n; r += grid_stride()) {
         int c = ctype[r];
         const float* wr = w + size_t(c) * n_rt;
@@ -2000,6 +2050,7 @@ __global__ void nl_param_deriv_kernel(int n, int n_rt, int n_coeff, int n_indep,
 __global__ void bb_coupling_kernel(int n, int n_rt, float scale, float center, float sharp, float hbw,
                                    const int* __restrict__ sys, const float* __restrict__ w, const float* __restrict__ sc,
                                    const float* __restrict__ hb, float* scs, float* hbs, double* pot) {
+    grid_dep_entry();
     for (int r = grid_stride_start(); r < n; r += grid_stride()) {
         const float* x = sc + size_t(r) * n_rt;
         float bl = 0.f;
@@ -2079,15 +2130,15 @@ struct CouplingNode : GNode {
                 if (!res_log) res_log = e.alloc<float>(size_t(n));
                 lg = res_log;
             }
-            sig_coupling_kernel<<<nblk(n), 256, 0, e.st>>>(n, n_rt, ctype, sysv, w, scale, center, sharp, a.out, a.sens,
+            ug::launch(sig_coupling_kernel, nblk(n), 256, 0, e.st, n, n_rt, ctype, sysv, w, scale, center, sharp, a.out, a.sens,
                                                            pot, lg);
         }
         else if (kind == NONLINEAR)
-            nl_coupling_kernel<<<nblk(n), 256, 0, e.st>>>(n, n_rt, n_coeff, offset, inv_dx, ctype, sysv, w, coeff, a.out,
+            ug::launch(nl_coupling_kernel, nblk(n), 256, 0, e.st, n, n_rt, n_coeff, offset, inv_dx, ctype, sysv, w, coeff, a.out,
                                                           a.sens, pot);
         else {
             auto& b = e.arg(*this, 1);
-            bb_coupling_kernel<<<nblk(n), 256, 0, e.st>>>(n, n_rt, s_scale, s_center, s_sharp, s_hbw, sysv, w, a.out, b.out,
+            ug::launch(bb_coupling_kernel, nblk(n), 256, 0, e.st, n, n_rt, s_scale, s_center, s_sharp, s_hbw, sysv, w, a.out, b.out,
                                                           a.sens, b.sens, pot);
         }
     }
@@ -2135,7 +2186,7 @@ struct CouplingNode : GNode {
         float* d = nullptr;
         UG_CK(cudaMalloc(&d, np * 4));
         UG_CK(cudaMemsetAsync(d, 0, np * 4, e.st));
-        nl_param_deriv_kernel<<<nblk(n), 256, 0, e.st>>>(n, n_rt, n_coeff, n_indep, offset, inv_dx, ctype, w, coeff,
+        ug::launch(nl_param_deriv_kernel, nblk(n), 256, 0, e.st, n, n_rt, n_coeff, n_indep, offset, inv_dx, ctype, w, coeff,
                                                          e.arg(*this, 0).out, d);
         UG_CK(cudaMemcpyAsync(r.data(), d, np * 4, cudaMemcpyDeviceToHost, e.st));
         UG_CK(cudaStreamSynchronize(e.st));
@@ -2150,6 +2201,7 @@ struct CouplingNode : GNode {
 __global__ void bb_pairs_kernel(DGraph g, const int* __restrict__ res_row, const int* __restrict__ nat,
                                 const float* __restrict__ refp, const int* __restrict__ sys, const float* __restrict__ af,
                                 float* as, double* pot) {
+    grid_dep_entry();
     int ne = *g.n_edge;
     const float c2 = 3.f * 3.f + 0.1f * 3.f;
     const float sharp = 1.f / (3.0f * 0.10f);
@@ -2262,7 +2314,7 @@ struct BackbonePairsNode : GNode {
         auto& a = e.arg(*this, 0);
         hg.bind(a, a);
         launch_pairs(hg.g, e.st);
-        bb_pairs_kernel<<<nblk(hg.g.cap), 256, 0, e.st>>>(hg.g, res_row, nat, refp, hg.g.sys1, a.out, a.sens,
+        ug::launch(bb_pairs_kernel, nblk(hg.g.cap), 256, 0, e.st, hg.g, res_row, nat, refp, hg.g.sys1, a.out, a.sens,
                                                           energy ? e.d_pot + size_t(pot_slot) * e.n_sys : nullptr);
     }
     DGraph* graph() override { return &hg.g; }
@@ -2672,16 +2724,18 @@ struct RotamerNode : GNode {
 };
 
 __global__ void add_pot_kernel(int n, const double* __restrict__ src, double* dst) {
+    grid_dep_entry();
     for (int s = grid_stride_start(); s < n; s += grid_stride()) dst[s] = src[s];
 }
 void RotamerNode::add_pot(Engine& e) {
-    add_pot_kernel<<<1, 256, 0, e.st>>>(e.n_sys, d_energy, e.d_pot + size_t(pot_slot) * e.n_sys);
+    ug::launch(add_pot_kernel, 1, 256, 0, e.st, e.n_sys, d_energy, e.d_pot + size_t(pot_slot) * e.n_sys);
 }
 
 bool is_prefix(const std::string& p, const std::string& s) { return s.compare(0, p.size(), p) == 0; }
 
 // ----------------------------------------------------------------- misc ---
 __global__ void sum_energy_kernel(int n_sys, int n_slots, const double* __restrict__ pot, double* __restrict__ out) {
+    grid_dep_entry();
     for (int s = grid_stride_start(); s < n_sys; s += grid_stride()) {
         double t = 0.0;
         for (int k = 0; k < n_slots; ++k) t += pot[size_t(k) * n_sys + s];
@@ -2692,9 +2746,11 @@ __global__ void sum_energy_kernel(int n_sys, int n_slots, const double* __restri
 // p -= dt F ; x += dt p   (integration_cycle, src/deriv_engine.cpp:317-331)
 // p -= h F  (the multistep integrator's slow-force kick)
 __global__ void kick_kernel(int n, float h, const float* __restrict__ f, float* __restrict__ mom) {
+    grid_dep_entry();
     for (int i = grid_stride_start(); i < n; i += grid_stride()) mom[i] -= h * f[i];
 }
 __global__ void integrate_kernel(int n, float dt, const float* __restrict__ f, float* __restrict__ mom, float* __restrict__ pos) {
+    grid_dep_entry();
     for (int i = grid_stride_start(); i < n; i += grid_stride()) {
         float p = mom[i] - dt * f[i];
         mom[i] = p;
@@ -2709,6 +2765,7 @@ __global__ void integrate_kernel(int n, float dt, const float* __restrict__ f, f
 __global__ void thermostat_kernel(int n_sys, const int* __restrict__ atom_off, const int* __restrict__ atom_sys,
                                   int n_atom, float delta_t, float timescale, const float* __restrict__ temp,
                                   const unsigned* __restrict__ seed, unsigned long long* round, float* mom) {
+    grid_dep_entry();
     for (int a = grid_stride_start(); a < n_atom; a += grid_stride()) {
         int s = atom_sys[a];
         float ms = expf(-delta_t / timescale);
@@ -2728,12 +2785,14 @@ __global__ void thermostat_kernel(int n_sys, const int* __restrict__ atom_off, c
     }
 }
 __global__ void round_advance_kernel(int n_sys, unsigned long long* round) {
+    grid_dep_entry();
     for (int s = grid_stride_start(); s < n_sys; s += grid_stride()) round[s] += 1;
 }
 
 // Move each system's centroid to the origin (xy_only: leave z alone); one
 // block of 256 threads per system (recenter, src/deriv_engine.cpp:39-50)
 __global__ void recenter_kernel(const int* __restrict__ atom_off, float* pos, int xy_only) {
+    grid_dep_entry();
     int s = blockIdx.x;
     int a0 = atom_off[s], a1 = atom_off[s + 1];
     __shared__ float red[3][256 / 32];
@@ -2997,7 +3056,7 @@ void Engine::compute(bool energy, int level) {
         }
         for (size_t i = nodes.size(); i-- > 0;)
             if (runs(i)) nodes[i]->backward(*this);
-        if (energy) sum_energy_kernel<<<1, 256, 0, st>>>(n_sys, n_pot_slots, d_pot, d_energy);
+        if (energy) ug::launch(sum_energy_kernel, 1, 256, 0, st, n_sys, n_pot_slots, d_pot, d_energy);
         UG_CK(cudaGetLastError());
         return;
     }
@@ -3045,21 +3104,21 @@ void Engine::compute(bool energy, int level) {
         UG_CK(cudaEventRecord(ev_lane[l], lanes[l]));
         UG_CK(cudaStreamWaitEvent(main, ev_lane[l], 0));
     }
-    if (energy) sum_energy_kernel<<<1, 256, 0, st>>>(n_sys, n_pot_slots, d_pot, d_energy);
+    if (energy) ug::launch(sum_energy_kernel, 1, 256, 0, st, n_sys, n_pot_slots, d_pot, d_energy);
     UG_CK(cudaGetLastError());
 }
 
 void Engine::thermalize(float dt, float timescale) {
     // (3 x interval) x dt in FP32, the reference's thermostat time step
     // (src/main.cpp:780)
-    thermostat_kernel<<<nblk(atom_total), 256, 0, st>>>(n_sys, atom_off_d, atom_sys_d, atom_total,
+    ug::launch(thermostat_kernel, nblk(atom_total), 256, 0, st, n_sys, atom_off_d, atom_sys_d, atom_total,
                                                         (float(inner_step) * thermo_span) * dt, timescale, d_temp, d_seed, d_round,
                                                         d_mom);
-    round_advance_kernel<<<1, 256, 0, st>>>(n_sys, d_round);
+    ug::launch(round_advance_kernel, 1, 256, 0, st, n_sys, d_round);
 }
 
 void Engine::recenter(bool xy_only) {
-    recenter_kernel<<<n_sys, 256, 0, st>>>(atom_off_d, d_pos, xy_only ? 1 : 0);
+    ug::launch(recenter_kernel, n_sys, 256, 0, st, atom_off_d, d_pos, xy_only ? 1 : 0);
     UG_CK(cudaGetLastError());
 }
 
@@ -3067,18 +3126,18 @@ void Engine::round(float dt, float timescale, bool thermostat) {
     if (thermostat) thermalize(dt, timescale);
     if (multistep) {
         compute(false, 1);  // slow forces: one kick of inner_step dt
-        kick_kernel<<<nblk(3LL * atom_total), 256, 0, st>>>(3 * atom_total, float(inner_step) * dt, nodes[0]->sens,
+        ug::launch(kick_kernel, nblk(3LL * atom_total), 256, 0, st, 3 * atom_total, float(inner_step) * dt, nodes[0]->sens,
                                                             d_mom);
         for (int stage = 0; stage < inner_step; ++stage) {
             compute(false, 0);
-            integrate_kernel<<<nblk(3LL * atom_total), 256, 0, st>>>(3 * atom_total, dt, nodes[0]->sens, d_mom, d_pos);
+            ug::launch(integrate_kernel, nblk(3LL * atom_total), 256, 0, st, 3 * atom_total, dt, nodes[0]->sens, d_mom, d_pos);
         }
         UG_CK(cudaGetLastError());
         return;
     }
     for (int stage = 0; stage < 3; ++stage) {
         compute(false);
-        integrate_kernel<<<nblk(3LL * atom_total), 256, 0, st>>>(3 * atom_total, dt, nodes[0]->sens, d_mom, d_pos);
+        ug::launch(integrate_kernel, nblk(3LL * atom_total), 256, 0, st, 3 * atom_total, dt, nodes[0]->sens, d_mom, d_pos);
     }
     UG_CK(cudaGetLastError());
 }

@@ -14,6 +14,7 @@
 #include <cstdio>
 
 #include "dev_math.cuh"
+#include "launch.cuh"
 #include "graph.h"
 #include "warm.h"
 
@@ -27,6 +28,7 @@ namespace cg = cooperative_groups;
 // chunk sums.
 __global__ void __launch_bounds__(1024) scan_kernel(const int* __restrict__ in, int* __restrict__ out, int n,
                                                     int* total_out, const int* __restrict__ skip_unless) {
+    grid_dep_entry();
     if (skip_unless && !*skip_unless) return;
     __shared__ int warp_sums[32];
     int t = threadIdx.x;
@@ -70,12 +72,13 @@ __global__ void __launch_bounds__(1024) scan_kernel(const int* __restrict__ in, 
 }
 
 void launch_scan(const int* in, int* out, int n, int* total_out, cudaStream_t st, const int* skip_unless) {
-    scan_kernel<<<1, 1024, 0, st>>>(in, out, n, total_out, skip_unless);
+    ug::launch(scan_kernel, 1, 1024, 0, st, in, out, n, total_out, skip_unless);
 }
 
 // --------------------------------------------------------- pair search ---
 __global__ void pack_kernel(const int* __restrict__ loc, const float* __restrict__ in, int w, int n,
                             float4* __restrict__ x) {
+    grid_dep_entry();
     for (int i = grid_stride_start(); i < n; i += grid_stride()) {
         const float* p = in + size_t(loc[i]) * w;
         x[i] = make_float4(p[0], p[1], p[2], 0.f);
@@ -83,8 +86,8 @@ __global__ void pack_kernel(const int* __restrict__ loc, const float* __restrict
 }
 
 void launch_pack_positions(const DGraph& g, cudaStream_t st) {
-    if (g.n1) pack_kernel<<<min(1024, (g.n1 + 255) / 256), 256, 0, st>>>(g.loc1, g.in1, g.w1, g.n1, g.x1);
-    if (!g.symmetric && g.n2) pack_kernel<<<min(1024, (g.n2 + 255) / 256), 256, 0, st>>>(g.loc2, g.in2, g.w2, g.n2, g.x2);
+    if (g.n1) ug::launch(pack_kernel, min(1024, (g.n1 + 255) / 256), 256, 0, st, g.loc1, g.in1, g.w1, g.n1, g.x1);
+    if (!g.symmetric && g.n2) ug::launch(pack_kernel, min(1024, (g.n2 + 255) / 256), 256, 0, st, g.loc2, g.in2, g.w2, g.n2, g.x2);
 }
 
 // One warp per row (4 consecutive set-1 elements of one system).  Pass 0
@@ -102,6 +105,7 @@ __device__ __forceinline__ float pair_d2(float4 a, float4 b) {
 
 template <int PASS, bool CACHED>
 __global__ void pair_kernel(DGraph g) {
+    grid_dep_entry();
     if (CACHED && !*g.any_flag) return;  // no system rebuilt in this evaluation
     int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     int lane = threadIdx.x & 31;
@@ -180,6 +184,7 @@ __global__ void pair_kernel(DGraph g) {
 }
 
 __global__ void cap_check_kernel(int* n_edge, int cap, int* status) {
+    grid_dep_entry();
     if (*n_edge > cap) {
         atomicOr(status, ST_EDGE_OVERFLOW);
         *n_edge = cap;
@@ -192,6 +197,7 @@ __global__ void cap_check_kernel(int* n_edge, int cap, int* status) {
 // requested (src/interaction_graph.h:51-91: same bound, same comparison).
 // (one block)
 __global__ void cache_flag_init_kernel(DGraph g) {
+    grid_dep_entry();
     __shared__ int any;
     if (threadIdx.x == 0) any = 0;
     __syncthreads();
@@ -206,6 +212,7 @@ __global__ void cache_flag_init_kernel(DGraph g) {
 }
 
 __global__ void cache_check_kernel(DGraph g) {
+    grid_dep_entry();
     float h = 0.5f * ((g.cutoff + g.buffer) - g.cutoff);
     float lim = h * h;
     int n = g.n1 + (g.symmetric ? 0 : g.n2);
@@ -226,6 +233,7 @@ __global__ void cache_check_kernel(DGraph g) {
 // after the rebuild search: per system candidate counts (capped by the
 // segment, overflow flagged), and the refine pass's tile prefix over systems
 __global__ void cache_commit_kernel(DGraph g) {
+    grid_dep_entry();
     if (!*g.any_flag) return;
     for (int s = grid_stride_start(); s < g.n_sys; s += grid_stride()) {
         if (!g.sys_flag[s]) continue;
@@ -245,6 +253,7 @@ __global__ void cache_commit_kernel(DGraph g) {
 // first thread also clears the rebuild-everything request and recomputes the
 // per-system prefix of active refine tiles
 __global__ void cache_positions_kernel(DGraph g) {
+    grid_dep_entry();
     if (!*g.any_flag) return;  // nothing rebuilt: positions, tiles and request unchanged
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         *g.cache_force = 0;
@@ -272,6 +281,7 @@ __global__ void cache_positions_kernel(DGraph g) {
 // a scan over tiles gives offsets, pass 1 writes them in order.
 template <int PASS>
 __global__ void __launch_bounds__(256) cache_refine_kernel(DGraph g) {
+    grid_dep_entry();
     __shared__ int warp_sum[8];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int n_active = g.active_off[g.n_sys];
@@ -340,26 +350,26 @@ void launch_pairs(const DGraph& g, cudaStream_t st) {
     }
     int blocks = min(4 * 152, (g.n_rows * 32 + 255) / 256);
     if (!g.cached) {
-        pair_kernel<0, false><<<blocks, 256, 0, st>>>(g);
+        ug::launch((pair_kernel<0, false>), blocks, 256, 0, st, g);
         launch_scan(g.row_count, g.row_off, g.n_rows, g.n_edge, st);
-        pair_kernel<1, false><<<blocks, 256, 0, st>>>(g);
-        cap_check_kernel<<<1, 1, 0, st>>>(g.n_edge, g.cap, g.status);
+        ug::launch((pair_kernel<1, false>), blocks, 256, 0, st, g);
+        ug::launch(cap_check_kernel, 1, 1, 0, st, g.n_edge, g.cap, g.status);
         return;
     }
     int ne = g.n1 + (g.symmetric ? 0 : g.n2);
     int eb = min(1024, (ne + 255) / 256);
-    cache_flag_init_kernel<<<1, 256, 0, st>>>(g);
-    cache_check_kernel<<<eb, 256, 0, st>>>(g);
-    pair_kernel<0, true><<<blocks, 256, 0, st>>>(g);
+    ug::launch(cache_flag_init_kernel, 1, 256, 0, st, g);
+    ug::launch(cache_check_kernel, eb, 256, 0, st, g);
+    ug::launch((pair_kernel<0, true>), blocks, 256, 0, st, g);
     launch_scan(g.row_count, g.row_off, g.n_rows, nullptr, st, g.any_flag);
-    pair_kernel<1, true><<<blocks, 256, 0, st>>>(g);
-    cache_commit_kernel<<<1, 256, 0, st>>>(g);
-    cache_positions_kernel<<<eb, 256, 0, st>>>(g);
+    ug::launch((pair_kernel<1, true>), blocks, 256, 0, st, g);
+    ug::launch(cache_commit_kernel, 1, 256, 0, st, g);
+    ug::launch(cache_positions_kernel, eb, 256, 0, st, g);
     int rblocks = min(8 * 152, g.max_tiles);
-    cache_refine_kernel<0><<<rblocks, 256, 0, st>>>(g);
+    ug::launch((cache_refine_kernel<0>), rblocks, 256, 0, st, g);
     launch_scan(g.tile_count, g.tile_off, g.max_tiles, g.n_edge, st);
-    cache_refine_kernel<1><<<rblocks, 256, 0, st>>>(g);
-    cap_check_kernel<<<1, 1, 0, st>>>(g.n_edge, g.cap, g.status);
+    ug::launch((cache_refine_kernel<1>), rblocks, 256, 0, st, g);
+    ug::launch(cap_check_kernel, 1, 1, 0, st, g.n_edge, g.cap, g.status);
 }
 
 // ------------------------------------------------------ edge evaluation ---
@@ -465,6 +475,7 @@ __device__ float edge_value(const DGraph& g, const float* p, const float* a, con
 
 template <int KIND>
 __global__ void edge_eval_kernel(DGraph g, const int* __restrict__ edge_sys_start, const int* __restrict__ edge_sys_end) {
+    grid_dep_entry();
     int ne = *g.n_edge;
     int dw = g.d1 + g.d2;
     for (int e = grid_stride_start(); e < ne; e += grid_stride()) {
@@ -492,6 +503,7 @@ __global__ void edge_eval_kernel(DGraph g, const int* __restrict__ edge_sys_star
 }
 
 __global__ void edge_sys_range_kernel(DGraph g, int* start, int* end) {
+    grid_dep_entry();
     for (int s = grid_stride_start(); s < g.n_sys; s += grid_stride()) {
         start[s] = min(g.row_off[g.sys_first_row[s]], g.cap);
         end[s] = min(g.row_off[g.sys_first_row[s + 1]], g.cap);
@@ -500,6 +512,7 @@ __global__ void edge_sys_range_kernel(DGraph g, int* start, int* end) {
 
 // per-system edge ranges from the edge list itself (edges are in system order)
 __global__ void edge_sys_bounds_kernel(DGraph g, int* start, int* end) {
+    grid_dep_entry();
     int n = min(*g.n_edge, g.cap);
     for (int e = grid_stride_start(); e < n; e += grid_stride()) {
         int s = g.sys1[g.edges[e].x];
@@ -514,22 +527,23 @@ void launch_edge_eval(const DGraph& g, int* sys_start, int* sys_end, cudaStream_
         if (g.cached) {
             cudaMemsetAsync(sys_start, 0, sizeof(int) * size_t(g.n_sys), st);
             cudaMemsetAsync(sys_end, 0, sizeof(int) * size_t(g.n_sys), st);
-            edge_sys_bounds_kernel<<<blocks, 256, 0, st>>>(g, sys_start, sys_end);
+            ug::launch(edge_sys_bounds_kernel, blocks, 256, 0, st, g, sys_start, sys_end);
         } else {
-            edge_sys_range_kernel<<<1, 256, 0, st>>>(g, sys_start, sys_end);
+            ug::launch(edge_sys_range_kernel, 1, 256, 0, st, g, sys_start, sys_end);
         }
     }
     switch (g.kind) {
-        case IK_ROTAMER: edge_eval_kernel<IK_ROTAMER><<<blocks, 256, 0, st>>>(g, sys_start, sys_end); break;
-        case IK_HBCOV: edge_eval_kernel<IK_HBCOV><<<blocks, 256, 0, st>>>(g, sys_start, sys_end); break;
-        case IK_PHB: edge_eval_kernel<IK_PHB><<<blocks, 256, 0, st>>>(g, sys_start, sys_end); break;
-        case IK_ENVCOV: edge_eval_kernel<IK_ENVCOV><<<blocks, 256, 0, st>>>(g, sys_start, sys_end); break;
-        case IK_HBENV: edge_eval_kernel<IK_HBENV><<<blocks, 256, 0, st>>>(g, sys_start, sys_end); break;
+        case IK_ROTAMER: ug::launch((edge_eval_kernel<IK_ROTAMER>), blocks, 256, 0, st, g, sys_start, sys_end); break;
+        case IK_HBCOV: ug::launch((edge_eval_kernel<IK_HBCOV>), blocks, 256, 0, st, g, sys_start, sys_end); break;
+        case IK_PHB: ug::launch((edge_eval_kernel<IK_PHB>), blocks, 256, 0, st, g, sys_start, sys_end); break;
+        case IK_ENVCOV: ug::launch((edge_eval_kernel<IK_ENVCOV>), blocks, 256, 0, st, g, sys_start, sys_end); break;
+        case IK_HBENV: ug::launch((edge_eval_kernel<IK_HBENV>), blocks, 256, 0, st, g, sys_start, sys_end); break;
         default: break;
     }
 }
 
 __global__ void edge_scatter_kernel(DGraph g) {
+    grid_dep_entry();
     int ne = *g.n_edge;
     int dw = g.d1 + g.d2;
     for (int e = grid_stride_start(); e < ne; e += grid_stride()) {
@@ -545,13 +559,14 @@ __global__ void edge_scatter_kernel(DGraph g) {
 }
 
 void launch_edge_scatter(const DGraph& g, cudaStream_t st) {
-    edge_scatter_kernel<<<2 * 152, 256, 0, st>>>(g);
+    ug::launch(edge_scatter_kernel, 2 * 152, 256, 0, st, g);
 }
 
 // dE/dparam for the quadspline graphs, accumulated per type pair with the
 // current edge sensitivities (src/interaction_graph.h:406-416, :498-550,
 // src/bead_interaction.h:87-131)
 __global__ void param_deriv_kernel(DGraph g, float* __restrict__ out) {
+    grid_dep_entry();
     int ne = *g.n_edge;
     for (int e = grid_stride_start(); e < ne; e += grid_stride()) {
         float s = g.esens[e];
@@ -600,7 +615,7 @@ __global__ void param_deriv_kernel(DGraph g, float* __restrict__ out) {
 }
 
 void launch_param_deriv(const DGraph& g, float* out, cudaStream_t st) {
-    param_deriv_kernel<<<2 * 152, 256, 0, st>>>(g, out);
+    ug::launch(param_deriv_kernel, 2 * 152, 256, 0, st, g, out);
 }
 
 // ------------------------------------------------------------ rotamer BP ---
@@ -612,6 +627,7 @@ __device__ __forceinline__ long long slot_index(const DBP& b, int r1, int r2) {
 // reset the residue-pair map entries of the previous evaluation and the
 // per-residue accumulators
 __global__ void bp_reset_kernel(DBP b) {
+    grid_dep_entry();
     int prev_n_ent = min(*b.n_ent, b.ent_cap);  // entries of the previous evaluation
     for (int e = grid_stride_start(); e < prev_n_ent; e += grid_stride())
         b.slot[slot_index(b, b.erow[e], b.col[e])] = -1;
@@ -626,6 +642,7 @@ __global__ void bp_reset_kernel(DBP b) {
 // 1-body energy per (residue, rotamer) from up to 4 input nodes (src/rotamer.cpp:862-884)
 __global__ void bp_bead_energy_kernel(DBP b, const float* p0, const float* p1, const float* p2, const float* p3,
                                       int n_in, int w0, int w1, int w2, int w3) {
+    grid_dep_entry();
     for (int i = grid_stride_start(); i < b.n_bead; i += grid_stride()) {
         int l = b.bead_loc[i];
         float e = p0[size_t(l) * w0];
@@ -639,6 +656,7 @@ __global__ void bp_bead_energy_kernel(DBP b, const float* p0, const float* p1, c
 // classify bead edges: mark multi-rotamer residue pairs; fold 1-rotamer
 // partners into node energies; sum 1-1 edges (src/rotamer.cpp:886-912)
 __global__ void bp_mark_kernel(DBP b, DGraph g) {
+    grid_dep_entry();
     int ne = *g.n_edge;
     for (int e = grid_stride_start(); e < ne; e += grid_stride()) {
         int2 ij = g.edges[e];
@@ -666,6 +684,7 @@ __global__ void bp_mark_kernel(DBP b, DGraph g) {
 // marked neighbours in increasing order
 template <int PASS>
 __global__ void bp_rows_kernel(DBP b) {
+    grid_dep_entry();
     int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     int lane = threadIdx.x & 31;
     int n_warps = (gridDim.x * blockDim.x) >> 5;
@@ -701,6 +720,7 @@ __global__ void bp_rows_kernel(DBP b) {
 }
 
 __global__ void bp_entry_init_kernel(DBP b) {
+    grid_dep_entry();
     int n = min(*b.n_ent, b.ent_cap);
     for (int e = grid_stride_start(); e < n; e += grid_stride()) {
         int rv = b.slot[slot_index(b, b.col[e], b.erow[e])];
@@ -715,6 +735,7 @@ __global__ void bp_entry_init_kernel(DBP b) {
 }
 
 __global__ void bp_cap_check_kernel(DBP b) {
+    grid_dep_entry();
     if (*b.n_ent > b.ent_cap) {
         atomicOr(b.status, ST_RES_EDGE_OVERFLOW);
         *b.n_ent = b.ent_cap;
@@ -722,6 +743,7 @@ __global__ void bp_cap_check_kernel(DBP b) {
 }
 
 __global__ void bp_edge_energy_kernel(DBP b, DGraph g) {
+    grid_dep_entry();
     int ne = *g.n_edge;
     for (int e = grid_stride_start(); e < ne; e += grid_stride()) {
         int2 ij = g.edges[e];
@@ -738,6 +760,7 @@ __global__ void bp_edge_energy_kernel(DBP b, DGraph g) {
 
 // node probabilities (src/rotamer.cpp:239-256, :398-405) and edge matrices
 __global__ void bp_node_prob_kernel(DBP b) {
+    grid_dep_entry();
     for (int r = grid_stride_start(); r < b.n_res; r += grid_stride()) {
         int n = b.nrot[r];
         float m = b.E1[r * 8];
@@ -751,6 +774,7 @@ __global__ void bp_node_prob_kernel(DBP b) {
 // one-body energy): one thread per entry, its 6x6 block as nine float4, zero
 // outside the (row rotamers) x (column rotamers) corner
 __global__ void bp_pair_prob_kernel(DBP b) {
+    grid_dep_entry();
     int n_ent = min(*b.n_ent, b.ent_cap);
     for (int e = grid_stride_start(); e < n_ent; e += grid_stride()) {
         int nu = b.nrot[b.erow[e]], nv = b.nrot[b.col[e]];
@@ -918,6 +942,7 @@ __device__ __forceinline__ float bp_beliefs(const DBP& b, int r0, int lo, int hi
 // bp_variants (the engine's autotuner picks one).
 template <int BP_CLUSTER, int BP_LANES, int THREADS>
 __global__ void __launch_bounds__(THREADS) bp_solve_kernel(DBP b, int want_energy, double* energy_out) {
+    grid_dep_entry();
     extern __shared__ float smem[];
     __shared__ double dred[32];
     __shared__ float s_dev[2][BP_CLUSTER];  // per chunk parity: every block's deviation maximum
@@ -1258,6 +1283,7 @@ void bp_variant_desc(int i, int* cluster, int* lanes, int* threads) {
 // average energies; and per input, the belief-weighted one-body energies.
 __global__ void bp_node_log_kernel(DBP b, const float* p0, const float* p1, const float* p2, const float* p3, int n_in,
                                    int w0, int w1, int w2, int w3) {
+    grid_dep_entry();
     for (int u = grid_stride_start(); u < b.n_res; u += grid_stride()) {
         int n = b.nrot[u];
         const float* m = b.marg + u * 8;
@@ -1305,6 +1331,7 @@ __global__ void bp_node_log_kernel(DBP b, const float* p0, const float* p1, cons
 // sensitivities, and 1-body sensitivities (src/rotamer.cpp:1057-1086)
 __global__ void bp_sens_kernel(DBP b, DGraph g, float* s0, float* s1, float* s2, float* s3, int n_in, int w0,
                                int w1, int w2, int w3) {
+    grid_dep_entry();
     int ne = *g.n_edge;
     for (int e = grid_stride_start(); e < ne; e += grid_stride()) {
         int2 ij = g.edges[e];
@@ -1348,17 +1375,17 @@ __global__ void bp_sens_kernel(DBP b, DGraph g, float* s0, float* s1, float* s2,
 void launch_bp_structure(DBP& b, const DGraph& g, cudaStream_t st) {
     int blocks = 2 * 152;
     // n_ent is rewritten only by the scan below, after this kernel completes
-    bp_reset_kernel<<<blocks, 256, 0, st>>>(b);
+    ug::launch(bp_reset_kernel, blocks, 256, 0, st, b);
     if (b.log_fe) cudaMemsetAsync(b.log_e11, 0, sizeof(float) * size_t(b.n_res), st);
-    bp_mark_kernel<<<blocks, 256, 0, st>>>(b, g);
+    ug::launch(bp_mark_kernel, blocks, 256, 0, st, b, g);
     int rb = min(4 * 152, (b.n_res * 32 + 255) / 256);
-    bp_rows_kernel<0><<<rb, 256, 0, st>>>(b);
+    ug::launch((bp_rows_kernel<0>), rb, 256, 0, st, b);
     launch_scan(b.row_count, b.row_ptr, b.n_res, b.n_ent, st);
-    bp_rows_kernel<1><<<rb, 256, 0, st>>>(b);
-    bp_cap_check_kernel<<<1, 1, 0, st>>>(b);
-    bp_entry_init_kernel<<<blocks, 256, 0, st>>>(b);
-    bp_edge_energy_kernel<<<blocks, 256, 0, st>>>(b, g);
-    bp_pair_prob_kernel<<<blocks, 256, 0, st>>>(b);
+    ug::launch((bp_rows_kernel<1>), rb, 256, 0, st, b);
+    ug::launch(bp_cap_check_kernel, 1, 1, 0, st, b);
+    ug::launch(bp_entry_init_kernel, blocks, 256, 0, st, b);
+    ug::launch(bp_edge_energy_kernel, blocks, 256, 0, st, b, g);
+    ug::launch(bp_pair_prob_kernel, blocks, 256, 0, st, b);
 }
 
 // The rest, after launch_bp_structure: one-body energies, node
@@ -1371,8 +1398,8 @@ void launch_bp(DBP& b, const DGraph& g, const float* const* in, float* const* in
     int blocks = 2 * 152;
     (void)prev_n_ent;
     if (b.log_fe) cudaMemsetAsync(b.log_1b, 0, sizeof(float) * size_t(b.n_res) * size_t(n_in), st);
-    bp_bead_energy_kernel<<<blocks, 256, 0, st>>>(b, in[0], in[1], in[2], in[3], n_in, w[0], w[1], w[2], w[3]);
-    bp_node_prob_kernel<<<blocks, 256, 0, st>>>(b);
+    ug::launch(bp_bead_energy_kernel, blocks, 256, 0, st, b, in[0], in[1], in[2], in[3], n_in, w[0], w[1], w[2], w[3]);
+    ug::launch(bp_node_prob_kernel, blocks, 256, 0, st, b);
     if (warm) launch_warm_start(*warm, pos, atom_off, b.res_off, b.prob, b.nrot, b.n_sys, b.n_res, st);
     size_t smem = bp_solve_smem_bytes(b.max_res_sys);
     const BpVariant& v = bp_variants()[b.variant];
@@ -1390,21 +1417,23 @@ void launch_bp(DBP& b, const DGraph& g, const float* const* in, float* const* in
         cfg.blockDim = dim3(unsigned(v.threads));
         cfg.dynamicSmemBytes = smem;
         cfg.stream = st;
-        cudaLaunchAttribute at[1];
+        cudaLaunchAttribute at[2];
         at[0].id = cudaLaunchAttributeClusterDimension;
         at[0].val.clusterDim.x = unsigned(v.cluster);
         at[0].val.clusterDim.y = 1;
         at[0].val.clusterDim.z = 1;
+        at[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        at[1].val.programmaticStreamSerializationAllowed = 1;
         cfg.attrs = at;
-        cfg.numAttrs = 1;
+        cfg.numAttrs = pdl_enabled() ? 2 : 1;
         void* args[] = {&b, &want_energy, &energy_out};
         cudaLaunchKernelExC(&cfg, v.fn, args);
     }
     if (timed) cudaEventRecordWithFlags(b.kt_ev[(*b.kt_used)++], st, cudaEventRecordExternal);
     if (b.log_fe)
-        bp_node_log_kernel<<<blocks, 256, 0, st>>>(b, in[0], in[1], in[2], in[3], n_in, w[0], w[1], w[2], w[3]);
-    bp_sens_kernel<<<blocks, 256, 0, st>>>(b, g, in_sens[0], in_sens[1], in_sens[2], in_sens[3], n_in, w[0], w[1],
-                                           w[2], w[3]);
+        ug::launch(bp_node_log_kernel, blocks, 256, 0, st, b, in[0], in[1], in[2], in[3], n_in, w[0], w[1], w[2], w[3]);
+    ug::launch(bp_sens_kernel, blocks, 256, 0, st, b, g, in_sens[0], in_sens[1], in_sens[2], in_sens[3], n_in, w[0],
+               w[1], w[2], w[3]);
     (void)scan_total;
 }
 

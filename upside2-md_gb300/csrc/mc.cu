@@ -6,6 +6,7 @@
 #include <cstring>
 
 #include "dev_math.cuh"
+#include "launch.cuh"
 #include "mc.h"
 
 namespace ug {
@@ -35,6 +36,7 @@ __device__ float dihedral(f3 r1, f3 r2, f3 r3, f3 r4) {
 // side is rotated about CA-N by the change of phi and about C-CA by the
 // change of psi.
 __global__ void mc_pivot_kernel(McDev m, float* pos, unsigned long long round) {
+    grid_dep_entry();
     const int s = blockIdx.x;
     const int l0 = m.piv_off[s], nloc = m.piv_off[s + 1] - l0;
     if (nloc == 0) return;  // block-uniform
@@ -104,6 +106,7 @@ __global__ void mc_pivot_kernel(McDev m, float* pos, unsigned long long round) {
 // Gaussian displacement or rotated about its centroid by a Gaussian angle
 // about a random axis.
 __global__ void mc_jump_kernel(McDev m, float* pos, unsigned long long round) {
+    grid_dep_entry();
     const int s = blockIdx.x;
     const int c0 = m.jmp_off[s], nch = m.jmp_off[s + 1] - c0;
     if (nch == 0) return;  // block-uniform
@@ -305,8 +308,8 @@ void McSampler::step(uint64_t round, int* accepted) {
         e.compute_checked(true);
         e.energies(e_old.data());
         UG_CK(cudaMemcpyAsync(saved_, e.d_pos, pos_bytes, cudaMemcpyDeviceToDevice, e.st));
-        if (k == 0) mc_pivot_kernel<<<S, 128, 0, e.st>>>(d_, e.d_pos, (unsigned long long)round);
-        else mc_jump_kernel<<<S, 256, 0, e.st>>>(d_, e.d_pos, (unsigned long long)round);
+        if (k == 0) ug::launch(mc_pivot_kernel, S, 128, 0, e.st, d_, e.d_pos, (unsigned long long)round);
+        else ug::launch(mc_jump_kernel, S, 256, 0, e.st, d_, e.d_pos, (unsigned long long)round);
         UG_CK(cudaGetLastError());
         e.compute_checked(true);
         e.energies(e_new.data());

@@ -18,12 +18,14 @@
 #include <mutex>
 
 #include "graph.h"
+#include "launch.cuh"
 
 namespace ug {
 
 template <int PASS>
 __global__ void point_pair_kernel(const float* __restrict__ pos, int n, float c2, int* __restrict__ row_count,
                                   const int* __restrict__ row_off, int2* __restrict__ pairs, int cap) {
+    grid_dep_entry();
     int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     int lane = threadIdx.x & 31;
     int n_warps = (gridDim.x * blockDim.x) >> 5;
@@ -88,9 +90,9 @@ cudaError_t launch_point_pairs(const float* pos, int n, float cutoff, int* pairs
     int blocks = min(8 * 152, (n_rows * 32 + 255) / 256);
     float c2 = cutoff * cutoff;
     int2* p2 = reinterpret_cast<int2*>(pairs);
-    point_pair_kernel<0><<<blocks, 256, 0, st>>>(pos, n, c2, row_count, row_off, p2, cap);
+    ug::launch((point_pair_kernel<0>), blocks, 256, 0, st, pos, n, c2, row_count, row_off, p2, cap);
     launch_scan(row_count, row_off, n_rows, n_pairs, st);
-    point_pair_kernel<1><<<blocks, 256, 0, st>>>(pos, n, c2, row_count, row_off, p2, cap);
+    ug::launch((point_pair_kernel<1>), blocks, 256, 0, st, pos, n, c2, row_count, row_off, p2, cap);
     return cudaGetLastError();
 }
 

@@ -15,6 +15,7 @@
 #include <cstdint>
 
 #include "dev_math.cuh"
+#include "launch.cuh"
 #include "warm.h"
 
 namespace ug {
@@ -44,6 +45,7 @@ __global__ void __launch_bounds__(128) gemm_bf16_kernel(const uint16_t* __restri
                                                         const uint16_t* __restrict__ B, long long b_r, long long b_c,
                                                         float* __restrict__ C, int ldc, int M, int N, int K,
                                                         int accumulate, const int* __restrict__ need) {
+    grid_dep_entry();
     if (need && !*need) return;  // block-uniform: nothing to compute this time
     __shared__ uint16_t As[GT_M][GT_K + 8];  // [m][k]
     __shared__ uint16_t Bs[GT_N][GT_K + 8];  // [n][k]
@@ -121,7 +123,7 @@ cudaError_t launch_gemm_bf16(const uint16_t* A, long long a_r, long long a_c, co
                              const int* need) {
     if (M <= 0 || N <= 0) return cudaSuccess;
     dim3 grid((N + GT_N - 1) / GT_N, (M + GT_M - 1) / GT_M);
-    gemm_bf16_kernel<<<grid, 128, 0, st>>>(A, a_r, a_c, B, b_r, b_c, C, ldc, M, N, K, accumulate, need);
+    ug::launch(gemm_bf16_kernel, grid, 128, 0, st, A, a_r, a_c, B, b_r, b_c, C, ldc, M, N, K, accumulate, need);
     return cudaGetLastError();
 }
 
@@ -129,6 +131,7 @@ cudaError_t launch_gemm_bf16(const uint16_t* A, long long a_r, long long a_c, co
 // H = bf16(act(Z + bias)), act = ReLU or identity
 __global__ void bias_act_kernel(const float* __restrict__ Z, const float* __restrict__ bias, uint16_t* __restrict__ H,
                                 float* __restrict__ Hf, int M, int N, int relu, const int* __restrict__ need) {
+    grid_dep_entry();
     if (need && !*need) return;
     long long n = (long long)M * N;
     for (long long i = grid_stride_start(); i < n; i += grid_stride()) {
@@ -144,6 +147,7 @@ __global__ void bias_act_kernel(const float* __restrict__ Z, const float* __rest
 // value is written back into X too (for the bias gradient).
 __global__ void to_bf16_kernel(float* __restrict__ X, const uint16_t* __restrict__ H, uint16_t* __restrict__ Y,
                                long long n) {
+    grid_dep_entry();
     for (long long i = grid_stride_start(); i < n; i += grid_stride()) {
         float v = X[i];
         if (H && !(bf2f(H[i]) > 0.f)) {
@@ -160,6 +164,7 @@ __global__ void to_bf16_kernel(float* __restrict__ X, const uint16_t* __restrict
 __global__ void softmax_xent_kernel(const float* __restrict__ Z, const float* __restrict__ T,
                                     const int* __restrict__ nrot, float* __restrict__ dZ, float* __restrict__ loss,
                                     int M, float scale) {
+    grid_dep_entry();
     for (int i = grid_stride_start(); i < M; i += grid_stride()) {
         int n = nrot[i];
         const float* z = Z + size_t(i) * WARM_OUT;
@@ -188,6 +193,7 @@ __global__ void softmax_xent_kernel(const float* __restrict__ Z, const float* __
 
 // column sums of X[M x N] (bias gradients)
 __global__ void colsum_kernel(const float* __restrict__ X, float* __restrict__ out, int M, int N) {
+    grid_dep_entry();
     int c = blockIdx.x;
     float s = 0.f;
     for (int r = threadIdx.x; r < M; r += blockDim.x) s += X[size_t(r) * N + c];
@@ -205,6 +211,7 @@ __global__ void colsum_kernel(const float* __restrict__ X, float* __restrict__ o
 __global__ void adam_kernel(float* __restrict__ w, const float* __restrict__ g, float* __restrict__ m,
                             float* __restrict__ v, uint16_t* __restrict__ wb, int n, float lr, float b1, float b2,
                             float eps, float c1, float c2) {
+    grid_dep_entry();
     for (int i = grid_stride_start(); i < n; i += grid_stride()) {
         float gi = g[i];
         float mi = b1 * m[i] + (1.f - b1) * gi;
@@ -221,27 +228,27 @@ static int nb(long long n) { return int(std::min<long long>(4 * 152, (n + 255) /
 
 cudaError_t launch_bias_act(const float* Z, const float* bias, uint16_t* H, float* Hf, int M, int N, int relu,
                             cudaStream_t st, const int* need) {
-    bias_act_kernel<<<nb((long long)M * N), 256, 0, st>>>(Z, bias, H, Hf, M, N, relu, need);
+    ug::launch(bias_act_kernel, nb((long long)M * N), 256, 0, st, Z, bias, H, Hf, M, N, relu, need);
     return cudaGetLastError();
 }
 cudaError_t launch_to_bf16(float* X, const uint16_t* H, uint16_t* Y, long long n, cudaStream_t st) {
-    to_bf16_kernel<<<nb(n), 256, 0, st>>>(X, H, Y, n);
+    ug::launch(to_bf16_kernel, nb(n), 256, 0, st, X, H, Y, n);
     return cudaGetLastError();
 }
 cudaError_t launch_softmax_xent(const float* Z, const float* T, const int* nrot, float* dZ, float* loss, int M,
                                 float scale, cudaStream_t st) {
-    softmax_xent_kernel<<<nb(M), 256, 0, st>>>(Z, T, nrot, dZ, loss, M, scale);
+    ug::launch(softmax_xent_kernel, nb(M), 256, 0, st, Z, T, nrot, dZ, loss, M, scale);
     return cudaGetLastError();
 }
 cudaError_t launch_colsum(const float* X, float* out, int M, int N, cudaStream_t st) {
     if (N <= 0) return cudaSuccess;
-    colsum_kernel<<<N, 256, 0, st>>>(X, out, M, N);
+    ug::launch(colsum_kernel, N, 256, 0, st, X, out, M, N);
     return cudaGetLastError();
 }
 cudaError_t launch_adam(float* w, const float* g, float* m, float* v, uint16_t* wb, int n, float lr, float b1, float b2,
                         float eps, int step, cudaStream_t st) {
     float c1 = 1.f / (1.f - powf(b1, float(step))), c2 = 1.f / (1.f - powf(b2, float(step)));
-    adam_kernel<<<nb(n), 256, 0, st>>>(w, g, m, v, wb, n, lr, b1, b2, eps, c1, c2);
+    ug::launch(adam_kernel, nb(n), 256, 0, st, w, g, m, v, wb, n, lr, b1, b2, eps, c1, c2);
     return cudaGetLastError();
 }
 
@@ -279,6 +286,7 @@ __device__ __forceinline__ float dihedral_angle(f3 p0, f3 p1, f3 p2, f3 p3) {
 __global__ void warm_features_kernel(WarmDev w, const float* __restrict__ pos, const int* __restrict__ atom_off,
                                      const int* __restrict__ res_off, const float* __restrict__ prob,
                                      const int* __restrict__ nrot) {
+    grid_dep_entry();
     if (w.need && !*w.need) return;  // block-uniform
     const int s = blockIdx.x;
     // only systems whose solve starts from the prediction need features
@@ -369,6 +377,7 @@ __global__ void warm_features_kernel(WarmDev w, const float* __restrict__ pos, c
 
 // predicted marginals: softmax of the logits over the node's rotamers
 __global__ void warm_softmax_kernel(WarmDev w, const int* __restrict__ nrot, int n_res) {
+    grid_dep_entry();
     if (w.need && !*w.need) return;
     for (int u = grid_stride_start(); u < n_res; u += grid_stride()) {
         int n = nrot[u];
@@ -396,12 +405,13 @@ void launch_warm_features(const WarmDev& w, const float* pos, const int* atom_of
         cudaFuncSetAttribute(warm_features_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
         configured = smem;
     }
-    warm_features_kernel<<<dim3(unsigned(n_sys), 4), 128, smem, st>>>(w, pos, atom_off, res_off, prob, nrot);
+    ug::launch(warm_features_kernel, dim3(unsigned(n_sys), 4), 128, smem, st, w, pos, atom_off, res_off, prob, nrot);
 }
 
 // need = 1 when some system's coming solve starts from the prediction (the
 // statistics are final: the previous solve updated them)
 __global__ void warm_need_kernel(WarmDev w) {
+    grid_dep_entry();
     __shared__ int any;
     if (threadIdx.x == 0) any = 0;
     __syncthreads();
@@ -415,7 +425,7 @@ cudaError_t launch_warm_start(const WarmDev& w, const float* pos, const int* ato
                               const float* prob, const int* nrot, int n_sys, int n_res, cudaStream_t st) {
     // when no system starts from the prediction in this solve, every kernel
     // below returns at once
-    warm_need_kernel<<<1, 256, 0, st>>>(w);
+    ug::launch(warm_need_kernel, 1, 256, 0, st, w);
     launch_warm_features(w, pos, atom_off, res_off, prob, nrot, n_sys, st);
     // X[n x 64] . W1[64 x 128] -> H1; H1 . W2 -> H2; H2 . W3[128 x 8] -> Z
     launch_gemm_bf16(w.X, WARM_IN, 1, w.W1, WARM_HID, 1, w.Zh, WARM_HID, n_res, WARM_HID, WARM_IN, 0, st, w.need);
@@ -424,7 +434,7 @@ cudaError_t launch_warm_start(const WarmDev& w, const float* pos, const int* ato
     launch_bias_act(w.Zh, w.b2, w.H2, nullptr, n_res, WARM_HID, 1, st, w.need);
     launch_gemm_bf16(w.H2, WARM_HID, 1, w.W3, WARM_OUT, 1, w.Z, WARM_OUT, n_res, WARM_OUT, WARM_HID, 0, st, w.need);
     launch_bias_act(w.Z, w.b3, nullptr, w.Z, n_res, WARM_OUT, 0, st, w.need);
-    warm_softmax_kernel<<<nb(n_res), 256, 0, st>>>(w, nrot, n_res);
+    ug::launch(warm_softmax_kernel, nb(n_res), 256, 0, st, w, nrot, n_res);
     return cudaGetLastError();
 }
 
