@@ -2701,6 +2701,11 @@ struct RotamerNode : GNode {
             UG_CK(cudaMemcpy(st.data(), b.warm_stat, 4 * st.size(), cudaMemcpyDeviceToHost));
             return st;
         }
+        if (w == "bp_row_ptr") {  // CSR row offsets of the BP entries, n_res + 1
+            std::vector<int> rp(size_t(b.n_res) + 1);
+            UG_CK(cudaMemcpy(rp.data(), b.row_ptr, 4 * rp.size(), cudaMemcpyDeviceToHost));
+            return std::vector<float>(rp.begin(), rp.end());
+        }
         if (w == "n_iter") {
             std::vector<int> it(size_t(e.n_sys));
             UG_CK(cudaMemcpy(it.data(), b.n_iter, 4 * it.size(), cudaMemcpyDeviceToHost));
