@@ -2436,6 +2436,8 @@ struct RotamerNode : GNode {
         b.eoff = e.alloc<float>(size_t(b.n_res));
         b.belief = e.alloc<float>(size_t(b.n_res) * 16);
         b.marg = e.alloc<float>(size_t(b.n_res) * 8);
+        b.nb_scratch = e.alloc<float>(size_t(b.n_res) * 16);
+        b.dsm_cap = b.nb_cap = 0;
         b.n_iter = e.alloc<int>(size_t(e.n_sys));
         b.e11 = e.alloc<double>(size_t(e.n_sys));
         b.bad_solves = e.alloc<unsigned long long>(size_t(e.n_sys));
@@ -3313,13 +3315,20 @@ std::vector<std::pair<std::string, float>> Engine::autotune(int n_round, float d
             drop_graph();
             capture(dt, timescale, 1);
             for (int r = 0; r < 2; ++r) launch_graph();  // caches rebuilt, clocks up
-            UG_CK(cudaEventRecord(ev[0], st));
-            for (int r = 0; r < n_round; ++r) launch_graph();
-            UG_CK(cudaEventRecord(ev[1], st));
-            UG_CK(cudaStreamSynchronize(st));
-            float ms = 0.f;
-            UG_CK(cudaEventElapsedTime(&ms, ev[0], ev[1]));
-            if (!(status(true) & (ST_EDGE_OVERFLOW | ST_RES_EDGE_OVERFLOW))) return ms / float(n_round);
+            // the fastest of three blocks of n_round rounds: close settings
+            // (BP variants within a few percent) are ranked by their speed,
+            // not by one block's noise
+            float best = 1e30f;
+            for (int rep = 0; rep < 3; ++rep) {
+                UG_CK(cudaEventRecord(ev[0], st));
+                for (int r = 0; r < n_round; ++r) launch_graph();
+                UG_CK(cudaEventRecord(ev[1], st));
+                UG_CK(cudaStreamSynchronize(st));
+                float ms = 0.f;
+                UG_CK(cudaEventElapsedTime(&ms, ev[0], ev[1]));
+                best = std::min(best, ms);
+            }
+            if (!(status(true) & (ST_EDGE_OVERFLOW | ST_RES_EDGE_OVERFLOW))) return best / float(n_round);
             for (auto& n : nodes) n->grow(*this);  // storage grew: time this setting again
         }
         return 1e30f;

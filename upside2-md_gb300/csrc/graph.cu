@@ -11,6 +11,7 @@
 //   environment coverage edges src/environment.cpp:114-228
 //   rotamer BP                 src/rotamer.cpp:239-302, :425-569, :854-1162
 #include <cooperative_groups.h>
+#include <algorithm>
 #include <cstdio>
 
 #include "dev_math.cuh"
@@ -821,16 +822,42 @@ __device__ __forceinline__ void renorm6(float* x, int n) {
     for (int k = 0; k < 6; ++k) x[k] *= inv;
 }
 
+// Where the solve's two message buffers live.  Global: b.msg + k ent_cap 8
+// + 8 e for every entry e of the batch.  Shared (dsm): each block holds both
+// buffers for its own entries [base, base + dsm_cap) in its shared memory
+// from s0 (buffer 0, buffer 1, then the destination table: own entry
+// f - base -> (owner rank << 20) | slot of rev(f) in the owner), and a sender
+// stores a message straight into the shared memory of the block that owns
+// the entry it writes (distributed shared memory).  Both phases then read
+// only local shared memory; the cluster barrier between them orders the
+// stores.  Global buffers and sizes are read from the kernel parameters.
+struct MsgLoc {
+    float* s0;
+    int base;
+    int dsm;
+    __device__ __forceinline__ float* shared(const DBP& b, int k) const {
+        return s0 + (k ? size_t(b.dsm_cap) * 8 : 0);
+    }
+    __device__ __forceinline__ int* dst_table(const DBP& b) const {
+        return reinterpret_cast<int*>(s0 + size_t(b.dsm_cap) * 16);
+    }
+    __device__ __forceinline__ float* own(const DBP& b, int k, int e) const {
+        return dsm ? shared(b, k) + size_t(e - base) * 8 : b.msg + (k ? size_t(b.ent_cap) * 8 : 0) + size_t(e) * 8;
+    }
+};
+
 // new message along every entry of [e0, e1): einfo[f] = (local index of the
-// row node v, reverse entry, local index of the column node u, 0)
-__device__ __forceinline__ void bp_messages(const DBP& b, int e0, int e1, const float* __restrict__ Nold,
-                                            const int* __restrict__ s_nrot, const float* __restrict__ Eold,
-                                            float* __restrict__ Ecur, int tid, int nt) {
+// row node v, reverse entry, local index of the column node u, 0); the old
+// message is read from buffer kold, the new one written to buffer kcur.
+// Beliefs are indexed from node nb_lo.
+__device__ __forceinline__ void bp_messages(const DBP& b, int e0, int e1, const float* __restrict__ Nold, int nb_lo,
+                                            const int* __restrict__ s_nrot, const MsgLoc& M, int kold, int kcur,
+                                            cg::cluster_group& cluster, int tid, int nt) {
     for (int f = e0 + tid; f < e1; f += nt) {
         int4 inf = b.einfo[f];
         int nv = s_nrot[inf.x], nu = s_nrot[inf.z];
-        const float* ob = Nold + inf.x * 8;
-        const float4* om = reinterpret_cast<const float4*>(Eold + size_t(f) * 8);
+        const float* ob = Nold + (inf.x - nb_lo) * 8;
+        const float4* om = reinterpret_cast<const float4*>(M.own(b, kold, f));
         float4 o0 = om[0], o1 = om[1];
         float omv[6] = {o0.x, o0.y, o0.z, o0.w, o1.x, o1.y};
         float cav[6];
@@ -853,7 +880,13 @@ __device__ __forceinline__ void bp_messages(const DBP& b, int e0, int e1, const 
             sum += mm[i];
         }
         float inv = 1.f / sum;
-        float4* out = reinterpret_cast<float4*>(Ecur + size_t(inf.y) * 8);
+        float4* out;
+        if (M.dsm) {
+            int d = M.dst_table(b)[f - M.base];
+            out = reinterpret_cast<float4*>(cluster.map_shared_rank(M.shared(b, kcur) + size_t(d & 0xFFFFF) * 8, d >> 20));
+        } else {
+            out = reinterpret_cast<float4*>(b.msg + (kcur ? size_t(b.ent_cap) * 8 : 0) + size_t(inf.y) * 8);
+        }
         out[0] = make_float4(mm[0] * inv, mm[1] * inv, mm[2] * inv, mm[3] * inv);
         out[1] = make_float4(mm[4] * inv, mm[5] * inv, 0.f, 0.f);
     }
@@ -866,13 +899,12 @@ __device__ __forceinline__ void bp_messages(const DBP& b, int e0, int e1, const 
 // BP_LANES loads.
 template <int BP_LANES>
 __device__ __forceinline__ float bp_beliefs(const DBP& b, int r0, int lo, int hi, int e1, const float* __restrict__ Nold,
-                                            float* __restrict__ Ncur, const int* __restrict__ s_nrot,
-                                            const float* __restrict__ Ecur, int mode, float damp, int tid,
-                                            int nt) {
+                                            float* __restrict__ Ncur, int nb_lo, const int* __restrict__ s_nrot,
+                                            const MsgLoc& M, int kcur, int mode, float damp, int tid, int nt) {
     float dev = 0.f;
     const int q = tid % BP_LANES, lane = tid & 31;
     const unsigned gmask = ((1u << BP_LANES) - 1u) << (lane & ~(BP_LANES - 1));
-    const float4* m4 = reinterpret_cast<const float4*>(Ecur);
+    auto m4 = [&](int e) { return reinterpret_cast<const float4*>(M.own(b, kcur, e)); };
     for (int ul = lo + tid / BP_LANES; ul < hi; ul += nt / BP_LANES) {  // group-uniform
         int n = s_nrot[ul];
         if (n == 1) continue;
@@ -888,14 +920,16 @@ __device__ __forceinline__ float bp_beliefs(const DBP& b, int r0, int lo, int hi
         };
         int e = eb + q;
         for (; e + BP_LANES < ee; e += 2 * BP_LANES) {  // two loads in flight
-            float4 a0 = m4[2 * e], c0 = m4[2 * e + 1];
-            float4 a1 = m4[2 * (e + BP_LANES)], c1 = m4[2 * (e + BP_LANES) + 1];
+            const float4 *p0 = m4(e), *p1 = m4(e + BP_LANES);
+            float4 a0 = p0[0], c0 = p0[1];
+            float4 a1 = p1[0], c1 = p1[1];
             float x0[6] = {a0.x, a0.y, a0.z, a0.w, c0.x, c0.y}, x1[6] = {a1.x, a1.y, a1.z, a1.w, c1.x, c1.y};
             fold(x0);
             fold(x1);
         }
         if (e < ee) {
-            float4 a0 = m4[2 * e], c0 = m4[2 * e + 1];
+            const float4* p0 = m4(e);
+            float4 a0 = p0[0], c0 = p0[1];
             float x0[6] = {a0.x, a0.y, a0.z, a0.w, c0.x, c0.y};
             fold(x0);
         }
@@ -911,7 +945,7 @@ __device__ __forceinline__ float bp_beliefs(const DBP& b, int r0, int lo, int hi
 #pragma unroll
         for (int k = 0; k < 6; ++k) bl[k] = k < n ? b.prob[u * 8 + k] * prod[k] : 0.f;
         renorm6(bl, n);
-        const float* o = Nold + ul * 8;
+        const float* o = Nold + (ul - nb_lo) * 8;
         if (mode == 1) {
             float mx = bl[0];
             for (int k = 1; k < n; ++k) mx = fmaxf(mx, bl[k]);
@@ -922,7 +956,7 @@ __device__ __forceinline__ float bp_beliefs(const DBP& b, int r0, int lo, int hi
                 if (k < n) dev = fmaxf(dev, bl[k] - o[k]);
             }
         }
-        float* c = Ncur + ul * 8;
+        float* c = Ncur + (ul - nb_lo) * 8;
 #pragma unroll
         for (int k = 0; k < 6; ++k) c[k] = bl[k];
         c[6] = c[7] = 0.f;
@@ -969,15 +1003,66 @@ __global__ void __launch_bounds__(THREADS) bp_solve_kernel(DBP b, int want_energ
     };
     const int lo = split(crank), hi = split(crank + 1);
     const int eo0 = min(b.row_ptr[r0 + lo], e1), eo1 = min(b.row_ptr[r0 + hi], e1);
-    float* NB[2] = {smem, smem + N * 8};
-    int* s_nrot = reinterpret_cast<int*>(smem + 2 * N * 8);
     float* EM[2] = {b.msg, b.msg + size_t(b.ent_cap) * 8};
     const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
 
-    auto sweep = [&](const float* Nold, float* Ncur, const float* Eold, float* Ecur, int mode, float damp) {
-        bp_messages(b, eo0, eo1, Nold, s_nrot, Eold, Ecur, tid, nt);
+    // Shared layout.  Full (dsm_cap 0): beliefs of all N nodes (both
+    // buffers), then the rotamer counts; messages in global memory.  Compact
+    // (dsm_cap > 0): rotamer counts of all N nodes, beliefs of the block's own
+    // nodes (nb_cap per buffer), then both message buffers of its own entries
+    // (dsm_cap slots each) and the destination table.  Compact is used when
+    // every block of the cluster fits (each block computes every block's
+    // ranges, so the decision is the same in all); otherwise the own beliefs
+    // go to the global scratch and the messages to global memory.
+    __shared__ int s_eb[BP_CLUSTER + 1], s_nb[BP_CLUSTER + 1];
+    if (tid <= BP_CLUSTER) {
+        int sp = split(tid);
+        s_nb[tid] = sp;
+        s_eb[tid] = min(b.row_ptr[r0 + sp], e1);
+    }
+    __syncthreads();
+    const bool compact = b.dsm_cap > 0;
+    bool fits = compact;
+    for (int c = 0; c < BP_CLUSTER; ++c)
+        if (s_eb[c + 1] - s_eb[c] > b.dsm_cap || s_nb[c + 1] - s_nb[c] > b.nb_cap) fits = false;
+    float* NB[2];
+    int* s_nrot;
+    int nb_lo = 0;
+    MsgLoc M;
+    M.base = eo0;
+    M.dsm = fits;
+    M.s0 = nullptr;
+    if (!compact) {
+        NB[0] = smem;
+        NB[1] = smem + N * 8;
+        s_nrot = reinterpret_cast<int*>(smem + 2 * N * 8);
+    } else {
+        s_nrot = reinterpret_cast<int*>(smem);
+        float* nbb = smem + ((N + 3) & ~3);
+        nb_lo = lo;
+        if (fits) {
+            NB[0] = nbb;
+            NB[1] = nbb + size_t(b.nb_cap) * 8;
+        } else {
+            NB[0] = b.nb_scratch + size_t(r0 + lo) * 8;
+            NB[1] = b.nb_scratch + (size_t(b.n_res) + r0 + lo) * 8;
+        }
+        M.s0 = nbb + size_t(b.nb_cap) * 16;
+        if (fits) {
+            int* dst = M.dst_table(b);
+            for (int f = eo0 + tid; f < eo1; f += nt) {
+                int rv = b.rev[f];  // same system: within [s_eb[0], s_eb[BP_CLUSTER])
+                int c = 0;
+                while (c + 1 < BP_CLUSTER && rv >= s_eb[c + 1]) ++c;
+                dst[f - eo0] = (c << 20) | (rv - s_eb[c]);
+            }
+        }
+    }
+
+    auto sweep = [&](const float* Nold, float* Ncur, int kold, int kcur, int mode, float damp) {
+        bp_messages(b, eo0, eo1, Nold, nb_lo, s_nrot, M, kold, kcur, cluster, tid, nt);
         cluster.sync();
-        return bp_beliefs<BP_LANES>(b, r0, lo, hi, e1, Nold, Ncur, s_nrot, Ecur, mode, damp, tid, nt);
+        return bp_beliefs<BP_LANES>(b, r0, lo, hi, e1, Nold, Ncur, nb_lo, s_nrot, M, kcur, mode, damp, tid, nt);
     };
     if (tid < 2) s_bmax[tid] = 0;
 
@@ -993,7 +1078,8 @@ __global__ void __launch_bounds__(THREADS) bp_solve_kernel(DBP b, int want_energ
     const float* init = use_prev ? b.marg : use_warm ? b.warm : b.prob;
     // N.old = N.cur = prob (N.old = prediction when warm); E.old = 1 (own entries)
     if (tid == 0) s_multi = 0;
-    for (int ul = tid; ul < N; ul += nt) {
+    for (int ul = tid; ul < N; ul += nt) s_nrot[ul] = b.nrot[r0 + ul];
+    for (int ul = lo + tid; ul < hi; ul += nt) {  // own nodes
         // a start row that is not a distribution (no previous solve yet) falls
         // back to prob for that node
         const float* w = init + (r0 + ul) * 8;
@@ -1003,10 +1089,9 @@ __global__ void __launch_bounds__(THREADS) bp_solve_kernel(DBP b, int want_energ
         if (!(ws > 0.5f)) w = b.prob + (r0 + ul) * 8;
 #pragma unroll
         for (int k = 0; k < 8; ++k) {
-            NB[0][ul * 8 + k] = b.prob[(r0 + ul) * 8 + k];
-            NB[1][ul * 8 + k] = w[k];
+            NB[0][(ul - nb_lo) * 8 + k] = b.prob[(r0 + ul) * 8 + k];
+            NB[1][(ul - nb_lo) * 8 + k] = w[k];
         }
-        s_nrot[ul] = b.nrot[r0 + ul];
     }
     __syncthreads();
     if (use_prev) {
@@ -1024,7 +1109,7 @@ __global__ void __launch_bounds__(THREADS) bp_solve_kernel(DBP b, int want_energ
                 int m = (a + z) >> 1;
                 if (pc[m] < v) a = m + 1; else z = m;
             }
-            float4* dst = reinterpret_cast<float4*>(EM[1] + size_t(f) * 8);
+            float4* dst = reinterpret_cast<float4*>(M.own(b, 1, f));
             if (a < pr[u + 1] && pc[a] == v) {
                 const float4* src = reinterpret_cast<const float4*>(pm + size_t(a) * 8);
                 dst[0] = src[0];
@@ -1034,7 +1119,8 @@ __global__ void __launch_bounds__(THREADS) bp_solve_kernel(DBP b, int want_energ
             }
         }
     } else if (!use_warm) {
-        for (int i = eo0 * 8 + tid; i < eo1 * 8; i += nt) EM[1][i] = 1.f;
+        float* m1 = M.own(b, 1, eo0);  // own entries are contiguous in either place
+        for (int i = tid; i < (eo1 - eo0) * 8; i += nt) m1[i] = 1.f;
     } else {
         // messages consistent with the start: the d incoming messages of node
         // u are all (start_u / prob_u)^(1/d), so that prob_u times their
@@ -1046,12 +1132,15 @@ __global__ void __launch_bounds__(THREADS) bp_solve_kernel(DBP b, int want_energ
             float m[8], sum = 0.f;
 #pragma unroll
             for (int k = 0; k < 8; ++k) {
-                m[k] = k < n ? powf((1e-10f + NB[1][ul * 8 + k]) / (1e-10f + NB[0][ul * 8 + k]), inv_d) : 0.f;
+                m[k] = k < n ? powf((1e-10f + NB[1][(ul - nb_lo) * 8 + k]) / (1e-10f + NB[0][(ul - nb_lo) * 8 + k]), inv_d)
+                             : 0.f;
                 sum += m[k];
             }
             float inv = 1.f / sum;
 #pragma unroll
-            for (int k = 0; k < 8; ++k) EM[1][size_t(f) * 8 + k] = k < n ? m[k] * inv : 1.f;
+            float* mf = M.own(b, 1, f);
+#pragma unroll
+            for (int k = 0; k < 8; ++k) mf[k] = k < n ? m[k] * inv : 1.f;
         }
     }
     __syncthreads();
@@ -1064,12 +1153,13 @@ __global__ void __launch_bounds__(THREADS) bp_solve_kernel(DBP b, int want_energ
     }
     // first sweep, undamped: new beliefs go to the buffer that then becomes
     // "old"; the other (prob) is max-normalised (src/rotamer.cpp:1135)
-    sweep(NB[1], NB[0], EM[1], EM[0], 0, 0.f);
+    if (M.dsm) cluster.sync();  // every block of the cluster runs before shared stores reach it
+    sweep(NB[1], NB[0], 1, 0, 0, 0.f);
     __syncthreads();
     for (int ul = lo + tid; ul < hi; ul += nt) {
         int n = s_nrot[ul];
         if (n == 1) continue;
-        float* c = NB[1] + ul * 8;
+        float* c = NB[1] + (ul - nb_lo) * 8;
         float mx = c[0];
         for (int k = 1; k < n; ++k) mx = fmaxf(mx, c[k]);
         float inv = 1.f / mx;
@@ -1096,7 +1186,7 @@ __global__ void __launch_bounds__(THREADS) bp_solve_kernel(DBP b, int want_energ
         for (int j = 0; j < chunk; ++j) {
             nc ^= 1;
             ec ^= 1;
-            bp_messages(b, eo0, eo1, NB[nc ^ 1], s_nrot, EM[ec ^ 1], EM[ec], tid, nt);
+            bp_messages(b, eo0, eo1, NB[nc ^ 1], nb_lo, s_nrot, M, ec ^ 1, ec, cluster, tid, nt);
             cluster.sync();
             if (pending) {  // the previous chunk's maximum, posted before this barrier
                 pending = false;
@@ -1111,7 +1201,8 @@ __global__ void __launch_bounds__(THREADS) bp_solve_kernel(DBP b, int want_energ
                     break;
                 }
             }
-            d = bp_beliefs<BP_LANES>(b, r0, lo, hi, e1, NB[nc ^ 1], NB[nc], s_nrot, EM[ec], 1, b.damping, tid, nt);
+            d = bp_beliefs<BP_LANES>(b, r0, lo, hi, e1, NB[nc ^ 1], NB[nc], nb_lo, s_nrot, M, ec, 1, b.damping, tid,
+                                     nt);
             if (j == chunk - 1) {
 #pragma unroll
                 for (int o = 16; o > 0; o >>= 1) d = fmaxf(d, __shfl_xor_sync(0xffffffffu, d, o));
@@ -1125,6 +1216,12 @@ __global__ void __launch_bounds__(THREADS) bp_solve_kernel(DBP b, int want_energ
         if (tid == 0) s_bmax[cpar ^ 1] = 0;
         cpar ^= 1;
         pending = true;
+    }
+    if (M.dsm) {  // final messages of own entries to global memory, for the tail and later kernels
+        const float4* src = reinterpret_cast<const float4*>(M.shared(b, ec));
+        float4* dstg = reinterpret_cast<float4*>(EM[ec] + size_t(eo0) * 8);
+        for (int i = tid; i < (eo1 - eo0) * 2; i += nt) dstg[i] = src[i];
+        __syncthreads();
     }
     if (tid == 0 && crank == 0) {
         b.n_iter[s] = iter;
@@ -1163,9 +1260,9 @@ __global__ void __launch_bounds__(THREADS) bp_solve_kernel(DBP b, int want_energ
             continue;
         }
         float sum = 0.f;
-        for (int k = 0; k < n; ++k) sum += Nf[ul * 8 + k];
+        for (int k = 0; k < n; ++k) sum += Nf[(ul - nb_lo) * 8 + k];
         float inv = 1.f / sum;
-        for (int k = 0; k < 8; ++k) b.marg[u * 8 + k] = k < n ? Nf[ul * 8 + k] * inv : 0.f;
+        for (int k = 0; k < 8; ++k) b.marg[u * 8 + k] = k < n ? Nf[(ul - nb_lo) * 8 + k] * inv : 0.f;
     }
     if (b.reuse) {  // leave the final state for the next evaluation's solve
         int* pr = b.prev_row_ptr + size_t(par) * (b.n_res + 1);
@@ -1401,8 +1498,24 @@ void launch_bp(DBP& b, const DGraph& g, const float* const* in, float* const* in
     ug::launch(bp_bead_energy_kernel, blocks, 256, 0, st, b, in[0], in[1], in[2], in[3], n_in, w[0], w[1], w[2], w[3]);
     ug::launch(bp_node_prob_kernel, blocks, 256, 0, st, b);
     if (warm) launch_warm_start(*warm, pos, atom_off, b.res_off, b.prob, b.nrot, b.n_sys, b.n_res, st);
-    size_t smem = bp_solve_smem_bytes(b.max_res_sys);
     const BpVariant& v = bp_variants()[b.variant];
+    // Compact layout when it is no larger than the full one: room for three
+    // times a block's share of nodes and ten entries per residue of its share
+    // (equilibrated proteins average six), so that the messages stay in
+    // shared memory without lowering the blocks an SM holds.
+    size_t smem = bp_solve_smem_bytes(b.max_res_sys);
+    {
+        const int N = b.max_res_sys, C = v.cluster;
+        int nb_cap = std::min(N, (3 * N + C - 1) / C);
+        int msg_cap = (10 * N + C - 1) / C;
+        size_t compact = 4 * size_t((N + 3) & ~3) + 64 * size_t(nb_cap) + 68 * size_t(msg_cap);
+        b.dsm_cap = b.nb_cap = 0;
+        if (compact <= smem && msg_cap >= 16 && msg_cap < (1 << 20)) {
+            b.dsm_cap = msg_cap;
+            b.nb_cap = nb_cap;
+            smem = compact;
+        }
+    }
     if (smem > 48 * 1024) cudaFuncSetAttribute(v.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
     // clusters above the portable 8 blocks have to be allowed per kernel
     if (v.cluster > 8) cudaFuncSetAttribute(v.fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);

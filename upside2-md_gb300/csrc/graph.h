@@ -118,6 +118,10 @@ struct DBP {
     int max_iter, chunk;
     int max_res_sys;            // largest residue count of one system (shared-memory sizing)
     int variant;                // launch variant of the solve (bp_variant_desc)
+    // solve's shared layout (set at launch): compact when dsm_cap > 0, with
+    // nb_cap own-node belief slots and dsm_cap own-entry message slots per block
+    int dsm_cap, nb_cap;
+    float* nb_scratch;          // 2 * n_res * 8: own beliefs of a compact solve whose cluster does not fit
     // bead level
     int n_bead;
     const int* bead_res;        // bead -> residue (global)
