@@ -227,7 +227,7 @@ def main():
         b.set_tuning(float(parts[0]), int(parts[1]), streams)
         tuned = {"chosen": "cache_buffer_scale=%s,bp_variant=%s,node_streams=%d (given)" % (parts[0], parts[1], streams)}
     elif not a.no_autotune:  # untimed; the state is restored after the trials
-        trials, chosen = b.autotune(5)
+        trials, chosen = b.autotune(8)
         tuned = {"chosen": chosen, "trial_ms_per_round": trials}
     pos_eq, mom_eq = b.get_pos(), b.get_mom()
     states = [(pos_eq[b.atom_off[i]:b.atom_off[i + 1]].copy(), mom_eq[b.atom_off[i]:b.atom_off[i + 1]].copy())

@@ -1499,18 +1499,32 @@ void launch_bp(DBP& b, const DGraph& g, const float* const* in, float* const* in
     ug::launch(bp_node_prob_kernel, blocks, 256, 0, st, b);
     if (warm) launch_warm_start(*warm, pos, atom_off, b.res_off, b.prob, b.nrot, b.n_sys, b.n_res, st);
     const BpVariant& v = bp_variants()[b.variant];
-    // Compact layout when it is no larger than the full one: room for three
-    // times a block's share of nodes and ten entries per residue of its share
-    // (equilibrated proteins average six), so that the messages stay in
-    // shared memory without lowering the blocks an SM holds.
+    // Compact layout: room for three times a block's share of nodes and ten
+    // entries per residue of its share (equilibrated proteins average six),
+    // used when it is no larger than the full layout or when the SMs still
+    // hold every block of the launch at once with it.
     size_t smem = bp_solve_smem_bytes(b.max_res_sys);
     {
+        static int n_sm = 0, per_sm = 0, per_block = 0, reserved = 0;
+        if (!n_sm) {
+            int dev = 0;
+            cudaGetDevice(&dev);
+            cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev);
+            cudaDeviceGetAttribute(&per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+            cudaDeviceGetAttribute(&per_block, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+            cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev);
+            n_sm = std::max(1, n_sm);
+        }
         const int N = b.max_res_sys, C = v.cluster;
         int nb_cap = std::min(N, (3 * N + C - 1) / C);
         int msg_cap = (10 * N + C - 1) / C;
         size_t compact = 4 * size_t((N + 3) & ~3) + 64 * size_t(nb_cap) + 68 * size_t(msg_cap);
+        int need = (b.n_sys * C + n_sm - 1) / n_sm;  // blocks per SM for a single wave
+        cudaFuncAttributes fa;
+        size_t stat = cudaFuncGetAttributes(&fa, v.fn) == cudaSuccess ? fa.sharedSizeBytes : size_t(2048);
+        long long room = std::min<long long>(per_block, per_sm / std::max(1, need) - reserved) - (long long)stat;
         b.dsm_cap = b.nb_cap = 0;
-        if (compact <= smem && msg_cap >= 16 && msg_cap < (1 << 20)) {
+        if ((compact <= smem || (long long)compact <= room) && msg_cap >= 16 && msg_cap < (1 << 20)) {
             b.dsm_cap = msg_cap;
             b.nb_cap = nb_cap;
             smem = compact;
