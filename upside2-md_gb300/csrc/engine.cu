@@ -1469,7 +1469,7 @@ struct HGraph {
     int per_elem_cap = 64;
     Engine* eng = nullptr;
     int* edge_bufs_int = nullptr;
-    void* bufs[4] = {nullptr, nullptr, nullptr, nullptr};
+    void* bufs[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
     void* cbufs[4] = {nullptr, nullptr, nullptr, nullptr};
     std::vector<int> cache_cap;  // per system candidate capacity (multiple of CACHE_TILE)
 
@@ -1523,7 +1523,9 @@ struct HGraph {
         UG_CK(cudaMalloc(&bufs[1], sizeof(float) * size_t(cap)));
         UG_CK(cudaMalloc(&bufs[2], sizeof(float) * size_t(cap) * dw));
         UG_CK(cudaMalloc(&bufs[3], sizeof(float) * size_t(cap)));
+        UG_CK(cudaMalloc(&bufs[4], sizeof(int) * size_t(cap)));
         g.edges = static_cast<int2*>(bufs[0]);
+        g.eaux = static_cast<int*>(bufs[4]);
         g.value = static_cast<float*>(bufs[1]);
         g.deriv = static_cast<float*>(bufs[2]);
         g.esens = static_cast<float*>(bufs[3]);

@@ -12,6 +12,7 @@
 //   rotamer BP                 src/rotamer.cpp:239-302, :425-569, :854-1162
 #include <cooperative_groups.h>
 #include <algorithm>
+#include <climits>
 #include <cstdio>
 
 #include "dev_math.cuh"
@@ -743,16 +744,29 @@ __global__ void bp_cap_check_kernel(DBP b) {
     }
 }
 
+// Summed pair energies of the entries; and per bead edge, where the
+// sensitivity pass finds the edge's weight (eaux): an edge-marginal element
+// (>= 0), 1 for two single-rotamer beads (BP_W_ONE), the node marginal of the
+// multi-rotamer partner (BP_W_NODE - index), or none (BP_W_NONE, entry lost to
+// overflow)
+#define BP_W_ONE (-1)
+#define BP_W_NODE (-2)
+#define BP_W_NONE INT_MIN
 __global__ void bp_edge_energy_kernel(DBP b, DGraph g) {
     grid_dep_entry();
     int ne = *g.n_edge;
     for (int e = grid_stride_start(); e < ne; e += grid_stride()) {
         int2 ij = g.edges[e];
         int r1 = b.bead_res[ij.x], r2 = b.bead_res[ij.y];
-        if (b.nrot[r1] == 1 || b.nrot[r2] == 1) continue;
-        int e12 = b.slot[slot_index(b, r1, r2)], e21 = b.slot[slot_index(b, r2, r1)];
-        if (e12 < 0 || e21 < 0) continue;
+        int n1 = b.nrot[r1], n2 = b.nrot[r2];
         int k1 = b.bead_rot[ij.x], k2 = b.bead_rot[ij.y];
+        if (n1 == 1 || n2 == 1) {
+            g.eaux[e] = n1 == 1 && n2 == 1 ? BP_W_ONE : BP_W_NODE - (n1 == 1 ? r2 * 8 + k2 : r1 * 8 + k1);
+            continue;
+        }
+        int e12 = b.slot[slot_index(b, r1, r2)], e21 = b.slot[slot_index(b, r2, r1)];
+        g.eaux[e] = e12 >= 0 ? e12 * 36 + k1 * 6 + k2 : BP_W_NONE;
+        if (e12 < 0 || e21 < 0) continue;
         float v = g.value[e];
         atomicAdd(&b.esum[size_t(e12) * 36 + k1 * 6 + k2], v);
         atomicAdd(&b.esum[size_t(e21) * 36 + k2 * 6 + k1], v);
@@ -1431,19 +1445,11 @@ __global__ void bp_sens_kernel(DBP b, DGraph g, float* s0, float* s1, float* s2,
     grid_dep_entry();
     int ne = *g.n_edge;
     for (int e = grid_stride_start(); e < ne; e += grid_stride()) {
-        int2 ij = g.edges[e];
-        int r1 = b.bead_res[ij.x], r2 = b.bead_res[ij.y];
-        int n1 = b.nrot[r1], n2 = b.nrot[r2];
-        int k1 = b.bead_rot[ij.x], k2 = b.bead_rot[ij.y];
-        float s;
-        if (n1 == 1 && n2 == 1) s = 1.f;
-        else if (n1 == 1) s = b.marg[r2 * 8 + k2];
-        else if (n2 == 1) s = b.marg[r1 * 8 + k1];
-        else {
-            int en = b.slot[slot_index(b, r1, r2)];
-            s = en >= 0 ? b.emarg[size_t(en) * 36 + k1 * 6 + k2] : 0.f;
-        }
+        // the edge's weight, located by the structure stage (bp_edge_energy_kernel)
+        const int w = g.eaux[e];
+        float s = w >= 0 ? b.emarg[w] : w == BP_W_ONE ? 1.f : w == BP_W_NONE ? 0.f : b.marg[BP_W_NODE - w];
         g.esens[e] = s;
+        int2 ij = g.edges[e];
         // the graph's adjoint (edge_scatter_kernel) for this edge, here rather
         // than in a kernel of its own
         if (s == 0.f) continue;

@@ -55,6 +55,7 @@ struct DGraph {
     float* value;
     float* deriv;               // cap * (d1+d2)
     float* esens;
+    int* eaux;                  // per-edge scratch (rotamer graph: the source of each edge's BP weight)
     float4* x1;                 // packed positions (xyz) of set 1 for the search
     float4* x2;
     int* status;
