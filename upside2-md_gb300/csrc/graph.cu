@@ -544,19 +544,67 @@ void launch_edge_eval(const DGraph& g, int* sys_start, int* sys_end, cudaStream_
     }
 }
 
+// Adds each lane's n values into row `key` of dst (row stride w; key < 0:
+// nothing).  Lanes holding the same key in a run of consecutive lanes (edges
+// of one set-1 element, which the pair search emits together) are summed
+// first with suffix sums over the run, and the run's first lane adds once.
+// Every lane of the warp calls it.
+constexpr int SCATTER_MAXD = 8;
+__device__ __forceinline__ void warp_run_add(float* dst, int w, int key, const float* v_in, int n) {
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const int prev = __shfl_up_sync(full, key, 1);
+    const unsigned heads = __ballot_sync(full, lane == 0 || prev != key);
+    const unsigned later = heads & ~((2u << lane) - 1u);  // run heads after this lane
+    const int run_end = later ? __ffs(later) - 1 : 32;    // first lane past this lane's run
+    float v[SCATTER_MAXD];
+#pragma unroll
+    for (int d = 0; d < SCATTER_MAXD; ++d) v[d] = d < n ? v_in[d] : 0.f;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        const bool same = lane + off < run_end;
+#pragma unroll
+        for (int d = 0; d < SCATTER_MAXD; ++d) {
+            float t = __shfl_down_sync(full, v[d], off);
+            if (same && d < n) v[d] += t;
+        }
+    }
+    if ((heads >> lane & 1u) && key >= 0) {
+        float* p = dst + size_t(key) * w;
+        for (int d = 0; d < n; ++d) atomicAdd(p + d, v[d]);
+    }
+}
+
 __global__ void edge_scatter_kernel(DGraph g) {
     grid_dep_entry();
-    int ne = *g.n_edge;
-    int dw = g.d1 + g.d2;
-    for (int e = grid_stride_start(); e < ne; e += grid_stride()) {
-        float s = g.esens[e];
-        if (s == 0.f) continue;
-        int2 ij = g.edges[e];
-        const float* da = g.deriv + size_t(e) * dw;
-        float* s1 = g.sens1 + size_t(g.loc1[ij.x]) * g.w1;
-        float* s2 = g.sens2 + size_t(g.loc2[ij.y]) * g.w2;
-        for (int d = 0; d < g.d1; ++d) atomicAdd(s1 + d, s * da[d]);
-        for (int d = 0; d < g.d2; ++d) atomicAdd(s2 + d, s * da[g.d1 + d]);
+    const int ne = *g.n_edge;
+    const int dw = g.d1 + g.d2;
+    const bool runs = g.d1 <= SCATTER_MAXD;
+    // warp-uniform trip count: every lane takes part in the run sums
+    const int stride = grid_stride(), first = grid_stride_start() - (threadIdx.x & 31);
+    for (int e0 = first; e0 < ne; e0 += stride) {
+        const int e = e0 + (threadIdx.x & 31);
+        float s = e < ne ? g.esens[e] : 0.f;
+        int key = -1;
+        float v1[SCATTER_MAXD];
+        if (s != 0.f) {
+            int2 ij = g.edges[e];
+            const float* da = g.deriv + size_t(e) * dw;
+            key = g.loc1[ij.x];
+            float* s2 = g.sens2 + size_t(g.loc2[ij.y]) * g.w2;
+            for (int d = 0; d < g.d2; ++d) atomicAdd(s2 + d, s * da[g.d1 + d]);
+            if (runs) {
+#pragma unroll
+                for (int d = 0; d < SCATTER_MAXD; ++d) v1[d] = d < g.d1 ? s * da[d] : 0.f;
+            } else {
+                float* s1 = g.sens1 + size_t(key) * g.w1;
+                for (int d = 0; d < g.d1; ++d) atomicAdd(s1 + d, s * da[d]);
+            }
+        } else {
+#pragma unroll
+            for (int d = 0; d < SCATTER_MAXD; ++d) v1[d] = 0.f;
+        }
+        if (runs) warp_run_add(g.sens1, g.w1, key, v1, g.d1);
     }
 }
 
@@ -1443,22 +1491,40 @@ __global__ void bp_node_log_kernel(DBP b, const float* p0, const float* p1, cons
 __global__ void bp_sens_kernel(DBP b, DGraph g, float* s0, float* s1, float* s2, float* s3, int n_in, int w0,
                                int w1, int w2, int w3) {
     grid_dep_entry();
-    int ne = *g.n_edge;
-    for (int e = grid_stride_start(); e < ne; e += grid_stride()) {
-        // the edge's weight, located by the structure stage (bp_edge_energy_kernel)
-        const int w = g.eaux[e];
-        float s = w >= 0 ? b.emarg[w] : w == BP_W_ONE ? 1.f : w == BP_W_NONE ? 0.f : b.marg[BP_W_NODE - w];
-        g.esens[e] = s;
-        int2 ij = g.edges[e];
+    const int ne = *g.n_edge;
+    const int dw = g.d1 + g.d2;
+    const bool runs = g.d1 <= SCATTER_MAXD;
+    const int stride = grid_stride(), first = grid_stride_start() - (threadIdx.x & 31);
+    for (int e0 = first; e0 < ne; e0 += stride) {  // warp-uniform trips (run sums)
+        const int e = e0 + (threadIdx.x & 31);
+        float s = 0.f;
+        int key = -1;
+        float v1[SCATTER_MAXD];
+#pragma unroll
+        for (int d = 0; d < SCATTER_MAXD; ++d) v1[d] = 0.f;
+        if (e < ne) {
+            // the edge's weight, located by the structure stage (bp_edge_energy_kernel)
+            const int w = g.eaux[e];
+            s = w >= 0 ? b.emarg[w] : w == BP_W_ONE ? 1.f : w == BP_W_NONE ? 0.f : b.marg[BP_W_NODE - w];
+            g.esens[e] = s;
+        }
         // the graph's adjoint (edge_scatter_kernel) for this edge, here rather
         // than in a kernel of its own
-        if (s == 0.f) continue;
-        const int dw = g.d1 + g.d2;
-        const float* da = g.deriv + size_t(e) * dw;
-        float* p1 = g.sens1 + size_t(g.loc1[ij.x]) * g.w1;
-        float* p2 = g.sens2 + size_t(g.loc2[ij.y]) * g.w2;
-        for (int d = 0; d < g.d1; ++d) atomicAdd(p1 + d, s * da[d]);
-        for (int d = 0; d < g.d2; ++d) atomicAdd(p2 + d, s * da[g.d1 + d]);
+        if (s != 0.f) {
+            int2 ij = g.edges[e];
+            const float* da = g.deriv + size_t(e) * dw;
+            key = g.loc1[ij.x];
+            float* p2 = g.sens2 + size_t(g.loc2[ij.y]) * g.w2;
+            for (int d = 0; d < g.d2; ++d) atomicAdd(p2 + d, s * da[g.d1 + d]);
+            if (runs) {
+#pragma unroll
+                for (int d = 0; d < SCATTER_MAXD; ++d) v1[d] = d < g.d1 ? s * da[d] : 0.f;
+            } else {
+                float* p1 = g.sens1 + size_t(key) * g.w1;
+                for (int d = 0; d < g.d1; ++d) atomicAdd(p1 + d, s * da[d]);
+            }
+        }
+        if (runs) warp_run_add(g.sens1, g.w1, key, v1, g.d1);
     }
     for (int i = grid_stride_start(); i < b.n_bead; i += grid_stride()) {
         float m = b.marg[b.bead_res[i] * 8 + b.bead_rot[i]];
