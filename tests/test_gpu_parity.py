@@ -221,3 +221,37 @@ def test_pair_cache_transparent(syn_configs):
         assert np.array_equal(b.node_edges(node), fresh.node_edges(node)), node
     assert np.abs(e_run - e_new).max() < 1e-4 * max(1.0, np.abs(e_new).max())
     assert rel_f(d_run, d_new) < 1e-4
+
+
+def test_bp_shared_layout_fallback(syn_configs):
+    """The BP solve's compact shared layout falls back to global-memory
+    messages and beliefs for a cluster whose entries overflow the reserved
+    message slots: with the slots capped at 16 (every cluster overflows) the
+    energy and forces still match the oracle, and match the shared-memory
+    solve of the same coordinates."""
+    import json
+    import subprocess
+    import sys
+    import oracle_py
+    import upside_gb300 as U
+    from conftest import ROOT
+    path, z = syn_configs[150]
+    x = z["pos"][1]
+    na = x.shape[0]
+    np.save(os.path.join(os.path.dirname(path), "x150.npy"), x)
+    code = ("import sys, json, numpy as np; sys.path.insert(0, %r); import upside_gb300 as U; "
+            "e = U.Upside(%r, %d); x = np.load(%r); "
+            "print(json.dumps([e.energy(x), e.deriv(x).tolist()]))"
+            % (os.path.join(ROOT, "upside2-md_gb300"), path, na, os.path.join(os.path.dirname(path), "x150.npy")))
+    env = dict(os.environ, UPSIDE_GB300_BP_MSG_SLOTS="16")
+    out = subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True, timeout=600)
+    assert out.returncode == 0, out.stderr[-2000:]
+    e_fb, d_fb = json.loads(out.stdout.strip().splitlines()[-1])
+    d_fb = np.array(d_fb, np.float32)
+    eng = U.Upside(path, na)
+    e_sh, d_sh = eng.energy(x), eng.deriv(x)
+    e64, d64 = oracle_py.Oracle(path, na, fp64=True).evaluate(x)
+    sc = energy_scale(eng, path)
+    assert abs(e_fb - e64) < E_ORC * sc and abs(e_sh - e64) < E_ORC * sc
+    assert rel_f(d_fb, d64) < F_ORC and rel_f(d_sh, d64) < F_ORC
+    assert abs(e_fb - e_sh) < E_ORC * sc and rel_f(d_fb, d_sh) < F_ORC

@@ -14,6 +14,7 @@
 #include <algorithm>
 #include <climits>
 #include <cstdio>
+#include <cstdlib>
 
 #include "dev_math.cuh"
 #include "launch.cuh"
@@ -1590,6 +1591,13 @@ void launch_bp(DBP& b, const DGraph& g, const float* const* in, float* const* in
         const int N = b.max_res_sys, C = v.cluster;
         int nb_cap = std::min(N, (3 * N + C - 1) / C);
         int msg_cap = (10 * N + C - 1) / C;
+        // UPSIDE_GB300_BP_MSG_SLOTS=n caps the message slots (at least 16), so
+        // that clusters overflow them and take the global-memory fallback
+        static const int slots_cap = [] {
+            const char* e = std::getenv("UPSIDE_GB300_BP_MSG_SLOTS");
+            return e ? std::max(16, std::atoi(e)) : 0;
+        }();
+        if (slots_cap) msg_cap = std::min(msg_cap, slots_cap);
         size_t compact = 4 * size_t((N + 3) & ~3) + 64 * size_t(nb_cap) + 68 * size_t(msg_cap);
         int need = (b.n_sys * C + n_sm - 1) / n_sm;  // blocks per SM for a single wave
         cudaFuncAttributes fa;
