@@ -124,3 +124,24 @@ def test_membrane_params(membrane_configs):
     b.evaluate()
     for nm in MEMB:
         assert abs(b.node_potential(nm)[0] - 2 * e0[nm]) < 1e-5 * max(abs(e0[nm]), 1.0), nm
+
+
+def test_membrane_driver_run(membrane_configs, tmp_path):
+    """The upside driver runs the curved-membrane configuration: frame 0
+    holds the potential of the initial coordinates, later frames stay
+    finite."""
+    import shutil
+    import upside_gb300 as U
+    from h5lite import H5File
+    paths, _ = membrane_configs
+    cfg = str(tmp_path / "memb.up")
+    shutil.copyfile(paths["curved"], cfg)
+    rt = float(np.float32(3) * np.float32(0.009))
+    U.upside_main(["--duration", repr(30 * rt), "--frame-interval", repr(10 * rt), "--temperature", "0.85",
+                   "--seed", "3", cfg], verbose=False)
+    f = H5File(cfg)
+    pos, pot = f.read("/output/pos"), f.read("/output/potential")
+    assert pos.shape[0] == 3 and np.all(np.isfinite(pos)) and np.all(np.isfinite(pot))
+    eng = U.Upside(paths["curved"], pos.shape[2])
+    x0 = f.read("/input/pos")[:, :, 0]
+    assert abs(eng.energy(x0) - pot[0, 0]) < 1e-4 * max(abs(pot[0, 0]), 1.0)

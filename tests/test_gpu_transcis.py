@@ -123,3 +123,23 @@ def test_trans_cis_dynamics_graph_matches_eager(transcis_config):
         assert b.status() & 3 == 0
     assert np.all(np.isfinite(res[0]))
     assert np.abs(res[0] - res[1]).max() < 1e-3
+
+
+def test_trans_cis_driver_run(transcis_config, tmp_path):
+    """The upside driver runs the trans-cis configuration with its frames
+    finite and frame 0 at the initial coordinates' potential."""
+    import shutil
+    import upside_gb300 as U
+    from h5lite import H5File
+    path, _ = transcis_config
+    cfg = str(tmp_path / "tc.up")
+    shutil.copyfile(path, cfg)
+    rt = float(np.float32(3) * np.float32(0.009))
+    U.upside_main(["--duration", repr(30 * rt), "--frame-interval", repr(10 * rt), "--temperature", "0.85",
+                   "--seed", "4", cfg], verbose=False)
+    f = H5File(cfg)
+    pos, pot = f.read("/output/pos"), f.read("/output/potential")
+    assert pos.shape[0] == 3 and np.all(np.isfinite(pos)) and np.all(np.isfinite(pot))
+    eng = U.Upside(path, pos.shape[2])
+    x0 = f.read("/input/pos")[:, :, 0]
+    assert abs(eng.energy(x0) - pot[0, 0]) < 1e-4 * max(abs(pot[0, 0]), 1.0)
