@@ -684,6 +684,39 @@ template <class T> struct CombineNode : Node<T> {
     }
 };
 
+// Sum: one row of n_dim, the weighted sum of chosen rows of the argument.
+// As in the reference, the adjoint weights entry i by weight[id_pos[i]]
+// rather than weight[i] (src/coord_operator.cpp:353-406); an id_pos outside
+// the weight list is refused instead of read past its end.
+template <class T> struct SumNode : Node<T> {
+    vector<int> ip, dim;
+    vector<T> wt;
+    SumNode(const H5& h) {
+        ip = h.ri("id_pos");
+        dim = h.ri("dim");
+        wt = h.rf<T>("weight");
+        int nd = int(h.attr("n_dim"));
+        if (int(dim.size()) != nd || wt.size() != ip.size()) throw Err("inconsistent sizes");
+        for (int i : ip)
+            if (i < 0 || i >= int(wt.size())) throw Err("id_pos outside the weight list");
+        this->alloc(1, nd);
+    }
+    void forward(Engine<T>& e, bool) override {
+        auto& a = e.arg(*this, 0);
+        for (int d = 0; d < this->width; ++d) {
+            T acc = 0;
+            for (size_t i = 0; i < ip.size(); ++i) acc += wt[i] * a.out[size_t(ip[i]) * a.width + dim[size_t(d)]];
+            this->out[size_t(d)] = acc;
+        }
+    }
+    void backward(Engine<T>& e) override {
+        auto& a = e.arg(*this, 0);
+        for (size_t i = 0; i < ip.size(); ++i)
+            for (int d = 0; d < this->width; ++d)
+                a.sens[size_t(ip[i]) * a.width + dim[size_t(d)]] += this->sens[size_t(d)] * wt[size_t(ip[i])];
+    }
+};
+
 // SigmoidEnergy / SigmoidLEnergy: a + b * compact_sigmoid(x - c, s) on one
 // column, optionally times a switch coordinate lambda; with use_cutoff only
 // x in [min, max] counts, otherwise x beyond c -+ 1/s takes the plateau
@@ -2259,6 +2292,7 @@ template <class T> std::unique_ptr<Node<T>> make_node(const string& name, const 
     if (is_prefix("Add", name)) return P(new CombineNode<T>(h, CombineNode<T>::ADD));
     if (is_prefix("Mean", name)) return P(new CombineNode<T>(h, CombineNode<T>::MEAN));
     if (is_prefix("Multiply", name)) return P(new CombineNode<T>(h, CombineNode<T>::MUL));
+    if (is_prefix("Sum", name)) return P(new SumNode<T>(h));
     if (is_prefix("affine_alignment", name)) return P(new AffineNode<T>(h));
     if (is_prefix("backbone_pairs", name)) return P(new BackbonePairsNode<T>(h));
     if (is_prefix("infer_H_O", name)) return P(new InferHONode<T>(h));

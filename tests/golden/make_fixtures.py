@@ -159,7 +159,8 @@ def synthetic(L, n_res, seed, n_frames=3, tmpdir="/tmp"):
 TRANS_CIS_NODES = ["Dihedral_OmegaTransCis", "SigmoidCoord_trans1", "SigmoidCoord_trans2", "SigmoidCoord_cis1",
                    "SigmoidCoord_cis2", "Add_lambda_trans", "Multiply_lambda_cis", "Mean_lambda_mix", "Multiply_dup",
                    "SigmoidEnergy_trans1", "SigmoidEnergy_cis0", "SigmoidEnergy_cis1", "SigmoidEnergy_trans0",
-                   "RamaMap2_trans", "RamaMap2_cis", "SigmoidLEnergy_mix", "SigmoidLEnergy_dup", "rama_coord",
+                   "RamaMap2_trans", "RamaMap2_cis", "SigmoidLEnergy_mix", "SigmoidLEnergy_dup", "Sum_lambda",
+                   "SigmoidLEnergy_sum", "rama_coord",
                    "rama_map_pot", "Spring_omega"]
 
 

@@ -2,7 +2,8 @@
 chain written by config_gen with two trans-cis prolines (listed out of
 residue order), a cis proline (CPR), two fixed rotamers, and extra switch
 nodes that no config script writes (Mean, a Multiply with a repeated and an
-empty output row, SigmoidLEnergy with and without cutoffs).  Shared by
+empty output row, a Sum whose entries are out of order, SigmoidLEnergy with
+and without cutoffs).  Shared by
 make_fixtures.py and the tests, which regenerate the configuration from it.
 """
 import numpy as np
@@ -41,6 +42,11 @@ def write(path, pos=None, n_res=N_RES, seed=SEED):
          {"integrator_level": 0, "use_cutoff": 0, "dim1": 0},
          {"id1": ar, "id2": ar, "a": [0.7, -0.4], "b": [1.5, 2.0], "c": [0.3, -2.0], "s": [1.0, 0.8],
           "min": [0., 0.], "max": [0., 0.]}),
+        ("Sum_lambda", ["SigmoidCoord_trans1"], {"n_dim": 1},
+         {"id_pos": [1, 0], "dim": [0], "weight": [0.7, 1.3]}),
+        ("SigmoidLEnergy_sum", ["Dihedral_OmegaTransCis", "Sum_lambda"],
+         {"integrator_level": 0, "use_cutoff": 0, "dim1": 0},
+         {"id1": [1], "id2": [0], "a": [0.3], "b": [1.2], "c": [-2.2], "s": [0.9], "min": [0.], "max": [0.]}),
         ("SigmoidLEnergy_dup", ["Dihedral_OmegaTransCis", "Multiply_dup"],
          {"integrator_level": 0, "use_cutoff": 1, "dim1": 0},
          {"id1": [0, 1, 0], "id2": [0, 1, 2], "a": [0.5, 1.0, 2.0], "b": [-1.0, 0.6, 1.0],

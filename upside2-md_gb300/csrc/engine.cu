@@ -742,6 +742,73 @@ struct CombineNode : GNode {
     }
 };
 
+// Sum: per system one row of n_dim, the weighted sum of chosen rows of the
+// argument; the adjoint weights entry i by weight[id_pos[i]], as the
+// reference does (src/coord_operator.cpp:353-406), and an id_pos outside the
+// weight list is refused.  A thread per (entry, component), FP32 atomics.
+__global__ void sum_fwd(int n, int nd, const int* __restrict__ src, const int* __restrict__ row,
+                        const float* __restrict__ wt, const int* __restrict__ dims, const float* __restrict__ x, int w,
+                        float* out) {
+    for (int t = grid_stride_start(); t < n * nd; t += grid_stride()) {
+        int i = t / nd, d = t - i * nd;
+        atomicAdd(out + size_t(row[i]) * nd + d, wt[i] * x[size_t(src[i]) * w + dims[d]]);
+    }
+}
+__global__ void sum_bwd(int n, int nd, const int* __restrict__ src, const int* __restrict__ row,
+                        const float* __restrict__ wt_adj, const int* __restrict__ dims, const float* __restrict__ sens,
+                        float* xs, int w) {
+    for (int t = grid_stride_start(); t < n * nd; t += grid_stride()) {
+        int i = t / nd, d = t - i * nd;
+        atomicAdd(xs + size_t(src[i]) * w + dims[d], sens[size_t(row[i]) * nd + d] * wt_adj[i]);
+    }
+}
+struct SumNode : GNode {
+    int n = 0;
+    int *src = nullptr, *row = nullptr, *dims = nullptr;
+    float *wt = nullptr, *wt_adj = nullptr;
+    SumNode(Engine& e, const Groups& g, const GNode& a) {
+        width = int(shared_attr(g, "n_dim"));
+        auto dm = read_i(g.f(0), g.p("dim"));
+        for (size_t s = 1; s < g.size(); ++s)
+            if (read_i(g.f(s), g.p("dim")) != dm) throw Error("dim differs between systems of one batch");
+        if (int(dm.size()) != width || width < 1) throw Error("dim needs n_dim entries");
+        for (int d : dm)
+            if (d < 0 || d >= a.width) throw Error("The dim you gave is out of range!");
+        std::vector<int> rw;
+        std::vector<float> w, wa;
+        off.push_back(0);
+        for (size_t s = 0; s < g.size(); ++s) {
+            auto ip = read_i(g.f(s), g.p("id_pos"));
+            auto ws = read_f(g.f(s), g.p("weight"));
+            if (ws.size() != ip.size()) throw Error("weight needs one entry per id_pos");
+            for (size_t i = 0; i < ip.size(); ++i) {
+                if (ip[i] < 0 || ip[i] >= int(ws.size())) throw Error("id_pos outside the weight list");
+                rw.push_back(int(s));
+                w.push_back(ws[i]);
+                wa.push_back(ws[size_t(ip[i])]);
+            }
+            off.push_back(int(s) + 1);
+        }
+        total = int(g.size());
+        n = int(rw.size());
+        src = e.upload(cat_rows(g, "id_pos", a.off));
+        row = e.upload(rw);
+        dims = e.upload(dm);
+        wt = e.upload(w);
+        wt_adj = e.upload(wa);
+    }
+    void forward(Engine& e, bool) override {
+        auto& a = e.arg(*this, 0);
+        UG_CK(cudaMemsetAsync(out, 0, sizeof(float) * size_t(total) * size_t(width), e.st));
+        ug::launch(sum_fwd, nblk(size_t(n) * width), 256, 0, e.st, n, width, src, row, wt, dims, a.out, a.width, out);
+    }
+    void backward(Engine& e) override {
+        auto& a = e.arg(*this, 0);
+        ug::launch(sum_bwd, nblk(size_t(n) * width), 256, 0, e.st, n, width, src, row, wt_adj, dims, sens, a.sens,
+                   a.width);
+    }
+};
+
 // SigmoidEnergy / SigmoidLEnergy: a + b * compact_sigmoid(x - c, s) on one
 // column, times a switch coordinate row for the L form; with use_cutoff only
 // x within [min, max] counts, otherwise x beyond c -+ 1/s takes the plateau
@@ -2894,6 +2961,7 @@ Engine::Engine(const std::vector<std::string>& paths, const std::vector<int>& n_
             else if (is_prefix("Add", nm)) n.reset(new CombineNode(*this, g, COMB_ADD, N(0), N(1)));
             else if (is_prefix("Mean", nm)) n.reset(new CombineNode(*this, g, COMB_MEAN, N(0), N(1)));
             else if (is_prefix("Multiply", nm)) n.reset(new CombineNode(*this, g, COMB_MUL, N(0), N(1)));
+            else if (is_prefix("Sum", nm)) n.reset(new SumNode(*this, g, N(0)));
             else if (is_prefix("Const3D", nm)) n.reset(new Const3DNode(*this, g, N(0)));
             else if (is_prefix("cb_membrane_potential", nm)) n.reset(new MembraneNode(*this, g, true, N(0), &N(1), N(2)));
             else if (is_prefix("hb_membrane_potential", nm)) n.reset(new MembraneNode(*this, g, false, N(0), nullptr, N(1)));
