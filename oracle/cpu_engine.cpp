@@ -763,32 +763,32 @@ template <class T> struct SigmoidEnergyNode : Node<T> {
     }
 };
 
-// Const3D: fixed 3-vectors, or positions of chosen rows of the argument
-// taken at the first evaluation and kept (ConstantCoord3D,
-// src/coord_const.cpp:107-179)
-template <class T> struct Const3DNode : Node<T> {
+// Const1D/2D/3D: fixed rows of k values, or chosen components of chosen rows
+// of the argument taken at the first evaluation and kept
+// (ConstantCoord1D/2D/3D, src/coord_const.cpp:9-179); one row per entry of id
+template <class T> struct ConstNode : Node<T> {
     bool by_coord, done = false;
     vector<int> id;
-    int dim[3];
-    Const3DNode(const H5& h) {
+    int dim[3] = {0, 0, 0};
+    ConstNode(const H5& h, int k) {
         by_coord = h.attr("initialized_by_coord") != 0;
-        for (int k = 0; k < 3; ++k) dim[k] = int(h.attr(k == 0 ? "dim1" : (k == 1 ? "dim2" : "dim3")));
-        if (by_coord) {
-            id = h.ri("id");
-            this->alloc(int(id.size()), 3);
-        } else {
+        if (k == 1) dim[0] = int(h.attr("dim"));
+        else
+            for (int c = 0; c < k; ++c) dim[c] = int(h.attr(c == 0 ? "dim1" : (c == 1 ? "dim2" : "dim3")));
+        id = h.ri("id");
+        this->alloc(int(id.size()), k);
+        if (!by_coord) {
             auto v = h.rd("value");
-            auto d = h.dims("value");
-            if (d.size() != 2 || d[1] != 3) throw Err("value must be (n, 3)");
-            this->alloc(int(d[0]), 3);
+            if (v.size() != id.size() * size_t(k)) throw Err("value must hold k numbers per entry of id");
             for (size_t i = 0; i < v.size(); ++i) this->out[i] = T(float(v[i]));
         }
     }
     void forward(Engine<T>& e, bool) override {
         if (!by_coord || done) return;
         auto& p = e.arg(*this, 0);
+        int k = this->width;
         for (size_t i = 0; i < id.size(); ++i)
-            for (int k = 0; k < 3; ++k) this->out[3 * i + size_t(k)] = p.out[size_t(id[i]) * p.width + dim[k]];
+            for (int c = 0; c < k; ++c) this->out[size_t(k) * i + size_t(c)] = p.out[size_t(id[i]) * p.width + dim[c]];
         done = true;
     }
 };
@@ -2283,7 +2283,9 @@ template <class T> std::unique_ptr<Node<T>> make_node(const string& name, const 
     if (is_prefix("rama_coord", name)) return P(new PasteRamaNode<T>(h));
     if (is_prefix("rama_map_pot", name)) return P(new RamaMapNode<T>(h));
     if (is_prefix("RamaMap2", name)) return P(new RamaMap2Node<T>(h));
-    if (is_prefix("Const3D", name)) return P(new Const3DNode<T>(h));
+    if (is_prefix("Const1D", name)) return P(new ConstNode<T>(h, 1));
+    if (is_prefix("Const2D", name)) return P(new ConstNode<T>(h, 2));
+    if (is_prefix("Const3D", name)) return P(new ConstNode<T>(h, 3));
     if (is_prefix("cb_membrane_potential", name)) return P(new MembraneCBNode<T>(h));
     if (is_prefix("hb_membrane_potential", name)) return P(new MembraneHBNode<T>(h));
     if (is_prefix("SigmoidCoord", name)) return P(new SigmoidCoordNode<T>(h));

@@ -189,7 +189,7 @@ def trans_cis(L, tmpdir="/tmp"):
 
 
 MEMBRANE_NODES = ["cb_membrane_potential", "hb_membrane_potential", "Const3D_curvature_center", "Const3D_probe",
-                  "placement_fixed_point_only_CB"]
+                  "Const1D_probe", "Const2D_fixed", "placement_fixed_point_only_CB"]
 
 
 def membrane(L, tmpdir="/tmp"):

@@ -54,7 +54,7 @@ def test_membrane_frames(membrane_configs, variant):
             eo, do = o.evaluate(x)
             assert abs(e - eo) < E_ORC * sc, k
             assert rel_f(d, do) < F_ORC, k
-        for nm in MEMB + ("Const3D_probe", "Const3D_curvature_center"):
+        for nm in MEMB + ("Const3D_probe", "Const3D_curvature_center", "Const1D_probe", "Const2D_fixed"):
             ref = z["%s/out/%s" % (variant, nm)][k]
             assert np.abs(eng.get_output(nm) - ref).max() <= 1e-5 * max(np.abs(ref).max(), 1.0), (k, nm)
         for nm in ("placement_fixed_point_only_CB",):

@@ -880,58 +880,61 @@ struct SigmoidEnergyNode : GNode {
     }
 };
 
-// ========================================================== Const3D ===
-// fixed 3-vectors, or chosen rows of the argument taken at the first
-// evaluation and kept (ConstantCoord3D, src/coord_const.cpp:107-179); a
-// per-row flag makes the capture happen once, also inside a replayed graph
-__global__ void const3d_kernel(int n, const float* __restrict__ val, const int* __restrict__ src, int w, int3 dim,
-                               const float* __restrict__ x, int* taken, float* __restrict__ out) {
-    grid_dep_entry();
+// ===================================================== Const1D/2D/3D ===
+// fixed rows of 1, 2 or 3 values, or chosen components of chosen rows of the
+// argument taken at the first evaluation and kept (ConstantCoord1D/2D/3D,
+// src/coord_const.cpp:9-179); a per-row flag makes the capture happen once,
+// also inside a replayed graph.  The node has one row per entry of "id".
+__global__ void const_kernel(int n, int k, const float* __restrict__ val, const int* __restrict__ src, int w,
+                             int3 dim, const float* __restrict__ x, int* taken, float* __restrict__ out) {
     for (int i = grid_stride_start(); i < n; i += grid_stride()) {
         if (!src) {
-            for (int k = 0; k < 3; ++k) out[3 * size_t(i) + k] = val[3 * size_t(i) + k];
+            for (int c = 0; c < k; ++c) out[size_t(i) * k + c] = val[size_t(i) * k + c];
         } else if (!taken[i]) {
             const float* r = x + size_t(src[i]) * w;
-            out[3 * size_t(i)] = r[dim.x];
-            out[3 * size_t(i) + 1] = r[dim.y];
-            out[3 * size_t(i) + 2] = r[dim.z];
+            out[size_t(i) * k] = r[dim.x];
+            if (k > 1) out[size_t(i) * k + 1] = r[dim.y];
+            if (k > 2) out[size_t(i) * k + 2] = r[dim.z];
             taken[i] = 1;
         }
     }
 }
-struct Const3DNode : GNode {
+struct ConstNode : GNode {
     float* val = nullptr;
     int *src = nullptr, *taken = nullptr;
     int3 dim{0, 1, 2};
-    Const3DNode(Engine& e, const Groups& g, const GNode& a) {
-        width = 3;
+    ConstNode(Engine& e, const Groups& g, const GNode& a, int k) {
+        width = k;
         bool by_coord = shared_attr(g, "initialized_by_coord") != 0.0;
-        dim = make_int3(int(shared_attr(g, "dim1")), int(shared_attr(g, "dim2")), int(shared_attr(g, "dim3")));
+        int dd[3] = {0, 0, 0};
+        if (k == 1) {
+            dd[0] = int(shared_attr(g, "dim"));
+        } else {
+            for (int c = 0; c < k; ++c) dd[c] = int(shared_attr(g, "dim" + std::to_string(c + 1)));
+        }
+        dim = make_int3(dd[0], dd[1], dd[2]);
+        off = offsets(counts(g, "id"));
+        total = off.back();
         if (by_coord) {
-            for (int d : {dim.x, dim.y, dim.z})
-                if (d < 0 || d >= a.width) throw Error("dim out of range");
-            off = offsets(counts(g, "id"));
-            total = off.back();
+            for (int c = 0; c < k; ++c)
+                if (dd[c] < 0 || dd[c] >= a.width) throw Error("dim out of range");
             src = e.upload(cat_rows(g, "id", a.off));
             taken = e.alloc<int>(size_t(std::max(1, total)));
             UG_CK(cudaMemsetAsync(taken, 0, 4 * size_t(std::max(1, total)), e.st));
         } else {
             std::vector<float> v;
-            off.push_back(0);
             for (size_t s = 0; s < g.size(); ++s) {
-                auto d = g.f(s).dims(g.p("value"));
-                if (d.size() != 2 || d[1] != 3) throw Error("value must be (n, 3)");
                 auto x = read_f(g.f(s), g.p("value"));
+                if (x.size() != size_t(off[s + 1] - off[s]) * size_t(k))
+                    throw Error("value must hold " + std::to_string(k) + " numbers per entry of id");
                 v.insert(v.end(), x.begin(), x.end());
-                off.push_back(off.back() + int(d[0]));
             }
-            total = off.back();
             val = e.upload(v);
         }
     }
     void forward(Engine& e, bool) override {
         auto& a = e.arg(*this, 0);
-        ug::launch(const3d_kernel, nblk(total), 256, 0, e.st, total, val, src, a.width, dim, a.out, taken, out);
+        ug::launch(const_kernel, nblk(total), 256, 0, e.st, total, width, val, src, a.width, dim, a.out, taken, out);
     }
 };
 
@@ -2962,7 +2965,9 @@ Engine::Engine(const std::vector<std::string>& paths, const std::vector<int>& n_
             else if (is_prefix("Mean", nm)) n.reset(new CombineNode(*this, g, COMB_MEAN, N(0), N(1)));
             else if (is_prefix("Multiply", nm)) n.reset(new CombineNode(*this, g, COMB_MUL, N(0), N(1)));
             else if (is_prefix("Sum", nm)) n.reset(new SumNode(*this, g, N(0)));
-            else if (is_prefix("Const3D", nm)) n.reset(new Const3DNode(*this, g, N(0)));
+            else if (is_prefix("Const1D", nm)) n.reset(new ConstNode(*this, g, N(0), 1));
+            else if (is_prefix("Const2D", nm)) n.reset(new ConstNode(*this, g, N(0), 2));
+            else if (is_prefix("Const3D", nm)) n.reset(new ConstNode(*this, g, N(0), 3));
             else if (is_prefix("cb_membrane_potential", nm)) n.reset(new MembraneNode(*this, g, true, N(0), &N(1), N(2)));
             else if (is_prefix("hb_membrane_potential", nm)) n.reset(new MembraneNode(*this, g, false, N(0), nullptr, N(1)));
             else if (is_prefix("affine_alignment", nm)) n.reset(new AffineNode(*this, g, O(0)));
