@@ -140,11 +140,13 @@ int ug_profile(UgBatch* b, int n_eval, char* names, int names_cap, float* ms, in
  * |x_i - x_j| < cutoff, the interaction-graph pair search of the engine
  * (replaces PairlistComputation's cache pass, src/interaction_graph.h:122-157,
  * for callers without an engine).  pos: n x 3 floats on the device; pairs:
- * device int32 (i, j) x cap; *n_pairs (device int32) receives the total number
- * of pairs, which may exceed cap (pairs past cap are not written).  Pair order:
- * i / 4, then j, then i % 4.  stream: a cudaStream_t or NULL.  Allocates its
- * scratch (2 ceil(n/4) + 1 ints) with cudaMalloc and synchronises the stream
- * before returning. */
+ * device int32 (i, j) x cap, 8-byte aligned (each pair is stored as one 8-byte
+ * word; an unaligned pointer is rejected); *n_pairs (device int32) receives the
+ * total number of pairs, which may exceed cap (pairs past cap are not written)
+ * and saturates at INT32_MAX when the true total does not fit.  cutoff must be
+ * finite and > 0.  Pair order: i / 4, then j, then i % 4.  stream: a
+ * cudaStream_t or NULL.  Allocates its scratch (2 ceil(n/4) + 1 ints) with
+ * cudaMalloc and synchronises the stream before returning. */
 int ug_pair_list(const float* pos, int n, float cutoff, int32_t* pairs, int cap, int32_t* n_pairs, void* stream);
 
 /* ug_pair_list without any device allocation (no counterpart in the
@@ -158,7 +160,10 @@ int ug_pair_list(const float* pos, int n, float cutoff, int32_t* pairs, int cap,
  * on `stream` and return without synchronising.  Nothing has to be zeroed
  * beforehand.  Calls that can run at the same time on one device (two streams,
  * two host threads) share the array and race: order them on one stream.
- * Output, order and arguments as ug_pair_list. */
+ * The looked-up address is kept for the life of the process, so the device's
+ * primary context must stay alive as long as the library is used (no
+ * cudaDeviceReset between calls).
+ * Output, order, alignment and arguments as ug_pair_list. */
 int ug_pair_list_noalloc(const float* pos, int n, float cutoff, int32_t* pairs, int cap, int32_t* n_pairs,
                          void* stream);
 

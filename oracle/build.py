@@ -11,7 +11,8 @@ import subprocess
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 PKG_CSRC = os.path.join(HERE, "..", "upside2-md_gb300", "csrc")
-REF = os.environ.get("UPSIDE_REFERENCE", "/root/reference")
+# the reference checkout: $UPSIDE_REFERENCE, else a "reference" directory beside the repository
+REF = os.environ.get("UPSIDE_REFERENCE", os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference"))
 
 
 def build_oracle():

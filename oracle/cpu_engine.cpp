@@ -214,46 +214,128 @@ template <class T> V3<T> rot_inv(const T* U, const V3<T>& r) {
             U[2] * r.x + U[5] * r.y + U[8] * r.z};
 }
 
-// Symmetric 4x4 eigen-decomposition by cyclic Jacobi rotations (own method;
-// the reference uses Householder + implicit QR, src/eig.cpp:233-275).
-// evec[k*4+i] = component i of eigenvector k; sorted so evals[0] is largest.
-template <class T> void jacobi4(const T F[4][4], T evals[4], T evec[16]) {
-    T A[4][4], V[4][4];
-    for (int i = 0; i < 4; ++i)
-        for (int j = 0; j < 4; ++j) { A[i][j] = F[i][j]; V[i][j] = (i == j); }
-    for (int sweep = 0; sweep < 30; ++sweep) {
-        T off = 0;
-        for (int p = 0; p < 4; ++p)
-            for (int q = p + 1; q < 4; ++q) off += A[p][q] * A[p][q];
-        if (off == T(0)) break;
-        for (int p = 0; p < 4; ++p)
-            for (int q = p + 1; q < 4; ++q) {
-                if (A[p][q] == T(0)) continue;
-                T theta = (A[q][q] - A[p][p]) / (T(2) * A[p][q]);
-                T t = (theta >= 0 ? T(1) : T(-1)) / (std::fabs(theta) + std::sqrt(theta * theta + T(1)));
-                T c = T(1) / std::sqrt(t * t + T(1)), s = t * c;
-                for (int k = 0; k < 4; ++k) {
-                    T akp = A[k][p], akq = A[k][q];
-                    A[k][p] = c * akp - s * akq;
-                    A[k][q] = s * akp + c * akq;
+// Symmetric 4x4 eigen-decomposition as the reference's AffineAlignment does it
+// (src/eig.cpp:57-275): Householder tridiagonalisation (Golub & van Loan 8.3.1),
+// then implicit symmetric QR steps with a Wilkinson shift (G&vL 8.3.2-8.3.3),
+// off-diagonals zeroed once |u_i| <= 1e-5 (|d_i| + |d_i+1|).  The reference
+// runs four consecutive residues through it as one SIMD group, so the
+// choice of the active block (and the end of the iteration) is made jointly:
+// a block is worked while ANY lane of the group still has a nonzero
+// off-diagonal there.  nl lanes (1..4) are given; evals[l*4+k] and
+// evec[l*16+k*4+i] (eigenvector k, component i) come back with the largest
+// eigenvalue swapped into slot 0 (src/eig.cpp:355-372), others unsorted.
+// Packed upper triangle: row i holds A(i,i..3).
+static inline int tri4(int i, int j) {
+    if (i > j) std::swap(i, j);
+    static const int row0[4] = {0, 4, 7, 9};
+    return row0[i] + (j - i);
+}
+template <class T> void qr4_group(int nl, const T (*F)[4][4], T* evals, T* evec) {
+    const T tol = T(1e-5), tiny = T(1e-20);
+    T A[4][10], d[4][4], u[4][3], Q[4][4][4], beta[4][2];
+    for (int l = 0; l < nl; ++l) {
+        for (int i = 0; i < 4; ++i)
+            for (int j = i; j < 4; ++j) A[l][tri4(i, j)] = F[l][i][j];
+        // two Householder reflections reduce A to tridiagonal form; each
+        // reflection vector v (v_0 = 1) is kept in place of the column
+        for (int k = 0; k < 2; ++k) {
+            const int m = 3 - k;
+            T* x = &A[l][tri4(k, k + 1)];  // the m entries A(k, k+1..3) are contiguous
+            T sig = tiny;
+            for (int i = 1; i < m; ++i) sig += x[i] * x[i];
+            T mu = std::sqrt(x[0] * x[0] + sig);
+            T s = x[0] > T(0) ? -sig / (x[0] + mu) : x[0] - mu;
+            T b = T(2) * s * s / (sig + s * s);
+            x[0] = mu;
+            for (int i = 1; i < m; ++i) x[i] /= s;
+            beta[l][k] = b;
+            auto v = [&](int j) { return j == 0 ? T(1) : A[l][tri4(k, k + 1 + j)]; };
+            T p[3], w[3], pv = 0;
+            for (int i = 0; i < m; ++i) {
+                p[i] = 0;
+                for (int j = 0; j < m; ++j) p[i] += A[l][tri4(i + k + 1, j + k + 1)] * v(j);
+                p[i] *= b;
+            }
+            for (int i = 0; i < m; ++i) pv += p[i] * v(i);
+            for (int i = 0; i < m; ++i) w[i] = p[i] - (T(0.5) * b * pv) * v(i);
+            for (int i = 0; i < m; ++i)
+                for (int j = i; j < m; ++j) A[l][tri4(i + k + 1, j + k + 1)] -= v(i) * w[j] + v(j) * w[i];
+        }
+        for (int i = 0; i < 4; ++i) d[l][i] = A[l][tri4(i, i)];
+        for (int i = 0; i < 3; ++i) u[l][i] = A[l][tri4(i, i + 1)];
+        // accumulated orthogonal factor H0 H1 (rows become eigenvectors)
+        auto v0 = [&](int j) { return j == 0 ? T(1) : A[l][tri4(0, 1 + j)]; };
+        auto v1 = [&](int j) { return j == 0 ? T(1) : A[l][tri4(1, 2 + j)]; };
+        T (*R)[4] = Q[l];
+        for (int i = 0; i < 4; ++i)
+            for (int j = i; j < 4; ++j) R[i][j] = (i == j) ? T(1) : T(0);
+        for (int i = 1; i < 4; ++i)
+            for (int j = i; j < 4; ++j) R[i][j] -= beta[l][0] * (v0(i - 1) * v0(j - 1));
+        for (int i = 2; i < 4; ++i)
+            for (int j = i; j < 4; ++j) R[i][j] -= beta[l][1] * (v1(i - 2) * v1(j - 2));
+        for (int i = 0; i < 4; ++i)
+            for (int j = i + 1; j < 4; ++j) R[j][i] = R[i][j];
+        T cpl = beta[l][0] * beta[l][1] * (v0(1) * v1(0) + v0(2) * v1(1));
+        for (int i = 2; i < 4; ++i)
+            for (int j = 1; j < 4; ++j) R[i][j] += cpl * v1(i - 2) * v0(j - 1);
+    }
+    for (int it = 0; it < 100; ++it) {
+        bool nz[3] = {false, false, false};
+        for (int l = 0; l < nl; ++l)
+            for (int i = 0; i < 3; ++i) {
+                if (std::fabs(u[l][i]) <= tol * (std::fabs(d[l][i]) + std::fabs(d[l][i + 1]))) u[l][i] = 0;
+                nz[i] = nz[i] || u[l][i] != T(0);
+            }
+        int q = nz[2] ? 0 : nz[1] ? 1 : nz[0] ? 2 : 3;
+        if (q == 3) break;
+        int p = 3 - q;
+        for (; p > 0; --p)
+            if (!nz[p - 1]) break;
+        const int n = 4 - q - p;
+        for (int l = 0; l < nl; ++l) {
+            T* dd = d[l] + p;
+            T* uu = u[l] + p;
+            T dv = T(0.5) * (dd[n - 2] - dd[n - 1]) + tiny;
+            T un = uu[n - 2];
+            T mu = dd[n - 1] - un * un / (dv + std::copysign(std::sqrt(dv * dv + un * un), dv));
+            T x = dd[0] - mu, z = uu[0];
+            for (int k = 0; k < n - 1; ++k) {
+                T c = 1, s = 0;
+                if (z != T(0)) {
+                    T ir = T(1) / std::sqrt(x * x + z * z);
+                    c = x * ir;
+                    s = -z * ir;
                 }
-                for (int k = 0; k < 4; ++k) {
-                    T apk = A[p][k], aqk = A[q][k];
-                    A[p][k] = c * apk - s * aqk;
-                    A[q][k] = s * apk + c * aqk;
+                for (int j = 0; j < 4; ++j) {
+                    T t1 = Q[l][p + k][j], t2 = Q[l][p + k + 1][j];
+                    Q[l][p + k][j] = c * t1 - s * t2;
+                    Q[l][p + k + 1][j] = s * t1 + c * t2;
                 }
-                for (int k = 0; k < 4; ++k) {
-                    T vkp = V[k][p], vkq = V[k][q];
-                    V[k][p] = c * vkp - s * vkq;
-                    V[k][q] = s * vkp + c * vkq;
+                if (k > 0) uu[k - 1] = c * x - s * z;
+                T a00 = dd[k], a11 = dd[k + 1], a01 = uu[k];
+                dd[k] = a00 * c * c - a01 * T(2) * c * s + a11 * s * s;
+                dd[k + 1] = a00 * s * s + a01 * T(2) * c * s + a11 * c * c;
+                uu[k] = (a00 - a11) * c * s + a01 * (c * c - s * s);
+                x = uu[k];
+                if (k < n - 2) {
+                    z = -uu[k + 1] * s;
+                    uu[k + 1] *= c;
                 }
             }
+        }
     }
-    int order[4] = {0, 1, 2, 3};
-    std::sort(order, order + 4, [&](int a, int b) { return A[a][a] > A[b][b]; });
-    for (int k = 0; k < 4; ++k) {
-        evals[k] = A[order[k]][order[k]];
-        for (int i = 0; i < 4; ++i) evec[k * 4 + i] = V[i][order[k]];
+    for (int l = 0; l < nl; ++l) {
+        T* ev = evals + 4 * l;
+        T* vc = evec + 16 * l;
+        for (int k = 0; k < 4; ++k) {
+            ev[k] = d[l][k];
+            for (int i = 0; i < 4; ++i) vc[4 * k + i] = Q[l][k][i];
+        }
+        for (int k = 1; k < 4; ++k)
+            if (ev[0] < ev[k]) {
+                std::swap(ev[0], ev[k]);
+                for (int i = 0; i < 4; ++i) std::swap(vc[i], vc[4 * k + i]);
+            }
     }
 }
 
@@ -978,6 +1060,7 @@ template <class T> struct AffineNode : Node<T> {
     }
     void forward(Engine<T>& e, bool) override {
         auto& p = e.arg(*this, 0);
+        T Fg[4][4][4];
         for (int r = 0; r < this->n_elem; ++r) {
             V3<T> x[3];
             for (int a = 0; a < 3; ++a) x[a] = ld3(&p.out[3 * size_t(atoms[3 * size_t(r) + a])]);
@@ -1002,10 +1085,16 @@ template <class T> struct AffineNode : Node<T> {
             F[3][3] = -R[0][0] - R[1][1] + R[2][2];
             for (int a = 0; a < 4; ++a)
                 for (int b = 0; b < a; ++b) F[a][b] = F[b][a];
-            jacobi4(F, &evals[4 * size_t(r)], &evecs[16 * size_t(r)]);
+            // residues 4g..4g+3 are solved together, as the reference's SIMD groups are
+            std::memcpy(Fg[r & 3], F, sizeof F);
             T* o = &this->out[7 * size_t(r)];
             o[0] = c.x; o[1] = c.y; o[2] = c.z;
-            for (int k = 0; k < 4; ++k) o[3 + k] = evecs[16 * size_t(r) + k];
+            if ((r & 3) == 3 || r == this->n_elem - 1) {
+                int r0 = r & ~3;
+                qr4_group(r - r0 + 1, Fg, &evals[4 * size_t(r0)], &evecs[16 * size_t(r0)]);
+                for (int l = r0; l <= r; ++l)
+                    for (int k = 0; k < 4; ++k) this->out[7 * size_t(l) + 3 + k] = evecs[16 * size_t(l) + k];
+            }
         }
     }
     void backward(Engine<T>& e) override {

@@ -65,6 +65,22 @@ def membrane_configs(tmp_path_factory, built):
     return paths, np.load(os.path.join(GOLDEN, "syn_membrane_ref.npz"))
 
 
+# Reference-facing bounds (energy: of sum_nodes |E_node|; force: of max |F|).
+# The frames' eigen-solve restates the reference's truncated QR, so what is
+# left is FP32 rounding; where the reference's own distance from the FP64
+# instantiation is larger than half the force bound (steep steric walls at
+# ~50 A coordinates), the bound is twice that distance.
+E_REF_TOL = 1e-5
+F_REF_TOL = 1e-4
+
+
+def ref_force_bound(ref_deriv, d64):
+    """relative max-force bound against the reference's derivative, given the
+    FP64 oracle's derivative at the same coordinates"""
+    dist = np.abs(ref_deriv - d64).max() / np.abs(ref_deriv).max()
+    return max(F_REF_TOL, 2.0 * dist)
+
+
 def quat_align(a, ref):
     """Flip the quaternion columns (3:7) of affine outputs to the sign of ref
     (q and -q are the same rotation)."""

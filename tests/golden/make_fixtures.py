@@ -41,7 +41,8 @@ import config_gen  # noqa: E402
 from h5lite import H5File  # noqa: E402
 import build as oracle_build  # noqa: E402
 
-REF = os.environ.get("UPSIDE_REFERENCE", "/root/reference")
+# the reference checkout: $UPSIDE_REFERENCE, else a "reference" directory beside the repository
+REF = os.environ.get("UPSIDE_REFERENCE", os.path.join(os.path.dirname(ROOT), "reference"))
 EX = os.path.join(REF, "example", "15.SpatialTransformation")
 
 
@@ -128,7 +129,8 @@ def synthetic(L, n_res, seed, n_frames=3, tmpdir="/tmp"):
     # every frame carries coordinate noise: the initial structure of a random
     # chain has residue 0's N, CA, C exactly coplanar with the reference frame
     # geometry, a degenerate case in which the reference eigen-solver returns
-    # a non-maximal eigenvector (parity notes)
+    # a non-maximal eigenvector: its Householder step meets an exactly zero
+    # column and the QR iteration converges to the wrong eigenpair
     frames = []
     prng = np.random.RandomState(seed + 1000)
     for k in range(n_frames):

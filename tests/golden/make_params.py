@@ -16,7 +16,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(HERE, "..", "..", "upside2-md_gb300"))
 from h5lite import H5File  # noqa: E402
 
-REF = os.environ.get("UPSIDE_REFERENCE", "/root/reference")
+# the reference checkout: $UPSIDE_REFERENCE, else a "reference" directory beside the repository
+REF = os.environ.get("UPSIDE_REFERENCE", os.path.join(HERE, "..", "..", "..", "reference"))
 P = os.path.join(REF, "parameters")
 
 

@@ -73,3 +73,41 @@ def test_pair_list_rejects_bad_arguments(built):
         U.pair_list(0, -1, 2.0, 0, 0, 0)
     with pytest.raises(RuntimeError):
         U.pair_list(0, 4, 2.0, 0, 0, 0)
+    with pytest.raises(RuntimeError, match="finite"):
+        U.pair_list(0, 4, float("inf"), 0, 0, 0)
+
+
+def test_pair_list_rejects_unaligned_output(built):
+    import torch
+    import upside_gb300 as U
+    pos = torch.zeros((8, 3), dtype=torch.float32, device="cuda")
+    buf = torch.zeros(64, dtype=torch.int32, device="cuda")
+    n_pairs = torch.zeros(1, dtype=torch.int32, device="cuda")
+    with pytest.raises(RuntimeError, match="aligned"):
+        U.pair_list(pos.data_ptr(), 8, 2.0, buf.data_ptr() + 4, 8, n_pairs.data_ptr())
+
+
+def test_pair_list_total_beyond_int32(built):
+    """70000 points within a small ball and a cutoff that covers them all:
+    n (n - 1) / 2 = 2.45e9 pairs, beyond int32.  The total saturates at
+    INT32_MAX, the first cap pairs come in order, and nothing outside the
+    caller's [0, cap) pairs is written (guard words on both sides)."""
+    import torch
+    import upside_gb300 as U
+    n, cap, guard = 70000, 1000, 64
+    rng = np.random.RandomState(5)
+    pos = torch.from_numpy(rng.rand(n, 3).astype(np.float32)).cuda()
+    buf = torch.full((cap + 2 * guard, 2), -1, dtype=torch.int32, device="cuda")
+    n_pairs = torch.zeros(1, dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
+    U.pair_list(pos.data_ptr(), n, 1e6, buf[guard].data_ptr(), cap, n_pairs.data_ptr())
+    out = buf.cpu().numpy()
+    assert int(n_pairs.item()) == 2 ** 31 - 1
+    assert np.all(out[:guard] == -1) and np.all(out[guard + cap:] == -1)
+    ii, jj = np.triu_indices(64, 1)
+    order = np.lexsort((ii % 4, jj, ii // 4))
+    first = np.stack([ii[order], jj[order]], 1)
+    first = first[first[:, 0] < 4]  # row 0 (points 0-3) comes first, j ascending
+    got = out[guard:guard + cap]
+    assert np.array_equal(got[:len(first)], first)
+    assert np.all(got[:, 0] < 4) and np.all(np.diff(got[:, 1]) >= 0)

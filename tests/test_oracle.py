@@ -8,16 +8,18 @@ Golden data (tests/golden, made by make_fixtures.py from the reference):
     derivative, per-node outputs and pair counts by type;
   * threefry_kat.txt: the reference's vendored Random123 Threefry outputs.
 
-Tolerances.  The reference evaluates with SSE approximate reciprocal square
-roots (one Newton step), approximate reciprocals, and an iterative 4x4 eigen
-solver stopped at a relative off-diagonal tolerance of 1e-5
-(src/Float4.h:201-238, src/eig.cpp:233-275); our restatement is exact IEEE
-FP32.  Measured against the FP64 instantiation, the reference itself deviates
-by up to ~5e-5 relative in energy and ~6e-4 relative in max force, so the
-reference-facing bounds below are 1e-4 in energy and 1e-3 in force.  Energy
-errors are measured relative to the energy scale sum_nodes |E_node| (the total
-is a sum of large, partly cancelling terms, so |E| itself can be near zero);
-force errors relative to max |F|.
+Tolerances.  The oracle restates the reference's affine eigen-solve (its
+Householder + implicit QR with the 1e-5 relative off-diagonal stop and the
+four-residue SIMD grouping, src/eig.cpp:57-275), so the truncation error of
+the frames is the reference's own.  What remains is FP32 rounding: the
+reference evaluates in FP32 with SSE approximate reciprocals (one Newton
+step, src/Float4.h:201-238).  Energy: 1e-5 of the energy scale
+sum_nodes |E_node| (the total is a sum of large, partly cancelling terms, so
+|E| itself can be near zero).  Force: 1e-4 of max |F|, or twice the
+reference's own distance from the FP64 instantiation where that is larger:
+at steep steric walls (src/backbone_steric.cpp:18-30) FP32 positions of ~50 A
+magnitude carry ~1e-4 relative force noise, and the reference shows it too
+(8e-5 from FP64 on the 150-residue fixture's second frame).
 """
 import ctypes
 import os
@@ -27,8 +29,14 @@ import pytest
 
 from conftest import GOLDEN, quat_align
 
-E_REF_TOL = 1e-4
-F_REF_TOL = 1e-3
+E_REF_TOL = 1e-5
+F_REF_TOL = 1e-4
+
+
+def f_ref_bound(ref_vs_fp64):
+    """force bound against the reference given the reference's own relative
+    max-force distance from the FP64 instantiation"""
+    return max(F_REF_TOL, 2.0 * ref_vs_fp64)
 
 
 def rel_e(a, b, scale=None):
@@ -56,24 +64,28 @@ def test_chig_golden_frames(built, fp64):
     z = np.load(os.path.join(GOLDEN, "chig_frames.npz"))
     path = os.path.join(GOLDEN, "chig.up")
     o = oracle_py.Oracle(path, 30, fp64=fp64)
+    o64 = oracle_py.Oracle(path, 30, fp64=True)
     for k in range(len(z["pos"])):
         e, d = o.evaluate(z["pos"][k])
         sc = energy_scale(o, path)
         assert rel_e(e, z["logged_potential"][k], sc) < E_REF_TOL, k
         assert rel_e(e, z["ref_energy"][k], sc) < E_REF_TOL, k
-        assert rel_f(d, z["ref_deriv"][k]) < F_REF_TOL, k
+        bound = f_ref_bound(rel_f(z["ref_deriv"][k], o64.evaluate(z["pos"][k])[1]))
+        assert rel_f(d, z["ref_deriv"][k]) < bound, k
 
 
 @pytest.mark.parametrize("n", [60, 150])
 def test_synthetic_energy_forces(syn_configs, n):
     import oracle_py
     path, z = syn_configs[n]
+    o64 = oracle_py.Oracle(path, z["pos"].shape[1], fp64=True)
+    bounds = [f_ref_bound(rel_f(z["ref_deriv"][k], o64.evaluate(z["pos"][k])[1])) for k in range(len(z["pos"]))]
     for fp64 in (False, True):
         o = oracle_py.Oracle(path, z["pos"].shape[1], fp64=fp64)
         for k in range(len(z["pos"])):
             e, d = o.evaluate(z["pos"][k])
             assert rel_e(e, z["ref_energy"][k], energy_scale(o, path)) < E_REF_TOL
-            assert rel_f(d, z["ref_deriv"][k]) < F_REF_TOL
+            assert rel_f(d, z["ref_deriv"][k]) < bounds[k], k
 
 
 def test_synthetic_nodes(syn_configs):
@@ -89,10 +101,13 @@ def test_synthetic_nodes(syn_configs):
         if nm == "affine_alignment":
             got = quat_align(got, ref)
         scale = max(np.abs(ref).max(), 1e-6)
-        assert np.abs(got - ref).max() <= 2e-3 * scale + 1e-5, nm
+        assert np.abs(got - ref).max() <= 1e-5 * scale + 1e-6, nm
         sref, sgot = z["sens/" + nm], o.node(nm, sens=True)
-        if nm != "protein_hbond":  # hb==0 rows: sensitivity of an exactly-zero score, see the design doc
-            assert np.abs(sgot - sref).max() <= 2e-2 * max(np.abs(sref).max(), 1e-6) + 1e-5, nm
+        # protein_hbond: at a score of exactly zero the reference adds no
+        # sensitivity (src/hbond.cpp:624-626), a discontinuity that rounding
+        # decides; it multiplies d(score)/dx ~ 0, so forces are unaffected
+        if nm != "protein_hbond":
+            assert np.abs(sgot - sref).max() <= 1e-4 * max(np.abs(sref).max(), 1e-6) + 1e-6, nm
 
 
 def test_pair_counts_match_reference(syn_configs):
@@ -154,11 +169,6 @@ def test_reference_engine_if_built(syn_configs):
     assert rel_f(d, z["ref_deriv"][2]) < 1e-5
 
 
-# The trans-cis frames are chains built from random torsions, with close
-# contacts where the reference's approximate reciprocal square roots move the
-# largest force by up to 1.1e-3 of max |F| from the FP64 instantiation (the
-# trans-cis nodes themselves agree to 1e-6; see the node checks below).
-F_REF_TOL_TC = 2e-3
 
 
 @pytest.mark.parametrize("fp64", [False, True])
@@ -172,10 +182,12 @@ def test_trans_cis_golden_frames(transcis_config, fp64):
     import oracle_py
     path, z = transcis_config
     o = oracle_py.Oracle(path, z["pos"].shape[1], fp64=fp64)
+    o64 = oracle_py.Oracle(path, z["pos"].shape[1], fp64=True)
     for k in range(len(z["pos"])):
+        bound = f_ref_bound(rel_f(z["ref_deriv"][k], o64.evaluate(z["pos"][k])[1]))
         e, d = o.evaluate(z["pos"][k])
         assert rel_e(e, z["ref_energy"][k], energy_scale(o, path)) < E_REF_TOL, k
-        assert rel_f(d, z["ref_deriv"][k]) < F_REF_TOL_TC, k
+        assert rel_f(d, z["ref_deriv"][k]) < bound, k
         for key in z.files:
             if not key.startswith("out/"):
                 continue
@@ -183,8 +195,8 @@ def test_trans_cis_golden_frames(transcis_config, fp64):
             for got, ref, tol in ((o.node(nm), z[key][k], 1e-5),
                                   # rama_coord's sensitivity also collects the
                                   # hbond energy's Rama derivative, where the
-                                  # reference's approximations enter (7e-5)
-                                  (o.node(nm, sens=True), z["sens/" + nm][k], 2e-4 if nm == "rama_coord" else 1e-5)):
+                                  # reference's FP32 rounding enters
+                                  (o.node(nm, sens=True), z["sens/" + nm][k], 1e-4 if nm == "rama_coord" else 1e-5)):
                 assert got.shape == ref.shape, nm
                 assert np.abs(got - ref).max() <= tol * max(np.abs(ref).max(), 1.0), (k, nm)
 
@@ -256,10 +268,12 @@ def test_membrane_golden_frames(membrane_configs, variant, fp64):
     paths, z = membrane_configs
     path = paths[variant]
     o = oracle_py.Oracle(path, z["pos"].shape[1], fp64=fp64)
+    o64 = oracle_py.Oracle(path, z["pos"].shape[1], fp64=True)
     for k in range(len(z["pos"])):
+        bound = f_ref_bound(rel_f(z[variant + "/ref_deriv"][k], o64.evaluate(z["pos"][k])[1]))
         e, d = o.evaluate(z["pos"][k])
         assert rel_e(e, z[variant + "/ref_energy"][k], energy_scale(o, path)) < E_REF_TOL, k
-        assert rel_f(d, z[variant + "/ref_deriv"][k]) < F_REF_TOL, k
+        assert rel_f(d, z[variant + "/ref_deriv"][k]) < bound, k
         for key in z.files:
             if not key.startswith(variant + "/out/"):
                 continue

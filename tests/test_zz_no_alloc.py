@@ -20,12 +20,12 @@ def _cloud(n, seed):
     return (rng.rand(n, 3) * side).astype(np.float32)
 
 
-def _call(fn, pos, n, cap):
+def _call(fn, pos, n, cap, cutoff=CUTOFF):
     import torch
     pairs = torch.full((max(cap, 1), 2), -1, dtype=torch.int32, device="cuda")
     n_pairs = torch.full((1,), -7, dtype=torch.int32, device="cuda")
     torch.cuda.synchronize()
-    fn(pos.data_ptr() if n else 0, n, CUTOFF, pairs.data_ptr(), cap, n_pairs.data_ptr(), 0)
+    fn(pos.data_ptr() if n else 0, n, cutoff, pairs.data_ptr(), cap, n_pairs.data_ptr(), 0)
     torch.cuda.synchronize()
     return pairs.cpu().numpy()[:cap], int(n_pairs.item())
 
@@ -39,6 +39,21 @@ def test_noalloc_matches_allocating(built, n):
     assert 0 < total <= 400000 or n == 5
     for _ in range(2):
         got, got_total = _call(U.pair_list_noalloc, pos, n, 400000)
+        assert got_total == total
+        assert np.array_equal(got[:total], ref[:total])
+
+
+@pytest.mark.parametrize("n", [262144, 262141])
+def test_noalloc_at_the_limit(built, n):
+    """The largest accepted sizes: every row of the fixed scratch in use (the
+    total lands in its last word), and a size that is not a multiple of 4."""
+    import torch
+    import upside_gb300 as U
+    pos = torch.from_numpy(_cloud(n, 23)).cuda()
+    ref, total = _call(U.pair_list, pos, n, 400000, cutoff=2.0)
+    assert 0 < total <= 400000
+    for _ in range(2):
+        got, got_total = _call(U.pair_list_noalloc, pos, n, 400000, cutoff=2.0)
         assert got_total == total
         assert np.array_equal(got[:total], ref[:total])
 

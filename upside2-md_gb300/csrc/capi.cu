@@ -668,8 +668,11 @@ int ug_mlp_adam(float* w, const float* g, float* m, float* v, uint16_t* wb, int 
 
 int ug_pair_list(const float* pos, int n, float cutoff, int32_t* pairs, int cap, int32_t* n_pairs, void* stream) {
     GUARD_BEGIN
-    if (n < 0 || cap < 0 || !(cutoff > 0.f)) throw ug::Error("ug_pair_list: need n >= 0, cap >= 0, cutoff > 0");
+    if (n < 0 || cap < 0 || !(cutoff > 0.f) || !std::isfinite(cutoff))
+        throw ug::Error("ug_pair_list: need n >= 0, cap >= 0, a finite cutoff > 0");
     if ((n > 0 && !pos) || (cap > 0 && !pairs) || !n_pairs) throw ug::Error("ug_pair_list: null device pointer");
+    if (reinterpret_cast<uintptr_t>(pairs) % 8)
+        throw ug::Error("ug_pair_list: pairs must be 8-byte aligned (pairs are stored as int32 pairs)");
     auto st = static_cast<cudaStream_t>(stream);
     size_t n_rows = (size_t(n) + 3) / 4;
     int* scratch = nullptr;
@@ -687,8 +690,10 @@ int ug_pair_list(const float* pos, int n, float cutoff, int32_t* pairs, int cap,
 int ug_pair_list_noalloc(const float* pos, int n, float cutoff, int32_t* pairs, int cap, int32_t* n_pairs,
                          void* stream) {
     GUARD_BEGIN
-    if (n < 0 || cap < 0 || !(cutoff > 0.f))
-        throw ug::Error("ug_pair_list_noalloc: need n >= 0, cap >= 0, cutoff > 0");
+    if (n < 0 || cap < 0 || !(cutoff > 0.f) || !std::isfinite(cutoff))
+        throw ug::Error("ug_pair_list_noalloc: need n >= 0, cap >= 0, a finite cutoff > 0");
+    if (reinterpret_cast<uintptr_t>(pairs) % 8)
+        throw ug::Error("ug_pair_list_noalloc: pairs must be 8-byte aligned (pairs are stored as int32 pairs)");
     if (n > ug::point_pairs_noalloc_max())
         throw ug::Error("ug_pair_list_noalloc: n = " + std::to_string(n) + " points exceeds the fixed scratch limit of " +
                         std::to_string(ug::point_pairs_noalloc_max()) + " points (use ug_pair_list)");

@@ -1139,95 +1139,181 @@ struct MembraneNode : GNode {
 
 // ===================================================== affine frames ===
 // Rigid frame (centroid, quaternion) per residue: the quaternion is the top
-// eigenvector of the 4x4 key matrix of the N/CA/C fit, found by cyclic
-// Jacobi rotations; the adjoint is first-order eigenvector perturbation
-// (AffineAlignment, src/eig.cpp:277-470).
-__device__ void jacobi4(float A[4][4], float V[4][4]) {
-    for (int i = 0; i < 4; ++i)
-        for (int j = 0; j < 4; ++j) V[i][j] = (i == j) ? 1.f : 0.f;
-    // Converged once the off-diagonal sum is 1e-8 of the diagonal's: an
-    // exact zero is almost never reached in FP32, and sweeps past this point
-    // rotate by rounding noise only (on residue-like frames it takes 3-4
-    // sweeps instead of 12, with the top eigenvector as close to an FP64
-    // solve, 7e-7 at most)
-    for (int sweep = 0; sweep < 12; ++sweep) {
-        float off = fabsf(A[0][1]) + fabsf(A[0][2]) + fabsf(A[0][3]) + fabsf(A[1][2]) + fabsf(A[1][3]) + fabsf(A[2][3]);
-        float dg = fabsf(A[0][0]) + fabsf(A[1][1]) + fabsf(A[2][2]) + fabsf(A[3][3]);
-        if (off == 0.f || off <= 1e-8f * dg) break;
-#pragma unroll
-        for (int p = 0; p < 3; ++p)
-#pragma unroll
-            for (int q = p + 1; q < 4; ++q) {
-                float apq = A[p][q];
-                if (apq == 0.f) continue;
-                float theta = (A[q][q] - A[p][p]) / (2.f * apq);
-                float t = copysignf(1.f, theta) / (fabsf(theta) + sqrtf(theta * theta + 1.f));
-                float c = rsqrtf(t * t + 1.f), s = t * c;
-#pragma unroll
-                for (int k = 0; k < 4; ++k) {
-                    float akp = A[k][p], akq = A[k][q];
-                    A[k][p] = c * akp - s * akq;
-                    A[k][q] = s * akp + c * akq;
-                }
-#pragma unroll
-                for (int k = 0; k < 4; ++k) {
-                    float apk = A[p][k], aqk = A[q][k];
-                    A[p][k] = c * apk - s * aqk;
-                    A[q][k] = s * apk + c * aqk;
-                }
-#pragma unroll
-                for (int k = 0; k < 4; ++k) {
-                    float vkp = V[k][p], vkq = V[k][q];
-                    V[k][p] = c * vkp - s * vkq;
-                    V[k][q] = s * vkp + c * vkq;
-                }
-            }
-    }
+// eigenvector of the 4x4 key matrix of the N/CA/C fit (AffineAlignment,
+// src/eig.cpp:277-470); the adjoint is first-order eigenvector perturbation.
+//
+// The eigen-solve follows the reference's method step for step, so that its
+// truncation error is the reference's: Householder tridiagonalisation, then
+// implicit symmetric QR steps with a Wilkinson shift (Golub & van Loan
+// 8.3.1-8.3.3), an off-diagonal being zeroed once |u_i| <= 1e-5 (|d_i| +
+// |d_i+1|) (src/eig.cpp:57-275).  The reference solves four consecutive
+// residues of a system as one SIMD group and picks the active block, and
+// stops, jointly for the group; here four consecutive threads form that
+// group and make the same choices with a vote over the group's lanes.
+
+// packed upper triangle of a symmetric 4x4: row i holds A(i, i..3)
+__host__ __device__ constexpr int tri4(int i, int j) {
+    return i > j ? 4 * j - j * (j - 1) / 2 + (i - j) : 4 * i - i * (i - 1) / 2 + (j - i);
 }
-__global__ void affine_fwd(int n, const int* __restrict__ atoms, const float* __restrict__ ref,
+template <int N> __device__ __forceinline__ float pick(const float (&v)[N], int i) {
+    float r = v[0];
+#pragma unroll
+    for (int k = 1; k < N; ++k) r = (i == k) ? v[k] : r;
+    return r;
+}
+// One lane of a group: A (packed key matrix) in, d (eigenvalues) and Q (rows
+// are eigenvectors) out, largest eigenvalue in slot 0 (src/eig.cpp:355-372).
+__device__ void qr4_lane(float (&A)[10], float (&d)[4], float (&Q)[4][4], unsigned gmask) {
+    const float tiny = 1e-20f;
+    float beta[2];
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+        const int m = 3 - k, o = tri4(k, k + 1);
+        float sig = tiny;
+#pragma unroll
+        for (int i = 1; i < m; ++i) sig += A[o + i] * A[o + i];
+        float x0 = A[o];
+        float mu = sqrtf(x0 * x0 + sig);
+        float s = x0 > 0.f ? -sig / (x0 + mu) : x0 - mu;
+        float b = 2.f * s * s / (sig + s * s);
+        A[o] = mu;
+        float is = 1.f / s;
+#pragma unroll
+        for (int i = 1; i < m; ++i) A[o + i] *= is;
+        beta[k] = b;
+        float v[3], p[3], w[3], pv = 0.f;
+#pragma unroll
+        for (int j = 0; j < m; ++j) v[j] = j == 0 ? 1.f : A[o + j];
+#pragma unroll
+        for (int i = 0; i < m; ++i) {
+            float acc = 0.f;
+#pragma unroll
+            for (int j = 0; j < m; ++j) acc += A[tri4(i + k + 1, j + k + 1)] * v[j];
+            p[i] = acc * b;
+        }
+#pragma unroll
+        for (int i = 0; i < m; ++i) pv += p[i] * v[i];
+#pragma unroll
+        for (int i = 0; i < m; ++i) w[i] = p[i] - (0.5f * b * pv) * v[i];
+#pragma unroll
+        for (int i = 0; i < m; ++i)
+#pragma unroll
+            for (int j = i; j < m; ++j) A[tri4(i + k + 1, j + k + 1)] -= v[i] * w[j] + v[j] * w[i];
+    }
+    float u[3];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) d[i] = A[tri4(i, i)];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) u[i] = A[tri4(i, i + 1)];
+    // the accumulated reflections H0 H1
+    const float v0[3] = {1.f, A[tri4(0, 2)], A[tri4(0, 3)]};
+    const float v1[2] = {1.f, A[tri4(1, 3)]};
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = i; j < 4; ++j) {
+            float r = (i == j) ? 1.f : 0.f;
+            if (i >= 1) r -= beta[0] * (v0[i - 1] * v0[j - 1]);
+            if (i >= 2) r -= beta[1] * (v1[i - 2] * v1[j - 2]);
+            Q[i][j] = r;
+            Q[j][i] = r;
+        }
+    const float cpl = beta[0] * beta[1] * (v0[1] * v1[0] + v0[2] * v1[1]);
+#pragma unroll
+    for (int i = 2; i < 4; ++i)
+#pragma unroll
+        for (int j = 1; j < 4; ++j) Q[i][j] += cpl * v1[i - 2] * v0[j - 1];
+    for (int it = 0; it < 100; ++it) {
+        bool nz[3];
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            if (fabsf(u[i]) <= 1e-5f * (fabsf(d[i]) + fabsf(d[i + 1]))) u[i] = 0.f;
+            nz[i] = __any_sync(gmask, u[i] != 0.f);
+        }
+        const int q = nz[2] ? 0 : nz[1] ? 1 : nz[0] ? 2 : 3;
+        if (q == 3) break;
+        int p = 3 - q;
+        while (p > 0 && (p == 1 ? nz[0] : p == 2 ? nz[1] : nz[2])) --p;
+        // block rows p..last of the tridiagonal matrix are worked
+        const int last = 3 - q;
+        const float dv = 0.5f * (pick(d, last - 1) - pick(d, last)) + tiny;
+        const float un = pick(u, last - 1);
+        const float mu = pick(d, last) - un * un / (dv + copysignf(sqrtf(dv * dv + un * un), dv));
+        float x = pick(d, p) - mu, z = pick(u, p);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            if (k < p || k >= last) continue;
+            float c = 1.f, sn = 0.f;
+            if (z != 0.f) {
+                float ir = rsqrtf(x * x + z * z);
+                c = x * ir;
+                sn = -z * ir;
+            }
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                float t1 = Q[k][j], t2 = Q[k + 1][j];
+                Q[k][j] = c * t1 - sn * t2;
+                Q[k + 1][j] = sn * t1 + c * t2;
+            }
+            if (k > p) u[k - 1] = c * x - sn * z;
+            float a00 = d[k], a11 = d[k + 1], a01 = u[k];
+            d[k] = a00 * c * c - a01 * 2.f * c * sn + a11 * sn * sn;
+            d[k + 1] = a00 * sn * sn + a01 * 2.f * c * sn + a11 * c * c;
+            u[k] = (a00 - a11) * c * sn + a01 * (c * c - sn * sn);
+            x = u[k];
+            if (k < last - 1) {
+                z = -u[k + 1] * sn;
+                u[k + 1] *= c;
+            }
+        }
+    }
+#pragma unroll
+    for (int k = 1; k < 4; ++k)
+        if (d[0] < d[k]) {
+            float t = d[0]; d[0] = d[k]; d[k] = t;
+#pragma unroll
+            for (int j = 0; j < 4; ++j) { t = Q[0][j]; Q[0][j] = Q[k][j]; Q[k][j] = t; }
+        }
+}
+// A thread per lane of each four-residue group (grp[g] = first residue of
+// group g, grp_n[g] = its residues, 1..4); lanes past the end repeat lane 0,
+// as the reference's padding does, and store nothing.
+__global__ void affine_fwd(int n_grp, const int* __restrict__ grp, const int* __restrict__ grp_n,
+                           const int* __restrict__ atoms, const float* __restrict__ ref,
                            const float* __restrict__ pos, float* __restrict__ out, float* __restrict__ eig) {
     grid_dep_entry();
-    for (int r = grid_stride_start(); r < n; r += grid_stride()) {
-        f3 x[3];
-        for (int a = 0; a < 3; ++a) x[a] = ld3(pos + 3 * size_t(atoms[3 * r + a]));
-        f3 c = (x[0] + x[1] + x[2]) * (1.f / 3.f);
-        for (int a = 0; a < 3; ++a) x[a] = x[a] - c;
-        const float* g = ref + 9 * size_t(r);
-        float R[3][3];
-        for (int i = 0; i < 3; ++i) {
-            R[i][0] = x[0].x * g[i] + x[1].x * g[3 + i] + x[2].x * g[6 + i];
-            R[i][1] = x[0].y * g[i] + x[1].y * g[3 + i] + x[2].y * g[6 + i];
-            R[i][2] = x[0].z * g[i] + x[1].z * g[3 + i] + x[2].z * g[6 + i];
-        }
-        float F[4][4];
-        F[0][0] = R[0][0] + R[1][1] + R[2][2];
-        F[0][1] = R[1][2] - R[2][1];
-        F[0][2] = R[2][0] - R[0][2];
-        F[0][3] = R[0][1] - R[1][0];
-        F[1][1] = R[0][0] - R[1][1] - R[2][2];
-        F[1][2] = R[0][1] + R[1][0];
-        F[1][3] = R[0][2] + R[2][0];
-        F[2][2] = -R[0][0] + R[1][1] - R[2][2];
-        F[2][3] = R[1][2] + R[2][1];
-        F[3][3] = -R[0][0] - R[1][1] + R[2][2];
-        F[1][0] = F[0][1]; F[2][0] = F[0][2]; F[3][0] = F[0][3];
-        F[2][1] = F[1][2]; F[3][1] = F[1][3]; F[3][2] = F[2][3];
-        float V[4][4];
-        jacobi4(F, V);
-        // sort eigenpairs by decreasing eigenvalue
-        int ord[4] = {0, 1, 2, 3};
-        for (int i = 0; i < 4; ++i)
-            for (int j = i + 1; j < 4; ++j)
-                if (F[ord[j]][ord[j]] > F[ord[i]][ord[i]]) { int t = ord[i]; ord[i] = ord[j]; ord[j] = t; }
-        float* E = eig + 20 * size_t(r);
-        for (int k = 0; k < 4; ++k) {
-            E[k] = F[ord[k]][ord[k]];
-            for (int i = 0; i < 4; ++i) E[4 + 4 * k + i] = V[i][ord[k]];
-        }
-        float* o = out + 7 * size_t(r);
-        o[0] = c.x; o[1] = c.y; o[2] = c.z;
-        for (int i = 0; i < 4; ++i) o[3 + i] = E[4 + i];
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int g = t >> 2, lane = t & 3;
+    if (g >= n_grp) return;  // whole groups leave together (blockDim is a multiple of 4)
+    const unsigned gmask = 0xfu << (threadIdx.x & 28);
+    const bool real = lane < grp_n[g];
+    const int r = grp[g] + (real ? lane : 0);
+    f3 x[3];
+    for (int a = 0; a < 3; ++a) x[a] = ld3(pos + 3 * size_t(atoms[3 * r + a]));
+    f3 c = (x[0] + x[1] + x[2]) * (1.f / 3.f);
+    for (int a = 0; a < 3; ++a) x[a] = x[a] - c;
+    const float* gm = ref + 9 * size_t(r);
+    float R[3][3];
+    for (int i = 0; i < 3; ++i) {
+        R[i][0] = x[0].x * gm[i] + x[1].x * gm[3 + i] + x[2].x * gm[6 + i];
+        R[i][1] = x[0].y * gm[i] + x[1].y * gm[3 + i] + x[2].y * gm[6 + i];
+        R[i][2] = x[0].z * gm[i] + x[1].z * gm[3 + i] + x[2].z * gm[6 + i];
     }
+    float A[10] = {R[0][0] + R[1][1] + R[2][2], R[1][2] - R[2][1], R[2][0] - R[0][2], R[0][1] - R[1][0],
+                   R[0][0] - R[1][1] - R[2][2], R[0][1] + R[1][0], R[0][2] + R[2][0],
+                   -R[0][0] + R[1][1] - R[2][2], R[1][2] + R[2][1],
+                   -R[0][0] - R[1][1] + R[2][2]};
+    float d[4], Q[4][4];
+    qr4_lane(A, d, Q, gmask);
+    if (!real) return;
+    float* E = eig + 20 * size_t(r);
+    for (int k = 0; k < 4; ++k) {
+        E[k] = d[k];
+        for (int i = 0; i < 4; ++i) E[4 + 4 * k + i] = Q[k][i];
+    }
+    float* o = out + 7 * size_t(r);
+    o[0] = c.x; o[1] = c.y; o[2] = c.z;
+    for (int i = 0; i < 4; ++i) o[3 + i] = Q[0][i];
 }
 __global__ void affine_bwd(int n, const int* __restrict__ atoms, const float* __restrict__ ref,
                            const float* __restrict__ eig, const float* __restrict__ sens, float* ps) {
@@ -1288,9 +1374,25 @@ struct AffineNode : GNode {
         atoms = e.upload(cat_idx(g, "atoms", &o));
         ref = e.upload(cat_f(g, "ref_geom"));
         eig = e.alloc<float>(size_t(total) * 20);
+        // four-residue groups of each system, as the reference forms them
+        std::vector<int> gs, gn;
+        for (size_t s = 0; s + 1 < off.size(); ++s)
+            for (int r = off[s]; r < off[s + 1]; r += 4) {
+                gs.push_back(r);
+                gn.push_back(std::min(4, off[s + 1] - r));
+            }
+        n_grp = int(gs.size());
+        if (n_grp) {
+            grp = e.upload(gs);
+            grp_n = e.upload(gn);
+        }
     }
+    int n_grp = 0;
+    int *grp = nullptr, *grp_n = nullptr;
     void forward(Engine& e, bool) override {
-        ug::launch(affine_fwd, nblk(total, 128), 128, 0, e.st, total, atoms, ref, e.arg(*this, 0).out, out, eig);
+        if (!n_grp) return;
+        ug::launch(affine_fwd, nblk(4 * n_grp, 128), 128, 0, e.st, n_grp, grp, grp_n, atoms, ref,
+                   e.arg(*this, 0).out, out, eig);
     }
     void backward(Engine& e) override {
         ug::launch(affine_bwd, nblk(total, 128), 128, 0, e.st, total, atoms, ref, eig, sens, e.arg(*this, 0).sens);

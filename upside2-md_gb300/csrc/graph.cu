@@ -33,40 +33,44 @@ __global__ void __launch_bounds__(1024) scan_kernel(const int* __restrict__ in, 
                                                     int* total_out, const int* __restrict__ skip_unless) {
     grid_dep_entry();
     if (skip_unless && !*skip_unless) return;
-    __shared__ int warp_sums[32];
+    // sums are carried in 64 bits and stored saturated at INT_MAX, so a total
+    // beyond the int range reads as "larger than any capacity" rather than
+    // wrapping to a negative offset
+    __shared__ long long warp_sums[32];
+    auto sat = [](long long x) { return int(x < 2147483647LL ? x : 2147483647LL); };
     int t = threadIdx.x;
     int per = (n + blockDim.x - 1) / blockDim.x;
     int lo = min(n, t * per), hi = min(n, lo + per);
-    int s = 0;
+    long long s = 0;
     for (int i = lo; i < hi; ++i) s += in[i];
     // block exclusive scan of s
     int lane = t & 31, w = t >> 5;
-    int v = s;
+    long long v = s;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-        int y = __shfl_up_sync(0xffffffffu, v, o);
+        long long y = __shfl_up_sync(0xffffffffu, v, o);
         if (lane >= o) v += y;
     }
     if (lane == 31) warp_sums[w] = v;
     __syncthreads();
     if (w == 0) {
-        int ws = warp_sums[lane];
+        long long ws = warp_sums[lane];
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
-            int y = __shfl_up_sync(0xffffffffu, ws, o);
+            long long y = __shfl_up_sync(0xffffffffu, ws, o);
             if (lane >= o) ws += y;
         }
         warp_sums[lane] = ws;
     }
     __syncthreads();
-    int excl = v - s + (w ? warp_sums[w - 1] : 0);
+    long long excl = v - s + (w ? warp_sums[w - 1] : 0);
     for (int i = lo; i < hi; ++i) {
-        out[i] = excl;
+        out[i] = sat(excl);
         excl += in[i];
     }
     if (t == blockDim.x - 1) {
-        out[n] = excl;
-        if (total_out) *total_out = excl;
+        out[n] = sat(excl);
+        if (total_out) *total_out = sat(excl);
     }
     if (n == 0 && t == 0) {
         out[0] = 0;

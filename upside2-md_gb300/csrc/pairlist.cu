@@ -12,7 +12,10 @@
 // Two passes with a scan between them: one warp per row of four points counts
 // its hits, a single-block scan turns counts into row offsets and the total,
 // and the second pass writes each row's pairs at its offset.  The scratch is
-// the row counts and row offsets (2 * ceil(n/4) + 1 ints).
+// the row counts and row offsets (2 * ceil(n/4) + 1 ints).  A row count is at
+// most n; the offsets and the total are summed in 64 bits and saturate at
+// INT32_MAX, so a total beyond the int32 range comes back as INT32_MAX (more
+// than any capacity) and no write leaves [0, cap).
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -41,7 +44,9 @@ __global__ void point_pair_kernel(const float* __restrict__ pos, int n, float c2
             ay[l] = ok ? pos[3 * (i1s + l) + 1] : 1e20f;
             az[l] = ok ? pos[3 * (i1s + l) + 2] : 1e20f;
         }
-        int base = PASS ? row_off[r] : 0;
+        // 64-bit running offset: row offsets saturate at INT_MAX (the scan),
+        // so a list too long for int32 writes nothing past the capacity
+        long long base = PASS ? row_off[r] : 0;
         int count = 0;
         for (int j0 = i1s + 1; j0 < n; j0 += 32) {
             int j = j0 + lane;
@@ -66,10 +71,10 @@ __global__ void point_pair_kernel(const float* __restrict__ pos, int n, float c2
                     int y = __shfl_up_sync(0xffffffffu, incl, o);
                     if (lane >= o) incl += y;
                 }
-                int p = base + incl - c;
+                long long p = base + incl - c;
                 for (int l = 0; l < 4; ++l)
                     if (mask & (1u << l)) {
-                        if (p < cap) pairs[p] = make_int2(i1s + l, j);
+                        if (p >= 0 && p < cap) pairs[p] = make_int2(i1s + l, j);
                         ++p;
                     }
                 base += __shfl_sync(0xffffffffu, incl, 31);

@@ -9,7 +9,8 @@
 
 Sequences are drawn uniformly over the 20 amino acids from the seed; initial
 structures are random (phi, psi) chains (py/upside_config.py:186-201).  Files
-are cached under a work directory keyed by the configuration and seed.
+are cached under a work directory keyed by the configuration, the seed and a
+hash of the generator.
 """
 import os
 
@@ -20,9 +21,22 @@ import config_gen
 WORK = os.environ.get("UPSIDE_GB300_WORK", "/tmp/upside_gb300_work")
 
 
+def _generator_key():
+    """Short hash of the config generator and its parameter bundle, so that
+    cached files are regenerated whenever either changes."""
+    import hashlib
+    h = hashlib.sha1()
+    for f in (config_gen.__file__, config_gen.DEFAULT_PARAMS):
+        if f and os.path.exists(f):
+            with open(f, "rb") as fh:
+                h.update(fh.read())
+    return h.hexdigest()[:10]
+
+
 def _cfg(name, seed, n_res, **kw):
     os.makedirs(WORK, exist_ok=True)
-    path = os.path.join(WORK, "%s_s%d_n%d.up" % (name, seed, n_res if isinstance(n_res, int) else sum(n_res)))
+    path = os.path.join(WORK, "%s_s%d_n%d_%s.up" % (name, seed, n_res if isinstance(n_res, int) else sum(n_res),
+                                                     _generator_key()))
     if not os.path.exists(path):
         rng = np.random.RandomState(seed)
         seq = config_gen.random_sequence(int(n_res) if isinstance(n_res, int) else int(sum(n_res)), rng)
