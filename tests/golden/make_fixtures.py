@@ -23,6 +23,11 @@ this script, which are committed (the GPU host has no reference checkout):
                      curved: frames, reference energy and derivative, and the
                      membrane nodes' outputs and sensitivities per frame
                      (python make_fixtures.py membrane writes only this file)
+  syn_graph_ref.npz  the reference's own edge lists of every interaction
+                     graph of syn60/syn150 per frame, and its parameter
+                     derivatives (get_param_deriv) of the rotamer, coverage
+                     and nonlinear-coupling nodes (python make_fixtures.py
+                     graph writes only this file)
 
 The reference engine is oracle/_ref/libupside_ref.so (oracle/build.py).
 """
@@ -249,7 +254,80 @@ def threefry_kat():
         f.write("# seed stream counter_lo_hi(step) atom out0 out1 out2 out3\n" + out)
 
 
+# interaction-graph nodes whose edge lists the reference build exposes
+# (oracle/ref_build/dump), by accessor
+EDGE_ACCESSORS = (("hb_environment_coverage", "hb_environment_coverage"),
+                  ("environment_coverage", "environment_coverage"),
+                  ("hbond_coverage", "hbond_coverage"), ("protein_hbond", "protein_hbond"),
+                  ("rotamer", "rotamer"))
+PARAM_DERIV_NODES = ("rotamer", "hbond_coverage", "hbond_coverage_hydrophobe", "nonlinear_coupling_environment")
+
+
+def ref_edges(L, eng, node):
+    """The reference's own edge list of an interaction-graph node, (index1,
+    index2) in its order, or None for other nodes."""
+    for prefix, acc in EDGE_ACCESSORS:
+        if node.startswith(prefix):
+            f = getattr(L, "ref_edges_" + acc)
+            f.restype = ctypes.c_int
+            f.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_void_p, ctypes.c_int]
+            n = f(eng.e, node.encode(), None, 0)
+            assert n >= 0, node
+            a = np.zeros((max(n, 1), 2), np.int32)
+            f(eng.e, node.encode(), a.ctypes.data, n)
+            return a[:n]
+    return None
+
+
+def edges_and_param_derivs(L, tmpdir="/tmp"):
+    """syn_graph_ref.npz: the reference's own pair lists and parameter
+    derivatives.
+
+      edges<N>/<k>/<node>  int16 (n_edge, 2): the edge list of every
+                           interaction-graph node of the syn<N> fixture after
+                           evaluating its frames 0..k in order on one engine
+                           (the pair caches carry over between frames, as in
+                           the reference)
+      pd/<k>/<node>        get_param_deriv of the syn60 fixture written with
+                           the nonlinear environment coupling (environment
+                           potential type 0) after evaluate_deriv at frame k
+    """
+    L.get_param_deriv.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_char_p]
+    out = {}
+    for n in (60, 150):
+        z = np.load(os.path.join(HERE, "syn%d_ref.npz" % n))
+        path = os.path.join(tmpdir, "syn%d_graph.up" % n)
+        config_gen.write_config(path, [s.decode() for s in z["seq"]], int(z["seed"]), pos=z["pos"][0])
+        eng = RefEngine(L, path, z["pos"].shape[1])
+        for k, x in enumerate(z["pos"]):
+            eng.eval(x)
+            for nm in H5File(path).list("/input/potential"):
+                e = ref_edges(L, eng, nm)
+                if e is not None:
+                    assert e.size == 0 or e.max() < 32767
+                    out["edges%d/%d/%s" % (n, k, nm)] = e.astype(np.int16)
+    z = np.load(os.path.join(HERE, "syn60_ref.npz"))
+    path = os.path.join(tmpdir, "syn60_env0.up")
+    config_gen.write_config(path, [s.decode() for s in z["seq"]], int(z["seed"]), pos=z["pos"][0],
+                            environment_potential_type=0)
+    eng = RefEngine(L, path, z["pos"].shape[1])
+    for k in (0, 1):
+        eng.eval(z["pos"][k])
+        for nm in PARAM_DERIV_NODES:
+            size = {"rotamer": 20 * 20 * 54, "hbond_coverage": 8 * 20 * 50,
+                    "hbond_coverage_hydrophobe": 12 * 20 * 50}.get(nm)
+            if size is None:
+                size = H5File(path).read("/input/potential/%s/coeff" % nm).size + 20 * 20
+            d = np.zeros(size, np.float32)
+            assert L.get_param_deriv(size, d.ctypes.data, eng.e, nm.encode()) == 0, nm
+            out["pd/%d/%s" % (k, nm)] = d
+    np.savez_compressed(os.path.join(HERE, "syn_graph_ref.npz"), **out)
+
+
 def main():
+    if sys.argv[1:] == ["graph"]:
+        edges_and_param_derivs(load_ref())
+        return
     if sys.argv[1:] == ["chig_run"]:
         chig_run_output()
         return
@@ -267,6 +345,7 @@ def main():
     synthetic(L, 150, 2, n_frames=2)
     trans_cis(L)
     membrane(L)
+    edges_and_param_derivs(L)
 
 
 if __name__ == "__main__":

@@ -163,6 +163,55 @@ def test_pair_lists_bit_exact(syn_configs):
         assert np.array_equal(ge[len(e0):] - np.array([n1, n2]), e1), node
 
 
+GRAPH_NODES = ["rotamer", "hbond_coverage", "hbond_coverage_hydrophobe", "protein_hbond",
+               "environment_coverage_sc", "environment_coverage_hb", "hb_environment_coverage_hn",
+               "hb_environment_coverage_oc"]
+
+
+def test_pair_lists_bit_exact_vs_reference(syn_configs):
+    """Every interaction graph's edge list on the GPU equals the reference
+    engine's own, pair for pair and in order (syn_graph_ref.npz: read out of
+    the reference's InteractionGraph, src/interaction_graph.h:51-258), with
+    the fixture's frames evaluated in order on one engine so that the pair
+    caches carry over as they do in the reference."""
+    import upside_gb300 as U
+    g = np.load(os.path.join(GOLDEN, "syn_graph_ref.npz"))
+    for n in (60, 150):
+        path, z = syn_configs[n]
+        b = U.Batch([path])
+        for k in range(len(z["pos"])):
+            b.set_pos(z["pos"][k])
+            b.evaluate()
+            for nm in GRAPH_NODES:
+                ref = g["edges%d/%d/%s" % (n, k, nm)].astype(np.int32)
+                got = b.node_edges(nm)
+                assert got.shape == ref.shape and np.array_equal(got, ref), (n, k, nm)
+
+
+def test_param_derivs_vs_reference(syn_configs, tmp_path):
+    """dE/d(parameters) of the GPU adjoint against the reference's own
+    get_param_deriv (src/engine_c_library.cpp:94-110): rotamer pair splines,
+    both hbond coverage graphs and the nonlinear environment coupling, at two
+    frames: 1e-3 of the largest component."""
+    import config_gen
+    import upside_gb300 as U
+    g = np.load(os.path.join(GOLDEN, "syn_graph_ref.npz"))
+    _, z = syn_configs[60]
+    path = str(tmp_path / "syn60_env0.up")
+    config_gen.write_config(path, [s.decode() for s in z["seq"]], int(z["seed"]), pos=z["pos"][0],
+                            environment_potential_type=0)
+    b = U.Batch([path])
+    for k in (0, 1):
+        b.set_pos(z["pos"][k])
+        b.evaluate()
+        for nm in ("rotamer", "hbond_coverage", "hbond_coverage_hydrophobe", "nonlinear_coupling_environment"):
+            ref = g["pd/%d/%s" % (k, nm)]
+            got = b.param_deriv(nm, ref.shape)
+            err = np.abs(got - ref).max() / np.abs(ref).max()
+            print("param deriv %s frame %d: %.2e of max" % (nm, k, err))
+            assert err <= 1e-3, (k, nm, err)
+
+
 def test_pair_counts_vs_reference(syn_configs):
     import upside_gb300 as U
     for n in (60, 150):

@@ -123,6 +123,61 @@ def test_pair_counts_match_reference(syn_configs):
                 assert np.array_equal(got, z[key]), nm
 
 
+GRAPH_NODES = ["rotamer", "hbond_coverage", "hbond_coverage_hydrophobe", "protein_hbond",
+               "environment_coverage_sc", "environment_coverage_hb", "hb_environment_coverage_hn",
+               "hb_environment_coverage_oc"]
+
+
+def test_pair_lists_match_reference_lists(syn_configs):
+    """The oracle's edge lists of every interaction graph equal the
+    reference's own, pair for pair and in order (syn_graph_ref.npz: read out
+    of the reference engine's InteractionGraph after each frame, frames
+    evaluated in order on one engine so that pair caches carry over)."""
+    import oracle_py
+    g = np.load(os.path.join(GOLDEN, "syn_graph_ref.npz"))
+    for n in (60, 150):
+        path, z = syn_configs[n]
+        o = oracle_py.Oracle(path, z["pos"].shape[1])
+        for k in range(len(z["pos"])):
+            o.evaluate(z["pos"][k])
+            for nm in GRAPH_NODES:
+                ref = g["edges%d/%d/%s" % (n, k, nm)].astype(np.int32)
+                got = o.edges(nm)
+                assert got.shape == ref.shape and np.array_equal(got, ref), (n, k, nm)
+
+
+PARAM_DERIV_NODES = ("rotamer", "hbond_coverage", "hbond_coverage_hydrophobe", "nonlinear_coupling_environment")
+
+
+@pytest.fixture(scope="module")
+def env0_config(syn_configs, tmp_path_factory):
+    """syn60 written with the nonlinear environment coupling (type 0)."""
+    import config_gen
+    _, z = syn_configs[60]
+    path = str(tmp_path_factory.mktemp("env0") / "syn60_env0.up")
+    config_gen.write_config(path, [s.decode() for s in z["seq"]], int(z["seed"]), pos=z["pos"][0],
+                            environment_potential_type=0)
+    return path, z
+
+
+def test_param_derivs_match_reference(env0_config):
+    """The oracle's dE/d(parameters) against the reference's get_param_deriv
+    (src/engine_c_library.cpp:94-110; src/interaction_graph.h:406-416 for
+    the rotamer and coverage graphs, src/environment.cpp:788-833 for the
+    nonlinear coupling): 1e-4 of the largest component (observed ~1e-5)."""
+    import oracle_py
+    g = np.load(os.path.join(GOLDEN, "syn_graph_ref.npz"))
+    path, z = env0_config
+    o = oracle_py.Oracle(path, z["pos"].shape[1])
+    for k in (0, 1):
+        o.evaluate(z["pos"][k])
+        for nm in PARAM_DERIV_NODES:
+            ref = g["pd/%d/%s" % (k, nm)]
+            got = o.param_deriv(nm)
+            assert got.shape == ref.shape, nm
+            assert np.abs(got - ref).max() <= 1e-4 * np.abs(ref).max(), (k, nm)
+
+
 def test_threefry_known_answers(built):
     import oracle_py
     L = oracle_py._lib()
