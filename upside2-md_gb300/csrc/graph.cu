@@ -913,15 +913,32 @@ struct MsgLoc {
     }
 };
 
+// Per-sweep constants of a block's own share in shared memory (compact layout
+// whose cluster fits): per own entry its row and column nodes (system-local),
+// per own node its prob row and first entry (clipped to the system's end).
+// When ok is false the sweeps read them from global memory.
+struct BpOwn {
+    int *row = nullptr, *col = nullptr, *rp = nullptr;
+    float* prob = nullptr;
+    bool ok = false;
+};
+
 // new message along every entry of [e0, e1): einfo[f] = (local index of the
 // row node v, reverse entry, local index of the column node u, 0); the old
 // message is read from buffer kold, the new one written to buffer kcur.
 // Beliefs are indexed from node nb_lo.
 __device__ __forceinline__ void bp_messages(const DBP& b, int e0, int e1, const float* __restrict__ Nold, int nb_lo,
-                                            const int* __restrict__ s_nrot, const MsgLoc& M, int kold, int kcur,
-                                            cg::cluster_group& cluster, int tid, int nt) {
+                                            const int* __restrict__ s_nrot, const MsgLoc& M, const BpOwn& OW,
+                                            int kold, int kcur, cg::cluster_group& cluster, int tid, int nt) {
     for (int f = e0 + tid; f < e1; f += nt) {
-        int4 inf = b.einfo[f];
+        int4 inf;
+        if (OW.ok) {
+            inf.x = OW.row[f - e0];
+            inf.z = OW.col[f - e0];
+            inf.y = 0;  // the destination table gives the reverse entry's slot
+        } else {
+            inf = b.einfo[f];
+        }
         int nv = s_nrot[inf.x], nu = s_nrot[inf.z];
         const float* ob = Nold + (inf.x - nb_lo) * 8;
         const float4* om = reinterpret_cast<const float4*>(M.own(b, kold, f));
@@ -934,7 +951,7 @@ __device__ __forceinline__ void bp_messages(const DBP& b, int e0, int e1, const 
         float P[36];
 #pragma unroll
         for (int q = 0; q < 9; ++q) {
-            float4 t = P4[q];
+            float4 t = __ldg(P4 + q);
             P[4 * q] = t.x; P[4 * q + 1] = t.y; P[4 * q + 2] = t.z; P[4 * q + 3] = t.w;
         }
         float mm[6], sum = 0.f;
@@ -967,7 +984,8 @@ __device__ __forceinline__ void bp_messages(const DBP& b, int e0, int e1, const 
 template <int BP_LANES>
 __device__ __forceinline__ float bp_beliefs(const DBP& b, int r0, int lo, int hi, int e1, const float* __restrict__ Nold,
                                             float* __restrict__ Ncur, int nb_lo, const int* __restrict__ s_nrot,
-                                            const MsgLoc& M, int kcur, int mode, float damp, int tid, int nt) {
+                                            const MsgLoc& M, const BpOwn& OW, int kcur, int mode, float damp, int tid,
+                                            int nt) {
     float dev = 0.f;
     const int q = tid % BP_LANES, lane = tid & 31;
     const unsigned gmask = ((1u << BP_LANES) - 1u) << (lane & ~(BP_LANES - 1));
@@ -976,7 +994,7 @@ __device__ __forceinline__ float bp_beliefs(const DBP& b, int r0, int lo, int hi
         int n = s_nrot[ul];
         if (n == 1) continue;
         int u = r0 + ul;
-        int eb = b.row_ptr[u], ee = min(b.row_ptr[u + 1], e1);
+        int eb = OW.ok ? OW.rp[ul - lo] : b.row_ptr[u], ee = OW.ok ? OW.rp[ul - lo + 1] : min(b.row_ptr[u + 1], e1);
         float prod[6] = {1.f, 1.f, 1.f, 1.f, 1.f, 1.f};
         // renormalised after every factor, so the product never underflows
         // (each message sums to 1)
@@ -1010,7 +1028,7 @@ __device__ __forceinline__ float bp_beliefs(const DBP& b, int r0, int lo, int hi
         if (q != 0) continue;
         float bl[6];
 #pragma unroll
-        for (int k = 0; k < 6; ++k) bl[k] = k < n ? b.prob[u * 8 + k] * prod[k] : 0.f;
+        for (int k = 0; k < 6; ++k) bl[k] = k < n ? (OW.ok ? OW.prob[(ul - lo) * 8 + k] : b.prob[u * 8 + k]) * prod[k] : 0.f;
         renorm6(bl, n);
         const float* o = Nold + (ul - nb_lo) * 8;
         if (mode == 1) {
@@ -1042,14 +1060,13 @@ __device__ __forceinline__ float bp_beliefs(const DBP& b, int r0, int lo, int hi
 // the belief phase, THREADS threads per block; the variants are listed in
 // bp_variants (the engine's autotuner picks one).
 template <int BP_CLUSTER, int BP_LANES, int THREADS>
-__global__ void __launch_bounds__(THREADS) bp_solve_kernel(DBP b, int want_energy, double* energy_out) {
+__global__ void __launch_bounds__(THREADS, 65536 / (THREADS * 64)) bp_solve_kernel(DBP b, int want_energy, double* energy_out) {
     grid_dep_entry();
     extern __shared__ float smem[];
     __shared__ double dred[32];
     __shared__ float s_dev[2][BP_CLUSTER];  // per chunk parity: every block's deviation maximum
     __shared__ int s_bmax[2];               // this block's maximum (non-negative float bits)
     __shared__ double s_en[BP_CLUSTER];
-    __shared__ int s_multi;
     cg::cluster_group cluster = cg::this_cluster();
     const int crank = int(cluster.block_rank());
     const int s = blockIdx.x / BP_CLUSTER;
@@ -1095,6 +1112,7 @@ __global__ void __launch_bounds__(THREADS) bp_solve_kernel(DBP b, int want_energ
     float* NB[2];
     int* s_nrot;
     int nb_lo = 0;
+    BpOwn OW;
     MsgLoc M;
     M.base = eo0;
     M.dsm = fits;
@@ -1115,6 +1133,14 @@ __global__ void __launch_bounds__(THREADS) bp_solve_kernel(DBP b, int want_energ
             NB[1] = b.nb_scratch + (size_t(b.n_res) + r0 + lo) * 8;
         }
         M.s0 = nbb + size_t(b.nb_cap) * 16;
+        // after the destination table, the per-sweep constants of the
+        // block's share: own nodes' prob rows and first entries, own entries'
+        // row and column nodes, so that a sweep reads only shared memory and P
+        OW.prob = M.s0 + size_t(b.dsm_cap) * 17;
+        OW.rp = reinterpret_cast<int*>(OW.prob + size_t(b.nb_cap) * 8);
+        OW.row = OW.rp + b.nb_cap + 1;
+        OW.col = OW.row + b.dsm_cap;
+        OW.ok = fits;
         if (fits) {
             int* dst = M.dst_table(b);
             for (int f = eo0 + tid; f < eo1; f += nt) {
@@ -1122,14 +1148,23 @@ __global__ void __launch_bounds__(THREADS) bp_solve_kernel(DBP b, int want_energ
                 int c = 0;
                 while (c + 1 < BP_CLUSTER && rv >= s_eb[c + 1]) ++c;
                 dst[f - eo0] = (c << 20) | (rv - s_eb[c]);
+                const int4 inf = b.einfo[f];
+                OW.row[f - eo0] = inf.x;
+                OW.col[f - eo0] = inf.z;
             }
+            for (int li = tid; li < hi - lo; li += nt) {
+                const float4* pr = reinterpret_cast<const float4*>(b.prob + size_t(r0 + lo + li) * 8);
+                reinterpret_cast<float4*>(OW.prob)[2 * li] = pr[0];
+                reinterpret_cast<float4*>(OW.prob)[2 * li + 1] = pr[1];
+            }
+            for (int li = tid; li <= hi - lo; li += nt) OW.rp[li] = min(b.row_ptr[r0 + lo + li], e1);
         }
     }
 
     auto sweep = [&](const float* Nold, float* Ncur, int kold, int kcur, int mode, float damp) {
-        bp_messages(b, eo0, eo1, Nold, nb_lo, s_nrot, M, kold, kcur, cluster, tid, nt);
+        bp_messages(b, eo0, eo1, Nold, nb_lo, s_nrot, M, OW, kold, kcur, cluster, tid, nt);
         cluster.sync();
-        return bp_beliefs<BP_LANES>(b, r0, lo, hi, e1, Nold, Ncur, nb_lo, s_nrot, M, kcur, mode, damp, tid, nt);
+        return bp_beliefs<BP_LANES>(b, r0, lo, hi, e1, Nold, Ncur, nb_lo, s_nrot, M, OW, kcur, mode, damp, tid, nt);
     };
     if (tid < 2) s_bmax[tid] = 0;
 
@@ -1144,7 +1179,6 @@ __global__ void __launch_bounds__(THREADS) bp_solve_kernel(DBP b, int want_energ
     const bool use_warm = use_prev || (b.warm && warm_start_used(b.warm_stat + 4 * s, b.warm_gain));
     const float* init = use_prev ? b.marg : use_warm ? b.warm : b.prob;
     // N.old = N.cur = prob (N.old = prediction when warm); E.old = 1 (own entries)
-    if (tid == 0) s_multi = 0;
     for (int ul = tid; ul < N; ul += nt) s_nrot[ul] = b.nrot[r0 + ul];
     for (int ul = lo + tid; ul < hi; ul += nt) {  // own nodes
         // a start row that is not a distribution (no previous solve yet) falls
@@ -1204,20 +1238,16 @@ __global__ void __launch_bounds__(THREADS) bp_solve_kernel(DBP b, int want_energ
                 sum += m[k];
             }
             float inv = 1.f / sum;
-#pragma unroll
             float* mf = M.own(b, 1, f);
 #pragma unroll
             for (int k = 0; k < 8; ++k) mf[k] = k < n ? m[k] * inv : 1.f;
         }
     }
     __syncthreads();
-    {  // multi-rotamer node count of the system, for the algorithmic-byte tally
-        int m = 0;
-        for (int u = tid; u < N; u += nt) m += s_nrot[u] > 1;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) m += __shfl_xor_sync(0xffffffffu, m, o);
-        if (lane == 0 && m) atomicAdd(&s_multi, m);
-    }
+    const int chunk = max(1, b.chunk);
+    int nc = 1, ec = 0;
+    float dev = 1e10f;
+    int iter = 0;
     // first sweep, undamped: new beliefs go to the buffer that then becomes
     // "old"; the other (prob) is max-normalised (src/rotamer.cpp:1135)
     if (M.dsm) cluster.sync();  // every block of the cluster runs before shared stores reach it
@@ -1242,18 +1272,15 @@ __global__ void __launch_bounds__(THREADS) bp_solve_kernel(DBP b, int want_energ
     // which nothing reads afterwards) is discarded and the state is the one
     // after the converged chunk: the same sweeps and results as a separate
     // barrier before every test.
-    const int chunk = max(1, b.chunk);
-    int nc = 1, ec = 0, cpar = 0;
+    int cpar = 0;
     bool pending = false;
-    float dev = 1e10f;
-    int iter = 0;
     while (iter < b.max_iter) {
         float d = 0.f;
         bool converged = false;
         for (int j = 0; j < chunk; ++j) {
             nc ^= 1;
             ec ^= 1;
-            bp_messages(b, eo0, eo1, NB[nc ^ 1], nb_lo, s_nrot, M, ec ^ 1, ec, cluster, tid, nt);
+            bp_messages(b, eo0, eo1, NB[nc ^ 1], nb_lo, s_nrot, M, OW, ec ^ 1, ec, cluster, tid, nt);
             cluster.sync();
             if (pending) {  // the previous chunk's maximum, posted before this barrier
                 pending = false;
@@ -1268,7 +1295,7 @@ __global__ void __launch_bounds__(THREADS) bp_solve_kernel(DBP b, int want_energ
                     break;
                 }
             }
-            d = bp_beliefs<BP_LANES>(b, r0, lo, hi, e1, NB[nc ^ 1], NB[nc], nb_lo, s_nrot, M, ec, 1, b.damping, tid,
+            d = bp_beliefs<BP_LANES>(b, r0, lo, hi, e1, NB[nc ^ 1], NB[nc], nb_lo, s_nrot, M, OW, ec, 1, b.damping, tid,
                                      nt);
             if (j == chunk - 1) {
 #pragma unroll
@@ -1304,17 +1331,6 @@ __global__ void __launch_bounds__(THREADS) bp_solve_kernel(DBP b, int want_energ
             ws[2] += 1.f;
             ws[3] = float(known | (1 << k));
         }
-        // algorithmic bytes of this launch for system s.  Per sweep, each
-        // directed entry is read by the message phase (einfo 16 B, P 144 B,
-        // old message 32 B), written once (new message 32 B) and read by the
-        // belief phase (32 B); each multi-rotamer node reads row_ptr[u..u+1]
-        // and prob (40 B).  Set-up reads prob and n_rot and writes the
-        // initial messages (36 B per node, 32 B per entry); the marginals
-        // write 36 B per node and touch 420 B per entry.
-        unsigned long long E = (unsigned long long)(e1 - e0), Nm = s_multi;
-        unsigned long long sweep = E * 256ull + Nm * 40ull;
-        b.alg_bytes[s] += (unsigned long long)(1 + iter) * sweep + (unsigned long long)N * 36ull + E * 32ull +
-                          (unsigned long long)N * 36ull + E * 420ull;
     }
     // node marginals of own nodes
     const float* Nf = NB[nc];
@@ -1345,31 +1361,80 @@ __global__ void __launch_bounds__(THREADS) bp_solve_kernel(DBP b, int want_energ
         if (tid == 0 && crank == 0) b.prev_valid[par * b.n_sys + s] = 1;
     }
     cluster.sync();  // every node marginal of the system is written
-    // edge marginals of own entries
+    // Edge marginals of own entries and, when asked, the Bethe free energy
+    // (src/rotamer.cpp:292-302, 451-471).  Each entry's 6x6 block is formed in
+    // registers from one load of P and the two nodes' cavity beliefs, stored
+    // once, and its energy term taken from the same registers: no store is
+    // re-read and no load waits behind a store.
     const float* Ef = EM[ec];
+    double en = 0.0;
+    // Algorithmic bytes of the solve, counted per undirected edge (u < v) of
+    // rotamer counts (nu, nv), with ru(n) = n rounded up to 4 floats: every
+    // sweep reads and writes both messages and both node beliefs,
+    // 4 (2 (ru(nu) + ru(nv)) + 2 ru(nu) + 2 ru(nv)) bytes, and the edge
+    // matrix is read once per solve, 4 nu ru(nv) bytes.
+    unsigned long long ab_sweep = 0, ab_once = 0;
     for (int e = eo0 + tid; e < eo1; e += nt) {
-        int u = b.erow[e], v = b.col[e];
-        int nu = b.nrot[u], nv = b.nrot[v];
-        const float* mu = Ef + size_t(e) * 8;
-        const float* mv = Ef + size_t(b.rev[e]) * 8;
+        const int u = b.erow[e], v = b.col[e];
+        const int nu = b.nrot[u], nv = b.nrot[v];
+        if (u < v) {
+            const unsigned ru = (nu + 3) & ~3, rv = (nv + 3) & ~3;
+            ab_sweep += 4ull * (2 * (ru + rv) + 2 * ru + 2 * rv);
+            ab_once += 4ull * nu * rv;
+        }
+        const float4* mu4 = reinterpret_cast<const float4*>(Ef + size_t(e) * 8);
+        const float4* mv4 = reinterpret_cast<const float4*>(Ef + size_t(b.rev[e]) * 8);
+        const float4* gu4 = reinterpret_cast<const float4*>(b.marg + size_t(u) * 8);
+        const float4* gv4 = reinterpret_cast<const float4*>(b.marg + size_t(v) * 8);
+        const float4 mu0 = mu4[0], mu1 = mu4[1], mv0 = mv4[0], mv1 = mv4[1];
+        const float4 gu0 = gu4[0], gu1 = gu4[1], gv0 = gv4[0], gv1 = gv4[1];
+        const float mu[6] = {mu0.x, mu0.y, mu0.z, mu0.w, mu1.x, mu1.y};
+        const float mv[6] = {mv0.x, mv0.y, mv0.z, mv0.w, mv1.x, mv1.y};
+        const float gu[6] = {gu0.x, gu0.y, gu0.z, gu0.w, gu1.x, gu1.y};
+        const float gv[6] = {gv0.x, gv0.y, gv0.z, gv0.w, gv1.x, gv1.y};
         float bu[6], bv[6];
-        for (int i = 0; i < 6; ++i) bu[i] = i < nu ? b.marg[u * 8 + i] / (1e-10f + mu[i]) : 0.f;
-        for (int j = 0; j < 6; ++j) bv[j] = j < nv ? b.marg[v * 8 + j] / (1e-10f + mv[j]) : 0.f;
-        const float* P = b.P + size_t(e) * 36;
-        float* mg = b.emarg + size_t(e) * 36;
+#pragma unroll
+        for (int i = 0; i < 6; ++i) {
+            bu[i] = i < nu ? gu[i] / (1e-10f + mu[i]) : 0.f;
+            bv[i] = i < nv ? gv[i] / (1e-10f + mv[i]) : 0.f;
+        }
+        // two passes over P's rows (loads only, no store in between): the
+        // normalisation, then the normalised block with its energy term
+        const float2* P2 = reinterpret_cast<const float2*>(b.P + size_t(e) * 36);
         float sum = 0.f;
-        for (int i = 0; i < 6; ++i)
-            for (int j = 0; j < 6; ++j) {
-                float x = P[i * 6 + j] * bu[i] * bv[j];
-                mg[i * 6 + j] = x;
-                sum += x;
+#pragma unroll
+        for (int i = 0; i < 6; ++i) {
+            const float2 a0 = P2[3 * i], a1 = P2[3 * i + 1], a2 = P2[3 * i + 2];
+            sum += bu[i] * (((a0.x * bv[0] + a0.y * bv[1]) + (a1.x * bv[2] + a1.y * bv[3])) + (a2.x * bv[4] + a2.y * bv[5]));
+        }
+        const float inv = 1.f / sum;
+        float2* mg2 = reinterpret_cast<float2*>(b.emarg + size_t(e) * 36);
+        float f = 0.f;
+#pragma unroll
+        for (int i = 0; i < 6; ++i) {
+            const float2 a0 = P2[3 * i], a1 = P2[3 * i + 1], a2 = P2[3 * i + 2];
+            const float p[6] = {a0.x, a0.y, a1.x, a1.y, a2.x, a2.y};
+            float y[6];
+#pragma unroll
+            for (int j = 0; j < 6; ++j) y[j] = p[j] * bu[i] * bv[j] * inv;
+            mg2[3 * i] = make_float2(y[0], y[1]);
+            mg2[3 * i + 1] = make_float2(y[2], y[3]);
+            mg2[3 * i + 2] = make_float2(y[4], y[5]);
+            if (want_energy && u < v && i < nu) {
+#pragma unroll
+                for (int j = 0; j < 6; ++j)
+                    if (j < nv) f += y[j] * logf((1e-10f + y[j]) / (1e-10f + p[j] * gu[i] * gv[j]));
             }
-        float inv = 1.f / sum;
-        for (int k = 0; k < 36; ++k) mg[k] *= inv;
+        }
+        en += double(f);
+    }
+    {
+        unsigned long long ab = (unsigned long long)(1 + iter) * ab_sweep + ab_once;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) ab += __shfl_xor_sync(0xffffffffu, ab, o);
+        if (lane == 0 && ab) atomicAdd(&b.alg_bytes[s], ab);
     }
     if (!want_energy) return;  // no shared-memory traffic between blocks after the last barrier
-    __syncthreads();
-    double en = 0.0;
     for (int ul = lo + tid; ul < hi; ul += nt) {
         int u = r0 + ul;
         int n = s_nrot[ul];
@@ -1378,20 +1443,6 @@ __global__ void __launch_bounds__(THREADS) bp_solve_kernel(DBP b, int want_energ
             float bk = b.marg[u * 8 + k];
             f += bk * logf((1e-10f + bk) / (1e-10f + b.prob[u * 8 + k]));
         }
-        en += double(f);
-    }
-    for (int e = eo0 + tid; e < eo1; e += nt) {
-        int u = b.erow[e], v = b.col[e];
-        if (!(u < v)) continue;
-        int nu = b.nrot[u], nv = b.nrot[v];
-        const float* p = b.emarg + size_t(e) * 36;
-        const float* P = b.P + size_t(e) * 36;
-        float f = 0.f;
-        for (int i = 0; i < nu; ++i)
-            for (int j = 0; j < nv; ++j) {
-                float x = p[i * 6 + j];
-                f += x * logf((1e-10f + x) / (1e-10f + P[i * 6 + j] * b.marg[u * 8 + i] * b.marg[v * 8 + j]));
-            }
         en += double(f);
     }
 #pragma unroll
@@ -1418,20 +1469,15 @@ struct BpVariant {
     const void* fn;
     int cluster, lanes, threads;
 };
+#define UG_BPV(C, L, T) {reinterpret_cast<const void*>(bp_solve_kernel<C, L, T>), C, L, T}
 static const BpVariant* bp_variants() {
     static const BpVariant v[] = {
-        {reinterpret_cast<const void*>(bp_solve_kernel<2, 8, 1024>), 2, 8, 1024},
-        {reinterpret_cast<const void*>(bp_solve_kernel<2, 4, 1024>), 2, 4, 1024},
-        {reinterpret_cast<const void*>(bp_solve_kernel<2, 16, 1024>), 2, 16, 1024},
-        {reinterpret_cast<const void*>(bp_solve_kernel<1, 8, 1024>), 1, 8, 1024},
-        {reinterpret_cast<const void*>(bp_solve_kernel<4, 8, 512>), 4, 8, 512},
-        {reinterpret_cast<const void*>(bp_solve_kernel<4, 4, 512>), 4, 4, 512},
-        {reinterpret_cast<const void*>(bp_solve_kernel<8, 4, 256>), 8, 4, 256},
-        {reinterpret_cast<const void*>(bp_solve_kernel<8, 8, 256>), 8, 8, 256},
-        {reinterpret_cast<const void*>(bp_solve_kernel<16, 4, 128>), 16, 4, 128},
+        UG_BPV(2, 8, 1024), UG_BPV(2, 4, 1024), UG_BPV(2, 16, 1024), UG_BPV(1, 8, 1024), UG_BPV(4, 8, 512),
+        UG_BPV(4, 4, 512),  UG_BPV(8, 4, 256),  UG_BPV(8, 8, 256),   UG_BPV(16, 4, 128),
     };
     return v;
 }
+#undef UG_BPV
 int bp_variant_count() { return 9; }
 void bp_variant_desc(int i, int* cluster, int* lanes, int* threads) {
     const BpVariant& v = bp_variants()[i];
@@ -1602,7 +1648,12 @@ void launch_bp(DBP& b, const DGraph& g, const float* const* in, float* const* in
             return e ? std::max(16, std::atoi(e)) : 0;
         }();
         if (slots_cap) msg_cap = std::min(msg_cap, slots_cap);
-        size_t compact = 4 * size_t((N + 3) & ~3) + 64 * size_t(nb_cap) + 68 * size_t(msg_cap);
+        msg_cap = (msg_cap + 3) & ~3;  // keeps the arrays after the destination table 16-byte aligned
+        // counts, own beliefs (2 x 8 floats), own messages (2 x 8 floats) and
+        // destination table, then own prob rows and first entries, own
+        // entries' row and column nodes
+        size_t compact = 4 * size_t((N + 3) & ~3) + 64 * size_t(nb_cap) + 68 * size_t(msg_cap) +
+                         36 * size_t(nb_cap) + 4 + 8 * size_t(msg_cap);
         int need = (b.n_sys * C + n_sm - 1) / n_sm;  // blocks per SM for a single wave
         cudaFuncAttributes fa;
         size_t stat = cudaFuncGetAttributes(&fa, v.fn) == cudaSuccess ? fa.sharedSizeBytes : size_t(2048);
