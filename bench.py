@@ -2,11 +2,13 @@
 
 python bench.py [--gpus N] [--steps K] [--warmup W] [--workload C4] [--impl gpu|reference]
 
-A step is the reference's unit: one force evaluation plus one integrator
-stage (src/main.cpp:1009-1012); a timed iteration is one integration round of
-the whole batch (thermostat + 3 x {force, p -= dt F, x += dt p}), i.e. 3 steps
-for every system.  residue-steps/s = sum over systems of residues x 3 x rounds
-/ time.  The default workload is C4 (64 chains, lengths uniform in [40,400]).
+A step is the reference's unit: the time per step it reports divides by the
+number of integration rounds (src/main.cpp:1009-1012), one round being the
+thermostat and one integration_cycle, 3 x {force, p -= dt F, x += dt p}
+(src/deriv_engine.cpp:317-331).  A timed iteration is one round of the whole
+batch (with replica exchange: one exchange interval of rounds and its
+exchange).  residue-steps/s = sum over systems of residues x rounds / time.
+The default workload is C4 (64 chains, lengths uniform in [40,400]).
 
 Multi-GPU: one process per GPU (torchrun); each rank advances its own batch of
 independently seeded systems ("replicas only", weak scaling); ranks only meet
@@ -176,7 +178,7 @@ def cpu_port_rate(configs, seconds, max_procs=None, states=None):
     ctx = mp.get_context("spawn")
     with ctx.Pool(procs) as pool:
         res = pool.map(_cpu_worker, jobs)
-    rate = sum(r * 3 * n / t for r, t, n in res)
+    rate = sum(r * n / t for r, t, n in res)
     sample = "%d systems (%s residues), %.0f s of whole integration rounds each, %d rounds total" % (
         procs, ",".join(str(n) for _, _, n in res[:8]) + ("..." if procs > 8 else ""), seconds,
         sum(r for r, _, _ in res))
@@ -201,7 +203,7 @@ def main():
         rate, cores, sample = cpu_port_rate(W["configs"], a.cpu_seconds)
         line = {"impl": "reference", "metric": METRIC, "value": rate, "unit": "residue-steps/s",
                 "n_gpus": a.gpus, "steps": a.steps, "warmup": a.warmup,
-                "ms_per_step": 1e3 * n_res_total * 3 / rate, "higher_is_better": True, "scaling": "weak",
+                "ms_per_step": 1e3 * n_res_total / rate, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded ff_2.1 proteins)",
                 "config": {"workload": a.workload, "systems": len(W["configs"]), "residues": n_res_total},
                 "cpu_baseline": {"value": rate, "unit": "residue-steps/s", "cores": cores, "kind": "port",
@@ -215,6 +217,8 @@ def main():
     b = U.Batch(W["configs"])
     b.set_pos(workloads.initial_positions(W["configs"]))
     b.set_thermostat(W["temps"], np.array(W["seeds"], np.uint32))
+    if W["swap_sets"]:  # replica exchange every 20 rounds, alternating sets, on the device
+        b.set_replica_exchange(W["swap_sets"], 1 + d.rank, W["exchange_interval"], 0)
     bp_start = set_bp_start(b, a.bp_start)
     # equilibrate: the random initial coils relax for a few hundred rounds
     # before the dynamics reach their steady state (untimed)
@@ -237,6 +241,7 @@ def main():
     if a.profile:
         for nm, ms in sorted(b.profile(5), key=lambda x: -x[1])[:25]:
             print("%-48s %8.3f ms" % (nm, ms), file=sys.stderr)
+    rounds_per_iter = b.timed_rounds()
     d.barrier()
     with Clocks(d.local) as clk:
         ms = b.bench(a.steps, flush_l2=True)
@@ -244,7 +249,7 @@ def main():
     peak, peak_kind = measured_peaks()
     roof = roofline(b, W, a, peak, peak_kind)
     t_dev = d.max(float(ms.sum()) / 1e3)
-    units = d.sum(n_res_total * 3 * a.steps)
+    units = d.sum(n_res_total * rounds_per_iter * a.steps)
     value = units / t_dev
     # end to end: the same rounds with the state round-tripped through pinned host memory
     ms_e2e = b.bench(a.steps, flush_l2=True, e2e=True)
@@ -262,16 +267,24 @@ def main():
     state_bytes = 2 * 12 * b.atom_total
     line = {
         "metric": METRIC, "value": value, "unit": "residue-steps/s", "n_gpus": d.world, "steps": a.steps,
-        "warmup": a.warmup, "ms_per_step": 1e3 * t_dev / a.steps, "higher_is_better": True, "scaling": "weak",
+        "warmup": a.warmup, "ms_per_step": 1e3 * t_dev / (a.steps * rounds_per_iter), "higher_is_better": True,
+        "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded ff_2.1 proteins, random initial chains)",
         "config": {"workload": a.workload, "systems": len(W["configs"]), "residues": n_res_total,
-                   "step": "one integration round = 3 force evaluations + integrator stages per system",
+                   "step": "one integration round per system (thermostat + integration_cycle: 3 force "
+                           "evaluations and integrator stages), the reference's step (src/main.cpp:1009-1012)",
+                   "force_evaluations_per_step": 3,
+                   "rounds_per_timed_iteration": rounds_per_iter,
+                   "replica_exchange": (None if not W["swap_sets"] else
+                                        "every %d rounds on the device, alternating even/odd sets, criterion 0"
+                                        % W["exchange_interval"]),
                    "equilibration_rounds": a.equilibrate, "autotune": tuned,
                    "l2": "256 MiB buffer rewritten before every timed round", "bp_init": bp_start,
                    "bp_sweeps_per_solve": bp_sweeps(b)},
         "e2e": {"value": e2e_value, "unit": "residue-steps/s", "h2d_bytes_per_step": state_bytes,
                 "d2h_bytes_per_step": state_bytes},
-        "gpu_launches": int(a.steps * (3 * launches + 5)),
+        "gpu_launches": int(a.steps * (rounds_per_iter * (3 * launches + 5) +
+                                       (2 * launches + 4 if W["swap_sets"] else 0))),
         "clocks": clk.summary(),
         "roofline": roof,
         "cpu_baseline": cpu,
@@ -328,7 +341,7 @@ def plain_single_rate(W, a, states, n_sample=6, rounds=8):
         s.set_thermostat([W["temps"][i]], np.array([W["seeds"][i]], np.uint32))
         s.run(3, use_graph=True, graph_rounds=1)
         ms = s.bench(rounds, flush_l2=True)
-        units += W["n_res"][i] * 3 * rounds
+        units += W["n_res"][i] * rounds
         t += float(ms.sum()) / 1e3
         del s
     return {"value": units / t, "unit": "residue-steps/s",

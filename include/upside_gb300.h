@@ -78,11 +78,35 @@ int ug_set_param(UgBatch* b, const char* node, const float* param, int n);
 int ug_get_param(UgBatch* b, const char* node, float* param, int n);
 int ug_param_deriv(UgBatch* b, const char* node, float* deriv, int n);
 
-/* Replica exchange over the batch: energies of all systems are evaluated,
- * then Metropolis swaps of coordinates between the neighbour pairs of the
- * given swap set (pairs[2*k], pairs[2*k+1]) with FP64 acceptance
- * (src/main.cpp:243-316).  accepted[k] receives 0/1. */
+/* One replica exchange over the batch, criterion 0 (ReplicaExchange::
+ * attempt_swaps, src/main.cpp:243-316): energies of all systems, coordinates
+ * of the given pairs (pairs[2*k], pairs[2*k+1]) swapped, energies again, and
+ * each swap whose log-Boltzmann change fails the Metropolis test undone.  All
+ * on the device: FP64 acceptance, uniforms from the replica-exchange Threefry
+ * stream (key (seed, 1), counter (round, 0, draw)).  accepted[k] receives
+ * 0/1.  Synchronises. */
 int ug_replica_exchange(UgBatch* b, int n_pairs, const int* pairs, uint32_t seed, uint64_t round, int* accepted);
+/* Periodic replica exchange inside the integration rounds (the reference's
+ * --replica-interval with alternating --swap-set lists, src/main.cpp:996-997):
+ * after every interval-th round (counted from this call) one exchange with the
+ * next swap set in turn (exchange k uses set k % n_sets and round key
+ * (k + 1) * interval), criterion 0 or 1 (src/main.cpp:276-313).  set_sizes[k]
+ * pairs of set k follow one another in pairs.  ug_run and ug_bench then run
+ * the exchanges on the device, in the captured graphs (a graph replay is one
+ * interval and its exchange).  n_sets = 0 removes the plan. */
+int ug_set_replica_exchange(UgBatch* b, int n_sets, const int* set_sizes, const int* pairs, uint32_t seed,
+                            int interval, int criterion);
+/* State of the periodic plan: replica index held by each system (n_sys),
+ * per pair of all sets its attempts and successes (cap_pairs entries at
+ * most), exchanges made, and the last exchange's accept flags (in the order
+ * of its set) and set index. */
+int ug_replica_state(UgBatch* b, int* replica, unsigned* n_attempt, unsigned* n_success, int cap_pairs,
+                     unsigned long long* n_exchanges, int* last_accepted, int* last_set);
+/* One exchange of the periodic plan now (the next set in turn, drawn with the
+ * round key of that exchange), outside the round schedule.  Synchronises. */
+int ug_exchange_now(UgBatch* b);
+/* Rounds per timed replay of ug_bench: 1, or the exchange interval. */
+int ug_timed_rounds(UgBatch* b);
 
 /* Monte Carlo moves over the batch (the reference's MultipleMonteCarloSampler,
  * src/monte_carlo_sampler.cpp:248-308): for every system with

@@ -20,8 +20,8 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC = os.environ.get("NVCC", "nvcc")
 CXX = os.environ.get("CXX", "g++")
 
-CU_SOURCES = ["engine.cu", "graph.cu", "pairlist.cu", "warm.cu", "capi.cu", "driver.cu", "mc.cu"]
-HEADERS = ["engine.h", "graph.h", "warm.h", "mc.h", "dev_math.cuh", "h5lite.h"]
+CU_SOURCES = ["engine.cu", "graph.cu", "pairlist.cu", "warm.cu", "capi.cu", "driver.cu", "mc.cu", "remd.cu"]
+HEADERS = ["engine.h", "graph.h", "warm.h", "mc.h", "remd.h", "dev_math.cuh", "launch.cuh", "h5lite.h"]
 
 
 def _stale(target, deps):

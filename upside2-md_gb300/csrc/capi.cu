@@ -9,6 +9,7 @@
 
 #include "engine.h"
 #include "mc.h"
+#include "remd.h"
 #include "warm.h"
 #include "../../include/engine_c_library.h"
 #include "../../include/upside_gb300.h"
@@ -48,6 +49,9 @@ struct UgBatch {
     std::unique_ptr<Engine> e;
     std::vector<std::string> paths;       // the systems' configurations
     std::unique_ptr<ug::McSampler> mc;    // their Monte Carlo moves, read at first use
+    // the plan of ug_replica_exchange (kept while its pairs and seed repeat)
+    std::unique_ptr<ug::Remd> oneshot;
+    std::vector<int> oneshot_key;
     // measured kernel over the last ug_bench: device ms, launches, algorithmic bytes
     double kt_ms = 0.0, kt_bytes = 0.0;
     long long kt_launches = 0;
@@ -419,12 +423,6 @@ int ug_node_potential(UgBatch* b, const char* node, double* out) {
     GUARD_END(1)
 }
 
-// Replica exchange, criterion 0 of the reference (src/main.cpp:270-294):
-// energies at the current coordinates, swap the coordinates of every pair of
-// the set, energies again, then undo each swap that fails the Metropolis test
-// on the change of the log Boltzmann factors.  Energies are FP64 sums and the
-// acceptance arithmetic is FP64; the uniform draws come from the replica
-// exchange Threefry stream keyed by (seed, stream 1) at counter (round, 0, 0, k).
 }  // extern "C"
 namespace ug {
 void threefry_host(const uint32_t c[4], const uint32_t k[4], uint32_t out[4]) {
@@ -463,43 +461,85 @@ using ug::swap_coords;
 using ug::threefry_host;
 extern "C" {
 
+// One exchange over the given pairs (criterion 0), on the device: the
+// replica-exchange kernels of remd.cu with the draws keyed by `round`.  The
+// plan for these pairs is kept between calls with the same pairs.
 int ug_replica_exchange(UgBatch* b, int n_pairs, const int* pairs, uint32_t seed, uint64_t round, int* accepted) {
     GUARD_BEGIN
     Engine& e = *b->e;
-    int S = e.n_sys;
-    std::vector<float> temp(static_cast<size_t>(S));
-    UG_CK(cudaMemcpy(temp.data(), e.d_temp, sizeof(float) * size_t(S), cudaMemcpyDeviceToHost));
-    std::vector<double> e_old(static_cast<size_t>(S)), e_new(static_cast<size_t>(S));
-    e.compute_checked(true);
-    e.energies(e_old.data());
-    float* tmp = nullptr;
-    int max_atom = *std::max_element(e.n_atom.begin(), e.n_atom.end());
-    UG_CK(cudaMalloc(&tmp, sizeof(float) * 3 * size_t(max_atom)));
-    for (int k = 0; k < n_pairs; ++k) swap_coords(e, pairs[2 * k], pairs[2 * k + 1], tmp);
-    e.compute_checked(true);
-    e.energies(e_new.data());
-    uint32_t key[4] = {seed, 1u, 0u, 0u};
-    uint32_t ctr[4] = {uint32_t(round & 0xffffffffu), uint32_t(round >> 32), 0u, 0u};
-    for (int k = 0; k < n_pairs; ++k) {
-        int s1 = pairs[2 * k], s2 = pairs[2 * k + 1];
-        double b1 = 1.0 / temp[size_t(s1)], b2 = 1.0 / temp[size_t(s2)];
-        double diff = (-b1 * e_new[size_t(s1)] - b2 * e_new[size_t(s2)]) - (-b1 * e_old[size_t(s1)] - b2 * e_old[size_t(s2)]);
-        bool reject = false;
-        if (diff < 0.0) {
-            uint32_t bits[4];
-            threefry_host(ctr, key, bits);
-            ctr[3]++;
-            double u = double(float(bits[0]) * (1.f / 4294967296.f) + (0.5f / 4294967296.f));
-            reject = std::exp(diff) < u;
-        }
-        if (reject) swap_coords(e, s1, s2, tmp);
-        if (accepted) accepted[k] = reject ? 0 : 1;
+    std::vector<int> key(pairs, pairs + 2 * size_t(n_pairs));
+    key.push_back(int(seed));
+    if (!b->oneshot || b->oneshot_key != key) {
+        std::vector<std::vector<std::pair<int, int>>> sets(1);
+        for (int k = 0; k < n_pairs; ++k) sets[0].emplace_back(pairs[2 * k], pairs[2 * k + 1]);
+        b->oneshot.reset(new ug::Remd(e, sets, seed, 0, 0, 0ull));
+        b->oneshot_key = key;
     }
-    e.sync();
-    cudaFree(tmp);
+    b->oneshot->enqueue((long long)round);
+    std::vector<int> rep, acc;
+    std::vector<unsigned> na, ns;
+    unsigned long long att = 0;
+    int set = 0;
+    b->oneshot->read(rep, na, ns, att, acc, set);
+    if (accepted)
+        for (int k = 0; k < n_pairs; ++k) accepted[k] = acc[size_t(k)];
     return 0;
     GUARD_END(1)
 }
+
+int ug_set_replica_exchange(UgBatch* b, int n_sets, const int* set_sizes, const int* pairs, uint32_t seed,
+                            int interval, int criterion) {
+    GUARD_BEGIN
+    Engine& e = *b->e;
+    if (n_sets <= 0) {
+        e.drop_graph();
+        e.remd.reset();
+        return 0;
+    }
+    std::vector<std::vector<std::pair<int, int>>> sets(static_cast<size_t>(n_sets));
+    size_t q = 0;
+    for (int k = 0; k < n_sets; ++k) {
+        if (set_sizes[k] < 0) throw ug::Error("negative swap set size");
+        for (int i = 0; i < set_sizes[k]; ++i, ++q) sets[size_t(k)].emplace_back(pairs[2 * q], pairs[2 * q + 1]);
+    }
+    e.drop_graph();
+    e.remd.reset(new ug::Remd(e, sets, seed, criterion, interval, 0ull));
+    e.remd_done = 0;
+    return 0;
+    GUARD_END(1)
+}
+
+int ug_replica_state(UgBatch* b, int* replica, unsigned* n_attempt, unsigned* n_success, int cap_pairs,
+                     unsigned long long* n_exchanges, int* last_accepted, int* last_set) {
+    GUARD_BEGIN
+    Engine& e = *b->e;
+    if (!e.remd) throw ug::Error("no replica exchange plan");
+    std::vector<int> rep, acc;
+    std::vector<unsigned> na, ns;
+    unsigned long long att = 0;
+    int set = -1;
+    e.remd->read(rep, na, ns, att, acc, set);
+    if (replica) std::copy(rep.begin(), rep.end(), replica);
+    if (int(na.size()) > cap_pairs) throw ug::Error("pair arrays too small");
+    if (n_attempt) std::copy(na.begin(), na.end(), n_attempt);
+    if (n_success) std::copy(ns.begin(), ns.end(), n_success);
+    if (n_exchanges) *n_exchanges = att;
+    if (last_accepted) std::copy(acc.begin(), acc.end(), last_accepted);
+    if (last_set) *last_set = set;
+    return 0;
+    GUARD_END(1)
+}
+
+int ug_exchange_now(UgBatch* b) {
+    GUARD_BEGIN
+    if (!b->e->remd) throw ug::Error("no replica exchange plan");
+    b->e->remd->enqueue();
+    b->e->sync();
+    return 0;
+    GUARD_END(1)
+}
+
+int ug_timed_rounds(UgBatch* b) { return b->e->timed_rounds(); }
 
 int ug_status(UgBatch* b, int clear) {
     GUARD_BEGIN
@@ -518,7 +558,12 @@ int ug_info(UgBatch* b, int* launches, int64_t* bytes) {
 int ug_bench(UgBatch* b, int n_round, float dt, float timescale, int flush_l2, int e2e, float* ms) {
     GUARD_BEGIN
     Engine& e = *b->e;
-    if (!e.graph_exec || e.graph_rounds != 1 || !e.graph_timed) e.capture_timed(dt, timescale);
+    // with periodic replica exchanges a timed replay is one interval and its
+    // exchange, started on an interval boundary
+    const int xi = e.remd ? e.remd->interval() : 0;
+    if (xi > 0 && e.remd_done % (unsigned long long)xi)
+        e.run_rounds(int(xi - e.remd_done % (unsigned long long)xi), dt, timescale, false, 1);
+    if (!e.graph_exec || e.graph_rounds != e.timed_rounds() || !e.graph_timed) e.capture_timed(dt, timescale);
     b->kt_ms = b->kt_bytes = 0.0;
     b->kt_launches = 0;
     double bytes0 = e.kernel_bytes();
@@ -569,6 +614,7 @@ int ug_bench(UgBatch* b, int n_round, float dt, float timescale, int flush_l2, i
         }
     }
     UG_CK(cudaStreamSynchronize(e.st));
+    e.remd_done += (unsigned long long)n_round * (unsigned long long)e.timed_rounds();
     b->kt_bytes = e.kernel_bytes() - bytes0;
     for (int r = 0; r < n_round; ++r) UG_CK(cudaEventElapsedTime(&ms[r], ev[2 * size_t(r)], ev[2 * size_t(r) + 1]));
     for (auto& x : ev) cudaEventDestroy(x);

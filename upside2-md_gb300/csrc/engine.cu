@@ -17,6 +17,7 @@
 
 #include "dev_math.cuh"
 #include "launch.cuh"
+#include "remd.h"
 #include "warm.h"
 
 namespace ug {
@@ -39,6 +40,16 @@ template <class T> T* Engine::upload(const std::vector<T>& v) {
     if (!v.empty()) UG_CK(cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, st));
     return p;
 }
+// instantiated here for the other translation units of the library
+template int* Engine::alloc<int>(size_t);
+template unsigned* Engine::alloc<unsigned>(size_t);
+template unsigned long long* Engine::alloc<unsigned long long>(size_t);
+template float* Engine::alloc<float>(size_t);
+template double* Engine::alloc<double>(size_t);
+template int* Engine::upload<int>(const std::vector<int>&);
+template int2* Engine::upload<int2>(const std::vector<int2>&);
+template float* Engine::upload<float>(const std::vector<float>&);
+
 bool pdl_enabled() {
     static const bool on = [] {
         const char* v = std::getenv("UPSIDE_GB300_PDL");
@@ -3151,6 +3162,7 @@ Engine::Engine(const std::vector<std::string>& paths, const std::vector<int>& n_
 }
 
 Engine::~Engine() {
+    remd.reset();
     if (graph_exec) cudaGraphExecDestroy(graph_exec);
     if (graph) cudaGraphDestroy(graph);
     for (auto& x : kt_ev) cudaEventDestroy(x);
@@ -3380,6 +3392,10 @@ void Engine::run_rounds(int n_round, float dt, float timescale, bool use_graph, 
     if (thermo_interval < 1) thermo_interval = 1;
     // the captured graph applies the thermostat every round
     if (thermo_interval > 1) use_graph = false;
+    // with periodic exchanges a graph replay is one whole interval and its
+    // exchange; rounds before the next interval boundary run eagerly
+    const int xi = remd ? remd->interval() : 0;
+    if (xi > 0) graph_rounds = xi;
     size_t n3 = 3 * size_t(atom_total);
     if (!snap_pos) {
         snap_pos = alloc<float>(n3);
@@ -3390,20 +3406,28 @@ void Engine::run_rounds(int n_round, float dt, float timescale, bool use_graph, 
     int done = 0, retries = 0;
     while (done < n_round) {
         int k = use_graph ? std::min(graph_rounds, n_round - done) : std::min(8, n_round - done);
+        const bool aligned = xi <= 0 || remd_done % (unsigned long long)xi == 0;
+        if (use_graph && !aligned)  // eager rounds up to the next exchange
+            k = std::min<long long>(k, (long long)xi - (long long)(remd_done % (unsigned long long)xi));
         UG_CK(cudaMemcpyAsync(snap_pos, d_pos, 4 * n3, cudaMemcpyDeviceToDevice, st));
         UG_CK(cudaMemcpyAsync(snap_mom, d_mom, 4 * n3, cudaMemcpyDeviceToDevice, st));
         UG_CK(cudaMemcpyAsync(snap_round, d_round, 8 * size_t(n_sys), cudaMemcpyDeviceToDevice, st));
-        if (use_graph && k == graph_rounds) {
+        if (remd) remd->snapshot(false);
+        if (use_graph && aligned && k == graph_rounds) {
             if (!graph_exec || this->graph_rounds != graph_rounds || graph_dt != dt || graph_timescale != timescale ||
-                graph_span != thermo_span || graph_multistep != multistep || graph_inner != inner_step || graph_timed)
+                graph_span != thermo_span || graph_multistep != multistep || graph_inner != inner_step || graph_timed ||
+                graph_remd != (xi > 0))
                 capture(dt, timescale, graph_rounds);
             launch_graph();
         } else {
-            for (int r = 0; r < k; ++r)
+            for (int r = 0; r < k; ++r) {
                 round(dt, timescale,
                       (first_round + static_cast<unsigned long long>(done + r)) %
                               static_cast<unsigned long long>(thermo_interval) ==
                           0);
+                if (xi > 0 && (remd_done + static_cast<unsigned long long>(r) + 1ull) % (unsigned long long)xi == 0)
+                    remd->enqueue();
+            }
         }
         int s = 0;
         UG_CK(cudaMemcpyAsync(&s, d_status, sizeof(int), cudaMemcpyDeviceToHost, st));
@@ -3413,6 +3437,7 @@ void Engine::run_rounds(int n_round, float dt, float timescale, bool use_graph, 
             UG_CK(cudaMemcpyAsync(d_pos, snap_pos, 4 * n3, cudaMemcpyDeviceToDevice, st));
             UG_CK(cudaMemcpyAsync(d_mom, snap_mom, 4 * n3, cudaMemcpyDeviceToDevice, st));
             UG_CK(cudaMemcpyAsync(d_round, snap_round, 8 * size_t(n_sys), cudaMemcpyDeviceToDevice, st));
+            if (remd) remd->snapshot(true);
             UG_CK(cudaMemsetAsync(d_status, 0, sizeof(int), st));
             sync();
             for (auto& n : nodes) n->grow(*this);
@@ -3421,6 +3446,7 @@ void Engine::run_rounds(int n_round, float dt, float timescale, bool use_graph, 
             continue;
         }
         done += k;
+        remd_done += static_cast<unsigned long long>(k);
     }
 }
 void Engine::sync() { UG_CK(cudaStreamSynchronize(st)); }
@@ -3429,9 +3455,14 @@ void Engine::capture(float dt, float timescale, int rounds) {
     if (graph_exec) { cudaGraphExecDestroy(graph_exec); graph_exec = nullptr; }
     if (graph) { cudaGraphDestroy(graph); graph = nullptr; }
     UG_CK(cudaStreamSynchronize(st));
+    const int xi = remd ? remd->interval() : 0;
     UG_CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-    for (int r = 0; r < rounds; ++r) round(dt, timescale, true);
+    for (int r = 0; r < rounds; ++r) {
+        round(dt, timescale, true);
+        if (xi > 0 && (r + 1) % xi == 0) remd->enqueue();
+    }
     UG_CK(cudaStreamEndCapture(st, &graph));
+    graph_remd = xi > 0;
     UG_CK(cudaGraphInstantiate(&graph_exec, graph, 0));
     graph_rounds = rounds;
     graph_timed = false;
@@ -3580,16 +3611,23 @@ void Engine::drop_graph() {
 
 // One-round graph whose measured-kernel launches are bracketed by event-record
 // nodes (kt_ev[0..kt_used)); each replay re-records them.
+int Engine::timed_rounds() const { return remd && remd->interval() > 0 ? remd->interval() : 1; }
+
 void Engine::capture_timed(float dt, float timescale) {
-    if (kt_ev.empty()) {
-        kt_ev.resize(16);
+    const int rounds = timed_rounds();
+    // two events around each of the measured kernel's launches: up to 8
+    // evaluations per round and 2 per exchange
+    const size_t need = 16 * size_t(rounds) + 8;
+    if (kt_ev.size() < need) {
+        for (auto& x : kt_ev) cudaEventDestroy(x);
+        kt_ev.assign(need, nullptr);
         for (auto& x : kt_ev) UG_CK(cudaEventCreate(&x));
     }
     kt_used = 0;
     bool any = false;
     for (auto& n : nodes) any |= n->set_kernel_timer(kt_ev.data(), &kt_used, int(kt_ev.size()));
     try {
-        capture(dt, timescale, 1);
+        capture(dt, timescale, rounds);
     } catch (...) {
         for (auto& n : nodes) n->set_kernel_timer(nullptr, nullptr, 0);
         throw;

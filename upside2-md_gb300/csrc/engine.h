@@ -23,6 +23,7 @@ void cuda_check(cudaError_t e, const char* what);
 #define UG_CK(x) ::ug::cuda_check((x), #x)
 
 class Engine;
+class Remd;
 
 // One `/input/potential/<node>` group of every system of the batch.
 struct Groups {
@@ -199,6 +200,16 @@ public:
     int kt_used = 0;
     void capture_timed(float dt, float timescale);
     double kernel_bytes();
+
+    // Replica exchange on the device (remd.h): with a plan whose interval is
+    // > 0, run_rounds exchanges after every interval-th round (counted from
+    // the plan) and a captured graph holds whole intervals with their
+    // exchange.  remd_done: rounds run since the plan was set.
+    std::unique_ptr<Remd> remd;
+    unsigned long long remd_done = 0;
+    bool graph_remd = false;  // the captured graph contains exchanges
+    // rounds of one timed graph: one, or one exchange interval
+    int timed_rounds() const;
 
     size_t device_bytes = 0;
     int launches_per_compute = 0;

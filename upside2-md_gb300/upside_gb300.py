@@ -59,6 +59,10 @@ def lib():
         L.ug_value_by_name.argtypes = [vp, cp, cp, vp, ip]
         L.ug_node_potential.argtypes = [vp, cp, vp]
         L.ug_replica_exchange.argtypes = [vp, ip, vp, ctypes.c_uint32, ctypes.c_uint64, vp]
+        L.ug_set_replica_exchange.argtypes = [vp, ip, vp, vp, ctypes.c_uint32, ip, ip]
+        L.ug_replica_state.argtypes = [vp, vp, vp, vp, ip, vp, vp, vp]
+        L.ug_timed_rounds.argtypes = [vp]
+        L.ug_exchange_now.argtypes = [vp]
         L.ug_status.argtypes = [vp, ip]
         L.ug_info.argtypes = [vp, vp, vp]
         L.ug_profile.argtypes = [vp, ip, ctypes.c_char_p, ip, vp, ip]
@@ -345,6 +349,39 @@ class Batch:
         self._chk(lib().ug_replica_exchange(self.h, len(pairs), pairs.ctypes.data, int(seed), int(round_),
                                             acc.ctypes.data))
         return acc
+
+    def set_replica_exchange(self, sets, seed, interval, criterion=0):
+        """Periodic replica exchange on the device: after every interval-th
+        round, one exchange with the next swap set in turn (sets: lists of
+        (s1, s2) pairs).  sets=[] removes the plan."""
+        sizes = np.array([len(s) for s in sets], np.int32)
+        pairs = np.ascontiguousarray(np.concatenate([np.asarray(s, np.int32).reshape(-1, 2) for s in sets])
+                                     if sets else np.zeros((0, 2), np.int32), dtype=np.int32)
+        self._chk(lib().ug_set_replica_exchange(self.h, len(sets), sizes.ctypes.data, pairs.ctypes.data,
+                                                int(seed), int(interval), int(criterion)))
+        self._remd_pairs = sum(len(s) for s in sets)
+        self._remd_max = max([len(s) for s in sets] or [0])
+
+    def replica_state(self):
+        """(replica index per system, attempts per pair, successes per pair,
+        exchanges made, last exchange's accept flags, last set)."""
+        n = max(1, self._remd_pairs)
+        rep = np.zeros(self.n_sys, np.int32)
+        na = np.zeros(n, np.uint32)
+        ns = np.zeros(n, np.uint32)
+        acc = np.zeros(max(1, self._remd_max), np.int32)
+        ne = ctypes.c_ulonglong()
+        last = ctypes.c_int()
+        self._chk(lib().ug_replica_state(self.h, rep.ctypes.data, na.ctypes.data, ns.ctypes.data, n,
+                                         ctypes.byref(ne), acc.ctypes.data, ctypes.byref(last)))
+        return rep, na[:self._remd_pairs], ns[:self._remd_pairs], ne.value, acc, last.value
+
+    def exchange_now(self):
+        """one exchange of the periodic plan now (next set, its round key)"""
+        self._chk(lib().ug_exchange_now(self.h))
+
+    def timed_rounds(self):
+        return lib().ug_timed_rounds(self.h)
 
     def status(self, clear=True):
         return lib().ug_status(self.h, int(clear))

@@ -4,6 +4,7 @@
   C2  1 chain of 300 residues, T=0.85
   C3  48 replicas of one 150-residue chain, T geometric 0.80 -> 1.00, replica
       exchange between alternating even/odd neighbour pairs every 20 steps
+      (rounds, the reference's step)
   C4  64 independent chains, lengths uniform in [40, 400], T uniform in [0.80, 0.95]
   C5  8 chains of 250 residues in one system (2000 residues), spaced apart
 
@@ -83,7 +84,7 @@ def workload(name, seed=1):
         odd = [(i, i + 1) for i in range(1, 47, 2)]
         swap_sets = [even, odd]
     return dict(configs=cfgs, n_res=n_res, temps=temps, seeds=[seed + i for i in range(len(cfgs))],
-                swap_sets=swap_sets)
+                swap_sets=swap_sets, exchange_interval=20 if swap_sets else 0)
 
 
 def initial_positions(configs):
