@@ -46,6 +46,8 @@ def parse():
     ap.add_argument("--equilibrate", type=int, default=300,
                     help="untimed integration rounds from the initial coils before the warm-up")
     ap.add_argument("--profile", action="store_true", help="print per-node device times to stderr")
+    ap.add_argument("--pbc", action="store_true",
+                    help="periodic box (the workload's box, 200 A for C5; a mode of this engine only)")
     return ap.parse_args()
 
 
@@ -217,6 +219,10 @@ def main():
     b = U.Batch(W["configs"])
     b.set_pos(workloads.initial_positions(W["configs"]))
     b.set_thermostat(W["temps"], np.array(W["seeds"], np.uint32))
+    if a.pbc:
+        if not W.get("box"):
+            raise SystemExit("--pbc: workload %s has no box" % a.workload)
+        b.set_box(*W["box"])
     if W["swap_sets"]:  # replica exchange every 20 rounds, alternating sets, on the device
         b.set_replica_exchange(W["swap_sets"], 1 + d.rank, W["exchange_interval"], 0)
     bp_start = set_bp_start(b, a.bp_start)
@@ -275,6 +281,7 @@ def main():
                            "evaluations and integrator stages), the reference's step (src/main.cpp:1009-1012)",
                    "force_evaluations_per_step": 3,
                    "rounds_per_timed_iteration": rounds_per_iter,
+                   "periodic_box": W.get("box") if a.pbc else None,
                    "replica_exchange": (None if not W["swap_sets"] else
                                         "every %d rounds on the device, alternating even/odd sets, criterion 0"
                                         % W["exchange_interval"]),

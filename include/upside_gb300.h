@@ -102,6 +102,14 @@ int ug_set_replica_exchange(UgBatch* b, int n_sets, const int* set_sizes, const 
  * of its set) and set index. */
 int ug_replica_state(UgBatch* b, int* replica, unsigned* n_attempt, unsigned* n_success, int cap_pairs,
                      unsigned long long* n_exchanges, int* last_accepted, int* last_set);
+/* Periodic box for every system of the batch (no counterpart in the
+ * reference, which has open boundaries): edge lengths lx, ly, lz in angstrom,
+ * 0 for an open direction.  Pair searches, pair terms (rotamer, hbond,
+ * coverage and environment graphs, backbone pairs) use the minimum image;
+ * bonded terms and coordinates are untouched (coordinates are never
+ * wrapped).  Rejects a box edge under twice a graph's cutoff plus candidate
+ * buffer. */
+int ug_set_box(UgBatch* b, float lx, float ly, float lz);
 /* One exchange of the periodic plan now (the next set in turn, drawn with the
  * round key of that exchange), outside the round schedule.  Synchronises. */
 int ug_exchange_now(UgBatch* b);

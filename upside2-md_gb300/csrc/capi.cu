@@ -530,6 +530,13 @@ int ug_replica_state(UgBatch* b, int* replica, unsigned* n_attempt, unsigned* n_
     GUARD_END(1)
 }
 
+int ug_set_box(UgBatch* b, float lx, float ly, float lz) {
+    GUARD_BEGIN
+    b->e->set_box(lx, ly, lz);
+    return 0;
+    GUARD_END(1)
+}
+
 int ug_exchange_now(UgBatch* b) {
     GUARD_BEGIN
     if (!b->e->remd) throw ug::Error("no replica exchange plan");

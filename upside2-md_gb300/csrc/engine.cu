@@ -2399,6 +2399,16 @@ __global__ void bb_pairs_kernel(DGraph g, const int* __restrict__ res_row, const
         quat_to_rot(A + 3, Ua);
         quat_to_rot(B + 3, Ub);
         f3 ta = mk(A[0], A[1], A[2]), tb = mk(B[0], B[1], B[2]);
+        // periodic box: the pair's atoms are compared at the minimum image of
+        // the frame centres (one shift for the whole residue pair)
+        f3 shift = mk(0, 0, 0);
+        if (g.box[0] > 0.f || g.box[1] > 0.f || g.box[2] > 0.f) {
+            f3 dt = ta - tb;
+            f3 mi = mk(g.box[0] > 0.f ? dt.x - g.box[0] * rintf(dt.x / g.box[0]) : dt.x,
+                       g.box[1] > 0.f ? dt.y - g.box[1] * rintf(dt.y / g.box[1]) : dt.y,
+                       g.box[2] > 0.f ? dt.z - g.box[2] * rintf(dt.z / g.box[2]) : dt.z);
+            shift = mi - dt;
+        }
         int na = nat[ij.x], nb = nat[ij.y];
         f3 xa[4], xb[4];
         for (int k = 0; k < na; ++k) xa[k] = rot(Ua, ld3(refp + 12 * size_t(ij.x) + 3 * k)) + ta;
@@ -2408,7 +2418,7 @@ __global__ void bb_pairs_kernel(DGraph g, const int* __restrict__ res_row, const
         bool hit = false;
         for (int i = 0; i < na; ++i)
             for (int j = 0; j < nb; ++j) {
-                f3 r = xa[i] - xb[j];
+                f3 r = xa[i] - xb[j] + shift;
                 float m2 = mag2(r);
                 if (m2 > c2) continue;
                 hit = true;
@@ -3336,6 +3346,29 @@ void Engine::round(float dt, float timescale, bool thermostat) {
         ug::launch(integrate_kernel, nblk(3LL * atom_total), 256, 0, st, 3 * atom_total, dt, nodes[0]->sens, d_mom, d_pos);
     }
     UG_CK(cudaGetLastError());
+}
+
+void Engine::set_box(float lx, float ly, float lz) {
+    if (!(lx >= 0.f && ly >= 0.f && lz >= 0.f) || !std::isfinite(lx) || !std::isfinite(ly) || !std::isfinite(lz))
+        throw Error("box edge lengths must be finite and >= 0 (0: open)");
+    for (auto& n : nodes)
+        if (DGraph* g = n->graph()) {
+            // the minimum image is unique only while a pair's cutoff (plus the
+            // candidate buffer) is under half the box
+            float reach = 2.f * (g->cutoff + g->buffer);
+            for (float L : {lx, ly, lz})
+                if (L > 0.f && L < reach)
+                    throw Error("box edge " + std::to_string(L) + " shorter than twice the reach of " + n->name +
+                                " (" + std::to_string(reach / 2.f) + ")");
+            g->box[0] = lx;
+            g->box[1] = ly;
+            g->box[2] = lz;
+            if (g->cached) UG_CK(cudaMemsetAsync(g->cache_force, 1, sizeof(int), st));
+        }
+    box[0] = lx;
+    box[1] = ly;
+    box[2] = lz;
+    drop_graph();
 }
 
 void Engine::compute_checked(bool energy, int level) {

@@ -144,6 +144,10 @@ public:
     float thermo_span = 1.f;
     // move each system's centroid to the origin (xy_only: x and y only)
     void recenter(bool xy_only);
+    // periodic box of every system (edge lengths, 0 = open): the pair lists
+    // and pair terms use the minimum image; coordinates are never wrapped
+    void set_box(float lx, float ly, float lz);
+    float box[3] = {0.f, 0.f, 0.f};
     // host helpers
     void set_pos(const float* pos_all);     // atom_total*3
     void get_pos(float* pos_all);

@@ -105,8 +105,13 @@ void launch_pack_positions(const DGraph& g, cudaStream_t st) {
 // runs only for the rows of systems flagged for a rebuild, with cutoff +
 // buffer, and writes each system's candidates into its own cache segment
 // (the reference's cache rebuild, src/interaction_graph.h:96-157).
-__device__ __forceinline__ float pair_d2(float4 a, float4 b) {
-    float dx = a.x - b.x, dy = a.y - b.y, dz = a.z - b.z;
+// minimum image of a displacement in the periodic box (no change when open)
+__device__ __forceinline__ float min_image1(float d, float L) { return L > 0.f ? d - L * rintf(d / L) : d; }
+__device__ __forceinline__ f3 min_image(f3 d, const float* box) {
+    return mk(min_image1(d.x, box[0]), min_image1(d.y, box[1]), min_image1(d.z, box[2]));
+}
+__device__ __forceinline__ float pair_d2(float4 a, float4 b, const float* box) {
+    float dx = min_image1(a.x - b.x, box[0]), dy = min_image1(a.y - b.y, box[1]), dz = min_image1(a.z - b.z, box[2]);
     return __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
 }
 
@@ -160,7 +165,7 @@ __global__ void pair_kernel(DGraph g) {
                 for (int l = 0; l < 4; ++l) {
                     if (l >= nl) break;
                     if (g.symmetric && !(i1s + l < j)) continue;
-                    if (pair_d2(a[l], b) < c2 && acceptable_ids(g.excl, ida[l], idb)) mask |= 1u << l;
+                    if (pair_d2(a[l], b, g.box) < c2 && acceptable_ids(g.excl, ida[l], idb)) mask |= 1u << l;
                 }
             }
             int c = __popc(mask);
@@ -316,7 +321,7 @@ __global__ void __launch_bounds__(256) cache_refine_kernel(DGraph g) {
             ij[q] = make_int2(0, 0);
             if (k < n) {
                 ij[q] = ce[k];
-                if (pair_d2(g.x1[ij[q].x], X2[ij[q].y]) < c2) mask |= 1u << q;
+                if (pair_d2(g.x1[ij[q].x], X2[ij[q].y], g.box) < c2) mask |= 1u << q;
             }
         }
         int c = __popc(mask);
@@ -381,8 +386,8 @@ void launch_pairs(const DGraph& g, cudaStream_t st) {
 
 // ------------------------------------------------------ edge evaluation ---
 __device__ float quadspline(int n_ka, int n_k, float inv_dtheta, float inv_dx, const float* p, const float* x1,
-                            const float* x2, float* d1, float* d2) {
-    f3 disp = ld3(x2) - ld3(x1), r1 = ld3(x1 + 3), r2 = ld3(x2 + 3);
+                            const float* x2, float* d1, float* d2, const float* box) {
+    f3 disp = min_image(ld3(x2) - ld3(x1), box), r1 = ld3(x1 + 3), r2 = ld3(x2 + 3);
     float dist2 = mag2(disp), inv_dist = rsqrtf(dist2);
     float dc = dist2 * (inv_dist * inv_dx);
     f3 u = disp * inv_dist;
@@ -406,8 +411,8 @@ __device__ float quadspline(int n_ka, int n_k, float inv_dtheta, float inv_dx, c
     return wv + aw * nv;
 }
 
-__device__ __forceinline__ bool phb_in_angle(const float* H, const float* O) {
-    f3 HO = ld3(H) - ld3(O);
+__device__ __forceinline__ bool phb_in_angle(const float* H, const float* O, const float* box) {
+    f3 HO = min_image(ld3(H) - ld3(O), box);
     float m2 = mag2(HO) + 1e-6f;
     f3 rHO = HO * rsqrtf(m2);
     return (dot(rHO, ld3(O + 3)) > 0.f) && (-dot(rHO, ld3(H + 3)) > 0.f);
@@ -416,9 +421,9 @@ __device__ __forceinline__ bool phb_in_angle(const float* H, const float* O) {
 template <int KIND>
 __device__ float edge_value(const DGraph& g, const float* p, const float* a, const float* b, float* da, float* db,
                             bool active) {
-    if (KIND == IK_ROTAMER) return quadspline(15, 12, 6.f, 1.f / 0.7f, p, a, b, da, db);
+    if (KIND == IK_ROTAMER) return quadspline(15, 12, 6.f, 1.f / 0.7f, p, a, b, da, db, g.box);
     if (KIND == IK_HBCOV) {
-        float cov = quadspline(15, 10, 6.f, 1.f / 0.625f, p, a, b, da, db);
+        float cov = quadspline(15, 10, 6.f, 1.f / 0.625f, p, a, b, da, db, g.box);
         float om = 1.f - a[6];
         float pre = om * om;
 #pragma unroll
@@ -427,8 +432,8 @@ __device__ float edge_value(const DGraph& g, const float* p, const float* a, con
         return pre * cov;
     }
     if (KIND == IK_PHB) {
-        f3 H = ld3(a), O = ld3(b), rHN = ld3(a + 3), rOC = ld3(b + 3);
-        f3 HO = H - O;
+        f3 rHN = ld3(a + 3), rOC = ld3(b + 3);
+        f3 HO = min_image(ld3(a) - ld3(b), g.box);
         float m2 = mag2(HO) + 1e-6f, inv = rsqrtf(m2), mg = m2 * inv;
         f3 rHO = HO * inv;
         float dHOC = dot(rHO, rOC), dOHN = -dot(rHO, rHN);
@@ -458,7 +463,7 @@ __device__ float edge_value(const DGraph& g, const float* p, const float* a, con
         return hb_log;
     }
     if (KIND == IK_ENVCOV || KIND == IK_HBENV) {
-        f3 disp = ld3(b) - ld3(a), r1 = ld3(a + 3);
+        f3 disp = min_image(ld3(b) - ld3(a), g.box), r1 = ld3(a + 3);
         float prob = KIND == IK_ENVCOV ? b[3] : 1.f;
         float d2 = mag2(disp), inv = rsqrtf(d2), dist = d2 * inv;
         f3 u = disp * inv;
@@ -501,7 +506,7 @@ __global__ void edge_eval_kernel(DGraph g, const int* __restrict__ edge_sys_star
             active = false;
             for (int k = g0; k < min(g0 + 4, en); ++k) {
                 int2 q = g.edges[k];
-                active |= phb_in_angle(g.in1 + size_t(g.loc1[q.x]) * g.w1, g.in2 + size_t(g.loc2[q.y]) * g.w2);
+                active |= phb_in_angle(g.in1 + size_t(g.loc1[q.x]) * g.w1, g.in2 + size_t(g.loc2[q.y]) * g.w2, g.box);
             }
         }
         float* da = g.deriv + size_t(e) * dw;
@@ -635,7 +640,7 @@ __global__ void param_deriv_kernel(DGraph g, float* __restrict__ out) {
         float inv_dx = g.kind == IK_ROTAMER ? 1.f / 0.7f : 1.f / 0.625f;
         float pre = 1.f;
         if (g.kind == IK_HBCOV) pre = (1.f - a[6]) * (1.f - a[6]);
-        f3 disp = ld3(b) - ld3(a), r1 = ld3(a + 3), r2 = ld3(b + 3);
+        f3 disp = min_image(ld3(b) - ld3(a), g.box), r1 = ld3(a + 3), r2 = ld3(b + 3);
         float dist2 = mag2(disp), inv_dist = rsqrtf(dist2);
         float dc = dist2 * (inv_dist * inv_dx);
         f3 u = disp * inv_dist;

@@ -21,6 +21,9 @@ enum Excl : int { EX_ROTAMER = 0, EX_SEQ1 = 1, EX_SEQ2 = 2 };
 // Pair list + per-edge values for one interaction graph over the whole batch.
 struct DGraph {
     int kind, excl, symmetric;
+    // periodic box edge lengths (0: open boundaries): pair distances then use
+    // the minimum image (a mode of this engine only; the reference has none)
+    float box[3];
     int d1, d2, n_param, n_type1, n_type2;
     float cutoff;
     // element sets (set2 == set1 when symmetric)

@@ -63,6 +63,7 @@ def lib():
         L.ug_replica_state.argtypes = [vp, vp, vp, vp, ip, vp, vp, vp]
         L.ug_timed_rounds.argtypes = [vp]
         L.ug_exchange_now.argtypes = [vp]
+        L.ug_set_box.argtypes = [vp, ctypes.c_float, ctypes.c_float, ctypes.c_float]
         L.ug_status.argtypes = [vp, ip]
         L.ug_info.argtypes = [vp, vp, vp]
         L.ug_profile.argtypes = [vp, ip, ctypes.c_char_p, ip, vp, ip]
@@ -375,6 +376,11 @@ class Batch:
         self._chk(lib().ug_replica_state(self.h, rep.ctypes.data, na.ctypes.data, ns.ctypes.data, n,
                                          ctypes.byref(ne), acc.ctypes.data, ctypes.byref(last)))
         return rep, na[:self._remd_pairs], ns[:self._remd_pairs], ne.value, acc, last.value
+
+    def set_box(self, lx, ly, lz):
+        """periodic box edge lengths (0: open direction); minimum image in
+        the pair terms"""
+        self._chk(lib().ug_set_box(self.h, float(lx), float(ly), float(lz)))
 
     def exchange_now(self):
         """one exchange of the periodic plan now (next set, its round key)"""

@@ -6,7 +6,8 @@
       exchange between alternating even/odd neighbour pairs every 20 steps
       (rounds, the reference's step)
   C4  64 independent chains, lengths uniform in [40, 400], T uniform in [0.80, 0.95]
-  C5  8 chains of 250 residues in one system (2000 residues), spaced apart
+  C5  8 chains of 250 residues in one system (2000 residues), spaced apart,
+      in a periodic box of side 200 A when the box mode is asked for
 
 Sequences are drawn uniformly over the 20 amino acids from the seed; initial
 structures are random (phi, psi) chains (py/upside_config.py:186-201).  Files
@@ -84,7 +85,8 @@ def workload(name, seed=1):
         odd = [(i, i + 1) for i in range(1, 47, 2)]
         swap_sets = [even, odd]
     return dict(configs=cfgs, n_res=n_res, temps=temps, seeds=[seed + i for i in range(len(cfgs))],
-                swap_sets=swap_sets, exchange_interval=20 if swap_sets else 0)
+                swap_sets=swap_sets, exchange_interval=20 if swap_sets else 0,
+                box=(200.0, 200.0, 200.0) if name == "C5" else None)
 
 
 def initial_positions(configs):
