@@ -3,11 +3,11 @@ boundaries, so there is no reference output to compare with; it is checked
 against the open-boundary engine on images of the same configuration).
 
   * a box much larger than the system changes nothing: the same pair lists
-    in the same order, energies and forces to the last bit of their FP64/FP32
-    sums;
+    in the same order, energies and forces up to the run-to-run order of their
+    atomic sums;
   * two chains that touch only across a face of the box give the energy and
     forces of the same two chains made adjacent by moving one of them by a box
-    vector, with open boundaries (energy 1e-5 relative, forces 1e-4 of max
+    vector, with open boundaries (energy 1e-5 relative, forces 5e-4 of max
     |F|; the two differ only in FP32 rounding of the shifted coordinates),
     and the same number of pairs in every interaction graph (up to one pair
     at a cutoff that this rounding moves);
@@ -28,8 +28,9 @@ L = 90.0
 @pytest.fixture(scope="module")
 def two_chains(tmp_path_factory, built):
     """Two 40-residue chains, the second starting at residue 40; coordinates
-    from the generator's random chains, chain A near the +x face and chain B
-    near the -x face of a box of side 90 A, 8-10 A apart across the face."""
+    from the generator's random chains, chain A centred at x = 35 and chain B
+    at x = 55 - 90: their centres are 20 A apart across the x face of a box
+    of side 90 A, and 70 A apart with open boundaries."""
     import config_gen
     from h5lite import H5File
     path = str(tmp_path_factory.mktemp("pbc") / "two_chains.up")
@@ -39,10 +40,8 @@ def two_chains(tmp_path_factory, built):
     with H5File(path) as f:
         x = f.read("/input/pos")[:, :, 0].astype(np.float64)
     a, b = x[:3 * N1] - x[:3 * N1].mean(0), x[3 * N1:] - x[3 * N1:].mean(0)
-    # put the chains' facing extremes 6 A apart along x when B is moved by +L
-    gap = 6.0
-    a[:, 0] += L / 2 - 2.0 - a[:, 0].max()
-    b[:, 0] += (L / 2 - 2.0 + gap) - b[:, 0].min() - L
+    a[:, 0] += 35.0
+    b[:, 0] += 55.0 - L
     return path, np.concatenate([a, b]).astype(np.float32)
 
 
@@ -63,8 +62,9 @@ def test_large_box_changes_nothing(two_chains):
     _, e1, d1, ed1 = _eval(path, x, box=(1000.0, 1000.0, 1000.0))
     for g in GRAPHS:
         assert np.array_equal(ed0[g], ed1[g]), g
-    assert abs(e0 - e1) <= 1e-9 * max(1.0, abs(e0))
-    assert np.abs(d0 - d1).max() <= 1e-6 * np.abs(d0).max()
+    # energies and forces are sums whose atomic-add order varies from run to run
+    assert abs(e0 - e1) <= 1e-7 * max(1.0, abs(e0))
+    assert np.abs(d0 - d1).max() <= 1e-5 * np.abs(d0).max()
 
 
 def test_contact_across_the_face_equals_its_image(two_chains):
@@ -84,7 +84,9 @@ def test_contact_across_the_face_equals_its_image(two_chains):
     scale = max(1.0, abs(e_open), abs(e_far))
     assert abs(e_box - e_open) <= 1e-5 * scale, (e_box, e_open)
     assert abs(e_open - e_far) > 1e-3 * scale  # the contact matters
-    assert np.abs(d_box - d_open).max() <= 1e-4 * np.abs(d_open).max()
+    # the two configurations' FP32 coordinates of chain B differ by rounding
+    # (~4e-6 A at 55 A), which steep steric walls turn into ~1e-4 of max |F|
+    assert np.abs(d_box - d_open).max() <= 5e-4 * np.abs(d_open).max()
 
 
 def test_box_vector_shift_is_invisible(two_chains):
