@@ -92,10 +92,17 @@ def test_training_fits_a_teacher(built):
 
 def test_warm_start_sweeps_and_forces(built, capsys):
     """What the starts gain on proteins the network never saw, at the same
-    coordinates and the reference tolerance: the learned start (with its
-    per-system fallback) needs no more sweeps than the uniform start; the
-    previous solve's marginals (a perfect belief prediction) need clearly
-    fewer; every start gives the uniform-start forces to BP's tolerance."""
+    coordinates and the reference tolerance, and the fallback that follows.
+
+    Measured result (asserted, so that a network that does pay would show
+    here): the learned start does not save the 8 sweeps its kernels cost
+    (feature and MLP kernels on the rotamer node's critical path, about ten
+    sweeps of device time), so the per-system fallback keeps the uniform start
+    everywhere.  No start built from node marginals can pay at that price:
+    the previous solve's converged marginals at the same coordinates (a
+    perfect marginal prediction) save only about 5 sweeps.  The previous
+    solve's messages save far more; every start gives the uniform-start
+    forces to BP's tolerance."""
     import upside_gb300 as U
     import workloads
     from warm_start import WEIGHTS, load, sweeps_per_solve
@@ -112,6 +119,11 @@ def test_warm_start_sweeps_and_forces(built, capsys):
     b.set_warm_start(load(), 1)
     learned = sweeps_per_solve(b, 4)
     _, f_learned = b.evaluate()
+    # per system: mean sweeps from the learned start, from uniform, solves, known bits
+    ws = np.asarray(b.value_by_name("rotamer", "warm_stat", 4 * b.n_sys)).reshape(-1, 4)
+    both = (ws[:, 3].astype(int) & 3) == 3
+    assert both.all()  # both starts were measured on every system
+    raw_learned, raw_uniform = float(ws[:, 0].mean()), float(ws[:, 1].mean())
     b.set_warm_start(None, 2)
     b.evaluate()
     previous = sweeps_per_solve(b, 4)
@@ -121,10 +133,14 @@ def test_warm_start_sweeps_and_forces(built, capsys):
     reuse = sweeps_per_solve(b, 4)
     _, f_reuse = b.evaluate()
     with capsys.disabled():
-        print("\nBP sweeps per solve: uniform %.2f learned %.2f previous-marginals %.2f previous-messages %.2f"
-              % (uniform, learned, previous, reuse))
+        print("\nBP sweeps per solve: uniform %.2f learned start %.2f (with fallback %.2f) previous-marginals %.2f "
+              "previous-messages %.2f" % (uniform, raw_learned, learned, previous, reuse))
+    # the negative result: the learned start saves fewer than the 8 sweeps it costs ...
+    assert raw_learned + 8.0 > raw_uniform, (raw_learned, raw_uniform)
+    # ... so the fallback keeps the uniform start and costs nothing
     assert learned <= 1.05 * uniform, (learned, uniform)
-    assert previous < 0.85 * uniform, (previous, uniform)
+    # even perfect marginals save less than the network's price
+    assert 0.5 * uniform < previous < 0.85 * uniform and uniform - previous < 8.0, (previous, uniform)
     assert reuse < 0.5 * uniform, (reuse, uniform)
     for f in (f_learned, f_previous, f_reuse):
         rel = np.abs(f - f_uniform).max() / np.abs(f_uniform).max()
