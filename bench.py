@@ -208,8 +208,8 @@ def main():
                 "ms_per_step": 1e3 * n_res_total / rate, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded ff_2.1 proteins)",
                 "config": {"workload": a.workload, "systems": len(W["configs"]), "residues": n_res_total},
-                "cpu_baseline": {"value": rate, "unit": "residue-steps/s", "cores": cores, "kind": "port",
-                                 "sample": sample},
+                "cpu_baseline": dict({"value": rate, "unit": "residue-steps/s", "cores": cores, "kind": "port",
+                                      "sample": sample}, **cpu_fields(rate)),
                 "e2e": {"value": rate, "unit": "residue-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line))
         return
@@ -267,7 +267,8 @@ def main():
     if d.rank == 0 and d.world == 1 and not a.no_cpu_baseline:
         rate, cores, sample = cpu_port_rate(W["configs"], a.cpu_seconds, states=states)
         sample += ", from the same equilibrated state as the GPU run"
-        cpu = {"value": rate, "unit": "residue-steps/s", "cores": cores, "kind": "port", "sample": sample}
+        cpu = dict({"value": rate, "unit": "residue-steps/s", "cores": cores, "kind": "port", "sample": sample},
+                   **cpu_fields(rate))
     if d.rank != 0:
         return
     state_bytes = 2 * 12 * b.atom_total
@@ -379,6 +380,31 @@ def plain_single_rate(W, a, states, n_sample=6, rounds=8):
     return {"value": units / t, "unit": "residue-steps/s",
             "sample": "systems %s of the workload (%s residues), %d rounds each, one system per engine" % (
                 ",".join(map(str, idx)), ",".join(str(W["n_res"][i]) for i in idx), rounds)}
+
+
+def reference_over_port():
+    """Measured speed ratio of the reference engine to the restatement on one
+    x86 core (profiles/cpu_reference_vs_port.md, line 'ratio: R'), or None."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "cpu_reference_vs_port.md")) as f:
+            for line in f:
+                if line.startswith("ratio:"):
+                    return float(line.split(":", 1)[1])
+    except (OSError, ValueError):
+        pass
+    return None
+
+
+def cpu_fields(rate):
+    """Estimate of the reference engine's rate on the same cores from the
+    restatement's measured rate and the measured x86 ratio between them."""
+    r = reference_over_port()
+    if not r:
+        return {}
+    return {"reference_over_port_x86": r, "reference_estimate": rate * r,
+            "reference_estimate_note": "restatement rate x the reference/restatement speed ratio measured on one "
+                                       "x86 core (profiles/cpu_reference_vs_port.md); the reference cannot be "
+                                       "built on the GPU host"}
 
 
 def ncu_traffic(workload):
