@@ -885,13 +885,28 @@ __global__ void bp_pair_prob_kernel(DBP b) {
 // src/rotamer.cpp:259-281, :500-569; the marginals and Bethe free energy
 // src/rotamer.cpp:425-471.  Node beliefs (both buffers) and rotamer counts
 // live in shared memory; P and messages stay in global memory (L2-resident).
+// Division in the sweeps is multiplication by a reciprocal from the special
+// function unit (__fdividef, about 2 ulp), as the reference multiplies by its
+// approximate reciprocal refined once (rcp, src/Float4.h:225-238).
 __device__ __forceinline__ void renorm6(float* x, int n) {
     float s = 0.f;
 #pragma unroll
     for (int k = 0; k < 6; ++k) s += k < n ? x[k] : 0.f;
-    float inv = 1.f / s;
+    float inv = __fdividef(1.f, s);
 #pragma unroll
     for (int k = 0; k < 6; ++k) x[k] *= inv;
+}
+// Exact rescaling of a non-negative product by a power of two so that its
+// largest entry lies in [1, 2): keeps a running product of messages (each
+// summing to 1) away from underflow without a division or any rounding.
+__device__ __forceinline__ void rescale6(float* x) {
+    float m = fmaxf(fmaxf(fmaxf(x[0], x[1]), fmaxf(x[2], x[3])), fmaxf(x[4], x[5]));
+    const int e = (__float_as_int(m) >> 23) & 0xff;
+    if (e >= 1 && e <= 253) {
+        const float sc = __int_as_float((254 - e) << 23);  // 2^(127 - e)
+#pragma unroll
+        for (int k = 0; k < 6; ++k) x[k] *= sc;
+    }
 }
 
 // Where the solve's two message buffers live.  Global: b.msg + k ent_cap 8
@@ -951,7 +966,7 @@ __device__ __forceinline__ void bp_messages(const DBP& b, int e0, int e1, const 
         float omv[6] = {o0.x, o0.y, o0.z, o0.w, o1.x, o1.y};
         float cav[6];
 #pragma unroll
-        for (int k = 0; k < 6; ++k) cav[k] = k < nv ? ob[k] / (1e-10f + omv[k]) : 0.f;
+        for (int k = 0; k < 6; ++k) cav[k] = k < nv ? __fdividef(ob[k], 1e-10f + omv[k]) : 0.f;
         const float4* P4 = reinterpret_cast<const float4*>(b.P + size_t(f) * 36);
         float P[36];
 #pragma unroll
@@ -968,7 +983,7 @@ __device__ __forceinline__ void bp_messages(const DBP& b, int e0, int e1, const 
             mm[i] = i < nu ? acc : 0.f;
             sum += mm[i];
         }
-        float inv = 1.f / sum;
+        float inv = __fdividef(1.f, sum);
         float4* out;
         if (M.dsm) {
             int d = M.dst_table(b)[f - M.base];
@@ -1001,12 +1016,14 @@ __device__ __forceinline__ float bp_beliefs(const DBP& b, int r0, int lo, int hi
         int u = r0 + ul;
         int eb = OW.ok ? OW.rp[ul - lo] : b.row_ptr[u], ee = OW.ok ? OW.rp[ul - lo + 1] : min(b.row_ptr[u + 1], e1);
         float prod[6] = {1.f, 1.f, 1.f, 1.f, 1.f, 1.f};
-        // renormalised after every factor, so the product never underflows
-        // (each message sums to 1)
+        // rescaled by a power of two after every factor, so the product never
+        // underflows (each message sums to 1); the sum normalisation of the
+        // reference's running product (src/rotamer.cpp:538-539) is applied
+        // once, to the finished belief below: the scale cancels there
         auto fold = [&](const float* a) {
 #pragma unroll
             for (int k = 0; k < 6; ++k) prod[k] *= a[k];
-            renorm6(prod, n);
+            rescale6(prod);
         };
         int e = eb + q;
         for (; e + BP_LANES < ee; e += 2 * BP_LANES) {  // two loads in flight
@@ -1039,7 +1056,7 @@ __device__ __forceinline__ float bp_beliefs(const DBP& b, int r0, int lo, int hi
         if (mode == 1) {
             float mx = bl[0];
             for (int k = 1; k < n; ++k) mx = fmaxf(mx, bl[k]);
-            float inv = 1.f / mx;
+            float inv = __fdividef(1.f, mx);
 #pragma unroll
             for (int k = 0; k < 6; ++k) {
                 bl[k] = damp != 0.f ? (1.f - damp) * inv * bl[k] + damp * o[k] : inv * bl[k];
