@@ -248,6 +248,9 @@ def main():
         for nm, ms in sorted(b.profile(5), key=lambda x: -x[1])[:25]:
             print("%-48s %8.3f ms" % (nm, ms), file=sys.stderr)
     rounds_per_iter = b.timed_rounds()
+    # one untimed pass of the timing loop itself (graph with its event nodes,
+    # L2 flush buffer, event reads), so that the timed rounds start warm
+    b.bench(max(3, a.warmup), flush_l2=True)
     d.barrier()
     with Clocks(d.local) as clk:
         ms = b.bench(a.steps, flush_l2=True)

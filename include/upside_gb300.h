@@ -153,7 +153,7 @@ int ug_bench_kernel(UgBatch* b, double* stats);
  * Tuned: the candidate-cache buffer of the pair lists (1, 2, 3, 4, 6 times the
  * reference's 1 + 0.2 cutoff; results do not depend on it), then the BP
  * solve's blocks per system, lanes per node and threads per block, then the
- * number of streams the node graph is spread over (1, 2, 4, 8).  report
+ * number of streams the node graph is spread over (1, 2, 4, 8, 16).  report
  * receives '\n'-separated "setting\tms_per_round" lines and a final
  * "chosen\tsetting" line.  Returns the number of candidates tried (or -1). */
 int ug_autotune(UgBatch* b, int n_round, float dt, float timescale, char* report, int cap);

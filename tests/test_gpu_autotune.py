@@ -40,10 +40,10 @@ def test_autotune_restores_state_and_reports(syn_configs):
     b.run(10, use_graph=True, graph_rounds=5)
     x, m = b.get_pos(), b.get_mom()
     trials, chosen = b.autotune(2)
-    # 5 buffer scales, 9 BP variants, 4 stream counts, and when the two
+    # 5 buffer scales, 9 BP variants, 5 stream counts, and when the two
     # fastest BP variants are within 8%, both timed again
     finals = [k for k in trials if k.startswith("final_bp_variant_")]
-    assert len(trials) == 5 + 9 + 4 + len(finals) and len(finals) in (0, 2) and chosen
+    assert len(trials) == 5 + 9 + 5 + len(finals) and len(finals) in (0, 2) and chosen
     assert all(v > 0 for v in trials.values())
     assert np.array_equal(b.get_pos(), x) and np.array_equal(b.get_mom(), m)
     b.run(2, use_graph=True, graph_rounds=1)

@@ -3606,7 +3606,7 @@ std::vector<std::pair<std::string, float>> Engine::autotune(int n_round, float d
     }
     // concurrent node lanes (streams) of the evaluation
     int best_lanes = lanes0;
-    for (int ln : {1, 2, 4, 8}) {
+    for (int ln : {1, 2, 4, 8, 16}) {
         float ms = ln == lanes0 ? best_ms : trial(best_scale, best_variant, ln);
         report.emplace_back("node_streams=" + std::to_string(ln), ms);
         if (ms < best_ms) { best_ms = ms; best_lanes = ln; }
