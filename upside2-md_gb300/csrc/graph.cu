@@ -115,28 +115,54 @@ __device__ __forceinline__ float pair_d2(float4 a, float4 b, const float* box) {
     return __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
 }
 
+// Partner tiles in shared memory: a block takes 8 consecutive rows (one per
+// warp), and for the union of their candidate ranges loads tiles of 256
+// partners (position and id) into shared memory once; each warp then scans
+// the part of every tile that lies in its own row's range, in increasing j,
+// so the rows' hits come out in exactly the order of a warp scanning its
+// range alone.
+constexpr int PAIR_TILE = 256;
 template <int PASS, bool CACHED>
-__global__ void pair_kernel(DGraph g) {
+__global__ void __launch_bounds__(256) pair_kernel(DGraph g) {
     grid_dep_entry();
     if (CACHED && !*g.any_flag) return;  // no system rebuilt in this evaluation
-    int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    int lane = threadIdx.x & 31;
-    int n_warps = (gridDim.x * blockDim.x) >> 5;
+    __shared__ float4 s_x[PAIR_TILE];
+    __shared__ int s_id[PAIR_TILE];
+    __shared__ int s_lo, s_hi;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const float rc = CACHED ? g.cutoff + g.buffer : g.cutoff;
     const float c2 = rc * rc;
     const float4* X2 = g.symmetric ? g.x1 : g.x2;
     const int* ID2 = g.symmetric ? g.id1 : g.id2;
-    for (int r = warp; r < g.n_rows; r += n_warps) {
-        int i1s = g.row_i1[r], i1e = g.row_i1_end[r];
-        int sys = 0;
-        if (CACHED) {
-            sys = g.sys1[i1s];
-            if (!g.sys_flag[sys]) continue;  // warp-uniform
+    const int n_rb = (g.n_rows + 7) >> 3;
+    for (int rb = blockIdx.x; rb < n_rb; rb += gridDim.x) {  // block-uniform
+        const int r = rb * 8 + warp;
+        bool active = r < g.n_rows;
+        int i1s = 0, i1e = 0, sys = 0, i2s = 0, i2e = 0;
+        if (active) {
+            i1s = g.row_i1[r];
+            i1e = g.row_i1_end[r];
+            if (CACHED) {
+                sys = g.sys1[i1s];
+                active = g.sys_flag[sys] != 0;  // warp-uniform
+            }
+            i2s = g.row_i2[r];
+            i2e = g.row_i2_end[r];
         }
-        int i2s = g.row_i2[r], i2e = g.row_i2_end[r];
+        if (threadIdx.x == 0) {
+            s_lo = 0x7fffffff;
+            s_hi = -1;
+        }
+        __syncthreads();
+        if (active && lane == 0 && i2s < i2e) {
+            atomicMin(&s_lo, i2s);
+            atomicMax(&s_hi, i2e);
+        }
+        __syncthreads();
+        const int lo = s_lo, hi = s_hi;
         float4 a[4];
         int ida[4];
-        int nl = min(4, i1e - i1s);
+        const int nl = active ? min(4, i1e - i1s) : 0;
 #pragma unroll
         for (int l = 0; l < 4; ++l) {
             a[l] = l < nl ? g.x1[i1s + l] : make_float4(1e20f, 1e20f, 1e20f, 0.f);
@@ -144,7 +170,7 @@ __global__ void pair_kernel(DGraph g) {
         }
         int base = 0, lim = g.cap;
         int2* out = g.edges;
-        if (PASS) {
+        if (PASS && active) {
             if (CACHED) {
                 int seg = g.cache_off[sys];
                 base = seg + g.row_off[r] - g.row_off[g.sys_first_row[sys]];
@@ -155,43 +181,55 @@ __global__ void pair_kernel(DGraph g) {
             }
         }
         int count = 0;
-        for (int j0 = i2s; j0 < i2e; j0 += 32) {
-            int j = j0 + lane;
-            unsigned mask = 0;
-            if (j < i2e) {
-                float4 b = X2[j];
-                int idb = ID2[j];
-#pragma unroll
-                for (int l = 0; l < 4; ++l) {
-                    if (l >= nl) break;
-                    if (g.symmetric && !(i1s + l < j)) continue;
-                    if (pair_d2(a[l], b, g.box) < c2 && acceptable_ids(g.excl, ida[l], idb)) mask |= 1u << l;
-                }
+        for (int t0 = lo; t0 < hi; t0 += PAIR_TILE) {  // block-uniform (lo > hi when no row is active)
+            __syncthreads();  // the previous tile is consumed
+            const int jt = t0 + threadIdx.x;
+            if (jt < hi) {
+                s_x[threadIdx.x] = X2[jt];
+                s_id[threadIdx.x] = ID2[jt];
             }
-            int c = __popc(mask);
-            if (PASS == 0) {
-                count += c;
-            } else {
-                int incl = c;
+            __syncthreads();
+            if (!active) continue;
+            const int c0 = max(t0, i2s), c1 = min(t0 + PAIR_TILE, i2e);
+            for (int j0 = c0; j0 < c1; j0 += 32) {  // warp-uniform
+                const int j = j0 + lane;
+                unsigned mask = 0;
+                if (j < c1) {
+                    const float4 bx = s_x[j - t0];
+                    const int idb = s_id[j - t0];
 #pragma unroll
-                for (int o = 1; o < 32; o <<= 1) {
-                    int y = __shfl_up_sync(0xffffffffu, incl, o);
-                    if (lane >= o) incl += y;
-                }
-                int pos = base + incl - c;
-                for (int l = 0; l < 4; ++l)
-                    if (mask & (1u << l)) {
-                        if (pos < lim) out[pos] = make_int2(i1s + l, j);
-                        ++pos;
+                    for (int l = 0; l < 4; ++l) {
+                        if (l >= nl) break;
+                        if (g.symmetric && !(i1s + l < j)) continue;
+                        if (pair_d2(a[l], bx, g.box) < c2 && acceptable_ids(g.excl, ida[l], idb)) mask |= 1u << l;
                     }
-                base += __shfl_sync(0xffffffffu, incl, 31);
+                }
+                const int c = __popc(mask);
+                if (PASS == 0) {
+                    count += c;
+                } else {
+                    int incl = c;
+#pragma unroll
+                    for (int o = 1; o < 32; o <<= 1) {
+                        int y = __shfl_up_sync(0xffffffffu, incl, o);
+                        if (lane >= o) incl += y;
+                    }
+                    int pos = base + incl - c;
+                    for (int l = 0; l < 4; ++l)
+                        if (mask & (1u << l)) {
+                            if (pos < lim) out[pos] = make_int2(i1s + l, j);
+                            ++pos;
+                        }
+                    base += __shfl_sync(0xffffffffu, incl, 31);
+                }
             }
         }
-        if (PASS == 0) {
+        if (PASS == 0 && active) {
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) count += __shfl_xor_sync(0xffffffffu, count, o);
             if (lane == 0) g.row_count[r] = count;
         }
+        __syncthreads();  // s_lo / s_hi are reset for the next row block
     }
 }
 
@@ -360,7 +398,7 @@ void launch_pairs(const DGraph& g, cudaStream_t st) {
         cudaMemsetAsync(g.row_off, 0, sizeof(int), st);
         return;
     }
-    int blocks = min(4 * 152, (g.n_rows * 32 + 255) / 256);
+    int blocks = min(4 * 152, (g.n_rows + 7) / 8);
     if (!g.cached) {
         ug::launch((pair_kernel<0, false>), blocks, 256, 0, st, g);
         launch_scan(g.row_count, g.row_off, g.n_rows, g.n_edge, st);
