@@ -21,7 +21,9 @@ def build_oracle():
     deps = srcs + [os.path.join(HERE, "cpu_engine.h"), os.path.join(PKG_CSRC, "h5lite.h")]
     if os.path.exists(lib) and all(os.path.getmtime(lib) > os.path.getmtime(d) for d in deps):
         return lib
-    cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-I", PKG_CSRC, "-o", lib] + srcs
+    # no contraction into fused multiply-adds, so that the restatement
+    # rounds alike on every host (aarch64 compilers contract by default)
+    cmd = ["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fPIC", "-shared", "-I", PKG_CSRC, "-o", lib] + srcs
     r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
     if r.returncode:
         raise RuntimeError("oracle build failed:\n" + r.stdout)

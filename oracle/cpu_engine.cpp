@@ -1029,6 +1029,665 @@ template <class T> struct MembraneHBNode : Node<T> {
     }
 };
 
+// ---------------------------------------------------------------- surface --
+// Lipid-exposed residues of a membrane protein (Surface, src/surface.cpp:54-696).
+// Residues whose N, CA, C and CB all lie inside the slab |z| < half +
+// zbuffer are the TM residues.  For each of n_rotation turns about z (by
+// a * pi/2 / n_rotation about the TM CBs' xy centre) the atoms and their
+// auxiliary points (a circle of the atom radius in the yz and xz planes)
+// are put on a voxel grid; the outermost occupied voxels of each x- and
+// y-row (method 0), or those next to lipid voxels found by a layer-wise
+// flood fill from the grid border (method 1), are surface voxels; within
+// them a grid of n_smallgrid cells per voxel picks the outermost CB per
+// fine row, and each picked CB gets a share of a lateral force proportional
+// to the surface area.  Output per residue: the fraction of turns since the
+// residue was first picked, and the mean picked force (x, y) turned back.
+// The node is a discrete function of float roundings, so it runs in float
+// whatever T is, in the reference's order of operations.  Its state carries
+// over between evaluations as the reference's does: the TM list beyond the
+// current TM count and the forces of residues not in the slab keep the
+// values of earlier evaluations.  The node has no derivative
+// (src/surface.cpp:692-694).
+namespace surface_arith {
+// The steps whose rounding decides voxel membership, each rounded
+// separately in the reference's order of operations (the library is built
+// without contraction into fused multiply-adds).  Against the reference
+// engine on 138 random frames the surface fractions matched exactly and the
+// force columns to a few units in the last place, except for 3 frames where
+// one turn picked a different CB for a fine row; fused forms of the turns,
+// the auxiliary offsets and the grid origin, a centre summed in partial sums
+// and reciprocal products in place of the divisions changed none of that.
+inline float rot_x(float rx, float c, float s, float dx, float dy) {
+    float a = c * dx, b = rx + a, e = s * dy;
+    return b - e;
+}
+inline float rot_y(float ry, float c, float s, float dx, float dy) {
+    float a = s * dx, b = ry + a, e = c * dy;
+    return b + e;
+}
+inline float aux_add(float x, float a, float r) {
+    float d = a * r;
+    return x + d;
+}
+}  // namespace surface_arith
+
+struct SurfaceCore {
+    int method = 1, n_rot = 0, n_aux = 0, ngz = 0, snx = 1, sny = 1, snz = 1, n_res = 0;
+    float half = 0, zbuf = 0, radius = 0, tm_min = 0, tm_max = 0, gx = 0, gy = 0, gz = 0, r_gz = 0, r_nrot = 0;
+    vector<int> index_cb, used, tm_list;
+    vector<float> aux, sfx, sfy, cp, sp, cm, sm;
+    struct Vox {
+        int nx, ny, nz;
+        vector<int> v;
+        int& at(int i, int j, int k) {
+            if (i < 0 || j < 0 || k < 0 || i >= nx || j >= ny || k >= nz) throw Err("surface voxel out of the grid");
+            return v[(size_t(i) * ny + j) * nz + k];
+        }
+    };
+    void init(const H5& h) {
+        method = int(h.attr("method_type"));
+        if (method != 0 && method != 1) throw Err("surface method_type must be 0 or 1");
+        index_cb = h.ri("index_cb");
+        n_res = int(index_cb.size());
+        n_rot = int(h.attr("n_rotation"));
+        if (n_rot < 1) throw Err("surface needs n_rotation >= 1");
+        auto ad = h.dims("auxiliary_point");
+        if (ad.size() != 2 || ad[1] != 2) throw Err("auxiliary_point must be (n_aux, 2)");
+        n_aux = int(ad[0]);
+        aux = h.rf<float>("auxiliary_point");
+        r_nrot = float(1. / n_rot);
+        float dangle = float(0.5 * double(3.141592653589793f) * double(r_nrot));
+        half = float(h.attr("half_thickness"));
+        zbuf = float(h.attr("zbuffer"));
+        radius = float(h.attr("atom_radius"));
+        tm_min = -half - zbuf;
+        tm_max = half + zbuf;
+        ngz = int(h.attr("n_gridz"));
+        if (ngz < 2) throw Err("surface needs n_gridz >= 2");
+        gx = float(h.attr("len_gridx"));
+        gy = float(h.attr("len_gridy"));
+        float ext = tm_max - tm_min;
+        ext = ext + 2 * radius;
+        gz = float((double(ext) + 0.1) / ngz);
+        r_gz = 1.f / gz;
+        snx = int(h.attr("n_smallgridx"));
+        sny = int(h.attr("n_smallgridy"));
+        snz = int(h.attr("n_smallgridz"));
+        if (snx < 1 || sny < 1 || snz < 1) throw Err("surface small grids need >= 1 cell");
+        int excl = int(h.attr("exclusion"));
+        if (excl == 1) used = h.ri("included_list");
+        else {
+            used.resize(size_t(n_res));
+            for (int i = 0; i < n_res; ++i) used[size_t(i)] = i;
+        }
+        for (int r : used)
+            if (r < 0 || r >= n_res) throw Err("surface included_list entry out of range");
+        tm_list.assign(used.size(), 0);
+        sfx.assign(size_t(n_res), 0.f);
+        sfy.assign(size_t(n_res), 0.f);
+        step = dangle;
+    }
+    float step = 0.f;
+    void angles() {
+        cp.clear(); sp.clear(); cm.clear(); sm.clear();
+        for (int a = 0; a < n_rot; ++a) {
+            float ang = float(a) * step;
+            cp.push_back(std::cos(ang));
+            sp.push_back(std::sin(ang));
+            cm.push_back(std::cos(-ang));
+            sm.push_back(std::sin(-ang));
+        }
+    }
+    static void rotate(vector<float>& x, vector<float>& y, float rx, float ry, float c, float s, int n) {
+        for (int i = 0; i < n; ++i) {
+            float dx = x[size_t(i)] - rx, dy = y[size_t(i)] - ry;
+            if (dx == 0 && dy == 0) continue;
+            x[size_t(i)] = surface_arith::rot_x(rx, c, s, dx, dy);
+            y[size_t(i)] = surface_arith::rot_y(ry, c, s, dx, dy);
+        }
+    }
+    static void minmax(const vector<float>& x, int n, bool init, float& mn, float& mx) {
+        for (int i = 0; i < n; ++i) {
+            float v = x[size_t(i)];
+            if (!init) { mn = mx = v; init = true; }
+            else if (v > mx) mx = v;
+            else if (v < mn) mn = v;
+        }
+    }
+    // pos(atom, d): float coordinate d of row `atom` of the concatenated
+    // backbone + CB positions; out: n_res x 3
+    template <class P> void compute(P pos, float* out) {
+        using surface_arith::aux_add;
+        angles();
+        int n_tm = 0;
+        for (int nr : used) {
+            auto in = [&](int row) { float z = pos(row, 2); return z < tm_max && z > tm_min; };
+            if (in(nr * 3) && in(nr * 3 + 1) && in(nr * 3 + 2) && in(index_cb[size_t(nr)])) tm_list[size_t(n_tm++)] = nr;
+        }
+        vector<int> tc(static_cast<size_t>(n_res), 0), surf_cb(static_cast<size_t>(n_tm), 0);
+        const size_t nt = static_cast<size_t>(n_tm);
+        vector<float> bbx(3 * nt), bby(3 * nt), bbz(3 * nt), cbx(nt), cby(nt), cbz(nt), fx(nt), fy(nt);
+        for (int ii = 0; ii < n_tm; ++ii) {
+            int nr = tm_list[size_t(ii)];
+            for (int j = 0; j < 3; ++j) {
+                bbx[size_t(ii * 3 + j)] = pos(nr * 3 + j, 0);
+                bby[size_t(ii * 3 + j)] = pos(nr * 3 + j, 1);
+                bbz[size_t(ii * 3 + j)] = pos(nr * 3 + j, 2);
+            }
+            cbx[size_t(ii)] = pos(index_cb[size_t(nr)], 0);
+            cby[size_t(ii)] = pos(index_cb[size_t(nr)], 1);
+            cbz[size_t(ii)] = pos(index_cb[size_t(nr)], 2);
+            sfx[size_t(nr)] = 0.f;
+            sfy[size_t(nr)] = 0.f;
+        }
+        float cx = 0.f, cy = 0.f;
+        for (int i = 0; i < n_tm; ++i) { cx += cbx[size_t(i)]; cy += cby[size_t(i)]; }
+        cx /= float(n_tm);
+        cy /= float(n_tm);
+        for (int a = 0; a < n_rot; ++a) {
+            rotate(cbx, cby, cx, cy, cp[size_t(a)], sp[size_t(a)], n_tm);
+            // only the first n_tm backbone entries turn (src/surface.cpp:240)
+            rotate(bbx, bby, cx, cy, cp[size_t(a)], sp[size_t(a)], n_tm);
+            float minx = 0.f, maxx = 0.f, miny = 0.f, maxy = 0.f;
+            minmax(bbx, 3 * n_tm, false, minx, maxx);
+            minmax(cbx, n_tm, true, minx, maxx);
+            minmax(bby, 3 * n_tm, false, miny, maxy);
+            minmax(cby, n_tm, true, miny, maxy);
+            minx -= radius; maxx += radius; miny -= radius; maxy += radius;
+            float lenx = maxx - minx, leny = maxy - miny;
+            int ngx = int((double(lenx) + 0.1) / double(gx)) + 3;
+            int ngy = int((double(leny) + 0.1) / double(gy)) + 3;
+            int ngz_ = ngz;
+            float blx = float(ngx) * gx, bly = float(ngy) * gy;
+            float side[3], s1[3], s2[3];
+            float hx = 0.5f * (blx - lenx), hy = 0.5f * (bly - leny);
+            side[0] = minx - hx;
+            side[1] = miny - hy;
+            side[2] = tm_min - radius;
+            s1[0] = float(ngx) / blx; s1[1] = float(ngy) / bly; s1[2] = r_gz;
+            s2[0] = float(snx * ngx) / blx; s2[1] = float(sny * ngy) / bly; s2[2] = float(snz) * r_gz;
+            auto cell = [&](float x, float y, float z, const float* sc, int v[3]) {
+                float p[3] = {x, y, z};
+                for (int d = 0; d < 3; ++d) {
+                    float t = p[d] - side[d];
+                    v[d] = int(std::floor(t * sc[d]));
+                }
+            };
+            Vox V{ngx, ngy, ngz_, vector<int>(size_t(ngx) * ngy * ngz_, -1)};
+            vector<int> vid(size_t(4 * n_tm) * 3);
+            auto mark_atom = [&](float x, float y, float z, int iv) {
+                int v[3];
+                cell(x, y, z, s1, v);
+                for (int d = 0; d < 3; ++d) vid[size_t(iv) * 3 + d] = v[d];
+                V.at(v[0], v[1], v[2]) = 1;
+                for (int j = 0; j < n_aux; ++j) {
+                    float ax = aux[size_t(2 * j)], az = aux[size_t(2 * j + 1)];
+                    cell(x + 0.0f, aux_add(y, ax, radius), aux_add(z, az, radius), s1, v);
+                    V.at(v[0], v[1], v[2]) = 1;
+                }
+                for (int j = 0; j < n_aux; ++j) {
+                    float ax = aux[size_t(2 * j)], az = aux[size_t(2 * j + 1)];
+                    cell(aux_add(x, ax, radius), y + 0.0f, aux_add(z, az, radius), s1, v);
+                    V.at(v[0], v[1], v[2]) = 1;
+                }
+            };
+            for (int nr = 0; nr < n_tm; ++nr) {
+                for (int i = 0; i < 3; ++i)
+                    mark_atom(bbx[size_t(nr * 3 + i)], bby[size_t(nr * 3 + i)], bbz[size_t(nr * 3 + i)], nr * 4 + i);
+                mark_atom(cbx[size_t(nr)], cby[size_t(nr)], cbz[size_t(nr)], nr * 4 + 3);
+            }
+            int nxz = ngx * ngz_, nyz = ngy * ngz_;
+            if (method == 0) {
+                int big = ngx * ngy * ngz_;
+                vector<int> xmn(size_t(nyz), big), xmx(size_t(nyz), -1), ymn(size_t(nxz), big), ymx(size_t(nxz), -1);
+                for (int i = 0; i < ngx; ++i)
+                    for (int j = 0; j < ngy; ++j)
+                        for (int k = 0; k < ngz_; ++k)
+                            if (V.at(i, j, k) == 1) {
+                                int ik = i * ngz_ + k, jk = j * ngz_ + k;
+                                xmn[size_t(jk)] = std::min(xmn[size_t(jk)], i);
+                                xmx[size_t(jk)] = std::max(xmx[size_t(jk)], i);
+                                ymn[size_t(ik)] = std::min(ymn[size_t(ik)], j);
+                                ymx[size_t(ik)] = std::max(ymx[size_t(ik)], j);
+                            }
+                for (int jk = 0; jk < nyz; ++jk) {
+                    int j = jk / ngz_, k = jk % ngz_;
+                    if (xmn[size_t(jk)] < big) V.at(xmn[size_t(jk)], j, k) += 10;
+                    if (xmx[size_t(jk)] > -1) V.at(xmx[size_t(jk)], j, k) += 100;
+                }
+                for (int ik = 0; ik < nxz; ++ik) {
+                    int i = ik / ngz_, k = ik % ngz_;
+                    if (ymn[size_t(ik)] < big) V.at(i, ymn[size_t(ik)], k) += 1000;
+                    if (ymx[size_t(ik)] > -1) V.at(i, ymx[size_t(ik)], k) += 10000;
+                }
+            } else {
+                for (int k = 0; k < ngz_; ++k) {
+                    for (int i = 0; i < ngx; ++i) { V.at(i, 0, k) = 0; V.at(i, ngy - 1, k) = 0; }
+                    for (int j = 0; j < ngy; ++j) { V.at(0, j, k) = 0; V.at(ngx - 1, j, k) = 0; }
+                }
+                // empty voxels next (3 x 3 in the layer) to a lipid voxel become
+                // lipid until none changes; the tail layers also want the
+                // neighbour's voxel in the layer towards the head group lipid.
+                // The result is the closure, whatever the order of visits.
+                auto fill = [&](int k, int kref) {
+                    bool changed = true;
+                    while (changed) {
+                        changed = false;
+                        for (int i = 1; i < ngx - 1; ++i)
+                            for (int j = 1; j < ngy - 1; ++j) {
+                                if (V.at(i, j, k) != -1) continue;
+                                bool hit = false;
+                                for (int ii = i - 1; ii < i + 2 && !hit; ++ii)
+                                    for (int jj = j - 1; jj < j + 2 && !hit; ++jj)
+                                        hit = V.at(ii, jj, k) == 0 && (kref < 0 || V.at(ii, jj, kref) == 0);
+                                if (hit) { V.at(i, j, k) = 0; changed = true; }
+                            }
+                    }
+                };
+                fill(0, -1);
+                fill(ngz_ - 1, -1);
+                for (int k = 1; k < ngz_ / 2; ++k) fill(k, k - 1);
+                // the top layer was closed above; the reference's second pass
+                // over it (reading one layer past the grid) converts nothing
+                for (int k = ngz_ - 2; k >= ngz_ / 2; --k) fill(k, k + 1);
+                for (int i = 1; i < ngx - 1; ++i)
+                    for (int j = 1; j < ngy - 1; ++j)
+                        for (int k = 0; k < ngz_; ++k)
+                            if (V.at(i, j, k) > 0) {
+                                int add = 0;
+                                if (V.at(i - 1, j, k) == 0) add += 10;
+                                if (V.at(i + 1, j, k) == 0) add += 100;
+                                if (V.at(i, j - 1, k) == 0) add += 1000;
+                                if (V.at(i, j + 1, k) == 0) add += 10000;
+                                V.at(i, j, k) += add;
+                            }
+            }
+            int big = ngx * snx + ngy * sny + ngz_ * snz;
+            int zs = ngz_ * snz;
+            size_t nfx = size_t(sny * snz) * size_t(nyz), nfy = size_t(snx * snz) * size_t(nxz);
+            vector<int> fxmn(nfx, big), fxmx(nfx, -1), fymn(nfy, big), fymx(nfy, -1);
+            vector<int> ixmn(nfx, -1), ixmx(nfx, -1), iymn(nfy, -1), iymx(nfy, -1);
+            auto at_fx = [&](vector<int>& a, int idx) -> int& {
+                if (idx < 0 || size_t(idx) >= a.size()) throw Err("surface fine row out of the grid");
+                return a[size_t(idx)];
+            };
+            auto labels = [&](int iv, int& v2, int& v3, int& v4, int& v5) {
+                int t = V.at(vid[size_t(iv) * 3], vid[size_t(iv) * 3 + 1], vid[size_t(iv) * 3 + 2]);
+                v5 = t / 10000;
+                v4 = (t % 10000) / 1000;
+                v3 = ((t % 10000) % 1000) / 100;
+                v2 = (((t % 10000) % 1000) % 100) / 10;
+                return t;
+            };
+            // surface backbone atoms and the auxiliary points of surface
+            // backbone atoms and CBs widen the fine extremes
+            auto widen = [&](float x, float y, float z, int iv, bool self) {
+                int v2, v3, v4, v5;
+                if (labels(iv, v2, v3, v4, v5) <= 1) return;
+                int q[3];
+                cell(x, y, z, s2, q);
+                if (self) {
+                    int kj = q[1] * zs + q[2], ki = q[0] * zs + q[2];
+                    if (v2 == 1 && q[0] < at_fx(fxmn, kj)) fxmn[size_t(kj)] = q[0];
+                    if (v3 == 1 && q[0] > at_fx(fxmx, kj)) fxmx[size_t(kj)] = q[0];
+                    if (v4 == 1 && q[1] < at_fx(fymn, ki)) fymn[size_t(ki)] = q[1];
+                    if (v5 == 1 && q[1] > at_fx(fymx, ki)) fymx[size_t(ki)] = q[1];
+                }
+                for (int j = 0; j < n_aux; ++j) {
+                    float ax = aux[size_t(2 * j)], az = aux[size_t(2 * j + 1)];
+                    int a[3];
+                    cell(x + 0.0f, aux_add(y, ax, radius), aux_add(z, az, radius), s2, a);
+                    int kj = a[1] * zs + q[2];
+                    if (v2 == 1 && a[0] < at_fx(fxmn, kj)) fxmn[size_t(kj)] = a[0];
+                    if (v3 == 1 && a[0] > at_fx(fxmx, kj)) fxmx[size_t(kj)] = a[0];
+                }
+                for (int j = 0; j < n_aux; ++j) {
+                    float ax = aux[size_t(2 * j)], az = aux[size_t(2 * j + 1)];
+                    int a[3];
+                    cell(aux_add(x, ax, radius), y + 0.0f, aux_add(z, az, radius), s2, a);
+                    int ki = a[0] * zs + q[2];
+                    if (v4 == 1 && a[1] < at_fx(fymn, ki)) fymn[size_t(ki)] = a[1];
+                    if (v5 == 1 && a[1] > at_fx(fymx, ki)) fymx[size_t(ki)] = a[1];
+                }
+            };
+            for (int nr = 0; nr < n_tm; ++nr)
+                for (int i = 0; i < 3; ++i)
+                    widen(bbx[size_t(nr * 3 + i)], bby[size_t(nr * 3 + i)], bbz[size_t(nr * 3 + i)], nr * 4 + i, true);
+            for (int nr = 0; nr < n_tm; ++nr) widen(cbx[size_t(nr)], cby[size_t(nr)], cbz[size_t(nr)], nr * 4 + 3, false);
+            // the outermost surface CB of each fine row (the last in residue
+            // order on ties)
+            for (int nr = 0; nr < n_tm; ++nr) {
+                int v2, v3, v4, v5;
+                if (labels(nr * 4 + 3, v2, v3, v4, v5) <= 1) continue;
+                int q[3];
+                cell(cbx[size_t(nr)], cby[size_t(nr)], cbz[size_t(nr)], s2, q);
+                int kj = q[1] * zs + q[2], ki = q[0] * zs + q[2];
+                if (v2 == 1 && q[0] <= at_fx(fxmn, kj)) { fxmn[size_t(kj)] = q[0]; ixmn[size_t(kj)] = nr; }
+                if (v3 == 1 && q[0] >= at_fx(fxmx, kj)) { fxmx[size_t(kj)] = q[0]; ixmx[size_t(kj)] = nr; }
+                if (v4 == 1 && q[1] <= at_fx(fymn, ki)) { fymn[size_t(ki)] = q[1]; iymn[size_t(ki)] = nr; }
+                if (v5 == 1 && q[1] >= at_fx(fymx, ki)) { fymx[size_t(ki)] = q[1]; iymx[size_t(ki)] = nr; }
+            }
+            int n_xmn = 0, n_xmx = 0, n_ymn = 0, n_ymx = 0, c_xmn = 0, c_xmx = 0, c_ymn = 0, c_ymx = 0;
+            for (int v : fxmn) n_xmn += v < big;
+            for (int v : fxmx) n_xmx += v > -1;
+            for (int v : fymn) n_ymn += v < big;
+            for (int v : fymx) n_ymx += v > -1;
+            for (int v : ixmn) c_xmn += v > -1;
+            for (int v : ixmx) c_xmx += v > -1;
+            for (int v : iymn) c_ymn += v > -1;
+            for (int v : iymx) c_ymx += v > -1;
+            float area_xz = gx / float(snx) * gz / float(snz);
+            float area_yz = gy / float(sny) * gz / float(snz);
+            float a_xmn = float(n_xmn) * area_yz, a_xmx = float(n_xmx) * area_yz;
+            float a_ymn = float(n_ymn) * area_xz, a_ymx = float(n_ymx) * area_xz;
+            float ax_ = a_xmn > a_xmx ? a_xmn : a_xmx;
+            float ay_ = a_ymn > a_ymx ? a_ymn : a_ymx;
+            float tfx = float(double(ax_) * 2.428602e-5), tfy = float(double(ay_) * 2.428602e-5);
+            float f_xmn = tfx / float(c_xmn), f_xmx = tfx / float(c_xmx);
+            float f_ymn = tfy / float(c_ymn), f_ymx = tfy / float(c_ymx);
+            std::fill(fx.begin(), fx.end(), 0.f);
+            std::fill(fy.begin(), fy.end(), 0.f);
+            for (int nr : ixmn) if (nr >= 0) { surf_cb[size_t(nr)] = 1; fx[size_t(nr)] = f_xmn; }
+            for (int nr : ixmx) if (nr >= 0) { surf_cb[size_t(nr)] = 1; fx[size_t(nr)] -= f_xmx; }
+            for (int nr : iymn) if (nr >= 0) { surf_cb[size_t(nr)] = 1; fy[size_t(nr)] = f_ymn; }
+            for (int nr : iymx) if (nr >= 0) { surf_cb[size_t(nr)] = 1; fy[size_t(nr)] -= f_ymx; }
+            for (int ns = 0; ns < n_tm; ++ns)
+                if (surf_cb[size_t(ns)]) tc[size_t(tm_list[size_t(ns)])] += 1;
+            for (int i = 0; i < n_tm; ++i) {
+                float f0 = fx[size_t(i)], f1 = fy[size_t(i)];
+                if (f0 == 0 && f1 == 0) continue;
+                fx[size_t(i)] = surface_arith::rot_x(0.f, cm[size_t(a)], sm[size_t(a)], f0, f1);
+                fy[size_t(i)] = surface_arith::rot_y(0.f, cm[size_t(a)], sm[size_t(a)], f0, f1);
+            }
+            rotate(cbx, cby, cx, cy, cm[size_t(a)], sm[size_t(a)], n_tm);
+            rotate(bbx, bby, cx, cy, cm[size_t(a)], sm[size_t(a)], n_tm);
+            for (int ns = 0; ns < n_tm; ++ns) {
+                if (!surf_cb[size_t(ns)]) continue;
+                int nr = tm_list[size_t(ns)];
+                sfx[size_t(nr)] += fx[size_t(ns)];
+                sfy[size_t(nr)] += fy[size_t(ns)];
+            }
+        }
+        // every entry of the TM list, including those left from earlier
+        // evaluations beyond the current count (src/surface.cpp:676-680)
+        for (int nr : tm_list) {
+            if (tc[size_t(nr)] <= 0) continue;
+            sfx[size_t(nr)] /= float(tc[size_t(nr)]);
+            sfy[size_t(nr)] /= float(tc[size_t(nr)]);
+        }
+        for (int nr = 0; nr < n_res; ++nr) {
+            out[3 * nr] = tc[size_t(nr)] > 0 ? float(tc[size_t(nr)]) * r_nrot : 0.f;
+            out[3 * nr + 1] = sfx[size_t(nr)];
+            out[3 * nr + 2] = sfy[size_t(nr)];
+        }
+    }
+};
+
+template <class T> struct SurfaceNode : Node<T> {
+    SurfaceCore S;
+    SurfaceNode(const H5& h) {
+        S.init(h);
+        this->alloc(S.n_res, 3);
+    }
+    void forward(Engine<T>& e, bool) override {
+        auto& p = e.arg(*this, 0);
+        if (p.width < 3) throw Err("surface needs coordinates of width 3");
+        for (int i = 0; i < S.n_res; ++i)
+            if (S.index_cb[size_t(i)] < 0 || S.index_cb[size_t(i)] >= p.n_elem || 3 * i + 2 >= p.n_elem)
+                throw Err("surface index_cb out of range");
+        vector<float> out(size_t(S.n_res) * 3);
+        S.compute([&](int row, int d) { return float(p.out[size_t(row) * p.width + d]); }, out.data());
+        for (size_t i = 0; i < out.size(); ++i) this->out[i] = T(out[i]);
+    }
+};
+
+// CB membrane energy with the surface score (MembraneSurfCBPotential,
+// src/membrane_potential.cpp:674-983): as cb_membrane_potential, but inside
+// the slab every burial bin but the first weights its depth spline by the
+// residue's surface score s and adds the residue type's inner spline with
+// weight 1 - s (outside the slab, bins past the first use s = 1)
+template <class T> struct MembraneSurfCBNode : Node<T> {
+    vector<int> cb_index, res_type;
+    vector<T> weights, bl_nodes, coeff, coeff_inner;
+    int n_restype, n_bl, n_node;
+    T bl_sharp, lr_node, lr_sharp, radius, sign, z0, zs, half;
+    bool curved;
+    MembraneSurfCBNode(const H5& h) {
+        this->potential_node = true;
+        cb_index = h.ri("cb_index");
+        res_type = h.ri("res_type");
+        weights = h.rf<T>("weights");
+        bl_nodes = h.rf<T>("bl_nodes");
+        auto d = h.dims("coeff");
+        if (d.size() != 3) throw Err("coeff must be (n_restype, n_bl, n_node)");
+        n_restype = int(d[0]); n_bl = int(d[1]); n_node = int(d[2]);
+        auto di = h.dims("coeff_inner");
+        if (di.size() != 2 || int(di[0]) != n_restype || int(di[1]) != n_node)
+            throw Err("coeff_inner must be (n_restype, n_node)");
+        if (int(bl_nodes.size()) != n_bl - 1) throw Err("bl_nodes must have n_bl - 1 entries");
+        if (res_type.size() != cb_index.size()) throw Err("res_type needs one entry per cb_index");
+        coeff = h.rf<T>("coeff");
+        coeff_inner = h.rf<T>("coeff_inner");
+        bl_sharp = T(float(h.attr("bl_range_sharpness")));
+        lr_node = T(float(h.attr("left_right_node")));
+        lr_sharp = T(float(h.attr("left_right_sharpness")));
+        curved = h.attr("use_curvature") != 0;
+        radius = T(float(h.attr("curvature_radius")));
+        sign = T(float(h.attr("curvature_sign")));
+        z0 = T(float(h.attr("z_start")));
+        zs = T(float(h.attr("z_scale")));
+        half = T(float(h.attr("half_thickness")));
+    }
+    void forward(Engine<T>& e, bool energy) override {
+        auto& cb = e.arg(*this, 0);
+        auto& env = e.arg(*this, 1);
+        auto& sf = e.arg(*this, 2);
+        auto& cc = e.arg(*this, 3);
+        radius = cc.out[2] * T(-1) * sign;
+        T pot = 0;
+        const size_t nb = static_cast<size_t>(n_bl);
+        vector<T> s1(nb), ds1(nb), s2(nb), ds2(nb), bs(nb), dbs(nb);
+        for (size_t nr = 0; nr < cb_index.size(); ++nr) {
+            int rt = res_type[nr], ri = cb_index[nr];
+            T bl = 0;
+            for (int a = 0; a < n_restype; ++a) bl += weights[size_t(a)] * env.out[size_t(ri) * n_restype + a];
+            for (int i = 0; i < n_bl - 1; ++i) {
+                T v, dd;
+                compact_sigmoid(bl - bl_nodes[size_t(i)], bl_sharp, v, dd);
+                s1[size_t(i)] = v; ds1[size_t(i)] = dd;
+                compact_sigmoid(bl_nodes[size_t(i)] - bl, bl_sharp, v, dd);
+                s2[size_t(i)] = v; ds2[size_t(i)] = -dd;
+            }
+            bs[0] = s1[0]; dbs[0] = ds1[0];
+            bs[nb - 1] = s2[nb - 2]; dbs[nb - 1] = ds2[nb - 2];
+            for (int i = 0; i < n_bl - 2; ++i) {
+                bs[size_t(i + 1)] = s2[size_t(i)] * s1[size_t(i + 1)];
+                dbs[size_t(i + 1)] = ds2[size_t(i)] * s1[size_t(i + 1)] + s2[size_t(i)] * ds1[size_t(i + 1)];
+            }
+            T* x = &cb.out[size_t(ri) * cb.width];
+            T gz[3];
+            T z = membrane_depth(x, &cc.out[0], curved, sign, radius, gz);
+            T sl, dsl;
+            compact_sigmoid(z - lr_node, lr_sharp, sl, dsl);
+            T ll = sl, lr = T(1) - sl, dll = dsl, dlr = -dsl;
+            T cl = (z - z0) * zs, cr = (-z - z0) * zs;
+            T dz = 0, dbl = 0;
+            for (int i = 0; i < n_bl; ++i) {
+                T sv = (i > 0 && (z > half || z < -half)) ? T(1) : sf.out[size_t(ri) * sf.width];
+                const T* c = &coeff[(size_t(rt) * n_bl + size_t(i)) * n_node];
+                T v, dv;
+                clamped(c, cl, n_node, v, dv);
+                T fl = v * sv, dfl = dv * zs * sv;
+                clamped(c, cr, n_node, v, dv);
+                T fr = v * sv, dfr = -dv * sv * zs;
+                if (sv < T(1)) {
+                    const T* ci = &coeff_inner[size_t(rt) * n_node];
+                    clamped(ci, cl, n_node, v, dv);
+                    fl += v * (T(1) - sv);
+                    dfl += dv * (T(1) - sv) * zs;
+                    clamped(ci, cr, n_node, v, dv);
+                    fr += v * (T(1) - sv);
+                    dfr -= dv * (T(1) - sv) * zs;
+                }
+                T fs = ll * fl + lr * fr;
+                T dfs = ll * dfl + dll * fl + lr * dfr + dlr * fr;
+                pot += bs[size_t(i)] * fs;
+                dbl += dbs[size_t(i)] * fs;
+                dz += bs[size_t(i)] * dfs;
+            }
+            T* xs = &cb.sens[size_t(ri) * cb.width];
+            for (int k = 0; k < 3; ++k) xs[k] += dz * gz[k];
+            for (int a = 0; a < n_restype; ++a) env.sens[size_t(ri) * n_restype + a] += weights[size_t(a)] * dbl;
+        }
+        this->pot = energy ? pot : T(0);
+    }
+};
+
+// backbone H/O membrane energy with the surface score
+// (MembraneSurfHBPotential, src/membrane_potential.cpp:989-1259): the
+// bonded / free splines of hb_membrane_potential weighted by
+// outer = s * compact_sigmoid(burial - 2.5, 2) of the residue, plus the
+// inner tables weighted by 1 - outer (s = 1 outside the slab)
+template <class T> struct MembraneSurfHBNode : Node<T> {
+    vector<int> hb_index, hb_type, hb_res;
+    vector<T> weights, coeff, coeff_inner;
+    int n_node, n_restype;
+    T lr_node, lr_sharp, radius, sign, z0, zs, half;
+    bool curved;
+    MembraneSurfHBNode(const H5& h) {
+        this->potential_node = true;
+        hb_index = h.ri("hb_index");
+        hb_type = h.ri("hb_type");
+        hb_res = h.ri("hb_res");
+        if (hb_type.size() != hb_index.size() || hb_res.size() != hb_index.size())
+            throw Err("hb_type and hb_res need one entry per hb_index");
+        weights = h.rf<T>("weights");
+        n_restype = int(weights.size());
+        auto d = h.dims("coeff");
+        if (d.size() != 3 || d[0] != 2 || d[1] != 2) throw Err("coeff must be (2, 2, n_node)");
+        n_node = int(d[2]);
+        auto di = h.dims("coeff_inner");
+        if (di.size() != 3 || di[0] != 2 || di[1] != 2 || int(di[2]) != n_node)
+            throw Err("coeff_inner must be (2, 2, n_node)");
+        coeff = h.rf<T>("coeff");
+        coeff_inner = h.rf<T>("coeff_inner");
+        lr_node = T(float(h.attr("left_right_node")));
+        lr_sharp = T(float(h.attr("left_right_sharpness")));
+        curved = h.attr("use_curvature") != 0;
+        radius = T(float(h.attr("curvature_radius")));
+        sign = T(float(h.attr("curvature_sign")));
+        z0 = T(float(h.attr("z_start")));
+        zs = T(float(h.attr("z_scale")));
+        half = T(float(h.attr("half_thickness")));
+    }
+    void forward(Engine<T>& e, bool energy) override {
+        auto& hb = e.arg(*this, 0);
+        auto& env = e.arg(*this, 1);
+        auto& sf = e.arg(*this, 2);
+        auto& cc = e.arg(*this, 3);
+        radius = cc.out[2] * T(-1) * sign;
+        T pot = 0;
+        for (size_t nv = 0; nv < hb_index.size(); ++nv) {
+            int rt = hb_type[nv], ri = hb_index[nv], rr = hb_res[nv];
+            T* x = &hb.out[size_t(ri) * hb.width];
+            T* xs = &hb.sens[size_t(ri) * hb.width];
+            T gz[3];
+            T z = membrane_depth(x, &cc.out[0], curved, sign, radius, gz);
+            T bl = 0;
+            for (int a = 0; a < n_restype; ++a) bl += weights[size_t(a)] * env.out[size_t(rr) * n_restype + a];
+            T sb, dsb;
+            compact_sigmoid(bl - T(2.5), T(2), sb, dsb);
+            T sv = sf.out[size_t(rr) * sf.width];
+            if (z > half || z < -half) sv = T(1);
+            T outer = sv * sb, d_outer = sv * dsb, inner = T(1) - outer, d_inner = -d_outer;
+            T p = x[6], u = T(1) - p, w1 = u * u, w2 = T(1) - w1;
+            T f1, df1, f2, df2, dZ = 0, dHB = 0, dBL = 0;
+            if (outer > T(0)) {
+                mirrored_spline(&coeff[size_t(rt) * 2 * n_node], n_node, z, z0, zs, lr_node, lr_sharp, f1, df1);
+                mirrored_spline(&coeff[(size_t(rt) * 2 + 1) * n_node], n_node, z, z0, zs, lr_node, lr_sharp, f2, df2);
+                pot += w1 * outer * f1 + w2 * outer * f2;
+                dHB += -T(2) * u * outer * f1 + T(2) * u * outer * f2;
+                dBL += w1 * d_outer * f1 + w2 * d_outer * f2;
+                dZ += w1 * outer * df1 + w2 * outer * df2;
+            }
+            if (inner > T(0)) {
+                mirrored_spline(&coeff_inner[size_t(rt) * 2 * n_node], n_node, z, z0, zs, lr_node, lr_sharp, f1, df1);
+                mirrored_spline(&coeff_inner[(size_t(rt) * 2 + 1) * n_node], n_node, z, z0, zs, lr_node, lr_sharp, f2,
+                                df2);
+                pot += w1 * inner * f1 + w2 * inner * f2;
+                dHB += -T(2) * u * inner * f1 + T(2) * u * inner * f2;
+                dBL += w1 * d_inner * f1 + w2 * d_inner * f2;
+                dZ += w1 * inner * df1 + w2 * inner * df2;
+            }
+            for (int k = 0; k < 3; ++k) xs[k] += dZ * gz[k];
+            xs[6] += dHB;
+            for (int a = 0; a < n_restype; ++a) env.sens[size_t(rr) * n_restype + a] += weights[size_t(a)] * dBL;
+        }
+        this->pot = energy ? pot : T(0);
+    }
+};
+
+// lateral pressure on surface residues (MembraneLateralPotential,
+// src/membrane_potential.cpp:1262-1354): a force (no energy) of
+// s * p(z) * compact_sigmoid(burial - midpoint, sharpness) along the
+// residue's surface force direction (columns 1-2 of the surface node), with
+// p the clamped spline of the pressure profile over z.  The reference
+// indexes the per-residue burial and type arrays by the residue number, so
+// every cb_index entry must be below the number of entries.
+template <class T> struct LateralNode : Node<T> {
+    vector<int> cb_index, restype;
+    vector<T> weights, midpoint, sharpness, params;
+    T min_z, inv_dz, half;
+    int n_knot;
+    LateralNode(const H5& h) {
+        this->potential_node = true;
+        cb_index = h.ri("cb_index");
+        restype = h.ri("restypes");
+        weights = h.rf<T>("weights");
+        midpoint = h.rf<T>("cov_midpoint");
+        sharpness = h.rf<T>("cov_sharpness");
+        params = h.rf<T>("params");
+        min_z = T(float(h.attr("min_z")));
+        inv_dz = T(float(h.attr("inv_dz")));
+        half = T(float(h.attr("half_thickness")));
+        n_knot = int(h.attr("n_knot"));
+        int n = int(cb_index.size());
+        if (int(restype.size()) != n) throw Err("restypes needs one entry per cb_index");
+        if (weights.size() != 20 || midpoint.size() != 20 || sharpness.size() != 20)
+            throw Err("weights, cov_midpoint and cov_sharpness need 20 entries");
+        if (int(params.size()) != n_knot) throw Err("params needs n_knot entries");
+        for (int r : cb_index)
+            if (r < 0 || r >= n) throw Err("cb_index entries must be below the number of entries");
+        for (int t : restype)
+            if (t < 0 || t >= 20) throw Err("restypes out of range");
+    }
+    void forward(Engine<T>& e, bool) override {
+        auto& cb = e.arg(*this, 0);
+        auto& env = e.arg(*this, 1);
+        auto& sf = e.arg(*this, 2);
+        int n = int(cb_index.size());
+        vector<T> wbl(size_t(n), T(0));
+        for (int r = 0; r < n; ++r)
+            for (int a = 0; a < 20; ++a) wbl[size_t(r)] += weights[size_t(a)] * env.out[size_t(r) * 20 + a];
+        for (int i = 0; i < n; ++i) {
+            int r = cb_index[size_t(i)];
+            T z = cb.out[size_t(r) * cb.width + 2];
+            T sv = sf.out[size_t(r) * sf.width];
+            if (z > half || z < -half) sv = T(1);
+            int t = restype[size_t(r)];
+            T cs, dcs;
+            compact_sigmoid(wbl[size_t(r)] - midpoint[size_t(t)], sharpness[size_t(t)], cs, dcs);
+            if (sv <= T(0) || cs == T(0)) continue;
+            T v, dv;
+            clamped(params.data(), (z - min_z) * inv_dz, n_knot, v, dv);
+            T fm = sv * v;
+            cb.sens[size_t(r) * cb.width] -= fm * cs * sf.out[size_t(r) * sf.width + 1];
+            cb.sens[size_t(r) * cb.width + 1] -= fm * cs * sf.out[size_t(r) * sf.width + 2];
+        }
+        this->pot = T(0);
+    }
+};
+
 // Rigid frame per residue from N, CA, C (AffineAlignment, src/eig.cpp:277-470).
 // Output (center, quaternion); sensitivity slots 3..5 carry the torque.
 template <class T> struct AffineNode : Node<T> {
@@ -2377,6 +3036,10 @@ template <class T> std::unique_ptr<Node<T>> make_node(const string& name, const 
     if (is_prefix("Const3D", name)) return P(new ConstNode<T>(h, 3));
     if (is_prefix("cb_membrane_potential", name)) return P(new MembraneCBNode<T>(h));
     if (is_prefix("hb_membrane_potential", name)) return P(new MembraneHBNode<T>(h));
+    if (is_prefix("cb_surf_membrane_potential", name)) return P(new MembraneSurfCBNode<T>(h));
+    if (is_prefix("hb_surf_membrane_potential", name)) return P(new MembraneSurfHBNode<T>(h));
+    if (is_prefix("membranelateral_potential", name)) return P(new LateralNode<T>(h));
+    if (is_prefix("surface", name)) return P(new SurfaceNode<T>(h));
     if (is_prefix("SigmoidCoord", name)) return P(new SigmoidCoordNode<T>(h));
     if (is_prefix("SigmoidEnergy", name)) return P(new SigmoidEnergyNode<T>(h, false));
     if (is_prefix("SigmoidLEnergy", name)) return P(new SigmoidEnergyNode<T>(h, true));

@@ -65,6 +65,21 @@ def membrane_configs(tmp_path_factory, built):
     return paths, np.load(os.path.join(GOLDEN, "syn_membrane_ref.npz"))
 
 
+@pytest.fixture(scope="session")
+def surface_configs(tmp_path_factory, built):
+    """The surface fixture configs (golden/surface_spec.py), by variant, and
+    their reference data."""
+    if GOLDEN not in sys.path:
+        sys.path.insert(0, GOLDEN)
+    import surface_spec
+    d = tmp_path_factory.mktemp("surf")
+    paths = {}
+    for var in surface_spec.VARIANTS:
+        paths[var] = str(d / ("syn_surface_%s.up" % var))
+        surface_spec.write(paths[var], var)
+    return paths, np.load(os.path.join(GOLDEN, "syn_surface_ref.npz"))
+
+
 # Reference-facing bounds (energy: of sum_nodes |E_node|; force: of max |F|).
 # The frames' eigen-solve restates the reference's truncated QR, so what is
 # left is FP32 rounding; where the reference's own distance from the FP64

@@ -23,6 +23,11 @@ this script, which are committed (the GPU host has no reference checkout):
                      curved: frames, reference energy and derivative, and the
                      membrane nodes' outputs and sensitivities per frame
                      (python make_fixtures.py membrane writes only this file)
+  syn_surface_ref.npz the surface fixture (surface_spec.py): per variant
+                     the frames' reference energy and derivative, the surface
+                     node's output and the sensitivities the surface-dependent
+                     membrane terms write (python make_fixtures.py surface
+                     writes only this file)
   syn_graph_ref.npz  the reference's own edge lists of every interaction
                      graph of syn60/syn150 per frame, and its parameter
                      derivatives (get_param_deriv) of the rotamer, coverage
@@ -225,6 +230,37 @@ def membrane(L, tmpdir="/tmp"):
     np.savez_compressed(os.path.join(HERE, "syn_membrane_ref.npz"), **out)
 
 
+SURFACE_OUT = ["surface", "cat_pos_bb_cb"]
+SURFACE_SENS = ["placement_fixed_point_only_CB", "protein_hbond", "environment_coverage_sc"]
+
+
+def surface(L, tmpdir="/tmp"):
+    """syn_surface_ref.npz: every variant of surface_spec.py at the same
+    frames, evaluated in order on one engine (the surface node keeps state):
+    the reference engine's energy, derivative, the surface node's output and
+    the sensitivities of the nodes the membrane terms read."""
+    import surface_spec as S
+    frames = S.frames()
+    out = {"pos": frames}
+    for var in S.VARIANTS:
+        path = os.path.join(tmpdir, "syn_surface_%s.up" % var)
+        S.write(path, var)
+        eng = RefEngine(L, path, frames.shape[1])
+        E, D = [], []
+        for x in frames:
+            e, d = eng.eval(x)
+            E.append(e)
+            D.append(d)
+            for nm in SURFACE_OUT:
+                out.setdefault("%s/out/%s" % (var, nm), []).append(eng.node(nm))
+            for nm in SURFACE_SENS:
+                out.setdefault("%s/sens/%s" % (var, nm), []).append(eng.node(nm, sens=True))
+        out[var + "/ref_energy"] = E
+        out[var + "/ref_deriv"] = D
+    out = {k: np.array(v) for k, v in out.items()}
+    np.savez_compressed(os.path.join(HERE, "syn_surface_ref.npz"), **out)
+
+
 KAT_SRC = r"""
 #include <cstdio>
 #include <cstdint>
@@ -337,6 +373,9 @@ def main():
     if sys.argv[1:] == ["membrane"]:
         membrane(load_ref())
         return
+    if sys.argv[1:] == ["surface"]:
+        surface(load_ref())
+        return
     threefry_kat()
     L = load_ref()
     chig(L)
@@ -345,6 +384,7 @@ def main():
     synthetic(L, 150, 2, n_frames=2)
     trans_cis(L)
     membrane(L)
+    surface(L)
     edges_and_param_derivs(L)
 
 

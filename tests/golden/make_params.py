@@ -37,7 +37,7 @@ def main():
         out["hbond_parameter"] = f.read("/parameter")
     out["bb_env"] = np.loadtxt(os.path.join(P, "ff_2.1", "bb_env.dat"))
     with H5File(os.path.join(P, "ff_2.1", "membrane.h5")) as f:
-        for k in ["names", "cb_energy", "hb_energy", "burial_nodes"]:
+        for k in ["names", "cb_energy", "hb_energy", "icb_energy", "ihb_energy", "burial_nodes"]:
             out["mem_" + k] = f.read("/" + k)
         for k in ["cb_z_min", "cb_z_max", "hb_z_min", "hb_z_max"]:
             out["mem_" + k] = np.float64(f.attr("/", k))

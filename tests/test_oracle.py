@@ -366,3 +366,86 @@ def test_config_membrane(membrane_configs):
     h = "/input/potential/hb_membrane_potential"
     assert f.attr(h, "z_start") == -33.0 - 15.0 and f.attr(h, "use_curvature") == 1
     assert np.array_equal(f.read("/input/potential/Const3D_curvature_center/value"), [[0., 0., 60.]])
+
+
+@pytest.mark.parametrize("variant", ["diffusion", "fast_curved", "included"])
+@pytest.mark.parametrize("fp64", [False, True])
+def test_surface_golden_frames(surface_configs, variant, fp64):
+    """The surface node and the surface-dependent membrane terms
+    (src/surface.cpp:54-696; cb_surf_membrane_potential,
+    hb_surf_membrane_potential, membranelateral_potential,
+    src/membrane_potential.cpp:674-1354) against the reference engine, the
+    frames evaluated in order on one engine as the surface node keeps state.
+    The surface fraction is a count of discrete decisions and matches
+    exactly; the surface force columns are sums of per-turn forces and match
+    to rounding."""
+    import oracle_py
+    paths, z = surface_configs
+    path = paths[variant]
+    o = oracle_py.Oracle(path, z["pos"].shape[1], fp64=fp64)
+    o64 = oracle_py.Oracle(path, z["pos"].shape[1], fp64=True)
+    for k in range(len(z["pos"])):
+        bound = f_ref_bound(rel_f(z[variant + "/ref_deriv"][k], o64.evaluate(z["pos"][k])[1]))
+        e, d = o.evaluate(z["pos"][k])
+        assert rel_e(e, z[variant + "/ref_energy"][k], energy_scale(o, path)) < E_REF_TOL, k
+        assert rel_f(d, z[variant + "/ref_deriv"][k]) < bound, k
+        ref = z[variant + "/out/surface"][k]
+        s = o.node("surface")
+        assert np.array_equal(s[:, 0], ref[:, 0]), k
+        assert np.abs(s[:, 1:] - ref[:, 1:]).max() <= 1e-5 * np.abs(ref[:, 1:]).max(), k
+        cat = z[variant + "/out/cat_pos_bb_cb"][k]
+        assert np.abs(o.node("cat_pos_bb_cb") - cat).max() <= 1e-5 * np.abs(cat).max(), k
+        for nm in ("placement_fixed_point_only_CB", "protein_hbond", "environment_coverage_sc"):
+            if fp64 and nm == "protein_hbond":
+                # the hbond probabilities of these unbonded coils are 0 in
+                # float and rounding residues (1e-14) in FP64, where the
+                # probability column's sensitivity picks up a different branch
+                continue
+            sref = z[variant + "/sens/" + nm][k]
+            assert np.abs(o.node(nm, sens=True) - sref).max() <= 1e-4 * max(np.abs(sref).max(), 1.0), (k, nm)
+
+
+def test_surface_fixture_exercises_terms(surface_configs):
+    """The frames give surface residues and residues inside and outside the
+    slab, both surface methods, and lateral forces of the order of the CB
+    membrane forces."""
+    _, z = surface_configs
+    for var in ("diffusion", "fast_curved", "included"):
+        frac = z[var + "/out/surface"][..., 0]
+        assert (frac > 0).sum() > 100 and (frac == 0).sum() > 20 and ((frac > 0) & (frac < 1)).any(), var
+        assert (np.abs(z[var + "/out/surface"][..., 1:]) > 0).mean() > 0.3, var
+    cbz = z["diffusion/out/cat_pos_bb_cb"][:, 180:, 2].ravel()
+    assert (np.abs(cbz) < 15).any() and (np.abs(cbz) > 15).any()
+    inc = z["included/out/surface"][..., 0]
+    assert (inc[:, :5] == 0).all() and (inc[:, 50:] == 0).all()
+
+
+def test_config_surface(surface_configs):
+    """Structure of the surface, channel and lateral writers
+    (py/upside_config.py:1544-1602, 1837-2021)."""
+    import config_gen
+    from h5lite import H5File
+    paths, _ = surface_configs
+    f = H5File(paths["included"])
+    g = "/input/potential/surface"
+    assert f.attr(g, "method_type") == 1 and f.attr(g, "n_rotation") == 20 and f.attr(g, "exclusion") == 1
+    assert f.attr(g, "n_smallgridz") == 2 and f.attr(g, "atom_radius") == np.float64(1.6)
+    assert np.array_equal(f.read(g + "/index_cb"), np.arange(60) + 180)
+    aux = f.read(g + "/auxiliary_point")
+    assert aux.shape == (18, 2) and np.allclose(np.hypot(aux[:, 0], aux[:, 1])[:12:2], 1.0, atol=1e-3)
+    assert np.array_equal(f.read(g + "/included_list"), np.arange(5, 50))
+    cb = "/input/potential/cb_surf_membrane_potential"
+    assert [a.decode() for a in f.attr(cb, "arguments")] == [
+        "placement_fixed_point_only_CB", "environment_coverage_sc", "surface", "Const3D_curvature_center"]
+    assert f.read(cb + "/coeff_inner").shape == (20, 18)
+    hb = "/input/potential/hb_surf_membrane_potential"
+    n = len(f.read(hb + "/hb_index"))
+    assert len(f.read(hb + "/hb_type")) == n and len(f.read(hb + "/hb_res")) == n
+    lat = "/input/potential/membranelateral_potential"
+    pp = f.read(lat + "/params")
+    assert f.attr(lat, "n_knot") == len(pp) == 63 + 2 and f.attr(lat, "min_z") == -32.0
+    # the clamped spline through the sampled profile reproduces its samples
+    vals = config_gen.clamped_spline_solve(np.linspace(0., 5., 7) ** 2)
+    b = (vals[:-2] + 4 * vals[1:-1] + vals[2:]) / 6
+    assert np.allclose(b, np.linspace(0., 5., 7) ** 2, atol=1e-4)
+    assert vals[0] == vals[2] and vals[-1] == vals[-3]

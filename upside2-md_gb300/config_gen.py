@@ -265,7 +265,8 @@ def write_config(path, seq, seed, chain_first_residue=(), pos=None, environment_
                  damping=0.4, chain_offsets=None, params=None, bp_tol=1e-3, moves=False,
                  jump_length_scale=5., jump_rotation_scale=30., trans_cis=None, fix_rotamer=None,
                  extra_nodes=(), membrane_thickness=None, membrane_exclude_residues=(), use_curvature=False,
-                 curvature_radius=200., curvature_sign=1):
+                 curvature_radius=200., curvature_sign=1, surface=None, surface_included_residues=(),
+                 channel_membrane=False, lateral_pressure=None):
     """Write an ff_2.1 `.up` file for `seq` (list of 3-letter codes).
 
     chain_first_residue: residue indices (excluding 0) where new chains start.
@@ -294,6 +295,19 @@ def write_config(path, seq, seed, chain_first_residue=(), pos=None, environment_
       (write_membrane_potential3, py/upside_config.py:1727-1835, and write_CB
       :379-395).  membrane_exclude_residues skip the CB term; use_curvature,
       curvature_radius and curvature_sign bend the bilayer into a sphere.
+    surface: write the `surface` node with this method (0 fast, 1 lipid
+      diffusion), as --surface / --surface-method do (write_surface_coord,
+      py/upside_config.py:1544-1602), over surface_included_residues if
+      given; needs membrane_thickness.
+    channel_membrane: write the surface-dependent membrane terms
+      (cb_surf_membrane_potential, hb_surf_membrane_potential with their
+      inner-residue tables) in place of cb/hb_membrane_potential, as
+      --channel-membrane-potential does (write_membrane_potential4,
+      py/upside_config.py:1837-1953); needs surface.
+    lateral_pressure: a --membrane-lateral-potential table (path or rows of
+      z, pressure in bar): the membranelateral_potential node
+      (write_membrane_lateral_potential, py/upside_config.py:1955-2021);
+      needs surface.
     """
     P = load_params(params)
     rng = np.random.RandomState(seed)
@@ -692,6 +706,10 @@ def write_config(path, seq, seed, chain_first_residue=(), pos=None, environment_
     c.ds(g + "/atoms", np.column_stack((N_id, N_id + 1, N_id + 2)))
     c.ds(g + "/ref_geom", ref_geom)
 
+    if (surface is not None or channel_membrane or lateral_pressure is not None) and membrane_thickness is None:
+        raise ValueError("the surface and channel/lateral membrane terms need membrane_thickness")
+    if (channel_membrane or lateral_pressure is not None) and surface is None:
+        raise ValueError("the channel and lateral membrane terms need the surface node")
     if membrane_thickness is not None:
         half = 0.5 * membrane_thickness
         names = [x.decode() for x in P["mem_names"]]
@@ -705,22 +723,37 @@ def write_config(path, seq, seed, chain_first_residue=(), pos=None, environment_
         c.ds(g + "/value", np.array([[0., 0., curvature_radius * -1 * curvature_sign]]))
         common = dict(integrator_level=0, left_right_node=0.0, half_thickness=half, use_curvature=int(use_curvature),
                       curvature_radius=curvature_radius, curvature_sign=curvature_sign)
-        g = c.grp("cb_membrane_potential",
-                  ["placement_fixed_point_only_CB", "environment_coverage_sc", "Const3D_curvature_center"],
+        surf = "surf_" if channel_membrane else ""
+        cb_args = ["placement_fixed_point_only_CB", "environment_coverage_sc"] + (["surface"] if surf else [])
+        g = c.grp("cb_%smembrane_potential" % surf, cb_args + ["Const3D_curvature_center"],
                   z_start=P["mem_cb_z_min"] - half, z_scale=1. / cb_dz, bl_range_sharpness=1.0,
                   left_right_sharpness=1. / cb_dz, **common)
         used = np.array([r for r in range(n_res) if r not in set(membrane_exclude_residues)], dtype=int)
+        res_type = np.array([names.index(seq[r]) for r in used], dtype=int)
         c.ds(g + "/cb_index", used)
-        c.ds(g + "/res_type", np.array([names.index(seq[r]) for r in used], dtype=int))
+        c.ds(g + "/res_type", res_type)
         c.ds(g + "/weights", weights[:20])
         c.ds(g + "/bl_nodes", nodes)
         c.ds(g + "/coeff", cb_e)
-        g = c.grp("hb_membrane_potential", ["protein_hbond", "Const3D_curvature_center"],
+        if surf:
+            c.ds(g + "/coeff_inner", P["mem_icb_energy"])
+        hb_args = ["protein_hbond"] + (["environment_coverage_sc", "surface"] if surf else [])
+        g = c.grp("hb_%smembrane_potential" % surf, hb_args + ["Const3D_curvature_center"],
                   z_start=P["mem_hb_z_min"] - half, z_scale=1. / hb_dz, left_right_sharpness=1. / hb_dz, **common)
         res_hb = np.concatenate([donors, acceptors])
-        c.ds(g + "/hb_index", np.array([i for i, r in enumerate(res_hb) if r not in excluded], dtype=int))
-        c.ds(g + "/hb_type", np.concatenate([np.zeros(n_don, dtype='i'), np.ones(n_acc, dtype='i')]))
+        hb_used = np.array([i for i, r in enumerate(res_hb) if r not in excluded], dtype=int)
+        hb_type = np.concatenate([np.zeros(n_don, dtype='i'), np.ones(n_acc, dtype='i')])
+        c.ds(g + "/hb_index", hb_used)
         c.ds(g + "/coeff", hb_e)
+        if surf:
+            # one type and residue per used entry (the reference's checks want
+            # hb_type and hb_res as long as hb_index)
+            c.ds(g + "/hb_type", hb_type[hb_used])
+            c.ds(g + "/hb_res", res_hb[hb_used].astype(int))
+            c.ds(g + "/weights", weights[:20])
+            c.ds(g + "/coeff_inner", P["mem_ihb_energy"])
+        else:
+            c.ds(g + "/hb_type", hb_type)
         ref_cb = np.zeros((4, 3))
         ref_cb[0] = (-1.19280531, -0.83127186, 0.)
         ref_cb[2] = (1.25222632, -0.87268266, 0.)
@@ -730,6 +763,18 @@ def write_config(path, seq, seed, chain_first_residue=(), pos=None, environment_
         c.ds(g + "/affine_residue", np.arange(n_res))
         c.ds(g + "/layer_index", np.zeros(n_res, dtype='i'))
         c.ds(g + "/placement_data", ref_cb[3][None])
+        if surface is not None:
+            _write_surface(c, n_res, int(surface), half, surface_included_residues)
+        if lateral_pressure is not None:
+            attrs, pp = _lateral_spline(lateral_pressure, half)
+            g = c.grp("membranelateral_potential", ["placement_fixed_point_only_CB", "environment_coverage_sc", "surface"],
+                      **attrs)
+            c.ds(g + "/cb_index", used)
+            c.ds(g + "/restypes", res_type)
+            c.ds(g + "/weights", weights[:20])
+            c.ds(g + "/cov_midpoint", np.ones(20) + 2.5)
+            c.ds(g + "/cov_sharpness", np.ones(20))
+            c.ds(g + "/params", pp)
 
     for name, args, attrs, dsets in extra_nodes:
         g = c.grp(name, args, **attrs)
@@ -755,6 +800,99 @@ def write_config(path, seq, seed, chain_first_residue=(), pos=None, environment_
 
     w.save(path)
     return np.asarray(pos, dtype=np.float32)
+
+
+# points on the circle of an atom's radius, in units of the radius, that
+# fill the voxels around each atom (write_surface_coord's table,
+# py/upside_config.py:1557-1575: the 6 directions of a hexagon at radius 1 and
+# 1/2 and the 6 midpoints between them at radius sqrt(3)/2)
+def _surface_aux_points():
+    pts = []
+    for k in range(6):
+        a = np.pi / 2 - k * np.pi / 3
+        pts.append((round(np.cos(a), 3), round(np.sin(a), 3)))
+        pts.append((round(0.5 * np.cos(a), 3), round(0.5 * np.sin(a), 3)))
+    for k in range(6):
+        a = np.pi / 3 - k * np.pi / 3
+        pts.append((round(0.866 * np.cos(a), 3), round(0.866 * np.sin(a), 3)))
+    return np.array(pts, dtype=np.float64) + 0.0
+
+
+def _write_surface(c, n_res, method, half, included):
+    if method not in (0, 1):
+        raise ValueError("surface method must be 0 (fast) or 1 (lipid diffusion)")
+    g = c.grp("cat_pos_bb_cb", ["pos", "placement_fixed_point_only_CB"], n_dim=3)
+    c.ds(g + "/index_pos1", np.arange(3 * n_res))
+    c.ds(g + "/index_pos2", np.arange(n_res))
+    attrs = dict(n_rotation=20, half_thickness=half, zbuffer=0.0, exclusion=1 if len(included) else 0,
+                 len_gridx=3.0, len_gridy=3.0, n_gridz=6, n_smallgridx=1, n_smallgridy=1, n_smallgridz=2,
+                 atom_radius=1.6, method_type=method)
+    g = c.grp("surface", ["cat_pos_bb_cb"], **attrs)
+    if len(included):
+        c.ds(g + "/included_list", np.array(included, dtype=int))
+    c.ds(g + "/index_cb", np.arange(n_res) + 3 * n_res)
+    c.ds(g + "/auxiliary_point", _surface_aux_points())
+
+
+def clamped_spline_solve(values):
+    """B-spline coefficients (len(values) + 2, float32) of the clamped spline
+    through `values` at the integer knots with zero end slopes: the
+    reference's clamped_spline_solve (src/spline.cpp:158-190, called through
+    py/upside_engine.py:138-150), a tridiagonal solve in double precision."""
+    d = np.asarray(values, dtype=np.float32).astype(np.float64)
+    n = d.size
+    if n < 2:
+        raise ValueError("clamped spline needs at least 2 values")
+    a = np.full(n, 1. / 6.)
+    b = np.full(n, 2. / 3.)
+    cc = np.full(n, 1. / 6.)
+    cc[0] *= 2.
+    a[n - 1] *= 2.
+    for k in range(1, n):
+        m = a[k] / b[k - 1]
+        b[k] -= m * cc[k - 1]
+        d[k] -= m * d[k - 1]
+    d[n - 1] /= b[n - 1]
+    for k in range(n - 2, -1, -1):
+        d[k] = (d[k] - cc[k] * d[k + 1]) / b[k]
+    out = np.zeros(n + 2, dtype=np.float32)
+    out[1:n + 1] = d
+    out[0] = out[2]
+    out[n + 1] = out[n - 1]
+    return out
+
+
+def read_lateral_pressure(table):
+    """(z, pressure) rows of a --membrane-lateral-potential table: a path to
+    a text file whose first line is "z lateral_pressure", or the rows."""
+    if not isinstance(table, str):
+        return np.asarray(table, dtype=float).reshape(-1, 2)
+    with open(table) as fh:
+        rows = [ln.split() for ln in fh if ln.strip()]
+    if [x.lower() for x in rows[0]] != ["z", "lateral_pressure"]:
+        raise ValueError('First line must be "z lateral_pressure"')
+    if not all(len(r) == 2 for r in rows):
+        raise ValueError("Invalid format")
+    return np.asarray(rows[1:], dtype=float).reshape(-1, 2)
+
+
+def _lateral_spline(table, half):
+    """Attributes and spline coefficients of membranelateral_potential.  The
+    pressure curve is interpolated by a cubic spline held constant beyond its
+    ends, sampled at 1 angstrom knots over [min z, max z] and fitted by the
+    clamped spline."""
+    import scipy.interpolate
+    f = read_lateral_pressure(table)
+    z0, p0 = f[:, 0], f[:, 1]
+    spl = scipy.interpolate.InterpolatedUnivariateSpline(z0, p0)
+    min_z, max_z = float(np.min(z0)), float(np.max(z0))
+    n_knot = int(max_z - min_z) + 1
+    z = np.linspace(min_z, max_z, n_knot)
+    vals = np.select([z < z0[0], z > z0[-1], np.ones_like(z, dtype=bool)],
+                     [np.zeros_like(z) + p0[0], np.zeros_like(z) + p0[-1], spl(z)])
+    pp = clamped_spline_solve(vals)
+    return dict(min_z=min_z, max_z=max_z, inv_dz=1. / (max_z - min_z), n_knot=len(pp), half_thickness=half,
+                integrator_level=0), pp
 
 
 def random_sequence(n_res, rng):
