@@ -1409,7 +1409,7 @@ struct SurfaceCore {
             }
         }
         // every entry of the TM list, including those left from earlier
-        // evaluations beyond the current count (src/surface.cpp:676-680)
+        // evaluations beyond the current count (src/surface.cpp:675-679)
         for (int nr : tm_list) {
             if (tc[size_t(nr)] <= 0) continue;
             sfx[size_t(nr)] /= float(tc[size_t(nr)]);

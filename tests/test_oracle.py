@@ -396,13 +396,15 @@ def test_surface_golden_frames(surface_configs, variant, fp64):
         cat = z[variant + "/out/cat_pos_bb_cb"][k]
         assert np.abs(o.node("cat_pos_bb_cb") - cat).max() <= 1e-5 * np.abs(cat).max(), k
         for nm in ("placement_fixed_point_only_CB", "protein_hbond", "environment_coverage_sc"):
-            if fp64 and nm == "protein_hbond":
-                # the hbond probabilities of these unbonded coils are 0 in
-                # float and rounding residues (1e-14) in FP64, where the
-                # probability column's sensitivity picks up a different branch
-                continue
-            sref = z[variant + "/sens/" + nm][k]
-            assert np.abs(o.node(nm, sens=True) - sref).max() <= 1e-4 * max(np.abs(sref).max(), 1.0), (k, nm)
+            sref, got = z[variant + "/sens/" + nm][k], o.node(nm, sens=True)
+            if nm == "protein_hbond":
+                # the probability column also holds hbond_energy's residue
+                # energy wherever the residue's summed hbond probability is
+                # not exactly 0 (src/hbond.cpp:618-619); for these unbonded
+                # coils that sum is 0 or a rounding residue of 1 - exp(-x)
+                # (1e-14 in FP64), so only the geometric columns are compared
+                sref, got = sref[:, :6], got[:, :6]
+            assert np.abs(got - sref).max() <= 1e-4 * max(np.abs(sref).max(), 1.0), (k, nm)
 
 
 def test_surface_fixture_exercises_terms(surface_configs):

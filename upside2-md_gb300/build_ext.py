@@ -21,7 +21,7 @@ NVCC = os.environ.get("NVCC", "nvcc")
 CXX = os.environ.get("CXX", "g++")
 
 CU_SOURCES = ["engine.cu", "graph.cu", "pairlist.cu", "warm.cu", "capi.cu", "driver.cu", "mc.cu", "remd.cu"]
-HEADERS = ["engine.h", "graph.h", "warm.h", "mc.h", "remd.h", "dev_math.cuh", "launch.cuh", "h5lite.h"]
+HEADERS = ["engine.h", "graph.h", "warm.h", "mc.h", "remd.h", "dev_math.cuh", "launch.cuh", "surface.cuh", "h5lite.h"]
 
 
 def _stale(target, deps):

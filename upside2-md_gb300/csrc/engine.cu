@@ -1148,6 +1148,8 @@ struct MembraneNode : GNode {
     }
 };
 
+#include "surface.cuh"
+
 // ===================================================== affine frames ===
 // Rigid frame (centroid, quaternion) per residue: the quaternion is the top
 // eigenvector of the 4x4 key matrix of the N/CA/C fit (AffineAlignment,
@@ -3093,6 +3095,12 @@ Engine::Engine(const std::vector<std::string>& paths, const std::vector<int>& n_
             else if (is_prefix("Const3D", nm)) n.reset(new ConstNode(*this, g, N(0), 3));
             else if (is_prefix("cb_membrane_potential", nm)) n.reset(new MembraneNode(*this, g, true, N(0), &N(1), N(2)));
             else if (is_prefix("hb_membrane_potential", nm)) n.reset(new MembraneNode(*this, g, false, N(0), nullptr, N(1)));
+            else if (is_prefix("cb_surf_membrane_potential", nm))
+                n.reset(new MembraneSurfNode(*this, g, true, N(0), N(1), N(2), N(3)));
+            else if (is_prefix("hb_surf_membrane_potential", nm))
+                n.reset(new MembraneSurfNode(*this, g, false, N(0), N(1), N(2), N(3)));
+            else if (is_prefix("membranelateral_potential", nm)) n.reset(new LateralNode(*this, g, N(0), N(1), N(2)));
+            else if (is_prefix("surface", nm)) n.reset(new SurfaceNode(*this, g, N(0)));
             else if (is_prefix("affine_alignment", nm)) n.reset(new AffineNode(*this, g, O(0)));
             else if (is_prefix("backbone_pairs", nm)) n.reset(new BackbonePairsNode(*this, g, O(0)));
             else if (is_prefix("infer_H_O", nm)) n.reset(new InferHONode(*this, g, O(0)));
@@ -3371,10 +3379,18 @@ void Engine::set_box(float lx, float ly, float lz) {
     drop_graph();
 }
 
+// status bits that end the call with an error
+static void fatal_status(int s) {
+    if (s & ST_SURFACE_GRID)
+        throw Error("surface: a turn's TM residues span more voxels along x or y than the surface kernel's grid holds "
+                    "(or a coordinate is not finite)");
+}
+
 void Engine::compute_checked(bool energy, int level) {
     for (int attempt = 0; attempt < 8; ++attempt) {
         compute(energy, level);
         int s = status(true);
+        fatal_status(s);
         if (!(s & (ST_EDGE_OVERFLOW | ST_RES_EDGE_OVERFLOW))) return;
         bool grew = false;
         for (auto& n : nodes) grew |= n->grow(*this);
@@ -3446,6 +3462,7 @@ void Engine::run_rounds(int n_round, float dt, float timescale, bool use_graph, 
         UG_CK(cudaMemcpyAsync(snap_mom, d_mom, 4 * n3, cudaMemcpyDeviceToDevice, st));
         UG_CK(cudaMemcpyAsync(snap_round, d_round, 8 * size_t(n_sys), cudaMemcpyDeviceToDevice, st));
         if (remd) remd->snapshot(false);
+        for (auto& n : nodes) n->keep_state(*this, false);
         if (use_graph && aligned && k == graph_rounds) {
             if (!graph_exec || this->graph_rounds != graph_rounds || graph_dt != dt || graph_timescale != timescale ||
                 graph_span != thermo_span || graph_multistep != multistep || graph_inner != inner_step || graph_timed ||
@@ -3465,12 +3482,17 @@ void Engine::run_rounds(int n_round, float dt, float timescale, bool use_graph, 
         int s = 0;
         UG_CK(cudaMemcpyAsync(&s, d_status, sizeof(int), cudaMemcpyDeviceToHost, st));
         UG_CK(cudaStreamSynchronize(st));
+        if (s & ST_SURFACE_GRID) {
+            UG_CK(cudaMemsetAsync(d_status, 0, sizeof(int), st));
+            fatal_status(s);
+        }
         if (s & overflow) {
             if (++retries > 8) throw Error("pair-list storage kept overflowing");
             UG_CK(cudaMemcpyAsync(d_pos, snap_pos, 4 * n3, cudaMemcpyDeviceToDevice, st));
             UG_CK(cudaMemcpyAsync(d_mom, snap_mom, 4 * n3, cudaMemcpyDeviceToDevice, st));
             UG_CK(cudaMemcpyAsync(d_round, snap_round, 8 * size_t(n_sys), cudaMemcpyDeviceToDevice, st));
             if (remd) remd->snapshot(true);
+            for (auto& n : nodes) n->keep_state(*this, true);
             UG_CK(cudaMemsetAsync(d_status, 0, sizeof(int), st));
             sync();
             for (auto& n : nodes) n->grow(*this);

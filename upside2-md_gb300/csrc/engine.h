@@ -61,6 +61,10 @@ struct GNode {
         throw Error("Value " + w + " not implemented");
     }
     virtual DGraph* graph() { return nullptr; }
+    // state that one evaluation leaves for the next (the surface node's):
+    // copied aside before a chunk of rounds and put back when the chunk is
+    // run again after a storage overflow
+    virtual void keep_state(Engine&, bool /*restore*/) {}
     // enlarge edge storage after an overflow; returns true if anything grew
     virtual bool grow(Engine&) { return false; }
     // measured kernel of this node: bracket its launches with events from
