@@ -153,6 +153,25 @@ def test_surface_dynamics(surface_configs):
     assert np.abs(res[0] - res[1]).max() < 1e-3
 
 
+def test_surface_large_grid(surface_configs):
+    """A frame spread over more voxels than the small tier's grid (64 per
+    axis) goes through the large tier: the surface output still equals the
+    oracle's, and turns of both tiers mix in one evaluation."""
+    import oracle_py
+    import upside_gb300 as U
+    paths, z = surface_configs
+    path = paths["diffusion"]
+    for f in (4.0, 7.0, 12.0):
+        x = z["pos"][0].copy()
+        x[:, :2] *= f
+        eng = U.Upside(path, len(x))
+        o = oracle_py.Oracle(path, len(x))
+        eng.deriv(x)
+        o.evaluate(x)
+        check_surface(eng.get_output("surface"), o.node("surface"), ("stretched", f))
+        assert (eng.get_output("surface")[:, 0] > 0).sum() > 10
+
+
 def test_surface_grid_capacity_error(surface_configs, capfd):
     """TM residues spread over more voxels than the kernel's grid holds end
     the evaluation with an error naming the surface node (the kernel skips

@@ -40,7 +40,7 @@
 enum : int { ST_SURFACE_GRID = 8 };  // a turn's grid exceeded the kernel's voxel capacity
 
 struct SurfDev {
-    int method, n_rot, n_aux, ngz, snx, sny, snz, cap;  // cap: voxels along x and y the grid holds
+    int method, n_rot, n_aux, ngz, snx, sny, snz, cap;  // cap: voxels along x and y the large grid holds
     float tm_min, tm_max, radius, gx, gy, r_gz, area_xz, area_yz, r_nrot;
     const float* aux;           // n_aux x 2 (in units of the radius)
     const float* trig;          // n_rot x 4: cos a, sin a, cos -a, sin -a
@@ -177,7 +177,6 @@ __device__ __forceinline__ unsigned surf_inner(int w, int n) {
     if (w == 0) m &= ~1u;
     return m;
 }
-constexpr int SURF_WMAX = 8;  // words per row the flood fill keeps in registers
 
 // Lipid closure of layer k (src/surface.cpp:380-451): empty interior voxels
 // with a lipid source among their 3 x 3 neighbours in the layer become lipid
@@ -185,6 +184,7 @@ constexpr int SURF_WMAX = 8;  // words per row the flood fill keeps in registers
 // tail layers (kr >= 0), is also lipid in layer kr.  One warp; rows are
 // updated in place (sets only grow, so any interleaving reaches the same
 // closure, and a pass in which no lane changes a row proves it reached).
+template <int SURF_WMAX>  // words per row the fill keeps in registers (W <= SURF_WMAX)
 __device__ void surf_fill(volatile unsigned* L, const unsigned* A, int k, int kr, int ngx, int ngy, int W, int lane) {
     const int max_pass = ngx * ngy + 2;
     for (int pass = 0; pass < max_pass; ++pass) {
@@ -270,19 +270,28 @@ __device__ __forceinline__ int surf_bsum(int v, int* sh) {
     return r;
 }
 
-// One turn of one system (src/surface.cpp:234-673).  Dynamic shared memory:
-// three masks of ngz x cap rows x cap/32 words (occupied; lipid or y-minimum
-// labels; y-maximum labels) and the fine extremes and picks.
-__global__ void __launch_bounds__(256, 1) surface_turn_kernel(SurfDev D, int* status) {
+// One turn of one system (src/surface.cpp:234-673), on a grid of at most
+// cap x cap voxels in x and y (cap <= 32 WMAX).  Two tiers: the small grid
+// runs every turn and leaves the turns whose grid is larger to the large one
+// (big[] flags, per system and turn); the large tier skips all others.
+// Dynamic shared memory: three masks of ngz x cap rows x cap/32 words
+// (occupied; lipid or y-minimum labels; y-maximum labels) and the fine
+// extremes and picks.
+template <int WMAX>
+__global__ void __launch_bounds__(256, WMAX <= 2 ? 4 : 1) surface_turn_kernel(SurfDev D, int cap, int tier, int* big, int* status) {
     grid_dep_entry();
     extern __shared__ unsigned smem_u[];
     const int a = blockIdx.x, s = blockIdx.y, tid = threadIdx.x, bd = blockDim.x;
+    if (tier == 1 && !big[s * D.n_rot + a]) return;
     const int u0 = D.used_off[s], nu = D.used_off[s + 1] - u0;
     const int ntm = D.n_tm[s];
     int* cnt = D.cnt + size_t(D.n_rot) * u0 + size_t(a) * nu;
     float* tf = D.tf + (size_t(D.n_rot) * u0 + size_t(a) * nu) * 2;
     for (int i = tid; i < ntm; i += bd) cnt[i] = 0;
-    if (ntm == 0) return;
+    if (ntm == 0) {
+        if (tid == 0 && tier == 0) big[s * D.n_rot + a] = 0;
+        return;
+    }
     const int na = 4 * ntm;
     const float* xy = D.xy + size_t(D.n_rot) * 8 * size_t(u0) + size_t(a) * na * 2;
     const float* zc = D.zc + 4 * size_t(u0);
@@ -310,9 +319,9 @@ __global__ void __launch_bounds__(256, 1) surface_turn_kernel(SurfDev D, int* st
         float lenx = __fsub_rn(maxx, minx), leny = __fsub_rn(maxy, miny);
         double qx = __ddiv_rn(__dadd_rn(double(lenx), 0.1), double(D.gx));
         double qy = __ddiv_rn(__dadd_rn(double(leny), 0.1), double(D.gy));
-        bool ok = qx >= 0. && qy >= 0. && qx < double(D.cap) && qy < double(D.cap);
+        bool ok = qx >= 0. && qy >= 0. && qx < double(cap) && qy < double(cap);
         int ngx = ok ? int(qx) + 3 : 3, ngy = ok ? int(qy) + 3 : 3;
-        ok = ok && ngx <= D.cap && ngy <= D.cap;
+        ok = ok && ngx <= cap && ngy <= cap;
         float blx = __fmul_rn(float(ngx), D.gx), bly = __fmul_rn(float(ngy), D.gy);
         s_f[0] = __fsub_rn(minx, __fmul_rn(0.5f, __fsub_rn(blx, lenx)));
         s_f[1] = __fsub_rn(miny, __fmul_rn(0.5f, __fsub_rn(bly, leny)));
@@ -329,22 +338,26 @@ __global__ void __launch_bounds__(256, 1) surface_turn_kernel(SurfDev D, int* st
         s_g[3] = ok ? 0 : 1;
         s_g[4] = ngx * D.snx + ngy * D.sny + D.ngz * D.snz;
         s_g[5] = D.ngz * D.snz;
-        if (!ok) atomicOr(status, ST_SURFACE_GRID);
+        // a finite extent beyond the small grid goes to the large tier; beyond
+        // the large grid, or not finite, it is an error
+        const bool finite = qx >= 0. && qy >= 0. && qx < 1e9 && qy < 1e9;
+        if (tier == 0) big[s * D.n_rot + a] = (!ok && finite) ? 1 : 0;
+        if (!ok && (tier == 1 || !finite)) atomicOr(status, ST_SURFACE_GRID);
     }
     __syncthreads();
-    const int ngx = s_g[0], ngy = s_g[1], W = s_g[2], big = s_g[4], zs = s_g[5], ngz = D.ngz;
+    const int ngx = s_g[0], ngy = s_g[1], W = s_g[2], big_int = s_g[4], zs = s_g[5], ngz = D.ngz;
     if (s_g[3]) {
         for (int i = tid; i < ntm; i += bd) tf[2 * i] = tf[2 * i + 1] = 0.f;
         return;
     }
     const float side[3] = {s_f[0], s_f[1], s_f[2]}, s1[3] = {s_f[3], s_f[4], s_f[5]}, s2[3] = {s_f[6], s_f[7], s_f[8]};
     const int nrow = ngz * ngy, nword = nrow * W;
-    const size_t mcap = size_t(ngz) * D.cap * (D.cap / 32);
+    const size_t mcap = size_t(ngz) * cap * (cap / 32);
     unsigned* A = smem_u;
     unsigned* M2 = A + mcap;  // method 1: lipid; method 0: y-minimum labels
     unsigned* M3 = M2 + mcap; // method 0: y-maximum labels
     const int nfx = D.sny * ngy * zs, nfy = D.snx * ngx * zs;
-    const size_t fcx = size_t(D.sny) * D.cap * size_t(D.ngz * D.snz), fcy = size_t(D.snx) * D.cap * size_t(D.ngz * D.snz);
+    const size_t fcx = size_t(D.sny) * cap * size_t(D.ngz * D.snz), fcy = size_t(D.snx) * cap * size_t(D.ngz * D.snz);
     int* fxmn = reinterpret_cast<int*>(M3 + mcap);
     int* fxmx = fxmn + fcx;
     int* ixmn = fxmx + fcx;
@@ -354,8 +367,8 @@ __global__ void __launch_bounds__(256, 1) surface_turn_kernel(SurfDev D, int* st
     int* iymn = fymx + fcy;
     int* iymx = iymn + fcy;
     for (int i = tid; i < nword; i += bd) A[i] = M2[i] = M3[i] = 0u;
-    for (int i = tid; i < nfx; i += bd) { fxmn[i] = big; fxmx[i] = -1; ixmn[i] = ixmx[i] = -1; }
-    for (int i = tid; i < nfy; i += bd) { fymn[i] = big; fymx[i] = -1; iymn[i] = iymx[i] = -1; }
+    for (int i = tid; i < nfx; i += bd) { fxmn[i] = big_int; fxmx[i] = -1; ixmn[i] = ixmx[i] = -1; }
+    for (int i = tid; i < nfy; i += bd) { fymn[i] = big_int; fymx[i] = -1; iymn[i] = iymx[i] = -1; }
     __syncthreads();
     // 3. occupied voxels: atoms and their auxiliary points (src/surface.cpp:272-321)
     const int per = 1 + 2 * D.n_aux;
@@ -396,13 +409,13 @@ __global__ void __launch_bounds__(256, 1) surface_turn_kernel(SurfDev D, int* st
         __syncthreads();
         const int lane = tid & 31, wid = tid >> 5;
         if (wid == 0) {
-            surf_fill(M2, A, 0, -1, ngx, ngy, W, lane);
-            for (int k = 1; k < ngz / 2; ++k) surf_fill(M2, A, k, k - 1, ngx, ngy, W, lane);
+            surf_fill<WMAX>(M2, A, 0, -1, ngx, ngy, W, lane);
+            for (int k = 1; k < ngz / 2; ++k) surf_fill<WMAX>(M2, A, k, k - 1, ngx, ngy, W, lane);
         } else if (wid == 1) {
             // the reference's pass over the top layer with the layer above
             // it (read past its grid) cannot add to a layer closed just before
-            surf_fill(M2, A, ngz - 1, -1, ngx, ngy, W, lane);
-            for (int k = ngz - 2; k >= ngz / 2; --k) surf_fill(M2, A, k, k + 1, ngx, ngy, W, lane);
+            surf_fill<WMAX>(M2, A, ngz - 1, -1, ngx, ngy, W, lane);
+            for (int k = ngz - 2; k >= ngz / 2; --k) surf_fill<WMAX>(M2, A, k, k + 1, ngx, ngy, W, lane);
         }
     } else {
         // per column the first and last occupied voxel along y
@@ -500,13 +513,13 @@ __global__ void __launch_bounds__(256, 1) surface_turn_kernel(SurfDev D, int* st
     // 6. areas and forces per picked CB (src/surface.cpp:596-622)
     int n_xmn = 0, n_xmx = 0, n_ymn = 0, n_ymx = 0, c_xmn = 0, c_xmx = 0, c_ymn = 0, c_ymx = 0;
     for (int i = tid; i < nfx; i += bd) {
-        n_xmn += fxmn[i] < big;
+        n_xmn += fxmn[i] < big_int;
         n_xmx += fxmx[i] > -1;
         if (ixmn[i] >= 0) { ++c_xmn; atomicOr(&cnt[ixmn[i]], 1); }
         if (ixmx[i] >= 0) { ++c_xmx; atomicAdd(&cnt[ixmx[i]], 4); }
     }
     for (int i = tid; i < nfy; i += bd) {
-        n_ymn += fymn[i] < big;
+        n_ymn += fymn[i] < big_int;
         n_ymx += fymx[i] > -1;
         if (iymn[i] >= 0) { ++c_ymn; atomicOr(&cnt[iymn[i]], 2); }
         if (iymx[i] >= 0) { ++c_ymx; atomicAdd(&cnt[iymx[i]], 1 << 16); }
@@ -602,10 +615,14 @@ __global__ void __launch_bounds__(256) surface_finish_kernel(SurfDev D, float* o
     }
 }
 
+constexpr int SURF_W_SMALL = 2, SURF_W_LARGE = 7;  // words per grid row of the two tiers (64 and 224 voxels)
+
 struct SurfaceNode : GNode {
     SurfDev D{};
     int n_sys = 0;
-    size_t smem = 0;
+    int cap_small = 0, cap_large = 0;
+    size_t smem_small = 0, smem_large = 0;
+    int* big = nullptr;
     size_t n_used_total = 0;
     int *snap_tm = nullptr;
     float* snap_sf = nullptr;
@@ -704,26 +721,39 @@ struct SurfaceNode : GNode {
         D.dcount = e.alloc<int>(nr);
         snap_tm = e.alloc<int>(nu);
         snap_sf = e.alloc<float>(2 * nr);
-        // the largest square grid (a multiple of 32 voxels) whose masks and
-        // fine rows fit in a block's shared memory
-        const size_t limit = 200 * 1024;
-        for (int cap = 256; cap >= 32; cap -= 32) {
-            const size_t masks = 3 * size_t(D.ngz) * cap * (cap / 32) * 4;
-            const size_t fine = 4 * 4 * size_t(D.ngz * D.snz) * cap * size_t(D.sny + D.snx);
-            if (masks + fine <= limit && size_t(D.sny) * cap * D.ngz * D.snz < 16384 &&
-                size_t(D.snx) * cap * D.ngz * D.snz < 16384) {
-                D.cap = cap;
-                smem = masks + fine;
-                break;
+        // per tier the largest square grid (a multiple of 32 voxels, at most
+        // 32 words per row of the tier) whose masks and fine rows fit in a
+        // block's shared memory
+        auto fit = [&](int wmax, int& cap, size_t& bytes) {
+            const size_t limit = 200 * 1024;
+            for (int c = 32 * wmax; c >= 32; c -= 32) {
+                const size_t masks = 3 * size_t(D.ngz) * c * (c / 32) * 4;
+                const size_t fine = 4 * 4 * size_t(D.ngz * D.snz) * c * size_t(D.sny + D.snx);
+                if (masks + fine <= limit && size_t(D.sny) * c * D.ngz * D.snz < 16384 &&
+                    size_t(D.snx) * c * D.ngz * D.snz < 16384) {
+                    cap = c;
+                    bytes = masks + fine;
+                    return;
+                }
             }
-        }
-        if (!D.cap) throw Error("surface grid parameters leave no room for a voxel grid in shared memory");
-        UG_CK(cudaFuncSetAttribute(surface_turn_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+            throw Error("surface grid parameters leave no room for a voxel grid in shared memory");
+        };
+        fit(SURF_W_SMALL, cap_small, smem_small);
+        fit(SURF_W_LARGE, cap_large, smem_large);
+        D.cap = cap_large;
+        big = e.alloc<int>(size_t(n_sys) * D.n_rot);
+        UG_CK(cudaFuncSetAttribute(surface_turn_kernel<SURF_W_SMALL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   int(smem_small)));
+        UG_CK(cudaFuncSetAttribute(surface_turn_kernel<SURF_W_LARGE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   int(smem_large)));
     }
     void forward(Engine& e, bool) override {
         auto& p = e.arg(*this, 0);
         ug::launch(surface_prep_kernel, n_sys, 256, 0, e.st, D, p.width, p.out);
-        ug::launch(surface_turn_kernel, dim3(D.n_rot, n_sys), 256, smem, e.st, D, e.d_status);
+        ug::launch(surface_turn_kernel<SURF_W_SMALL>, dim3(D.n_rot, n_sys), 256, smem_small, e.st, D, cap_small, 0, big,
+                   e.d_status);
+        ug::launch(surface_turn_kernel<SURF_W_LARGE>, dim3(D.n_rot, n_sys), 256, smem_large, e.st, D, cap_large, 1, big,
+                   e.d_status);
         ug::launch(surface_finish_kernel, n_sys, 256, 0, e.st, D, out);
     }
     // the state the next evaluation reads (TM list, forces of every residue)
