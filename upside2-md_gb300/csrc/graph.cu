@@ -30,7 +30,8 @@ namespace cg = cooperative_groups;
 // block: each thread owns a contiguous chunk, then a block-level scan of the
 // chunk sums.
 __global__ void __launch_bounds__(1024) scan_kernel(const int* __restrict__ in, int* __restrict__ out, int n,
-                                                    int* total_out, const int* __restrict__ skip_unless) {
+                                                    int* total_out, const int* __restrict__ skip_unless, int cap,
+                                                    int* status, int bit) {
     grid_dep_entry();
     if (skip_unless && !*skip_unless) return;
     // sums are carried in 64 bits and stored saturated at INT_MAX, so a total
@@ -70,7 +71,16 @@ __global__ void __launch_bounds__(1024) scan_kernel(const int* __restrict__ in, 
     }
     if (t == blockDim.x - 1) {
         out[n] = sat(excl);
-        if (total_out) *total_out = sat(excl);
+        if (total_out) {
+            // with a capacity: a total beyond it is flagged and capped (the
+            // fill pass writes no further)
+            int tot = sat(excl);
+            if (cap >= 0 && tot > cap) {
+                atomicOr(status, bit);
+                tot = cap;
+            }
+            *total_out = tot;
+        }
     }
     if (n == 0 && t == 0) {
         out[0] = 0;
@@ -78,8 +88,9 @@ __global__ void __launch_bounds__(1024) scan_kernel(const int* __restrict__ in, 
     }
 }
 
-void launch_scan(const int* in, int* out, int n, int* total_out, cudaStream_t st, const int* skip_unless) {
-    ug::launch(scan_kernel, 1, 1024, 0, st, in, out, n, total_out, skip_unless);
+void launch_scan(const int* in, int* out, int n, int* total_out, cudaStream_t st, const int* skip_unless, int cap,
+                 int* status, int bit) {
+    ug::launch(scan_kernel, 1, 1024, 0, st, in, out, n, total_out, skip_unless, cap, status, bit);
 }
 
 // --------------------------------------------------------- pair search ---
@@ -231,15 +242,20 @@ __global__ void __launch_bounds__(256) pair_kernel(DGraph g) {
         }
         __syncthreads();  // s_lo / s_hi are reset for the next row block
     }
-}
-
-__global__ void cap_check_kernel(int* n_edge, int cap, int* status) {
-    grid_dep_entry();
-    if (*n_edge > cap) {
-        atomicOr(status, ST_EDGE_OVERFLOW);
-        *n_edge = cap;
+    if (PASS == 1 && CACHED) {
+        // the rebuilt systems' positions become their new reference positions
+        // (the search reads x1 / x2 only)
+        const int n = g.n1 + (g.symmetric ? 0 : g.n2);
+        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+            const bool first = i < g.n1;
+            const int k = first ? i : i - g.n1;
+            if (!g.sys_flag[first ? g.sys1[k] : g.sys2[k]]) continue;
+            if (first) g.xc1[k] = g.x1[k];
+            else g.xc2[k] = g.x2[k];
+        }
     }
 }
+
 
 // ----------------------------------------------------- candidate cache ---
 // A system's cache is rebuilt when any of its elements moved more than half
@@ -261,6 +277,7 @@ __global__ void cache_flag_init_kernel(DGraph g) {
     if (threadIdx.x == 0) *g.any_flag = any;
 }
 
+// (also packs the positions the search reads)
 __global__ void cache_check_kernel(DGraph g) {
     grid_dep_entry();
     float h = 0.5f * ((g.cutoff + g.buffer) - g.cutoff);
@@ -270,7 +287,10 @@ __global__ void cache_check_kernel(DGraph g) {
         bool first = i < g.n1;
         int k = first ? i : i - g.n1;
         int sys = first ? g.sys1[k] : g.sys2[k];
-        float4 x = first ? g.x1[k] : g.x2[k];
+        const float* p = first ? g.in1 + size_t(g.loc1[k]) * g.w1 : g.in2 + size_t(g.loc2[k]) * g.w2;
+        const float4 x = make_float4(p[0], p[1], p[2], 0.f);
+        if (first) g.x1[k] = x;
+        else g.x2[k] = x;
         float4 c = first ? g.xc1[k] : g.xc2[k];
         float dx = x.x - c.x, dy = x.y - c.y, dz = x.z - c.z;
         if (lim < dx * dx + dy * dy + dz * dz) {
@@ -281,11 +301,12 @@ __global__ void cache_check_kernel(DGraph g) {
 }
 
 // after the rebuild search: per system candidate counts (capped by the
-// segment, overflow flagged), and the refine pass's tile prefix over systems
+// segment, overflow flagged), then the refine pass's tile prefix over systems
+// and the end of a rebuild-everything request (one block)
 __global__ void cache_commit_kernel(DGraph g) {
     grid_dep_entry();
-    if (!*g.any_flag) return;
-    for (int s = grid_stride_start(); s < g.n_sys; s += grid_stride()) {
+    if (!*g.any_flag) return;  // nothing rebuilt: counts, tiles and request unchanged
+    for (int s = threadIdx.x; s < g.n_sys; s += blockDim.x) {
         if (!g.sys_flag[s]) continue;
         atomicAdd(g.rebuilds, 1ull);
         int cnt = g.row_off[g.sys_first_row[s + 1]] - g.row_off[g.sys_first_row[s]];
@@ -297,15 +318,8 @@ __global__ void cache_commit_kernel(DGraph g) {
         }
         g.cache_n[s] = cnt;
     }
-}
-
-// positions of the rebuilt systems become their new reference positions; the
-// first thread also clears the rebuild-everything request and recomputes the
-// per-system prefix of active refine tiles
-__global__ void cache_positions_kernel(DGraph g) {
-    grid_dep_entry();
-    if (!*g.any_flag) return;  // nothing rebuilt: positions, tiles and request unchanged
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
         *g.cache_force = 0;
         int t = 0;
         for (int s = 0; s < g.n_sys; ++s) {
@@ -313,15 +327,6 @@ __global__ void cache_positions_kernel(DGraph g) {
             t += (g.cache_n[s] + CACHE_TILE - 1) / CACHE_TILE;
         }
         g.active_off[g.n_sys] = t;
-    }
-    int n = g.n1 + (g.symmetric ? 0 : g.n2);
-    for (int i = grid_stride_start(); i < n; i += grid_stride()) {
-        bool first = i < g.n1;
-        int k = first ? i : i - g.n1;
-        int sys = first ? g.sys1[k] : g.sys2[k];
-        if (!g.sys_flag[sys]) continue;
-        if (first) g.xc1[k] = g.x1[k];
-        else g.xc2[k] = g.x2[k];
     }
 }
 
@@ -391,19 +396,23 @@ __global__ void __launch_bounds__(256) cache_refine_kernel(DGraph g) {
     }
 }
 
+// Launches per evaluation: full search 4 (pack, count, scan with the edge
+// capacity check, fill); cached 9 (rebuild flags, movement check with the
+// position packing, rebuild count, scan, rebuild fill with the new reference
+// positions, commit, refine count, scan with the capacity check, refine fill).
 void launch_pairs(const DGraph& g, cudaStream_t st) {
-    launch_pack_positions(g, st);
     if (g.n_rows == 0) {
+        launch_pack_positions(g, st);
         cudaMemsetAsync(g.n_edge, 0, sizeof(int), st);
         cudaMemsetAsync(g.row_off, 0, sizeof(int), st);
         return;
     }
     int blocks = min(4 * 152, (g.n_rows + 7) / 8);
     if (!g.cached) {
+        launch_pack_positions(g, st);
         ug::launch((pair_kernel<0, false>), blocks, 256, 0, st, g);
-        launch_scan(g.row_count, g.row_off, g.n_rows, g.n_edge, st);
+        launch_scan(g.row_count, g.row_off, g.n_rows, g.n_edge, st, nullptr, g.cap, g.status);
         ug::launch((pair_kernel<1, false>), blocks, 256, 0, st, g);
-        ug::launch(cap_check_kernel, 1, 1, 0, st, g.n_edge, g.cap, g.status);
         return;
     }
     int ne = g.n1 + (g.symmetric ? 0 : g.n2);
@@ -414,12 +423,10 @@ void launch_pairs(const DGraph& g, cudaStream_t st) {
     launch_scan(g.row_count, g.row_off, g.n_rows, nullptr, st, g.any_flag);
     ug::launch((pair_kernel<1, true>), blocks, 256, 0, st, g);
     ug::launch(cache_commit_kernel, 1, 256, 0, st, g);
-    ug::launch(cache_positions_kernel, eb, 256, 0, st, g);
     int rblocks = min(8 * 152, g.max_tiles);
     ug::launch((cache_refine_kernel<0>), rblocks, 256, 0, st, g);
-    launch_scan(g.tile_count, g.tile_off, g.max_tiles, g.n_edge, st);
+    launch_scan(g.tile_count, g.tile_off, g.max_tiles, g.n_edge, st, nullptr, g.cap, g.status);
     ug::launch((cache_refine_kernel<1>), rblocks, 256, 0, st, g);
-    ug::launch(cap_check_kernel, 1, 1, 0, st, g.n_edge, g.cap, g.status);
 }
 
 // ------------------------------------------------------ edge evaluation ---
@@ -832,13 +839,6 @@ __global__ void bp_entry_init_kernel(DBP b) {
     for (int i = grid_stride_start(); i < n * 36; i += grid_stride()) b.esum[i] = 0.f;
 }
 
-__global__ void bp_cap_check_kernel(DBP b) {
-    grid_dep_entry();
-    if (*b.n_ent > b.ent_cap) {
-        atomicOr(b.status, ST_RES_EDGE_OVERFLOW);
-        *b.n_ent = b.ent_cap;
-    }
-}
 
 // Summed pair energies of the entries; and per bead edge, where the
 // sensitivity pass finds the edge's weight (eaux): an edge-marginal element
@@ -1660,9 +1660,8 @@ void launch_bp_structure(DBP& b, const DGraph& g, cudaStream_t st) {
     ug::launch(bp_mark_kernel, blocks, 256, 0, st, b, g);
     int rb = min(4 * 152, (b.n_res * 32 + 255) / 256);
     ug::launch((bp_rows_kernel<0>), rb, 256, 0, st, b);
-    launch_scan(b.row_count, b.row_ptr, b.n_res, b.n_ent, st);
+    launch_scan(b.row_count, b.row_ptr, b.n_res, b.n_ent, st, nullptr, b.ent_cap, b.status, ST_RES_EDGE_OVERFLOW);
     ug::launch((bp_rows_kernel<1>), rb, 256, 0, st, b);
-    ug::launch(bp_cap_check_kernel, 1, 1, 0, st, b);
     ug::launch(bp_entry_init_kernel, blocks, 256, 0, st, b);
     ug::launch(bp_edge_energy_kernel, blocks, 256, 0, st, b, g);
     ug::launch(bp_pair_prob_kernel, blocks, 256, 0, st, b);

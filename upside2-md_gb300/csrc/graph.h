@@ -174,7 +174,10 @@ void bp_variant_desc(int i, int* cluster, int* lanes, int* threads);
 
 // --------------------------------------------------------------- launchers --
 // skip_unless: optional device flag; the scan does nothing when it reads 0
-void launch_scan(const int* in, int* out, int n, int* total_out, cudaStream_t st, const int* skip_unless = nullptr);
+// exclusive scan by one block; skip_unless: run only if *skip_unless; cap >= 0:
+// a total beyond cap sets `bit` in *status and is stored as cap
+void launch_scan(const int* in, int* out, int n, int* total_out, cudaStream_t st, const int* skip_unless = nullptr,
+                 int cap = -1, int* status = nullptr, int bit = ST_EDGE_OVERFLOW);
 void launch_pack_positions(const DGraph& g, cudaStream_t st);
 void launch_pairs(const DGraph& g, cudaStream_t st);
 void launch_edge_eval(const DGraph& g, int* sys_start, int* sys_end, cudaStream_t st);
