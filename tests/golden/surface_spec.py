@@ -23,10 +23,9 @@ def lateral_table():
     """A synthetic lateral pressure profile (z, bar) over [-32, 30], large
     and nonzero at its lower end (where the reference's spline coordinate
     reads it inside the profile's range), so that the lateral forces are of
-    the order of the other membrane forces."""
-    z = np.arange(-32., 31., 2.)
-    p = 4000. * np.cos(z / 6.) * np.exp(-(z / 25.) ** 2) + 1500.
-    return np.column_stack((z, p))
+    the order of the other membrane forces (the M1 workload's profile)."""
+    import workloads
+    return workloads.lateral_pressure_profile()
 
 
 def write(path, variant, pos=None, n_res=N_RES, seed=SEED):

@@ -8,6 +8,10 @@
   C4  64 independent chains, lengths uniform in [40, 400], T uniform in [0.80, 0.95]
   C5  8 chains of 250 residues in one system (2000 residues), spaced apart,
       in a periodic box of side 200 A when the box mode is asked for
+  M1  64 chains, lengths uniform in [40, 200], T uniform in [0.80, 0.95], in a
+      30 A membrane with the surface node (lipid-diffusion method) and the
+      surface-dependent CB, H/O and lateral-pressure terms (not one of the
+      five; it measures the membrane path)
 
 Sequences are drawn uniformly over the 20 amino acids from the seed; initial
 structures are random (phi, psi) chains (py/upside_config.py:186-201).  Files
@@ -48,6 +52,13 @@ def _cfg(name, seed, n_res, **kw):
     return path
 
 
+def lateral_pressure_profile():
+    """A synthetic lateral pressure profile (z, bar) over [-32, 30] A."""
+    z = np.arange(-32., 31., 2.)
+    p = 4000. * np.cos(z / 6.) * np.exp(-(z / 25.) ** 2) + 1500.
+    return np.column_stack((z, p))
+
+
 def n_res_of(path):
     from h5lite import H5File
     with H5File(path) as f:
@@ -76,6 +87,12 @@ def workload(name, seed=1):
         offsets = np.array([[60.0 * (k % 4) - 90.0, 60.0 * (k // 4) - 30.0, 0.0] for k in range(8)])
         cfgs = [_cfg("C5", seed, 2000, chain_first_residue=starts, chain_offsets=offsets)]
         temps = [0.85]
+    elif name == "M1":
+        rng = np.random.RandomState(2000 + seed)
+        lengths = rng.randint(40, 201, size=64)
+        cfgs = [_cfg("M1c%02d" % i, seed * 100 + i, int(n), membrane_thickness=30., surface=1, channel_membrane=True,
+                     lateral_pressure=lateral_pressure_profile()) for i, n in enumerate(lengths)]
+        temps = list(rng.uniform(0.80, 0.95, size=64))
     else:
         raise ValueError("unknown workload " + name)
     n_res = [n_res_of(c) for c in cfgs]
