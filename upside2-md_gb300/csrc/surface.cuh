@@ -455,9 +455,9 @@ __global__ void __launch_bounds__(256, WMAX <= 2 ? 4 : 1) surface_turn_kernel(Su
         return int(v[0] == lo) | (int(v[0] == hi) << 1) | (bit(M2, r, v[0]) << 2) | (bit(M3, r, v[0]) << 3);
     };
     // 5. fine extremes over the surface atoms, their auxiliary points and the
-    // CBs' auxiliary points and CBs (src/surface.cpp:471-594)
-    for (int p = tid; p < na * per; p += bd) {
-        const int k = p / per, j = p - k * per;
+    // CBs' auxiliary points and CBs (src/surface.cpp:471-594): a thread per
+    // atom; only atoms in a surface voxel go through their points
+    for (int k = tid; k < na; k += bd) {
         float x, y, z;
         point(k, 0, x, y, z);
         int v[3], q[3];
@@ -466,25 +466,27 @@ __global__ void __launch_bounds__(256, WMAX <= 2 ? 4 : 1) surface_turn_kernel(Su
         const int lab = labels(v);
         if (!lab) continue;
         surf_cell(x, y, z, side, s2, q);
-        int c[3];
-        if (j == 0) {
-            c[0] = q[0]; c[1] = q[1];
-        } else {
-            float px, py, pz;
-            point(k, j, px, py, pz);
-            surf_cell(px, py, pz, side, s2, c);
-        }
-        if (j <= D.n_aux) {  // the point itself or a y-offset point: x extremes of its fine row
-            const int kj = c[1] * zs + q[2];
-            if (kj < 0 || kj >= nfx) { atomicOr(status, ST_SURFACE_GRID); continue; }
-            if (lab & 1) atomicMin(&fxmn[kj], c[0]);
-            if (lab & 2) atomicMax(&fxmx[kj], c[0]);
-        }
-        if (j == 0 || j > D.n_aux) {  // the point itself or an x-offset point: y extremes
-            const int ki = c[0] * zs + q[2];
-            if (ki < 0 || ki >= nfy) { atomicOr(status, ST_SURFACE_GRID); continue; }
-            if (lab & 4) atomicMin(&fymn[ki], c[1]);
-            if (lab & 8) atomicMax(&fymx[ki], c[1]);
+        for (int j = 0; j < per; ++j) {
+            int c[3];
+            if (j == 0) {
+                c[0] = q[0]; c[1] = q[1];
+            } else {
+                float px, py, pz;
+                point(k, j, px, py, pz);
+                surf_cell(px, py, pz, side, s2, c);
+            }
+            if (j <= D.n_aux) {  // the point itself or a y-offset point: x extremes of its fine row
+                const int kj = c[1] * zs + q[2];
+                if (kj < 0 || kj >= nfx) { atomicOr(status, ST_SURFACE_GRID); continue; }
+                if (lab & 1) atomicMin(&fxmn[kj], c[0]);
+                if (lab & 2) atomicMax(&fxmx[kj], c[0]);
+            }
+            if (j == 0 || j > D.n_aux) {  // the point itself or an x-offset point: y extremes
+                const int ki = c[0] * zs + q[2];
+                if (ki < 0 || ki >= nfy) { atomicOr(status, ST_SURFACE_GRID); continue; }
+                if (lab & 4) atomicMin(&fymn[ki], c[1]);
+                if (lab & 8) atomicMax(&fymx[ki], c[1]);
+            }
         }
     }
     __syncthreads();
