@@ -2768,7 +2768,6 @@ struct RotamerNode : GNode {
         wd.max_chain = max_chain;
         size_t n = size_t(b.n_res);
         wd.X = e.alloc<uint16_t>(n * WARM_IN);
-        wd.Zh = e.alloc<float>(n * WARM_HID);
         wd.H1 = e.alloc<uint16_t>(n * WARM_HID);
         wd.H2 = e.alloc<uint16_t>(n * WARM_HID);
         wd.Z = e.alloc<float>(n * WARM_OUT);

@@ -41,10 +41,15 @@ constexpr int GT_M = 64, GT_N = 64, GT_K = 32;
 
 __device__ __forceinline__ uint32_t pack2(uint16_t lo, uint16_t hi) { return uint32_t(lo) | (uint32_t(hi) << 16); }
 
+// With bias given, the epilogue writes act(A.B + bias) instead of C: as
+// bf16 to H and / or as FP32 to Hf (both row-major, ldc), act = ReLU or
+// identity; the sum is the one bias_act_kernel forms from a stored C.
 __global__ void __launch_bounds__(128) gemm_bf16_kernel(const uint16_t* __restrict__ A, long long a_r, long long a_c,
                                                         const uint16_t* __restrict__ B, long long b_r, long long b_c,
                                                         float* __restrict__ C, int ldc, int M, int N, int K,
-                                                        int accumulate, const int* __restrict__ need) {
+                                                        int accumulate, const int* __restrict__ need,
+                                                        const float* __restrict__ bias, uint16_t* __restrict__ H,
+                                                        float* __restrict__ Hf, int relu) {
     grid_dep_entry();
     if (need && !*need) return;  // block-uniform: nothing to compute this time
     __shared__ uint16_t As[GT_M][GT_K + 8];  // [m][k]
@@ -112,8 +117,15 @@ __global__ void __launch_bounds__(128) gemm_bf16_kernel(const uint16_t* __restri
                 int row = m0 + wm + i * 16 + g + (r >= 2 ? 8 : 0);
                 int col = n0 + wn + j * 8 + 2 * t + (r & 1);
                 if (row < M && col < N) {
-                    float* c = C + size_t(row) * ldc + col;
-                    *c = accumulate ? *c + acc[i][j][r] : acc[i][j][r];
+                    if (bias) {
+                        float v = acc[i][j][r] + bias[col];
+                        if (relu) v = fmaxf(v, 0.f);
+                        if (H) H[size_t(row) * ldc + col] = f2bf(v);
+                        if (Hf) Hf[size_t(row) * ldc + col] = v;
+                    } else {
+                        float* c = C + size_t(row) * ldc + col;
+                        *c = accumulate ? *c + acc[i][j][r] : acc[i][j][r];
+                    }
                 }
             }
 }
@@ -123,8 +135,18 @@ cudaError_t launch_gemm_bf16(const uint16_t* A, long long a_r, long long a_c, co
                              const int* need) {
     if (M <= 0 || N <= 0) return cudaSuccess;
     dim3 grid((N + GT_N - 1) / GT_N, (M + GT_M - 1) / GT_M);
-    ug::launch(gemm_bf16_kernel, grid, 128, 0, st, A, a_r, a_c, B, b_r, b_c, C, ldc, M, N, K, accumulate, need);
+    ug::launch(gemm_bf16_kernel, grid, 128, 0, st, A, a_r, a_c, B, b_r, b_c, C, ldc, M, N, K, accumulate, need,
+               static_cast<const float*>(nullptr), static_cast<uint16_t*>(nullptr), static_cast<float*>(nullptr), 0);
     return cudaGetLastError();
+}
+// act(A.B + bias) into H (bf16) and / or Hf (FP32), row stride N
+static void launch_gemm_bf16_act(const uint16_t* A, long long a_r, long long a_c, const uint16_t* B, long long b_r,
+                                 long long b_c, int M, int N, int K, const float* bias, uint16_t* H, float* Hf,
+                                 int relu, cudaStream_t st, const int* need) {
+    if (M <= 0 || N <= 0) return;
+    dim3 grid((N + GT_N - 1) / GT_N, (M + GT_M - 1) / GT_M);
+    ug::launch(gemm_bf16_kernel, grid, 128, 0, st, A, a_r, a_c, B, b_r, b_c, static_cast<float*>(nullptr), N, M, N, K,
+               0, need, bias, H, Hf, relu);
 }
 
 // ---------------------------------------------------------- epilogues ---
@@ -287,8 +309,19 @@ __global__ void warm_features_kernel(WarmDev w, const float* __restrict__ pos, c
                                      const int* __restrict__ res_off, const float* __restrict__ prob,
                                      const int* __restrict__ nrot) {
     grid_dep_entry();
-    if (w.need && !*w.need) return;  // block-uniform
     const int s = blockIdx.x;
+    if (w.stat && w.need && blockIdx.x == 0 && blockIdx.y == 0) {
+        // need = 1 when some system's coming solve starts from the prediction
+        // (the statistics are final: the previous solve updated them); the
+        // network's kernels read it after this kernel
+        __shared__ int any;
+        if (threadIdx.x == 0) any = 0;
+        __syncthreads();
+        for (int u = threadIdx.x; u < w.n_sys; u += blockDim.x)
+            if (warm_start_used(w.stat + 4 * u)) any = 1;
+        __syncthreads();
+        if (threadIdx.x == 0) *w.need = any;
+    }
     // only systems whose solve starts from the prediction need features
     if (w.stat && !warm_start_used(w.stat + 4 * s)) return;
     extern __shared__ float wsm[];
@@ -408,32 +441,18 @@ void launch_warm_features(const WarmDev& w, const float* pos, const int* atom_of
     ug::launch(warm_features_kernel, dim3(unsigned(n_sys), 4), 128, smem, st, w, pos, atom_off, res_off, prob, nrot);
 }
 
-// need = 1 when some system's coming solve starts from the prediction (the
-// statistics are final: the previous solve updated them)
-__global__ void warm_need_kernel(WarmDev w) {
-    grid_dep_entry();
-    __shared__ int any;
-    if (threadIdx.x == 0) any = 0;
-    __syncthreads();
-    for (int s = threadIdx.x; s < w.n_sys; s += blockDim.x)
-        if (warm_start_used(w.stat + 4 * s)) any = 1;
-    __syncthreads();
-    if (threadIdx.x == 0) *w.need = any;
-}
-
 cudaError_t launch_warm_start(const WarmDev& w, const float* pos, const int* atom_off, const int* res_off,
                               const float* prob, const int* nrot, int n_sys, int n_res, cudaStream_t st) {
-    // when no system starts from the prediction in this solve, every kernel
-    // below returns at once
-    ug::launch(warm_need_kernel, 1, 256, 0, st, w);
+    // the features kernel sets need; when no system starts from the
+    // prediction in this solve, every kernel after it returns at once
     launch_warm_features(w, pos, atom_off, res_off, prob, nrot, n_sys, st);
-    // X[n x 64] . W1[64 x 128] -> H1; H1 . W2 -> H2; H2 . W3[128 x 8] -> Z
-    launch_gemm_bf16(w.X, WARM_IN, 1, w.W1, WARM_HID, 1, w.Zh, WARM_HID, n_res, WARM_HID, WARM_IN, 0, st, w.need);
-    launch_bias_act(w.Zh, w.b1, w.H1, nullptr, n_res, WARM_HID, 1, st, w.need);
-    launch_gemm_bf16(w.H1, WARM_HID, 1, w.W2, WARM_HID, 1, w.Zh, WARM_HID, n_res, WARM_HID, WARM_HID, 0, st, w.need);
-    launch_bias_act(w.Zh, w.b2, w.H2, nullptr, n_res, WARM_HID, 1, st, w.need);
-    launch_gemm_bf16(w.H2, WARM_HID, 1, w.W3, WARM_OUT, 1, w.Z, WARM_OUT, n_res, WARM_OUT, WARM_HID, 0, st, w.need);
-    launch_bias_act(w.Z, w.b3, nullptr, w.Z, n_res, WARM_OUT, 0, st, w.need);
+    // relu(X[n x 64] . W1[64 x 128] + b1) -> H1; relu(H1 . W2 + b2) -> H2;
+    // H2 . W3[128 x 8] + b3 -> Z
+    launch_gemm_bf16_act(w.X, WARM_IN, 1, w.W1, WARM_HID, 1, n_res, WARM_HID, WARM_IN, w.b1, w.H1, nullptr, 1, st, w.need);
+    launch_gemm_bf16_act(w.H1, WARM_HID, 1, w.W2, WARM_HID, 1, n_res, WARM_HID, WARM_HID, w.b2, w.H2, nullptr, 1, st,
+                         w.need);
+    launch_gemm_bf16_act(w.H2, WARM_HID, 1, w.W3, WARM_OUT, 1, n_res, WARM_OUT, WARM_HID, w.b3, nullptr, w.Z, 0, st,
+                         w.need);
     ug::launch(warm_softmax_kernel, nb(n_res), 256, 0, st, w, nrot, n_res);
     return cudaGetLastError();
 }

@@ -34,6 +34,7 @@ __host__ __device__ inline bool warm_start_used(const float* ws, float min_gain 
 
 struct WarmDev {
     int* need;             // device flag: some system starts from the prediction in this solve
+                           // (set by the features kernel)
     const float* stat;     // per-system sweep statistics (4 floats each)
     int n_sys;
     const int* node_res;   // BP node -> chain residue index within its system
@@ -46,7 +47,6 @@ struct WarmDev {
     const float* b2;
     const uint16_t* W3;    // WARM_HID x WARM_OUT
     const float* b3;
-    float* Zh;             // n_node x WARM_HID pre-activations (scratch)
     uint16_t* H1;          // n_node x WARM_HID
     uint16_t* H2;
     float* Z;              // n_node x WARM_OUT logits
