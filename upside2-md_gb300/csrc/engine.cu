@@ -2665,8 +2665,10 @@ struct RotamerNode : GNode {
     void forward_early(Engine& e) override {
         auto& beads = e.arg(*this, 0);
         hg.bind(beads, beads);
-        hg.search_and_eval(e.st);
         DBP bl = launch_state(e);
+        launch_bp_reset(bl, e.st);
+        launch_pairs(hg.g, e.st);
+        launch_rotamer_edges(bl, hg.g, e.st);
         launch_bp_structure(bl, hg.g, e.st);
     }
     // the bound DBP with the logging pointers of this evaluation
@@ -2768,9 +2770,6 @@ struct RotamerNode : GNode {
         wd.max_chain = max_chain;
         size_t n = size_t(b.n_res);
         wd.X = e.alloc<uint16_t>(n * WARM_IN);
-        wd.H1 = e.alloc<uint16_t>(n * WARM_HID);
-        wd.H2 = e.alloc<uint16_t>(n * WARM_HID);
-        wd.Z = e.alloc<float>(n * WARM_OUT);
         wd.belief = e.alloc<float>(n * 8);
         wd.W1 = e.alloc<uint16_t>(size_t(WARM_IN) * WARM_HID);
         wd.W2 = e.alloc<uint16_t>(size_t(WARM_HID) * WARM_HID);

@@ -758,16 +758,25 @@ __global__ void bp_bead_energy_kernel(DBP b, const float* p0, const float* p1, c
     }
 }
 
-// classify bead edges: mark multi-rotamer residue pairs; fold 1-rotamer
-// partners into node energies; sum 1-1 edges (src/rotamer.cpp:886-912)
-__global__ void bp_mark_kernel(DBP b, DGraph g) {
+// The rotamer graph's edge values and derivatives (edge_eval_kernel) and, from
+// each value at once, the classification of the bead edges: multi-rotamer
+// residue pairs marked in the dense map, 1-rotamer partners folded into node
+// energies, 1-1 edges summed (src/rotamer.cpp:886-912).  The slot reset
+// (bp_reset_kernel) runs before the pair search.
+__global__ void rotamer_edge_kernel(DGraph g, DBP b) {
     grid_dep_entry();
-    int ne = *g.n_edge;
+    const int ne = *g.n_edge;
+    const int dw = g.d1 + g.d2;
     for (int e = grid_stride_start(); e < ne; e += grid_stride()) {
-        int2 ij = g.edges[e];
-        int r1 = b.bead_res[ij.x], r2 = b.bead_res[ij.y];
-        int n1 = b.nrot[r1], n2 = b.nrot[r2];
-        float v = g.value[e];
+        const int2 ij = g.edges[e];
+        const float* pa = g.in1 + size_t(g.loc1[ij.x]) * g.w1;
+        const float* pb = g.in2 + size_t(g.loc2[ij.y]) * g.w2;
+        const float* p = g.param + (size_t(g.type1[ij.x]) * g.n_type2 + g.type2[ij.y]) * g.n_param;
+        float* da = g.deriv + size_t(e) * dw;
+        const float v = edge_value<IK_ROTAMER>(g, p, pa, pb, da, da + g.d1, true);
+        g.value[e] = v;
+        const int r1 = b.bead_res[ij.x], r2 = b.bead_res[ij.y];
+        const int n1 = b.nrot[r1], n2 = b.nrot[r2];
         if (n1 > 1 && n2 > 1) {
             b.slot[slot_index(b, r1, r2)] = -2;
             b.slot[slot_index(b, r2, r1)] = -2;
@@ -1651,13 +1660,19 @@ __global__ void bp_sens_kernel(DBP b, DGraph g, float* s0, float* s1, float* s2,
 // entries (CSR rows, reverse entries, descriptors), folded 1-rotamer partner
 // energies, the summed pair energies and their probability matrices.  It needs no one-body energy, so the
 // engine runs it as soon as the bead positions are known, while the one-body
-// inputs are still being computed.
+// inputs are still being computed.  Order: launch_bp_reset, the pair search,
+// launch_rotamer_edges (values and marks), launch_bp_structure.
+void launch_bp_reset(DBP& b, cudaStream_t st) {
+    // n_ent is rewritten only by the entry scan of launch_bp_structure, after
+    // this kernel completes
+    ug::launch(bp_reset_kernel, 2 * 152, 256, 0, st, b);
+    if (b.log_fe) cudaMemsetAsync(b.log_e11, 0, sizeof(float) * size_t(b.n_res), st);
+}
+void launch_rotamer_edges(DBP& b, const DGraph& g, cudaStream_t st) {
+    ug::launch(rotamer_edge_kernel, 2 * 152, 256, 0, st, g, b);
+}
 void launch_bp_structure(DBP& b, const DGraph& g, cudaStream_t st) {
     int blocks = 2 * 152;
-    // n_ent is rewritten only by the scan below, after this kernel completes
-    ug::launch(bp_reset_kernel, blocks, 256, 0, st, b);
-    if (b.log_fe) cudaMemsetAsync(b.log_e11, 0, sizeof(float) * size_t(b.n_res), st);
-    ug::launch(bp_mark_kernel, blocks, 256, 0, st, b, g);
     int rb = min(4 * 152, (b.n_res * 32 + 255) / 256);
     ug::launch((bp_rows_kernel<0>), rb, 256, 0, st, b);
     launch_scan(b.row_count, b.row_ptr, b.n_res, b.n_ent, st, nullptr, b.ent_cap, b.status, ST_RES_EDGE_OVERFLOW);

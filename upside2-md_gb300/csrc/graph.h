@@ -186,6 +186,8 @@ void launch_param_deriv(const DGraph& g, float* out, cudaStream_t st);
 // in: up to 4 one-body energy inputs (bead rows), in_sens their sensitivities
 // warm: learned warm start (null: off); pos / atom_off feed its features
 struct WarmDev;
+void launch_bp_reset(DBP& b, cudaStream_t st);
+void launch_rotamer_edges(DBP& b, const DGraph& g, cudaStream_t st);
 void launch_bp_structure(DBP& b, const DGraph& g, cudaStream_t st);
 void launch_bp(DBP& b, const DGraph& g, const float* const* in, float* const* in_sens, const int* w, int n_in,
                int prev_n_ent, int* scan_total, int want_energy, double* energy_out, const WarmDev* warm,

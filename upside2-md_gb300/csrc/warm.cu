@@ -41,15 +41,10 @@ constexpr int GT_M = 64, GT_N = 64, GT_K = 32;
 
 __device__ __forceinline__ uint32_t pack2(uint16_t lo, uint16_t hi) { return uint32_t(lo) | (uint32_t(hi) << 16); }
 
-// With bias given, the epilogue writes act(A.B + bias) instead of C: as
-// bf16 to H and / or as FP32 to Hf (both row-major, ldc), act = ReLU or
-// identity; the sum is the one bias_act_kernel forms from a stored C.
 __global__ void __launch_bounds__(128) gemm_bf16_kernel(const uint16_t* __restrict__ A, long long a_r, long long a_c,
                                                         const uint16_t* __restrict__ B, long long b_r, long long b_c,
                                                         float* __restrict__ C, int ldc, int M, int N, int K,
-                                                        int accumulate, const int* __restrict__ need,
-                                                        const float* __restrict__ bias, uint16_t* __restrict__ H,
-                                                        float* __restrict__ Hf, int relu) {
+                                                        int accumulate, const int* __restrict__ need) {
     grid_dep_entry();
     if (need && !*need) return;  // block-uniform: nothing to compute this time
     __shared__ uint16_t As[GT_M][GT_K + 8];  // [m][k]
@@ -117,15 +112,8 @@ __global__ void __launch_bounds__(128) gemm_bf16_kernel(const uint16_t* __restri
                 int row = m0 + wm + i * 16 + g + (r >= 2 ? 8 : 0);
                 int col = n0 + wn + j * 8 + 2 * t + (r & 1);
                 if (row < M && col < N) {
-                    if (bias) {
-                        float v = acc[i][j][r] + bias[col];
-                        if (relu) v = fmaxf(v, 0.f);
-                        if (H) H[size_t(row) * ldc + col] = f2bf(v);
-                        if (Hf) Hf[size_t(row) * ldc + col] = v;
-                    } else {
-                        float* c = C + size_t(row) * ldc + col;
-                        *c = accumulate ? *c + acc[i][j][r] : acc[i][j][r];
-                    }
+                    float* c = C + size_t(row) * ldc + col;
+                    *c = accumulate ? *c + acc[i][j][r] : acc[i][j][r];
                 }
             }
 }
@@ -135,18 +123,8 @@ cudaError_t launch_gemm_bf16(const uint16_t* A, long long a_r, long long a_c, co
                              const int* need) {
     if (M <= 0 || N <= 0) return cudaSuccess;
     dim3 grid((N + GT_N - 1) / GT_N, (M + GT_M - 1) / GT_M);
-    ug::launch(gemm_bf16_kernel, grid, 128, 0, st, A, a_r, a_c, B, b_r, b_c, C, ldc, M, N, K, accumulate, need,
-               static_cast<const float*>(nullptr), static_cast<uint16_t*>(nullptr), static_cast<float*>(nullptr), 0);
+    ug::launch(gemm_bf16_kernel, grid, 128, 0, st, A, a_r, a_c, B, b_r, b_c, C, ldc, M, N, K, accumulate, need);
     return cudaGetLastError();
-}
-// act(A.B + bias) into H (bf16) and / or Hf (FP32), row stride N
-static void launch_gemm_bf16_act(const uint16_t* A, long long a_r, long long a_c, const uint16_t* B, long long b_r,
-                                 long long b_c, int M, int N, int K, const float* bias, uint16_t* H, float* Hf,
-                                 int relu, cudaStream_t st, const int* need) {
-    if (M <= 0 || N <= 0) return;
-    dim3 grid((N + GT_N - 1) / GT_N, (M + GT_M - 1) / GT_M);
-    ug::launch(gemm_bf16_kernel, grid, 128, 0, st, A, a_r, a_c, B, b_r, b_c, static_cast<float*>(nullptr), N, M, N, K,
-               0, need, bias, H, Hf, relu);
 }
 
 // ---------------------------------------------------------- epilogues ---
@@ -408,28 +386,6 @@ __global__ void warm_features_kernel(WarmDev w, const float* __restrict__ pos, c
     }
 }
 
-// predicted marginals: softmax of the logits over the node's rotamers
-__global__ void warm_softmax_kernel(WarmDev w, const int* __restrict__ nrot, int n_res) {
-    grid_dep_entry();
-    if (w.need && !*w.need) return;
-    for (int u = grid_stride_start(); u < n_res; u += grid_stride()) {
-        int n = nrot[u];
-        const float* z = w.Z + size_t(u) * WARM_OUT;
-        float* b = w.belief + size_t(u) * 8;
-        float mx = z[0];
-        for (int k = 1; k < n; ++k) mx = fmaxf(mx, z[k]);
-        float p[8], s = 0.f;
-#pragma unroll
-        for (int k = 0; k < 8; ++k) {
-            p[k] = k < n ? expf(z[k] - mx) : 0.f;
-            s += p[k];
-        }
-        float inv = 1.f / s;
-#pragma unroll
-        for (int k = 0; k < 8; ++k) b[k] = p[k] * inv;
-    }
-}
-
 void launch_warm_features(const WarmDev& w, const float* pos, const int* atom_off, const int* res_off,
                           const float* prob, const int* nrot, int n_sys, cudaStream_t st) {
     size_t smem = size_t(w.max_chain) * 2 * sizeof(f3);
@@ -441,19 +397,143 @@ void launch_warm_features(const WarmDev& w, const float* pos, const int* atom_of
     ug::launch(warm_features_kernel, dim3(unsigned(n_sys), 4), 128, smem, st, w, pos, atom_off, res_off, prob, nrot);
 }
 
+// The whole network for a tile of 64 residues in one block (4 warps, 16 rows
+// each): the transposed weights are staged in shared memory once per block,
+// each warp carries its rows through the three layers (its activations stay
+// in its own 16 rows of one shared buffer) and finishes with the softmax over
+// each residue's rotamers (the predicted marginals).  The K steps and the
+// mma.sync shape are those of gemm_bf16_kernel (which the training path
+// uses), in the same order.
+constexpr int MLP_ROWS = 64;
+constexpr int MLP_PAD = 8;  // bf16 row padding of the staged buffers (bank spread)
+template <int NT>  // n-tiles of 8 columns
+__device__ __forceinline__ void mlp_layer(const uint16_t* Hs, int hld, const uint16_t* Wt, int wld, int K, int row0,
+                                          int g, int t, float (&acc)[NT][4]) {
+#pragma unroll
+    for (int j = 0; j < NT; ++j)
+#pragma unroll
+        for (int r = 0; r < 4; ++r) acc[j][r] = 0.f;
+    for (int kk = 0; kk < K; kk += 16) {
+        const int r = row0 + g;
+        const uint32_t a0 = pack2(Hs[r * hld + kk + 2 * t], Hs[r * hld + kk + 2 * t + 1]);
+        const uint32_t a1 = pack2(Hs[(r + 8) * hld + kk + 2 * t], Hs[(r + 8) * hld + kk + 2 * t + 1]);
+        const uint32_t a2 = pack2(Hs[r * hld + kk + 2 * t + 8], Hs[r * hld + kk + 2 * t + 9]);
+        const uint32_t a3 = pack2(Hs[(r + 8) * hld + kk + 2 * t + 8], Hs[(r + 8) * hld + kk + 2 * t + 9]);
+#pragma unroll
+        for (int j = 0; j < NT; ++j) {
+            const int c = j * 8 + g;
+            const uint32_t b0 = pack2(Wt[c * wld + kk + 2 * t], Wt[c * wld + kk + 2 * t + 1]);
+            const uint32_t b1 = pack2(Wt[c * wld + kk + 2 * t + 8], Wt[c * wld + kk + 2 * t + 9]);
+            asm volatile(
+                "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 "
+                "{%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};\n"
+                : "+f"(acc[j][0]), "+f"(acc[j][1]), "+f"(acc[j][2]), "+f"(acc[j][3])
+                : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+        }
+    }
+}
+__global__ void __launch_bounds__(128) warm_mlp_kernel(WarmDev w, const int* __restrict__ nrot, int n_res) {
+    grid_dep_entry();
+    if (w.need && !*w.need) return;  // block-uniform: no system starts from the prediction
+    extern __shared__ uint16_t mlp_sm[];
+    constexpr int LD_IN = WARM_IN + MLP_PAD, LD_HID = WARM_HID + MLP_PAD;
+    uint16_t* W1t = mlp_sm;                        // [WARM_HID][LD_IN]
+    uint16_t* W2t = W1t + WARM_HID * LD_IN;        // [WARM_HID][LD_HID]
+    uint16_t* W3t = W2t + WARM_HID * LD_HID;       // [WARM_OUT][LD_HID]
+    uint16_t* Xs = W3t + WARM_OUT * LD_HID;        // [MLP_ROWS][LD_IN]
+    uint16_t* Hs = Xs + MLP_ROWS * LD_IN;          // [MLP_ROWS][LD_HID]
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, g = lane >> 2, t = lane & 3;
+    for (int x = tid; x < WARM_IN * WARM_HID; x += 128) {  // W1 is [k][n]
+        const int k = x / WARM_HID, n = x % WARM_HID;
+        W1t[n * LD_IN + k] = w.W1[x];
+    }
+    for (int x = tid; x < WARM_HID * WARM_HID; x += 128) {
+        const int k = x / WARM_HID, n = x % WARM_HID;
+        W2t[n * LD_HID + k] = w.W2[x];
+    }
+    for (int x = tid; x < WARM_HID * WARM_OUT; x += 128) {
+        const int k = x / WARM_OUT, n = x % WARM_OUT;
+        W3t[n * LD_HID + k] = w.W3[x];
+    }
+    const int m0 = blockIdx.x * MLP_ROWS;
+    for (int x = tid; x < MLP_ROWS * WARM_IN; x += 128) {
+        const int r = x / WARM_IN, k = x % WARM_IN;
+        Xs[r * LD_IN + k] = m0 + r < n_res ? w.X[size_t(m0 + r) * WARM_IN + k] : uint16_t(0);
+    }
+    __syncthreads();
+    const int row0 = warp * 16;
+    float acc[WARM_HID / 8][4];
+    // layer 1: relu(X . W1 + b1) -> this warp's rows of Hs
+    mlp_layer(Xs, LD_IN, W1t, LD_IN, WARM_IN, row0, g, t, acc);
+#pragma unroll
+    for (int j = 0; j < WARM_HID / 8; ++j)
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            const int row = row0 + g + (r >= 2 ? 8 : 0), col = j * 8 + 2 * t + (r & 1);
+            Hs[row * LD_HID + col] = f2bf(fmaxf(acc[j][r] + w.b1[col], 0.f));
+        }
+    __syncwarp();
+    // layer 2: relu(H1 . W2 + b2), written over the warp's own rows once read
+    mlp_layer(Hs, LD_HID, W2t, LD_HID, WARM_HID, row0, g, t, acc);
+    __syncwarp();
+#pragma unroll
+    for (int j = 0; j < WARM_HID / 8; ++j)
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            const int row = row0 + g + (r >= 2 ? 8 : 0), col = j * 8 + 2 * t + (r & 1);
+            Hs[row * LD_HID + col] = f2bf(fmaxf(acc[j][r] + w.b2[col], 0.f));
+        }
+    __syncwarp();
+    // layer 3: H2 . W3 + b3 -> logits; softmax over the residue's rotamers
+    float a3[1][4];
+    mlp_layer(Hs, LD_HID, W3t, LD_HID, WARM_HID, row0, g, t, a3);
+#pragma unroll
+    for (int half = 0; half < 2; ++half) {
+        const int u = m0 + row0 + g + 8 * half;
+        float z0 = a3[0][2 * half] + w.b3[2 * t], z1 = a3[0][2 * half + 1] + w.b3[2 * t + 1];
+        // the residue's 8 logits from the 4 lanes of its quad, in order
+        float z[8];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            z[2 * q] = __shfl_sync(0xffffffffu, z0, (lane & ~3) | q);
+            z[2 * q + 1] = __shfl_sync(0xffffffffu, z1, (lane & ~3) | q);
+        }
+        if (u >= n_res || t != 0) continue;
+        const int n = nrot[u];
+        float mx = z[0];
+        for (int k = 1; k < n; ++k) mx = fmaxf(mx, z[k]);
+        float p[8], sum = 0.f;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            p[k] = k < n ? expf(z[k] - mx) : 0.f;
+            sum += p[k];
+        }
+        const float inv = 1.f / sum;
+        float* b = w.belief + size_t(u) * 8;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) b[k] = p[k] * inv;
+    }
+}
+constexpr size_t warm_mlp_smem() {
+    return sizeof(uint16_t) * (size_t(WARM_HID) * (WARM_IN + MLP_PAD) + size_t(WARM_HID) * (WARM_HID + MLP_PAD) +
+                               size_t(WARM_OUT) * (WARM_HID + MLP_PAD) + size_t(MLP_ROWS) * (WARM_IN + MLP_PAD) +
+                               size_t(MLP_ROWS) * (WARM_HID + MLP_PAD));
+}
+
 cudaError_t launch_warm_start(const WarmDev& w, const float* pos, const int* atom_off, const int* res_off,
                               const float* prob, const int* nrot, int n_sys, int n_res, cudaStream_t st) {
     // the features kernel sets need; when no system starts from the
     // prediction in this solve, every kernel after it returns at once
     launch_warm_features(w, pos, atom_off, res_off, prob, nrot, n_sys, st);
-    // relu(X[n x 64] . W1[64 x 128] + b1) -> H1; relu(H1 . W2 + b2) -> H2;
-    // H2 . W3[128 x 8] + b3 -> Z
-    launch_gemm_bf16_act(w.X, WARM_IN, 1, w.W1, WARM_HID, 1, n_res, WARM_HID, WARM_IN, w.b1, w.H1, nullptr, 1, st, w.need);
-    launch_gemm_bf16_act(w.H1, WARM_HID, 1, w.W2, WARM_HID, 1, n_res, WARM_HID, WARM_HID, w.b2, w.H2, nullptr, 1, st,
-                         w.need);
-    launch_gemm_bf16_act(w.H2, WARM_HID, 1, w.W3, WARM_OUT, 1, n_res, WARM_OUT, WARM_HID, w.b3, nullptr, w.Z, 0, st,
-                         w.need);
-    ug::launch(warm_softmax_kernel, nb(n_res), 256, 0, st, w, nrot, n_res);
+    // relu(X[n x 64] . W1[64 x 128] + b1) -> relu(. W2 + b2) -> . W3[128 x 8]
+    // + b3 -> softmax over the rotamers, in one kernel
+    static bool configured = false;
+    if (!configured) {
+        cudaFuncSetAttribute(warm_mlp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(warm_mlp_smem()));
+        configured = true;
+    }
+    if (n_res > 0)
+        ug::launch(warm_mlp_kernel, (n_res + MLP_ROWS - 1) / MLP_ROWS, 128, warm_mlp_smem(), st, w, nrot, n_res);
     return cudaGetLastError();
 }
 

@@ -47,9 +47,6 @@ struct WarmDev {
     const float* b2;
     const uint16_t* W3;    // WARM_HID x WARM_OUT
     const float* b3;
-    uint16_t* H1;          // n_node x WARM_HID
-    uint16_t* H2;
-    float* Z;              // n_node x WARM_OUT logits
     float* belief;         // n_node x 8 predicted marginals
 };
 
