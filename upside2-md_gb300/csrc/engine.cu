@@ -2624,6 +2624,14 @@ struct RotamerNode : GNode {
         b.row_ptr = e.alloc<int>(size_t(b.n_res) + 1);
         b.bead_res = e.upload(bead_res);
         b.bead_rot = e.upload(bead_rot);
+        if (std::is_sorted(bead_res.begin(), bead_res.end())) {
+            // beads grouped by residue: the one-body energies and node
+            // probabilities come from one pass per residue
+            std::vector<int> rbo(size_t(b.n_res) + 1, 0);
+            for (int r : bead_res) rbo[size_t(r) + 1] += 1;
+            for (size_t r = 0; r < size_t(b.n_res); ++r) rbo[r + 1] += rbo[r];
+            b.res_bead_off = e.upload(rbo);
+        }
         b.bead_loc = hg.g.loc1;
         b.n_ent = e.alloc<int>(1);
         alloc_entries(e, std::max(1024, 48 * b.n_res));

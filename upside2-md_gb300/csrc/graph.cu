@@ -259,27 +259,18 @@ __global__ void __launch_bounds__(256) pair_kernel(DGraph g) {
 
 // ----------------------------------------------------- candidate cache ---
 // A system's cache is rebuilt when any of its elements moved more than half
-// the buffer since its last rebuild, or when a rebuild of every system was
-// requested (src/interaction_graph.h:51-91: same bound, same comparison).
-// (one block)
-__global__ void cache_flag_init_kernel(DGraph g) {
-    grid_dep_entry();
-    __shared__ int any;
-    if (threadIdx.x == 0) any = 0;
-    __syncthreads();
-    int f = *g.cache_force;
-    for (int s = threadIdx.x; s < g.n_sys; s += blockDim.x) {
-        int x = f | g.sys_over[s];
-        g.sys_flag[s] = x;
-        if (x) any = 1;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) *g.any_flag = any;
-}
-
-// (also packs the positions the search reads)
+// the buffer since its last rebuild, when its segment overflowed at the last
+// rebuild, or when a rebuild of every system was requested
+// (src/interaction_graph.h:51-91: same bound, same comparison).
+// This kernel also packs the positions the search reads.  The flags it sets
+// were cleared, down to the systems whose segment overflowed, by the
+// previous evaluation's refine (cache_refine_kernel<1>, block 0).
 __global__ void cache_check_kernel(DGraph g) {
     grid_dep_entry();
+    if (*g.cache_force) {
+        for (int s = grid_stride_start(); s < g.n_sys; s += grid_stride()) g.sys_flag[s] = 1;
+        if (blockIdx.x == 0 && threadIdx.x == 0) *g.any_flag = 1;
+    }
     float h = 0.5f * ((g.cutoff + g.buffer) - g.cutoff);
     float lim = h * h;
     int n = g.n1 + (g.symmetric ? 0 : g.n2);
@@ -338,6 +329,20 @@ template <int PASS>
 __global__ void __launch_bounds__(256) cache_refine_kernel(DGraph g) {
     grid_dep_entry();
     __shared__ int warp_sum[8];
+    if (PASS == 1 && blockIdx.x == 0) {
+        // the next evaluation's rebuild flags: the systems whose segment
+        // overflowed (nothing later in this evaluation reads the flags)
+        __shared__ int s_any;
+        if (threadIdx.x == 0) s_any = 0;
+        __syncthreads();
+        for (int s = threadIdx.x; s < g.n_sys; s += blockDim.x) {
+            const int o = g.sys_over[s];
+            g.sys_flag[s] = o;
+            if (o) s_any = 1;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) *g.any_flag = s_any;
+    }
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int n_active = g.active_off[g.n_sys];
     const float c2 = g.cutoff * g.cutoff;
@@ -397,9 +402,10 @@ __global__ void __launch_bounds__(256) cache_refine_kernel(DGraph g) {
 }
 
 // Launches per evaluation: full search 4 (pack, count, scan with the edge
-// capacity check, fill); cached 9 (rebuild flags, movement check with the
-// position packing, rebuild count, scan, rebuild fill with the new reference
-// positions, commit, refine count, scan with the capacity check, refine fill).
+// capacity check, fill); cached 8 (movement check with the position packing,
+// rebuild count, scan, rebuild fill with the new reference positions,
+// commit, refine count, scan with the capacity check, refine fill with the
+// next evaluation's rebuild flags).
 void launch_pairs(const DGraph& g, cudaStream_t st) {
     if (g.n_rows == 0) {
         launch_pack_positions(g, st);
@@ -417,7 +423,6 @@ void launch_pairs(const DGraph& g, cudaStream_t st) {
     }
     int ne = g.n1 + (g.symmetric ? 0 : g.n2);
     int eb = min(1024, (ne + 255) / 256);
-    ug::launch(cache_flag_init_kernel, 1, 256, 0, st, g);
     ug::launch(cache_check_kernel, eb, 256, 0, st, g);
     ug::launch((pair_kernel<0, true>), blocks, 256, 0, st, g);
     launch_scan(g.row_count, g.row_off, g.n_rows, nullptr, st, g.any_flag);
@@ -879,6 +884,41 @@ __global__ void bp_edge_energy_kernel(DBP b, DGraph g) {
 }
 
 // node probabilities (src/rotamer.cpp:239-256, :398-405) and edge matrices
+// One-body energies and node probabilities in one pass (beads grouped by
+// residue): each residue's beads summed in bead order, as the reference fills
+// its node holders (src/rotamer.cpp:862-884), then bp_node_prob_kernel's
+// probabilities
+__global__ void bp_bead_prob_kernel(DBP b, const float* p0, const float* p1, const float* p2, const float* p3,
+                                    int n_in, int w0, int w1, int w2, int w3) {
+    grid_dep_entry();
+    for (int r = grid_stride_start(); r < b.n_res; r += grid_stride()) {
+        float E[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) E[k] = 0.f;
+        for (int i = b.res_bead_off[r]; i < b.res_bead_off[r + 1]; ++i) {
+            const int l = b.bead_loc[i];
+            float e = p0[size_t(l) * w0];
+            if (n_in > 1) e += p1[size_t(l) * w1];
+            if (n_in > 2) e += p2[size_t(l) * w2];
+            if (n_in > 3) e += p3[size_t(l) * w3];
+            const int k = b.bead_rot[i];
+#pragma unroll
+            for (int q = 0; q < 8; ++q)
+                if (q == k) E[q] += e;
+        }
+        const int n = b.nrot[r];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) b.E1[r * 8 + k] = E[k];
+        float m = E[0];
+#pragma unroll
+        for (int k = 1; k < 8; ++k)
+            if (k < n) m = fminf(m, E[k]);
+#pragma unroll
+        for (int k = 0; k < 8; ++k) b.prob[r * 8 + k] = k < n ? expf(m - E[k]) * expf(-b.E1x[r * 8 + k]) : 0.f;
+        b.eoff[r] = m;
+    }
+}
+
 __global__ void bp_node_prob_kernel(DBP b) {
     grid_dep_entry();
     for (int r = grid_stride_start(); r < b.n_res; r += grid_stride()) {
@@ -1692,8 +1732,13 @@ void launch_bp(DBP& b, const DGraph& g, const float* const* in, float* const* in
     int blocks = 2 * 152;
     (void)prev_n_ent;
     if (b.log_fe) cudaMemsetAsync(b.log_1b, 0, sizeof(float) * size_t(b.n_res) * size_t(n_in), st);
-    ug::launch(bp_bead_energy_kernel, blocks, 256, 0, st, b, in[0], in[1], in[2], in[3], n_in, w[0], w[1], w[2], w[3]);
-    ug::launch(bp_node_prob_kernel, blocks, 256, 0, st, b);
+    if (b.res_bead_off) {
+        ug::launch(bp_bead_prob_kernel, blocks, 256, 0, st, b, in[0], in[1], in[2], in[3], n_in, w[0], w[1], w[2], w[3]);
+    } else {
+        ug::launch(bp_bead_energy_kernel, blocks, 256, 0, st, b, in[0], in[1], in[2], in[3], n_in, w[0], w[1], w[2],
+                   w[3]);
+        ug::launch(bp_node_prob_kernel, blocks, 256, 0, st, b);
+    }
     if (warm) launch_warm_start(*warm, pos, atom_off, b.res_off, b.prob, b.nrot, b.n_sys, b.n_res, st);
     const BpVariant& v = bp_variants()[b.variant];
     // Compact layout: room for three times a block's share of nodes and ten

@@ -131,6 +131,7 @@ struct DBP {
     const int* bead_res;        // bead -> residue (global)
     const int* bead_rot;        // bead -> rotamer
     const int* bead_loc;        // bead -> row in the bead node output
+    const int* res_bead_off;    // residue -> its first bead (n_res+1) when the beads are in residue order, else null
     double* e11;                // per system sum of energies of 1-1 bead edges
     unsigned long long* bad_solves;  // per system: solves that ran into max_iter (cumulative)
     // per-node decomposition for the driver's logs (null: not computed):
