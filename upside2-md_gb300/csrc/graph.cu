@@ -133,10 +133,12 @@ __device__ __forceinline__ float pair_d2(float4 a, float4 b, const float* box) {
 // so the rows' hits come out in exactly the order of a warp scanning its
 // range alone.
 constexpr int PAIR_TILE = 256;
+__device__ void cache_commit(DGraph& g);
 template <int PASS, bool CACHED>
 __global__ void __launch_bounds__(256) pair_kernel(DGraph g) {
     grid_dep_entry();
     if (CACHED && !*g.any_flag) return;  // no system rebuilt in this evaluation
+    if (PASS == 1 && CACHED && blockIdx.x == 0) cache_commit(g);  // counts and tiles for the refine
     __shared__ float4 s_x[PAIR_TILE];
     __shared__ int s_id[PAIR_TILE];
     __shared__ int s_lo, s_hi;
@@ -293,10 +295,9 @@ __global__ void cache_check_kernel(DGraph g) {
 
 // after the rebuild search: per system candidate counts (capped by the
 // segment, overflow flagged), then the refine pass's tile prefix over systems
-// and the end of a rebuild-everything request (one block)
-__global__ void cache_commit_kernel(DGraph g) {
-    grid_dep_entry();
-    if (!*g.any_flag) return;  // nothing rebuilt: counts, tiles and request unchanged
+// and the end of a rebuild-everything request; run by one block (block 0 of
+// the rebuild's fill pass, from the scanned row offsets)
+__device__ void cache_commit(DGraph& g) {
     for (int s = threadIdx.x; s < g.n_sys; s += blockDim.x) {
         if (!g.sys_flag[s]) continue;
         atomicAdd(g.rebuilds, 1ull);
@@ -402,10 +403,10 @@ __global__ void __launch_bounds__(256) cache_refine_kernel(DGraph g) {
 }
 
 // Launches per evaluation: full search 4 (pack, count, scan with the edge
-// capacity check, fill); cached 8 (movement check with the position packing,
-// rebuild count, scan, rebuild fill with the new reference positions,
-// commit, refine count, scan with the capacity check, refine fill with the
-// next evaluation's rebuild flags).
+// capacity check, fill); cached 7 (movement check with the position packing,
+// rebuild count, scan, rebuild fill with the commit and the new reference
+// positions, refine count, scan with the capacity check, refine fill with
+// the next evaluation's rebuild flags).
 void launch_pairs(const DGraph& g, cudaStream_t st) {
     if (g.n_rows == 0) {
         launch_pack_positions(g, st);
@@ -427,7 +428,6 @@ void launch_pairs(const DGraph& g, cudaStream_t st) {
     ug::launch((pair_kernel<0, true>), blocks, 256, 0, st, g);
     launch_scan(g.row_count, g.row_off, g.n_rows, nullptr, st, g.any_flag);
     ug::launch((pair_kernel<1, true>), blocks, 256, 0, st, g);
-    ug::launch(cache_commit_kernel, 1, 256, 0, st, g);
     int rblocks = min(8 * 152, g.max_tiles);
     ug::launch((cache_refine_kernel<0>), rblocks, 256, 0, st, g);
     launch_scan(g.tile_count, g.tile_off, g.max_tiles, g.n_edge, st, nullptr, g.cap, g.status);
@@ -746,6 +746,7 @@ __global__ void bp_reset_kernel(DBP b) {
         b.E1x[r] = 0.f;
     }
     for (int s = grid_stride_start(); s < b.n_sys; s += grid_stride()) b.e11[s] = 0.0;
+    for (int r = grid_stride_start(); r < b.n_res; r += grid_stride()) b.row_count[r] = 0;
     if (b.reuse && blockIdx.x == 0 && threadIdx.x == 0) *b.parity ^= 1;  // new evaluation
 }
 
@@ -783,8 +784,9 @@ __global__ void rotamer_edge_kernel(DGraph g, DBP b) {
         const int r1 = b.bead_res[ij.x], r2 = b.bead_res[ij.y];
         const int n1 = b.nrot[r1], n2 = b.nrot[r2];
         if (n1 > 1 && n2 > 1) {
-            b.slot[slot_index(b, r1, r2)] = -2;
-            b.slot[slot_index(b, r2, r1)] = -2;
+            // each residue pair counts once in both rows' entry counts
+            if (atomicExch(&b.slot[slot_index(b, r1, r2)], -2) != -2) atomicAdd(&b.row_count[r1], 1);
+            if (atomicExch(&b.slot[slot_index(b, r2, r1)], -2) != -2) atomicAdd(&b.row_count[r2], 1);
         } else if (n1 == 1 && n2 == 1) {
             atomicAdd(&b.e11[b.res_sys[r1]], double(v));
             if (b.log_e11) {
@@ -799,9 +801,9 @@ __global__ void rotamer_edge_kernel(DGraph g, DBP b) {
     }
 }
 
-// warp per residue row of the dense map: count (PASS 0) or emit (PASS 1) the
-// marked neighbours in increasing order
-template <int PASS>
+// warp per residue row of the dense map: emit the marked neighbours in
+// increasing order at the row's scanned offset (the rows' counts come from the
+// marking, rotamer_edge_kernel)
 __global__ void bp_rows_kernel(DBP b) {
     grid_dep_entry();
     int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -812,47 +814,28 @@ __global__ void bp_rows_kernel(DBP b) {
         int s = b.res_sys[r];
         int rbase = b.res_off[s];
         long long row = b.slot_off[s] + (long long)b.res_local[r] * N;
-        int pos = PASS ? b.row_ptr[r] : 0;
-        int cnt = 0;
+        int pos = b.row_ptr[r];
         for (int c0 = 0; c0 < N; c0 += 32) {
             int c = c0 + lane;
             bool hit = c < N && b.slot[row + c] == -2;
             unsigned m = __ballot_sync(0xffffffffu, hit);
-            if (PASS == 0) {
-                cnt += __popc(m);
-            } else {
-                if (hit) {
-                    int p = pos + __popc(m & ((1u << lane) - 1u));
-                    if (p < b.ent_cap) {
-                        b.col[p] = rbase + c;
-                        b.erow[p] = r;
-                        b.slot[row + c] = p;
-                    } else {
-                        b.slot[row + c] = -1;
-                    }
+            if (hit) {
+                int p = pos + __popc(m & ((1u << lane) - 1u));
+                if (p < b.ent_cap) {
+                    b.col[p] = rbase + c;
+                    b.erow[p] = r;
+                    b.slot[row + c] = p;
+                    float4* z = reinterpret_cast<float4*>(b.esum + size_t(p) * 36);  // summed below
+#pragma unroll
+                    for (int q = 0; q < 9; ++q) z[q] = make_float4(0.f, 0.f, 0.f, 0.f);
+                } else {
+                    b.slot[row + c] = -1;
                 }
-                pos += __popc(m);
             }
+            pos += __popc(m);
         }
-        if (PASS == 0 && lane == 0) b.row_count[r] = cnt;
     }
 }
-
-__global__ void bp_entry_init_kernel(DBP b) {
-    grid_dep_entry();
-    int n = min(*b.n_ent, b.ent_cap);
-    for (int e = grid_stride_start(); e < n; e += grid_stride()) {
-        int rv = b.slot[slot_index(b, b.col[e], b.erow[e])];
-        if (rv < 0) {  // partner entry lost to overflow: point at itself, flag it
-            atomicOr(b.status, ST_RES_EDGE_OVERFLOW);
-            rv = e;
-        }
-        b.rev[e] = rv;
-        b.einfo[e] = make_int4(b.res_local[b.erow[e]], rv, b.res_local[b.col[e]], 0);
-    }
-    for (int i = grid_stride_start(); i < n * 36; i += grid_stride()) b.esum[i] = 0.f;
-}
-
 
 // Summed pair energies of the entries; and per bead edge, where the
 // sensitivity pass finds the edge's weight (eaux): an edge-marginal element
@@ -862,8 +845,21 @@ __global__ void bp_entry_init_kernel(DBP b) {
 #define BP_W_ONE (-1)
 #define BP_W_NODE (-2)
 #define BP_W_NONE INT_MIN
+// The same kernel completes the entries (reverse entry and descriptor; a
+// partner entry lost to overflow points at itself and is flagged); the
+// entries' energy sums were zeroed as the rows emitted them.
 __global__ void bp_edge_energy_kernel(DBP b, DGraph g) {
     grid_dep_entry();
+    const int n = min(*b.n_ent, b.ent_cap);
+    for (int e = grid_stride_start(); e < n; e += grid_stride()) {
+        int rv = b.slot[slot_index(b, b.col[e], b.erow[e])];
+        if (rv < 0) {
+            atomicOr(b.status, ST_RES_EDGE_OVERFLOW);
+            rv = e;
+        }
+        b.rev[e] = rv;
+        b.einfo[e] = make_int4(b.res_local[b.erow[e]], rv, b.res_local[b.col[e]], 0);
+    }
     int ne = *g.n_edge;
     for (int e = grid_stride_start(); e < ne; e += grid_stride()) {
         int2 ij = g.edges[e];
@@ -883,7 +879,6 @@ __global__ void bp_edge_energy_kernel(DBP b, DGraph g) {
     }
 }
 
-// node probabilities (src/rotamer.cpp:239-256, :398-405) and edge matrices
 // One-body energies and node probabilities in one pass (beads grouped by
 // residue): each residue's beads summed in bead order, as the reference fills
 // its node holders (src/rotamer.cpp:862-884), then bp_node_prob_kernel's
@@ -919,6 +914,7 @@ __global__ void bp_bead_prob_kernel(DBP b, const float* p0, const float* p1, con
     }
 }
 
+// node probabilities (src/rotamer.cpp:239-256, :398-405)
 __global__ void bp_node_prob_kernel(DBP b) {
     grid_dep_entry();
     for (int r = grid_stride_start(); r < b.n_res; r += grid_stride()) {
@@ -1714,10 +1710,8 @@ void launch_rotamer_edges(DBP& b, const DGraph& g, cudaStream_t st) {
 void launch_bp_structure(DBP& b, const DGraph& g, cudaStream_t st) {
     int blocks = 2 * 152;
     int rb = min(4 * 152, (b.n_res * 32 + 255) / 256);
-    ug::launch((bp_rows_kernel<0>), rb, 256, 0, st, b);
     launch_scan(b.row_count, b.row_ptr, b.n_res, b.n_ent, st, nullptr, b.ent_cap, b.status, ST_RES_EDGE_OVERFLOW);
-    ug::launch((bp_rows_kernel<1>), rb, 256, 0, st, b);
-    ug::launch(bp_entry_init_kernel, blocks, 256, 0, st, b);
+    ug::launch(bp_rows_kernel, rb, 256, 0, st, b);
     ug::launch(bp_edge_energy_kernel, blocks, 256, 0, st, b, g);
     ug::launch(bp_pair_prob_kernel, blocks, 256, 0, st, b);
 }
