@@ -1177,6 +1177,13 @@ __global__ void __launch_bounds__(THREADS, 65536 / (THREADS * 64)) bp_solve_kern
     const int s = blockIdx.x / BP_CLUSTER;
     const int r0 = b.res_off[s], r1 = b.res_off[s + 1], N = r1 - r0;
     const int e0 = b.row_ptr[r0], e1 = min(b.row_ptr[r1], b.ent_cap);
+    const bool compact = b.dsm_cap > 0;
+    // the system's row starts, staged in shared memory for the block splits
+    // (binary searches there instead of chains of dependent global loads);
+    // the layout below overwrites the staging area after the splits
+    int* s_rp = reinterpret_cast<int*>(compact ? smem + ((N + 3) & ~3) : smem);
+    for (int i = threadIdx.x; i <= N; i += blockDim.x) s_rp[i] = b.row_ptr[r0 + i];
+    __syncthreads();
     // own nodes [lo, hi) (system-local): block c starts at the first node whose
     // row begins at or after c/BP_CLUSTER of the system's entries
     auto split = [&](int c) -> int {
@@ -1186,12 +1193,12 @@ __global__ void __launch_bounds__(THREADS, 65536 / (THREADS * 64)) bp_solve_kern
         int a = 0, z = N;  // first ul in [0, N] with row_ptr[r0 + ul] >= target
         while (a < z) {
             int m = (a + z) >> 1;
-            if (b.row_ptr[r0 + m] >= target) z = m; else a = m + 1;
+            if (s_rp[m] >= target) z = m; else a = m + 1;
         }
         return a;
     };
     const int lo = split(crank), hi = split(crank + 1);
-    const int eo0 = min(b.row_ptr[r0 + lo], e1), eo1 = min(b.row_ptr[r0 + hi], e1);
+    const int eo0 = min(s_rp[lo], e1), eo1 = min(s_rp[hi], e1);
     float* EM[2] = {b.msg, b.msg + size_t(b.ent_cap) * 8};
     const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
 
@@ -1207,10 +1214,9 @@ __global__ void __launch_bounds__(THREADS, 65536 / (THREADS * 64)) bp_solve_kern
     if (tid <= BP_CLUSTER) {
         int sp = split(tid);
         s_nb[tid] = sp;
-        s_eb[tid] = min(b.row_ptr[r0 + sp], e1);
+        s_eb[tid] = min(s_rp[sp], e1);
     }
     __syncthreads();
-    const bool compact = b.dsm_cap > 0;
     bool fits = compact;
     for (int c = 0; c < BP_CLUSTER; ++c)
         if (s_eb[c + 1] - s_eb[c] > b.dsm_cap || s_nb[c + 1] - s_nb[c] > b.nb_cap) fits = false;
