@@ -93,6 +93,10 @@ void launch_scan(const int* in, int* out, int n, int* total_out, cudaStream_t st
     ug::launch(scan_kernel, 1, 1024, 0, st, in, out, n, total_out, skip_unless, cap, status, bit);
 }
 
+// blocks of the grid-stride kernels over edges and entries: their loops are
+// chains of dependent loads, so more warps in flight shorten them
+constexpr int EDGE_BLOCKS = 8 * 152;
+
 // --------------------------------------------------------- pair search ---
 __global__ void pack_kernel(const int* __restrict__ loc, const float* __restrict__ in, int w, int n,
                             float4* __restrict__ x) {
@@ -584,7 +588,7 @@ __global__ void edge_sys_bounds_kernel(DGraph g, int* start, int* end) {
 }
 
 void launch_edge_eval(const DGraph& g, int* sys_start, int* sys_end, cudaStream_t st) {
-    int blocks = 2 * 152;
+    int blocks = EDGE_BLOCKS;
     if (g.kind == IK_PHB) {
         if (g.cached) {
             cudaMemsetAsync(sys_start, 0, sizeof(int) * size_t(g.n_sys), st);
@@ -669,7 +673,7 @@ __global__ void edge_scatter_kernel(DGraph g) {
 }
 
 void launch_edge_scatter(const DGraph& g, cudaStream_t st) {
-    ug::launch(edge_scatter_kernel, 2 * 152, 256, 0, st, g);
+    ug::launch(edge_scatter_kernel, EDGE_BLOCKS, 256, 0, st, g);
 }
 
 // dE/dparam for the quadspline graphs, accumulated per type pair with the
@@ -1711,10 +1715,10 @@ void launch_bp_reset(DBP& b, cudaStream_t st) {
     if (b.log_fe) cudaMemsetAsync(b.log_e11, 0, sizeof(float) * size_t(b.n_res), st);
 }
 void launch_rotamer_edges(DBP& b, const DGraph& g, cudaStream_t st) {
-    ug::launch(rotamer_edge_kernel, 2 * 152, 256, 0, st, g, b);
+    ug::launch(rotamer_edge_kernel, EDGE_BLOCKS, 256, 0, st, g, b);
 }
 void launch_bp_structure(DBP& b, const DGraph& g, cudaStream_t st) {
-    int blocks = 2 * 152;
+    int blocks = EDGE_BLOCKS;
     int rb = min(4 * 152, (b.n_res * 32 + 255) / 256);
     launch_scan(b.row_count, b.row_ptr, b.n_res, b.n_ent, st, nullptr, b.ent_cap, b.status, ST_RES_EDGE_OVERFLOW);
     ug::launch(bp_rows_kernel, rb, 256, 0, st, b);
@@ -1729,7 +1733,7 @@ void launch_bp_structure(DBP& b, const DGraph& g, cudaStream_t st) {
 void launch_bp(DBP& b, const DGraph& g, const float* const* in, float* const* in_sens, const int* w, int n_in,
                int prev_n_ent, int* scan_total, int want_energy, double* energy_out, const WarmDev* warm,
                const float* pos, const int* atom_off, cudaStream_t st) {
-    int blocks = 2 * 152;
+    int blocks = EDGE_BLOCKS;
     (void)prev_n_ent;
     if (b.log_fe) cudaMemsetAsync(b.log_1b, 0, sizeof(float) * size_t(b.n_res) * size_t(n_in), st);
     if (b.res_bead_off) {
