@@ -418,7 +418,7 @@ void launch_pairs(const DGraph& g, cudaStream_t st) {
         cudaMemsetAsync(g.row_off, 0, sizeof(int), st);
         return;
     }
-    int blocks = min(4 * 152, (g.n_rows + 7) / 8);
+    int blocks = min(EDGE_BLOCKS, (g.n_rows + 7) / 8);
     if (!g.cached) {
         launch_pack_positions(g, st);
         ug::launch((pair_kernel<0, false>), blocks, 256, 0, st, g);
@@ -1711,7 +1711,7 @@ __global__ void bp_sens_kernel(DBP b, DGraph g, float* s0, float* s1, float* s2,
 void launch_bp_reset(DBP& b, cudaStream_t st) {
     // n_ent is rewritten only by the entry scan of launch_bp_structure, after
     // this kernel completes
-    ug::launch(bp_reset_kernel, 2 * 152, 256, 0, st, b);
+    ug::launch(bp_reset_kernel, EDGE_BLOCKS, 256, 0, st, b);
     if (b.log_fe) cudaMemsetAsync(b.log_e11, 0, sizeof(float) * size_t(b.n_res), st);
 }
 void launch_rotamer_edges(DBP& b, const DGraph& g, cudaStream_t st) {
@@ -1719,7 +1719,7 @@ void launch_rotamer_edges(DBP& b, const DGraph& g, cudaStream_t st) {
 }
 void launch_bp_structure(DBP& b, const DGraph& g, cudaStream_t st) {
     int blocks = EDGE_BLOCKS;
-    int rb = min(4 * 152, (b.n_res * 32 + 255) / 256);
+    int rb = min(EDGE_BLOCKS, (b.n_res * 32 + 255) / 256);
     launch_scan(b.row_count, b.row_ptr, b.n_res, b.n_ent, st, nullptr, b.ent_cap, b.status, ST_RES_EDGE_OVERFLOW);
     ug::launch(bp_rows_kernel, rb, 256, 0, st, b);
     ug::launch(bp_edge_energy_kernel, blocks, 256, 0, st, b, g);
