@@ -2075,31 +2075,11 @@ struct HBondEnergyNode : GNode {
 // ===================================================== hbond_coverage ===
 // coverage of side-chain beads by backbone H/O or hydrophobe points
 // (HBondCoverage, src/hbond.cpp:438-484)
-__global__ void zero_kernel(float* p, int n) {
-    grid_dep_entry();
-    for (int i = grid_stride_start(); i < n; i += grid_stride()) p[i] = 0.f;
-}
-__global__ void cov_accum(DGraph g, float* out, int by_first, int n_aa, const int* __restrict__ aa2) {
-    grid_dep_entry();
-    int ne = *g.n_edge;
-    for (int e = grid_stride_start(); e < ne; e += grid_stride()) {
-        int2 ij = g.edges[e];
-        int row = by_first ? (aa2 ? ij.x * n_aa + aa2[ij.y] : ij.x) : ij.y;
-        atomicAdd(out + row, g.value[e]);
-    }
-}
-__global__ void cov_esens(DGraph g, const float* __restrict__ sens, int by_first, int n_aa, const int* __restrict__ aa2) {
-    grid_dep_entry();
-    int ne = *g.n_edge;
-    for (int e = grid_stride_start(); e < ne; e += grid_stride()) {
-        int2 ij = g.edges[e];
-        int row = by_first ? (aa2 ? ij.x * n_aa + aa2[ij.y] : ij.x) : ij.y;
-        g.esens[e] = sens[row];
-    }
-}
 // one node class for hbond_coverage (rows = set 2), environment_coverage
 // (rows = set-1 element x amino-acid type of the bead's residue) and
-// hb_environment_coverage (rows = set 1)
+// hb_environment_coverage (rows = set 1).  The rows' sums are formed by the
+// graph's own kernels: zeroed by its pair search, added to by its edge
+// evaluation, and read back per edge by its scatter (DGraph cov_*).
 struct CoverageNode : GNode {
     HGraph hg;
     int by_first = 0, n_aa = 0;
@@ -2136,14 +2116,15 @@ struct CoverageNode : GNode {
     }
     void forward(Engine& e, bool) override {
         hg.bind(e.arg(*this, 0), e.arg(*this, 1));
+        hg.g.cov_out = out;
+        hg.g.cov_sens = sens;
+        hg.g.cov_n = total;
+        hg.g.cov_by_first = by_first;
+        hg.g.cov_n_aa = n_aa;
+        hg.g.cov_aa2 = aa2;
         hg.search_and_eval(e.st);
-        ug::launch(zero_kernel, nblk(total), 256, 0, e.st, out, total);
-        ug::launch(cov_accum, nblk(hg.g.cap), 256, 0, e.st, hg.g, out, by_first, n_aa, aa2);
     }
-    void backward(Engine& e) override {
-        ug::launch(cov_esens, nblk(hg.g.cap), 256, 0, e.st, hg.g, sens, by_first, n_aa, aa2);
-        launch_edge_scatter(hg.g, e.st);
-    }
+    void backward(Engine& e) override { launch_edge_scatter(hg.g, e.st); }
     std::vector<float> get_param(Engine&) override { return hg.param_host; }
     void set_param(Engine&, const std::vector<float>& p) override { hg.set_param(p); }
     std::vector<float> param_deriv(Engine& e) override {

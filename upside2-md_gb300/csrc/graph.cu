@@ -273,6 +273,7 @@ __global__ void __launch_bounds__(256) pair_kernel(DGraph g) {
 // previous evaluation's refine (cache_refine_kernel<1>, block 0).
 __global__ void cache_check_kernel(DGraph g) {
     grid_dep_entry();
+    for (int i = grid_stride_start(); i < g.cov_n; i += grid_stride()) g.cov_out[i] = 0.f;  // coverage sums
     if (*g.cache_force) {
         for (int s = grid_stride_start(); s < g.n_sys; s += grid_stride()) g.sys_flag[s] = 1;
         if (blockIdx.x == 0 && threadIdx.x == 0) *g.any_flag = 1;
@@ -412,6 +413,8 @@ __global__ void __launch_bounds__(256) cache_refine_kernel(DGraph g) {
 // positions, refine count, scan with the capacity check, refine fill with
 // the next evaluation's rebuild flags).
 void launch_pairs(const DGraph& g, cudaStream_t st) {
+    // coverage sums: zeroed by the movement check on the cached path
+    if (g.cov_out && (g.n_rows == 0 || !g.cached)) cudaMemsetAsync(g.cov_out, 0, sizeof(float) * size_t(g.cov_n), st);
     if (g.n_rows == 0) {
         launch_pack_positions(g, st);
         cudaMemsetAsync(g.n_edge, 0, sizeof(int), st);
@@ -539,6 +542,11 @@ __device__ float edge_value(const DGraph& g, const float* p, const float* a, con
     return 0.f;
 }
 
+// the coverage row an edge adds into
+__device__ __forceinline__ int cov_row(const DGraph& g, int2 ij) {
+    return g.cov_by_first ? (g.cov_aa2 ? ij.x * g.cov_n_aa + g.cov_aa2[ij.y] : ij.x) : ij.y;
+}
+
 template <int KIND>
 __global__ void edge_eval_kernel(DGraph g, const int* __restrict__ edge_sys_start, const int* __restrict__ edge_sys_end) {
     grid_dep_entry();
@@ -564,7 +572,10 @@ __global__ void edge_eval_kernel(DGraph g, const int* __restrict__ edge_sys_star
             }
         }
         float* da = g.deriv + size_t(e) * dw;
-        g.value[e] = edge_value<KIND>(g, p, a, b, da, da + g.d1, active);
+        const float v = edge_value<KIND>(g, p, a, b, da, da + g.d1, active);
+        g.value[e] = v;
+        if (KIND == IK_HBCOV || KIND == IK_ENVCOV || KIND == IK_HBENV)
+            if (g.cov_out) atomicAdd(g.cov_out + cov_row(g, ij), v);
     }
 }
 
@@ -648,7 +659,15 @@ __global__ void edge_scatter_kernel(DGraph g) {
     const int stride = grid_stride(), first = grid_stride_start() - (threadIdx.x & 31);
     for (int e0 = first; e0 < ne; e0 += stride) {
         const int e = e0 + (threadIdx.x & 31);
-        float s = e < ne ? g.esens[e] : 0.f;
+        float s = 0.f;
+        if (e < ne) {
+            if (g.cov_sens) {  // a coverage graph: the edge's sensitivity is its row's
+                s = g.cov_sens[cov_row(g, g.edges[e])];
+                g.esens[e] = s;
+            } else {
+                s = g.esens[e];
+            }
+        }
         int key = -1;
         float v1[SCATTER_MAXD];
         if (s != 0.f) {

@@ -83,6 +83,15 @@ struct DGraph {
     int* tile_off;              // max_tiles + 1
     unsigned long long* rebuilds;  // running count of system cache rebuilds
     int* any_flag;              // device scalar: some system is rebuilt in this evaluation
+    // coverage sums (hbond / environment coverage nodes; cov_out nullptr:
+    // none): the edge evaluation adds each edge value into cov_out[row(e)],
+    // and the scatter takes each edge's sensitivity from cov_sens[row(e)],
+    // with row(e) = cov_by_first ? (cov_aa2 ? i1 * cov_n_aa + cov_aa2[i2] : i1)
+    // : i2.  The pair search zeroes the cov_n sums first.
+    float* cov_out;
+    const float* cov_sens;
+    int cov_n, cov_by_first, cov_n_aa;
+    const int* cov_aa2;
 };
 
 // candidates per refine tile (one 256-thread block, 4 per thread)
