@@ -1902,37 +1902,18 @@ struct HGraph {
 
 // ====================================================== protein_hbond ===
 // hbond score per donor / acceptor in multiplicative space (ProteinHBond, src/hbond.cpp:357-435)
-__global__ void phb_init(int n, const int* __restrict__ src_row, const float* __restrict__ in, float* __restrict__ out) {
+// Each row: the donor's or acceptor's 6 input columns and its score
+// 1 - exp(-sum of its edge values).  The sums are zeroed by the graph's pair
+// search and added to by its edge evaluation (DGraph phb_row1/2); this
+// kernel copies the inputs and finishes the scores.  The scatter forms each
+// edge's sensitivity from its two rows.
+__global__ void phb_final(int n, const int* __restrict__ src_row, const float* __restrict__ in, float* out) {
     grid_dep_entry();
     for (int i = grid_stride_start(); i < n; i += grid_stride()) {
         const float* x = in + 6 * size_t(src_row[i]);
         float* o = out + 7 * size_t(i);
         for (int d = 0; d < 6; ++d) o[d] = x[d];
-        o[6] = 0.f;
-    }
-}
-__global__ void phb_accum(DGraph g, const int* __restrict__ row1, const int* __restrict__ row2, float* out) {
-    grid_dep_entry();
-    int ne = *g.n_edge;
-    for (int e = grid_stride_start(); e < ne; e += grid_stride()) {
-        int2 ij = g.edges[e];
-        float v = g.value[e];
-        atomicAdd(out + 7 * size_t(row1[ij.x]) + 6, v);
-        atomicAdd(out + 7 * size_t(row2[ij.y]) + 6, v);
-    }
-}
-__global__ void phb_final(int n, float* out) {
-    grid_dep_entry();
-    for (int i = grid_stride_start(); i < n; i += grid_stride()) out[7 * size_t(i) + 6] = 1.f - expf(-out[7 * size_t(i) + 6]);
-}
-__global__ void phb_esens(DGraph g, const int* __restrict__ row1, const int* __restrict__ row2, const float* __restrict__ out,
-                          const float* __restrict__ sens) {
-    grid_dep_entry();
-    int ne = *g.n_edge;
-    for (int e = grid_stride_start(); e < ne; e += grid_stride()) {
-        int2 ij = g.edges[e];
-        size_t a = 7 * size_t(row1[ij.x]) + 6, b = 7 * size_t(row2[ij.y]) + 6;
-        g.esens[e] = sens[a] * (1.f - out[a]) + sens[b] * (1.f - out[b]);
+        o[6] = 1.f - expf(-o[6]);
     }
 }
 __global__ void phb_pass(int n, const int* __restrict__ src_row, const float* __restrict__ sens, float* in_sens) {
@@ -1967,14 +1948,17 @@ struct ProteinHBondNode : GNode {
     void forward(Engine& e, bool) override {
         auto& in = e.arg(*this, 0);
         hg.bind(in, in);
-        ug::launch(phb_init, nblk(total), 256, 0, e.st, total, src, in.out, out);
+        hg.g.cov_out = out;
+        hg.g.cov_sens = sens;
+        hg.g.cov_n = total;
+        hg.g.cov_w = 7;
+        hg.g.phb_row1 = row1;
+        hg.g.phb_row2 = row2;
         hg.search_and_eval(e.st);
-        ug::launch(phb_accum, nblk(hg.g.cap), 256, 0, e.st, hg.g, row1, row2, out);
-        ug::launch(phb_final, nblk(total), 256, 0, e.st, total, out);
+        ug::launch(phb_final, nblk(total), 256, 0, e.st, total, src, in.out, out);
     }
     void backward(Engine& e) override {
         auto& in = e.arg(*this, 0);
-        ug::launch(phb_esens, nblk(hg.g.cap), 256, 0, e.st, hg.g, row1, row2, out, sens);
         launch_edge_scatter(hg.g, e.st);
         ug::launch(phb_pass, nblk(total), 256, 0, e.st, total, src, sens, in.sens);
     }
@@ -2119,6 +2103,7 @@ struct CoverageNode : GNode {
         hg.g.cov_out = out;
         hg.g.cov_sens = sens;
         hg.g.cov_n = total;
+        hg.g.cov_w = 1;
         hg.g.cov_by_first = by_first;
         hg.g.cov_n_aa = n_aa;
         hg.g.cov_aa2 = aa2;

@@ -273,7 +273,8 @@ __global__ void __launch_bounds__(256) pair_kernel(DGraph g) {
 // previous evaluation's refine (cache_refine_kernel<1>, block 0).
 __global__ void cache_check_kernel(DGraph g) {
     grid_dep_entry();
-    for (int i = grid_stride_start(); i < g.cov_n; i += grid_stride()) g.cov_out[i] = 0.f;  // coverage sums
+    for (int i = grid_stride_start(); i < g.cov_n; i += grid_stride())  // coverage sums
+        g.cov_out[size_t(i) * g.cov_w + g.cov_w - 1] = 0.f;
     if (*g.cache_force) {
         for (int s = grid_stride_start(); s < g.n_sys; s += grid_stride()) g.sys_flag[s] = 1;
         if (blockIdx.x == 0 && threadIdx.x == 0) *g.any_flag = 1;
@@ -412,9 +413,14 @@ __global__ void __launch_bounds__(256) cache_refine_kernel(DGraph g) {
 // rebuild count, scan, rebuild fill with the commit and the new reference
 // positions, refine count, scan with the capacity check, refine fill with
 // the next evaluation's rebuild flags).
+__global__ void cov_zero_kernel(DGraph g) {
+    grid_dep_entry();
+    for (int i = grid_stride_start(); i < g.cov_n; i += grid_stride()) g.cov_out[size_t(i) * g.cov_w + g.cov_w - 1] = 0.f;
+}
+
 void launch_pairs(const DGraph& g, cudaStream_t st) {
     // coverage sums: zeroed by the movement check on the cached path
-    if (g.cov_out && (g.n_rows == 0 || !g.cached)) cudaMemsetAsync(g.cov_out, 0, sizeof(float) * size_t(g.cov_n), st);
+    if (g.cov_out && (g.n_rows == 0 || !g.cached)) ug::launch(cov_zero_kernel, EDGE_BLOCKS, 256, 0, st, g);
     if (g.n_rows == 0) {
         launch_pack_positions(g, st);
         cudaMemsetAsync(g.n_edge, 0, sizeof(int), st);
@@ -574,8 +580,14 @@ __global__ void edge_eval_kernel(DGraph g, const int* __restrict__ edge_sys_star
         float* da = g.deriv + size_t(e) * dw;
         const float v = edge_value<KIND>(g, p, a, b, da, da + g.d1, active);
         g.value[e] = v;
-        if (KIND == IK_HBCOV || KIND == IK_ENVCOV || KIND == IK_HBENV)
+        if (KIND == IK_HBCOV || KIND == IK_ENVCOV || KIND == IK_HBENV) {
             if (g.cov_out) atomicAdd(g.cov_out + cov_row(g, ij), v);
+        } else if (KIND == IK_PHB) {
+            if (g.phb_row1) {
+                atomicAdd(g.cov_out + 7 * size_t(g.phb_row1[ij.x]) + 6, v);
+                atomicAdd(g.cov_out + 7 * size_t(g.phb_row2[ij.y]) + 6, v);
+            }
+        }
     }
 }
 
@@ -661,7 +673,12 @@ __global__ void edge_scatter_kernel(DGraph g) {
         const int e = e0 + (threadIdx.x & 31);
         float s = 0.f;
         if (e < ne) {
-            if (g.cov_sens) {  // a coverage graph: the edge's sensitivity is its row's
+            if (g.phb_row1) {  // protein hbonds: from the donor's and the acceptor's scores
+                const int2 ij = g.edges[e];
+                const size_t a = 7 * size_t(g.phb_row1[ij.x]) + 6, c = 7 * size_t(g.phb_row2[ij.y]) + 6;
+                s = g.cov_sens[a] * (1.f - g.cov_out[a]) + g.cov_sens[c] * (1.f - g.cov_out[c]);
+                g.esens[e] = s;
+            } else if (g.cov_sens) {  // a coverage graph: the edge's sensitivity is its row's
                 s = g.cov_sens[cov_row(g, g.edges[e])];
                 g.esens[e] = s;
             } else {

@@ -87,11 +87,17 @@ struct DGraph {
     // none): the edge evaluation adds each edge value into cov_out[row(e)],
     // and the scatter takes each edge's sensitivity from cov_sens[row(e)],
     // with row(e) = cov_by_first ? (cov_aa2 ? i1 * cov_n_aa + cov_aa2[i2] : i1)
-    // : i2.  The pair search zeroes the cov_n sums first.
+    // : i2.  The pair search zeroes the cov_n sums first (the last column of
+    // rows cov_w wide).  Protein hbonds (phb_row1 set): each edge value goes
+    // into the last column of both its donor's and its acceptor's row
+    // (phb_row1[i1], phb_row2[i2]), and the scatter forms the edge's
+    // sensitivity from both rows' (src/hbond.cpp:357-435).
     float* cov_out;
     const float* cov_sens;
-    int cov_n, cov_by_first, cov_n_aa;
+    int cov_n, cov_w, cov_by_first, cov_n_aa;
     const int* cov_aa2;
+    const int* phb_row1;
+    const int* phb_row2;
 };
 
 // candidates per refine tile (one 256-thread block, 4 per thread)
