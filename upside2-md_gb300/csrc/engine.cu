@@ -1655,7 +1655,7 @@ struct HGraph {
     Engine* eng = nullptr;
     int* edge_bufs_int = nullptr;
     void* bufs[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
-    void* cbufs[4] = {nullptr, nullptr, nullptr, nullptr};
+    void* cbufs[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
     std::vector<int> cache_cap;  // per system candidate capacity (multiple of CACHE_TILE)
 
     ~HGraph() {
@@ -1685,11 +1685,13 @@ struct HGraph {
         UG_CK(cudaMalloc(&cbufs[1], sizeof(int) * off.size()));
         UG_CK(cudaMalloc(&cbufs[2], sizeof(int) * (size_t(g.max_tiles) + 1)));
         UG_CK(cudaMalloc(&cbufs[3], sizeof(int) * (size_t(g.max_tiles) + 1)));
+        UG_CK(cudaMalloc(&cbufs[4], size_t(CACHE_TILE / 4) * std::max<size_t>(1, size_t(g.max_tiles))));
         UG_CK(cudaMemcpy(cbufs[1], off.data(), sizeof(int) * off.size(), cudaMemcpyHostToDevice));
         g.cache_edges = static_cast<int2*>(cbufs[0]);
         g.cache_off = static_cast<const int*>(cbufs[1]);
         g.tile_count = static_cast<int*>(cbufs[2]);
         g.tile_off = static_cast<int*>(cbufs[3]);
+        g.refine_mask = static_cast<unsigned char*>(cbufs[4]);
         UG_CK(cudaMemset(g.cache_n, 0, sizeof(int) * size_t(g.n_sys)));
         UG_CK(cudaMemset(g.sys_over, 0, sizeof(int) * size_t(g.n_sys)));
         UG_CK(cudaMemset(g.active_off, 0, sizeof(int) * (size_t(g.n_sys) + 1)));

@@ -370,14 +370,21 @@ __global__ void __launch_bounds__(256) cache_refine_kernel(DGraph g) {
         const int2* ce = g.cache_edges + g.cache_off[s];
         unsigned mask = 0;
         int2 ij[4];
+        unsigned char* tm = g.refine_mask + size_t(t) * (CACHE_TILE / 4) + tid;
+        if (PASS == 0) {
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            int k = first + q;
-            ij[q] = make_int2(0, 0);
-            if (k < n) {
-                ij[q] = ce[k];
-                if (pair_d2(g.x1[ij[q].x], X2[ij[q].y], g.box) < c2) mask |= 1u << q;
+            for (int q = 0; q < 4; ++q) {
+                int k = first + q;
+                if (k < n) {
+                    const int2 c = ce[k];
+                    if (pair_d2(g.x1[c.x], X2[c.y], g.box) < c2) mask |= 1u << q;
+                }
             }
+            *tm = (unsigned char)mask;  // the fill pass writes these candidates
+        } else {
+            mask = *tm;
+#pragma unroll
+            for (int q = 0; q < 4; ++q) ij[q] = (mask >> q & 1u) ? ce[first + q] : make_int2(0, 0);
         }
         int c = __popc(mask);
         int incl = c;

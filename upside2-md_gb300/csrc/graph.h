@@ -81,6 +81,7 @@ struct DGraph {
     int max_tiles;              // refine tiles if every segment were full
     int* tile_count;            // max_tiles + 1
     int* tile_off;              // max_tiles + 1
+    unsigned char* refine_mask; // per refine tile and thread: which of its 4 candidates are edges
     unsigned long long* rebuilds;  // running count of system cache rebuilds
     int* any_flag;              // device scalar: some system is rebuilt in this evaluation
     // coverage sums (hbond / environment coverage nodes; cov_out nullptr:
