@@ -27,8 +27,15 @@ namespace cg = cooperative_groups;
 
 // ---------------------------------------------------------------- scan ---
 // Exclusive scan of n ints into out[0..n] (out[n] = total) by one 1024-thread
-// block: each thread owns a contiguous chunk, then a block-level scan of the
-// chunk sums.
+// block, in tiles of SCAN_K x 1024: a tile is loaded into shared memory with
+// coalesced, independent loads, each thread scans its SCAN_K consecutive
+// elements there, a block-level scan of the thread sums (plus the carry of
+// the tiles before) gives their offsets, and the tile is stored back
+// coalesced.  Shared-memory indices are padded by one word per 32, so the
+// threads' runs of SCAN_K fall into different banks.
+constexpr int SCAN_K = 8, SCAN_TILE = 1024 * SCAN_K;
+__device__ __forceinline__ int scan_pad(int i) { return i + (i >> 5); }
+
 __global__ void __launch_bounds__(1024) scan_kernel(const int* __restrict__ in, int* __restrict__ out, int n,
                                                     int* total_out, const int* __restrict__ skip_unless, int cap,
                                                     int* status, int bit) {
@@ -38,53 +45,73 @@ __global__ void __launch_bounds__(1024) scan_kernel(const int* __restrict__ in, 
     // beyond the int range reads as "larger than any capacity" rather than
     // wrapping to a negative offset
     __shared__ long long warp_sums[32];
+    __shared__ int sm[SCAN_TILE + SCAN_TILE / 32];
     auto sat = [](long long x) { return int(x < 2147483647LL ? x : 2147483647LL); };
-    int t = threadIdx.x;
-    int per = (n + blockDim.x - 1) / blockDim.x;
-    int lo = min(n, t * per), hi = min(n, lo + per);
-    long long s = 0;
-    for (int i = lo; i < hi; ++i) s += in[i];
-    // block exclusive scan of s
-    int lane = t & 31, w = t >> 5;
-    long long v = s;
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+    long long carry = 0;
+    for (int base = 0; base < n; base += SCAN_TILE) {  // block-uniform
+        const int m = min(SCAN_TILE, n - base);
 #pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        long long y = __shfl_up_sync(0xffffffffu, v, o);
-        if (lane >= o) v += y;
-    }
-    if (lane == 31) warp_sums[w] = v;
-    __syncthreads();
-    if (w == 0) {
-        long long ws = warp_sums[lane];
+        for (int k = 0; k < SCAN_K; ++k) {
+            const int i = k * 1024 + t;
+            sm[scan_pad(i)] = i < m ? in[base + i] : 0;
+        }
+        __syncthreads();
+        int x[SCAN_K];
+        long long s = 0;
+#pragma unroll
+        for (int j = 0; j < SCAN_K; ++j) {
+            x[j] = sm[scan_pad(t * SCAN_K + j)];
+            s += x[j];
+        }
+        // block exclusive scan of s
+        long long v = s;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
-            long long y = __shfl_up_sync(0xffffffffu, ws, o);
-            if (lane >= o) ws += y;
+            long long y = __shfl_up_sync(0xffffffffu, v, o);
+            if (lane >= o) v += y;
         }
-        warp_sums[lane] = ws;
+        if (lane == 31) warp_sums[w] = v;
+        __syncthreads();
+        if (w == 0) {
+            long long ws = warp_sums[lane];
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                long long y = __shfl_up_sync(0xffffffffu, ws, o);
+                if (lane >= o) ws += y;
+            }
+            warp_sums[lane] = ws;
+        }
+        __syncthreads();
+        long long excl = carry + v - s + (w ? warp_sums[w - 1] : 0);
+        const long long tile_total = warp_sums[31];
+        // each thread rewrites only the run it read
+#pragma unroll
+        for (int j = 0; j < SCAN_K; ++j) {
+            sm[scan_pad(t * SCAN_K + j)] = sat(excl);
+            excl += x[j];
+        }
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < SCAN_K; ++k) {
+            const int i = k * 1024 + t;
+            if (i < m) out[base + i] = sm[scan_pad(i)];
+        }
+        carry += tile_total;
+        __syncthreads();  // sm and warp_sums are reused by the next tile
     }
-    __syncthreads();
-    long long excl = v - s + (w ? warp_sums[w - 1] : 0);
-    for (int i = lo; i < hi; ++i) {
-        out[i] = sat(excl);
-        excl += in[i];
-    }
-    if (t == blockDim.x - 1) {
-        out[n] = sat(excl);
+    if (t == 0) {
+        out[n] = sat(carry);
         if (total_out) {
             // with a capacity: a total beyond it is flagged and capped (the
             // fill pass writes no further)
-            int tot = sat(excl);
+            int tot = sat(carry);
             if (cap >= 0 && tot > cap) {
                 atomicOr(status, bit);
                 tot = cap;
             }
             *total_out = tot;
         }
-    }
-    if (n == 0 && t == 0) {
-        out[0] = 0;
-        if (total_out) *total_out = 0;
     }
 }
 
