@@ -889,24 +889,37 @@ __global__ void bp_rows_kernel(DBP b) {
         int rbase = b.res_off[s];
         long long row = b.slot_off[s] + (long long)b.res_local[r] * N;
         int pos = b.row_ptr[r];
-        for (int c0 = 0; c0 < N; c0 += 32) {
-            int c = c0 + lane;
-            bool hit = c < N && b.slot[row + c] == -2;
-            unsigned m = __ballot_sync(0xffffffffu, hit);
-            if (hit) {
-                int p = pos + __popc(m & ((1u << lane) - 1u));
-                if (p < b.ent_cap) {
-                    b.col[p] = rbase + c;
-                    b.erow[p] = r;
-                    b.slot[row + c] = p;
-                    float4* z = reinterpret_cast<float4*>(b.esum + size_t(p) * 36);  // summed below
+        // the row's slots are read a batch of ROWS_BATCH x 32 at a time, all
+        // loads in flight together, before any of them is rewritten (only
+        // this warp touches the row)
+        constexpr int ROWS_BATCH = 16;
+        for (int c00 = 0; c00 < N; c00 += 32 * ROWS_BATCH) {
+            int v[ROWS_BATCH];
 #pragma unroll
-                    for (int q = 0; q < 9; ++q) z[q] = make_float4(0.f, 0.f, 0.f, 0.f);
-                } else {
-                    b.slot[row + c] = -1;
-                }
+            for (int k = 0; k < ROWS_BATCH; ++k) {
+                const int c = c00 + 32 * k + lane;
+                v[k] = c < N ? b.slot[row + c] : -1;
             }
-            pos += __popc(m);
+#pragma unroll
+            for (int k = 0; k < ROWS_BATCH; ++k) {
+                const int c = c00 + 32 * k + lane;
+                const bool hit = v[k] == -2;  // c < N
+                unsigned m = __ballot_sync(0xffffffffu, hit);
+                if (hit) {
+                    int p = pos + __popc(m & ((1u << lane) - 1u));
+                    if (p < b.ent_cap) {
+                        b.col[p] = rbase + c;
+                        b.erow[p] = r;
+                        b.slot[row + c] = p;
+                        float4* z = reinterpret_cast<float4*>(b.esum + size_t(p) * 36);  // summed below
+#pragma unroll
+                        for (int q = 0; q < 9; ++q) z[q] = make_float4(0.f, 0.f, 0.f, 0.f);
+                    } else {
+                        b.slot[row + c] = -1;
+                    }
+                }
+                pos += __popc(m);
+            }
         }
     }
 }
