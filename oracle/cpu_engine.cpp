@@ -2066,6 +2066,15 @@ template <class T> struct IGraph {
     vector<T> x1, x2;  // packed positions
     vector<std::pair<int, int>> edges;
     vector<T> value, deriv, esens;  // deriv: per edge d1+d2 floats
+    // candidate cache (src/interaction_graph.h:51-258): the pairs within
+    // cutoff + buffer (buffer 1 + 0.2 cutoff, :396) at the positions of the
+    // last rebuild, refined to the cutoff at every evaluation; rebuilt when an
+    // element moved more than half the buffer since (:58-91).  The refined
+    // list is the brute-force list at the cutoff, in the same order.
+    vector<std::pair<int, int>> cand;
+    vector<T> xc1, xc2;
+    T cache_cutoff = 0;
+    bool cache_valid = false;
 
     void load(const H5& h, IKind k) {
         kind = k;
@@ -2111,6 +2120,7 @@ template <class T> struct IGraph {
             }
             cutoff = std::max(cutoff, c);
         }
+        cache_valid = false;
     }
     void gather(const Node<T>& n1, const Node<T>* n2) {
         x1.resize(3 * loc1.size());
@@ -2128,8 +2138,37 @@ template <class T> struct IGraph {
     // compute pair list, edge values and derivatives
     void compute(const Node<T>& n1, const Node<T>* n2) {
         gather(n1, n2);
-        find_pairs(symmetric, int(loc1.size()), int(loc2.size()), x1, symmetric ? x1 : x2, id1, id2, cutoff, rule,
-                   edges);
+        const vector<T>& y2 = symmetric ? x1 : x2;
+        bool ok = cache_valid && xc1.size() == x1.size() && (symmetric || xc2.size() == x2.size());
+        if (ok) {
+            const T h = T(0.5f) * (cache_cutoff - cutoff), lim = h * h;
+            auto moved = [&](const vector<T>& x, const vector<T>& xc) {
+                for (size_t i = 0; i < x.size(); i += 3) {
+                    T dx = x[i] - xc[i], dy = x[i + 1] - xc[i + 1], dz = x[i + 2] - xc[i + 2];
+                    if (lim < dx * dx + dy * dy + dz * dz) return true;
+                }
+                return false;
+            };
+            ok = !moved(x1, xc1) && (symmetric || !moved(x2, xc2));
+        }
+        if (!ok) {
+            cache_cutoff = cutoff + (T(1) + T(0.2f) * cutoff);
+            find_pairs(symmetric, int(loc1.size()), int(loc2.size()), x1, y2, id1, id2, cache_cutoff, rule, cand);
+            xc1 = x1;
+            if (!symmetric) xc2 = x2;
+            cache_valid = true;
+        }
+        // refine: the candidates within the cutoff now, in cache order
+        // (src/interaction_graph.h:203-258), by find_pairs' own distance test
+        edges.clear();
+        const T c2 = cutoff * cutoff;
+        for (const auto& pr : cand) {
+            T dx = x1[3 * size_t(pr.first)] - y2[3 * size_t(pr.second)];
+            T dy = x1[3 * size_t(pr.first) + 1] - y2[3 * size_t(pr.second) + 1];
+            T dz = x1[3 * size_t(pr.first) + 2] - y2[3 * size_t(pr.second) + 2];
+            T d2 = dx * dx + dy * dy + dz * dz;
+            if (d2 < c2) edges.push_back(pr);
+        }
         size_t ne = edges.size();
         value.assign(ne, T(0));
         deriv.assign(ne * size_t(d1 + d2), T(0));
