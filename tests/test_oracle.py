@@ -224,6 +224,21 @@ def test_reference_engine_if_built(syn_configs):
     assert rel_f(d, z["ref_deriv"][2]) < 1e-5
 
 
+def test_reference_profile_if_built():
+    """oracle/ref_profile.py, where the reference engine is built here: its
+    profiling build and its own per-node timer report, which names the
+    rotamer node's two timers."""
+    import subprocess
+    import sys
+    ref = os.path.join(os.path.dirname(GOLDEN), "..", "oracle", "_ref", "libupside_ref.so")
+    if not os.path.exists(ref):
+        pytest.skip("reference engine not built on this host")
+    script = os.path.join(os.path.dirname(GOLDEN), "..", "oracle", "ref_profile.py")
+    out = subprocess.run([sys.executable, script, "--systems", "1", "--seconds", "0.2", "--relax", "2"],
+                         capture_output=True, text=True, timeout=900, env=dict(os.environ, OMP_NUM_THREADS="1"))
+    assert out.returncode == 0, out.stderr[-2000:]
+    assert "rotamer_solve" in out.stdout and "rotamer_fill" in out.stdout and "(total)" in out.stdout
+
 
 
 @pytest.mark.parametrize("fp64", [False, True])
